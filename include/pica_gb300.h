@@ -1,0 +1,180 @@
+/*
+ * pica_gb300.h -- C ABI of the GB300 particle-in-cell step.
+ *
+ * pica (the reference) is a header-only C++ library whose hot path is a set of
+ * per-particle operators driven by a host loop: the Yee grid, the Yee solver,
+ * the CIC field interpolator, the Boris pusher, the CIC current depositor and
+ * the supercell ensemble.  Per-particle calls cannot be fast on a GPU, so this
+ * ABI exposes the same operators at ensemble granularity: one call advances
+ * every particle of every supercell.  A host loop that used the reference
+ * classes calls these entry points once per step instead (see INTEGRATION.md
+ * for the header-level C++ mirror and the ctypes binding).
+ *
+ * Conventions
+ *  - Every function returns a status (PICA_OK = 0, negative = error); no C++
+ *    exception crosses this boundary.  pica_last_error() gives the message.
+ *  - The context owns all device memory.  Calls on one context are
+ *    single-threaded and are enqueued on the context's stream.
+ *  - Host arrays use pica's layouts: grid arrays are N^3, z fastest,
+ *    index (i*ny + j)*nz + k (utility/Array.h:140-144); particles are SoA
+ *    with positions in cm and momenta normalised as u = p/(m c)
+ *    (particles/Particle.h:68-72, particles/ParticleArray.h:195-199).
+ *  - Units are CGS, with pica's constants (math/Constants.h:10-18), including
+ *    pi = 3.14159265358.
+ */
+#ifndef PICA_GB300_H
+#define PICA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PICA_ABI_VERSION 1
+
+/* Status codes. */
+#define PICA_OK 0
+#define PICA_ERR_INVALID (-1)   /* bad argument or configuration          */
+#define PICA_ERR_CUDA (-2)      /* CUDA runtime error                     */
+#define PICA_ERR_OOM (-3)       /* device or host allocation failed       */
+#define PICA_ERR_OVERFLOW (-4)  /* supercell capacity could not be grown  */
+#define PICA_ERR_MIGRATION (-5) /* a particle crossed more than one supercell in one step */
+#define PICA_ERR_STATE (-6)     /* call out of order (e.g. push twice without migrate) */
+#define PICA_ERR_NOT_BUILT (-7) /* form / shape / depositor combination not compiled */
+#define PICA_ERR_LIMIT (-8)     /* size beyond a documented fixed limit   */
+
+/* Precision forms. */
+#define PICA_FORM_FP64_PLAIN 0  /* FP64 absolute positions; pica's own arithmetic */
+#define PICA_FORM_FP32_CELL 1   /* int cell index + FP32 in-cell offset, FP32 push */
+
+/* Form factors (field interpolation and charge shape). */
+#define PICA_SHAPE_CIC 1
+#define PICA_SHAPE_TSC 2
+
+/* Current depositors. */
+#define PICA_DEPOSIT_DIRECT 0     /* pica CurrentDepositorCIC: q w v at the new position */
+#define PICA_DEPOSIT_ESIRKEPOV 1  /* charge-conserving (Esirkepov 2001) */
+
+typedef struct pica_config {
+    int32_t n[3];        /* grid cells per dimension (periodic domain [0, n h))         */
+    int32_t sc[3];       /* cells per supercell per dimension; n % sc == 0, sc <= 8      */
+    double h[3];         /* cell size, cm                                                */
+    double dt;           /* time step, s                                                 */
+    int32_t form;        /* PICA_FORM_*                                                  */
+    int32_t shape;       /* PICA_SHAPE_*                                                 */
+    int32_t deposit;     /* PICA_DEPOSIT_*                                               */
+    int32_t nspecies;    /* 1..4 (pica ParticleTypes table, particles/Particle.h:21-31)  */
+    double mass[4];      /* g                                                            */
+    double charge[4];    /* statC                                                        */
+    double slack;        /* spare slots per supercell as a fraction of its count (0 -> 0.15) */
+    int32_t resort_every;/* re-balance supercell capacities every k steps (0 = on overflow only) */
+    int32_t threads;     /* host threads for upload/download/generation (0 = hardware) */
+} pica_config;
+
+typedef struct pica_diag {
+    double field_energy;   /* sum over nodes of (E^2 + B^2) h^3 / (8 pi)         */
+    double kinetic_energy; /* sum over particles of w m c^2 (gamma - 1)          */
+    double total_charge;   /* sum over particles of q w                           */
+    double gauss_max;      /* max over cells |div E - 4 pi (rho + bg)|            */
+    double rho_max;        /* max over cells |rho| of the particles               */
+    double pad_[3];
+} pica_diag;
+
+/* Synthetic plasma description for pica_plasma_generate (host-side set-up). */
+typedef struct pica_plasma_spec {
+    int32_t n[3];          /* cells                                              */
+    int32_t species;       /* species index written for every particle           */
+    double h[3];           /* cell size, cm                                      */
+    double ppc;            /* mean particles per cell                            */
+    double density_mod;    /* a: per-cell count = round(ppc (1 + a cos(2 pi (i+1/2)/nx)))  */
+    double drift_u;        /* beam drift u = gamma beta along drift_axis         */
+    double sigma_u;        /* Maxwellian spread of each u component              */
+    double weight;         /* macro-particle factor                              */
+    uint64_t seed;
+    int32_t nbeams;        /* 1: one thermal population; 2: beams at +drift_u and -drift_u */
+    int32_t drift_axis;    /* 0, 1, 2                                            */
+} pica_plasma_spec;
+
+typedef struct pica_ctx pica_ctx;
+
+int         pica_abi_version(void);
+const char* pica_status_string(int status);
+
+/* Context.  Replaces constructing YeeGrid<Three,Real>(origin, step, size)
+ * (grid/YeeGrid.h:193-256) together with EnsembleSupercells<PA>(min, max,
+ * numCells, numCellsPerSupercell) (particles/EnsembleSupercells.h:25-34) and
+ * BorisPusher<Particle,Real>(dt) (particlePush/BorisPusher.h:23-30). */
+int         pica_ctx_create(const pica_config* cfg, pica_ctx** out);
+int         pica_ctx_destroy(pica_ctx* ctx);
+/* Stream for all work of this context (a cudaStream_t; NULL = legacy default stream). */
+int         pica_set_stream(pica_ctx* ctx, void* stream);
+int         pica_synchronize(pica_ctx* ctx);
+const char* pica_last_error(pica_ctx* ctx);
+/* Kernels this context has launched since creation (for launch accounting). */
+int64_t     pica_launch_count(pica_ctx* ctx);
+
+/* Particles.  Replaces EnsembleSupercells::add (EnsembleSupercells.h:41-45) for
+ * every particle: particles are routed to supercells by
+ * floor(x / supercellSize) in input order.  species may be NULL (all 0). */
+int     pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const double* y, const double* z,
+                              const double* ux, const double* uy, const double* uz, const double* w,
+                              const int32_t* species);
+int64_t pica_num_particles(pica_ctx* ctx);
+/* Download in ensemble order: species, then supercell (linear (sx*nsy+sy)*nsz+sz),
+ * then slot -- the order of EnsembleSupercells::getParticles(idx)[i].  Any pointer may be NULL. */
+int     pica_download_particles(pica_ctx* ctx, double* x, double* y, double* z, double* ux, double* uy,
+                                double* uz, double* w, int32_t* species, int32_t* supercell);
+/* Per-supercell particle counts, counts[species * nsupercells + s]. */
+int     pica_get_counts(pica_ctx* ctx, int32_t* counts);
+
+/* Fields: f9 = {ex, ey, ez, bx, by, bz, jx, jy, jz}, each N^3 doubles.
+ * Replaces element access YeeGrid::ex(i,j,k) ... (grid/YeeGrid.h:293-333). */
+int     pica_upload_fields(pica_ctx* ctx, const double* const* f9);
+int     pica_download_fields(pica_ctx* ctx, double* const* f9);
+
+/* Operators.
+ * pica_push_deposit: for every supercell, FieldInterpolatorCICSupercell::get
+ *   (fieldInterpolation/FieldInterpolatorYeeGrid.h:197-242) or its TSC form,
+ *   BorisPusher::push (particlePush/BorisPusher.h:33-47) and
+ *   CurrentDepositorCICSupercell::deposit + flush (currentDeposition/
+ *   CurrentDepositorYeeGrid.h:178-226) or Esirkepov deposition.  J is cleared
+ *   first; the deposit is periodic.  Leaves the ensemble awaiting pica_migrate.
+ * pica_update_b / pica_update_e: YeeSolver::updateB / updateE
+ *   (fieldSolver/YeeSolver.h:177-213 / 132-175) on the periodic grid.
+ * pica_migrate: wraps positions periodically and moves particles whose
+ *   supercell changed (pica has no migration; order: stayers in slot order,
+ *   then arrivals by direction code, each in source-slot order).
+ * pica_step: push_deposit; update_b(dt/2); update_e(dt); update_b(dt/2); migrate. */
+int     pica_push_deposit(pica_ctx* ctx);
+int     pica_update_b(pica_ctx* ctx, double dt);
+int     pica_update_e(pica_ctx* ctx, double dt);
+int     pica_migrate(pica_ctx* ctx);
+int     pica_step(pica_ctx* ctx, int32_t nsteps);
+
+/* FP64 reductions on the device.  bg_density is a uniform background charge
+ * density (statC/cm^3) added to rho, e.g. immobile neutralising ions. */
+int     pica_diagnostics(pica_ctx* ctx, double bg_density, pica_diag* out);
+/* Charge density at cell centres (N^3 doubles, host), shape of the configured form factor. */
+int     pica_charge_density(pica_ctx* ctx, double* rho);
+/* Field energy sum over the grid (FP64, deterministic two-pass reduction). */
+int     pica_field_energy(pica_ctx* ctx, double* out);
+
+/* Device state, for host loops that keep the particle state in host memory
+ * between steps: raw copies of the current particle buffer (the device
+ * layout, slot arrays of pica_state_slots() entries per species and
+ * component) with cudaMemcpyAsync on the context stream.  comp: FP64 form
+ * 0..6 = x y z ux uy uz w (double); FP32 form 0 = packed cell (uint32),
+ * 1..7 = ox oy oz ux uy uz w (float). */
+int64_t pica_state_slots(pica_ctx* ctx, int32_t species);
+int     pica_state_copy(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device);
+
+/* Host-side plasma set-up (no device work). */
+int64_t pica_plasma_count(const pica_plasma_spec* spec);
+int     pica_plasma_generate(const pica_plasma_spec* spec, int32_t threads, double* x, double* y, double* z,
+                             double* ux, double* uy, double* uz, double* w, int32_t* species);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

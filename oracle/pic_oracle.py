@@ -1,0 +1,183 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads oracle/build/libpic_oracle.so (the restatement, ``Oracle(kind="port")``)
+or oracle/_ref/libpica_ref.so (the harness over pica's own headers,
+``Oracle(kind="reference")``).  Only tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py import this module; the pica_gb300 package never
+does.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "build", "libpic_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libpica_ref.so")
+
+FORM_FP64_PLAIN, FORM_FP32_CELL = 0, 1
+SHAPE_CIC, SHAPE_TSC = 1, 2
+DEPOSIT_DIRECT, DEPOSIT_ESIRKEPOV = 0, 1
+
+
+class OrcConfig(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32 * 3), ("sc", C.c_int32 * 3), ("h", C.c_double * 3), ("dt", C.c_double),
+        ("form", C.c_int32), ("shape", C.c_int32), ("deposit", C.c_int32), ("nspecies", C.c_int32),
+        ("mass", C.c_double * 4), ("charge", C.c_double * 4), ("threads", C.c_int32), ("pad_", C.c_int32),
+    ]
+
+
+class OrcDiag(C.Structure):
+    _fields_ = [("field_energy", C.c_double), ("kinetic_energy", C.c_double), ("total_charge", C.c_double),
+                ("gauss_max", C.c_double), ("rho_max", C.c_double), ("pad_", C.c_double * 3)]
+
+
+def build(reference=True):
+    """Compile the restatement (and, where the pica sources exist, the harness)."""
+    targets = ["oracle"] + (["ref"] if reference else [])
+    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+
+
+_libs = {}
+
+
+def _lib(kind):
+    if kind not in _libs:
+        path = PORT_SO if kind == "port" else REF_SO
+        if not os.path.exists(path):
+            build(reference=(kind == "reference"))
+        lib = C.CDLL(path)
+        p = "orc_" if kind == "port" else "ref_"
+        vp, dp, ip, i64 = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_int64
+        sig = {
+            "create": (vp, [C.POINTER(OrcConfig)]), "destroy": (None, [vp]),
+            "load": (C.c_int, [vp, i64] + [dp] * 7 + [ip]),
+            "set_fields": (C.c_int, [vp, C.POINTER(dp)]), "get_fields": (C.c_int, [vp, C.POINTER(dp)]),
+            "step": (C.c_int, [vp, C.c_int32]), "num_particles": (i64, [vp]),
+            "get_particles": (C.c_int, [vp] + [dp] * 7 + [ip, ip]),
+            "get_counts": (C.c_int, [vp, ip]), "num_migrations": (i64, [vp]),
+            "get_migrations": (C.c_int, [vp, ip, ip, ip, ip]),
+        }
+        if kind == "port":
+            fp = C.POINTER(C.c_float)
+            sig.update({
+                "get_particles_cell": (C.c_int, [vp, ip] + [fp] * 7),
+                "charge_density": (C.c_int, [vp, dp]),
+                "diagnostics": (C.c_int, [vp, C.c_double, C.POINTER(OrcDiag)]),
+            })
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, p + name)
+            fn.restype, fn.argtypes = res, args
+        _libs[kind] = (lib, p)
+    return _libs[kind]
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Oracle:
+    """One CPU simulation.  kind = "port" (restatement) or "reference" (pica headers)."""
+
+    def __init__(self, n, sc, h, dt, form=FORM_FP64_PLAIN, shape=SHAPE_CIC, deposit=DEPOSIT_DIRECT,
+                 species=((9.10938215e-28, -4.80320427e-10),), threads=0, kind="port"):
+        self.lib, self.p = _lib(kind)
+        cfg = OrcConfig()
+        for d in range(3):
+            cfg.n[d], cfg.sc[d], cfg.h[d] = int(n[d]), int(sc[d]), float(h[d])
+        cfg.dt, cfg.form, cfg.shape, cfg.deposit = float(dt), form, shape, deposit
+        cfg.nspecies = len(species)
+        for i, (m, q) in enumerate(species):
+            cfg.mass[i], cfg.charge[i] = m, q
+        cfg.threads = threads
+        self.cfg = cfg
+        self.n = tuple(int(v) for v in n)
+        self.nsc = tuple(int(n[d]) // int(sc[d]) for d in range(3))
+        self.nspecies = len(species)
+        self.h_ = self._f("create")(C.byref(cfg))
+        if not self.h_:
+            raise ValueError("oracle rejected the configuration")
+
+    def _f(self, name):
+        return getattr(self.lib, self.p + name)
+
+    def __del__(self):
+        if getattr(self, "h_", None):
+            self._f("destroy")(self.h_)
+            self.h_ = None
+
+    def load(self, x, y, z, ux, uy, uz, w, species=None):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z, ux, uy, uz, w)]
+        sp = None if species is None else np.ascontiguousarray(species, dtype=np.int32)
+        rc = self._f("load")(self.h_, len(arrs[0]), *[_dp(a) for a in arrs], None if sp is None else _ip(sp))
+        if rc:
+            raise RuntimeError(f"load failed: {rc}")
+
+    def set_fields(self, f9):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in f9]
+        ptrs = (C.POINTER(C.c_double) * 9)(*[_dp(a) for a in arrs])
+        self._keep = arrs
+        if self._f("set_fields")(self.h_, ptrs):
+            raise RuntimeError("set_fields failed")
+
+    def get_fields(self):
+        out = [np.zeros(self.n, dtype=np.float64) for _ in range(9)]
+        ptrs = (C.POINTER(C.c_double) * 9)(*[_dp(a) for a in out])
+        if self._f("get_fields")(self.h_, ptrs):
+            raise RuntimeError("get_fields failed")
+        return out
+
+    def step(self, nsteps=1):
+        rc = self._f("step")(self.h_, int(nsteps))
+        if rc:
+            raise RuntimeError(f"oracle step failed: {rc}")
+
+    def num_particles(self):
+        return int(self._f("num_particles")(self.h_))
+
+    def particles(self):
+        n = self.num_particles()
+        a = [np.zeros(n) for _ in range(7)]
+        sp, sc = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        if self._f("get_particles")(self.h_, *[_dp(v) for v in a], _ip(sp), _ip(sc)):
+            raise RuntimeError("get_particles failed")
+        return dict(zip(("x", "y", "z", "ux", "uy", "uz", "w"), a), species=sp, supercell=sc)
+
+    def particles_cell(self):
+        n = self.num_particles()
+        cell = np.zeros(n, np.int32)
+        f = [np.zeros(n, np.float32) for _ in range(7)]
+        if self._f("get_particles_cell")(self.h_, _ip(cell), *[_fp(v) for v in f]):
+            raise RuntimeError("get_particles_cell failed")
+        return dict(zip(("ox", "oy", "oz", "ux", "uy", "uz", "w"), f), cell=cell)
+
+    def counts(self):
+        c = np.zeros(self.nspecies * int(np.prod(self.nsc)), np.int32)
+        self._f("get_counts")(self.h_, _ip(c))
+        return c.reshape(self.nspecies, -1)
+
+    def migrations(self):
+        n = int(self._f("num_migrations")(self.h_))
+        a = [np.zeros(n, np.int32) for _ in range(4)]
+        self._f("get_migrations")(self.h_, *[_ip(v) for v in a])
+        return np.stack(a, axis=1)
+
+    def charge_density(self):
+        rho = np.zeros(self.n)
+        self._f("charge_density")(self.h_, _dp(rho))
+        return rho
+
+    def diagnostics(self, bg_density=0.0):
+        d = OrcDiag()
+        self._f("diagnostics")(self.h_, float(bg_density), C.byref(d))
+        return {k: getattr(d, k) for k in ("field_energy", "kinetic_energy", "total_charge", "gauss_max", "rho_max")}

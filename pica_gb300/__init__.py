@@ -1,0 +1,207 @@
+"""pica_gb300: pica's particle-in-cell step on one GB300 (sm_103a).
+
+Host-side mirror of pica's operator API for the hot path.  pica drives
+per-particle objects (YeeGrid, YeeSolver, FieldInterpolatorCIC[Supercell],
+BorisPusher, CurrentDepositorCIC[Supercell], EnsembleSupercells); here one
+``Simulation`` owns the device-resident grid and supercell ensemble and each
+operator call advances every particle at once through the C ABI
+(include/pica_gb300.h).  The compute runs only in the CUDA library; there is
+no CPU fallback.
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._lib import PicaConfig, PicaDiag, PicaPlasmaSpec, load
+
+FORM_FP64_PLAIN, FORM_FP32_CELL = 0, 1
+SHAPE_CIC, SHAPE_TSC = 1, 2
+DEPOSIT_DIRECT, DEPOSIT_ESIRKEPOV = 0, 1
+
+# pica math/Constants.h:10-14 (CGS; pi truncated as in the reference)
+PI = 3.14159265358
+LIGHT_VELOCITY = 29979245800.0
+ELECTRON_CHARGE = -4.80320427e-10
+ELECTRON_MASS = 9.10938215e-28
+
+ELECTRON = (ELECTRON_MASS, ELECTRON_CHARGE)
+
+
+class PicaError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"pica_gb300 error {status}: {message}")
+        self.status = status
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Simulation:
+    """A periodic Yee grid plus a supercell ensemble of particles on the GPU.
+
+    Arguments mirror pica: ``n`` = YeeGrid size in cells, ``h`` = step,
+    ``supercell`` = EnsembleSupercells numCellsPerSupercell, ``species`` =
+    the ParticleTypes table as (mass, charge) pairs, ``dt`` = BorisPusher dt.
+    """
+
+    def __init__(self, n, h, dt, supercell=(2, 2, 2), form=FORM_FP64_PLAIN, shape=SHAPE_CIC,
+                 deposit=DEPOSIT_DIRECT, species=(ELECTRON,), slack=0.15, resort_every=0, threads=0):
+        self.lib = load()
+        cfg = PicaConfig()
+        for d in range(3):
+            cfg.n[d], cfg.sc[d], cfg.h[d] = int(n[d]), int(supercell[d]), float(h[d])
+        cfg.dt, cfg.form, cfg.shape, cfg.deposit = float(dt), int(form), int(shape), int(deposit)
+        cfg.nspecies = len(species)
+        for i, (m, q) in enumerate(species):
+            cfg.mass[i], cfg.charge[i] = float(m), float(q)
+        cfg.slack, cfg.resort_every, cfg.threads = float(slack), int(resort_every), int(threads)
+        self.cfg = cfg
+        self.n = tuple(int(v) for v in n)
+        self.h = tuple(float(v) for v in h)
+        self.dt = float(dt)
+        self.form = int(form)
+        self.nsc = tuple(self.n[d] // int(supercell[d]) for d in range(3))
+        self.nspecies = len(species)
+        self.species = tuple(species)
+        handle = C.c_void_p()
+        rc = self.lib.pica_ctx_create(C.byref(cfg), C.byref(handle))
+        if rc:
+            raise PicaError(rc, self.lib.pica_status_string(rc).decode())
+        self.ctx = handle
+
+    # -- lifetime ------------------------------------------------------------
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.pica_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise PicaError(rc, self.lib.pica_last_error(self.ctx).decode() or self.lib.pica_status_string(rc).decode())
+
+    def set_stream(self, stream_ptr):
+        """Enqueue all work on this cudaStream_t (an int, e.g. torch.cuda.current_stream().cuda_stream)."""
+        self._check(self.lib.pica_set_stream(self.ctx, C.c_void_p(int(stream_ptr))))
+
+    def synchronize(self):
+        self._check(self.lib.pica_synchronize(self.ctx))
+
+    def launch_count(self):
+        return int(self.lib.pica_launch_count(self.ctx))
+
+    # -- data ----------------------------------------------------------------
+    def upload_particles(self, x, y, z, ux, uy, uz, w, species=None):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z, ux, uy, uz, w)]
+        sp = None if species is None else np.ascontiguousarray(species, dtype=np.int32)
+        self._check(self.lib.pica_upload_particles(self.ctx, len(arrs[0]), *[_dp(a) for a in arrs],
+                                                   None if sp is None else _ip(sp)))
+
+    def num_particles(self):
+        n = int(self.lib.pica_num_particles(self.ctx))
+        if n < 0:
+            self._check(n)
+        return n
+
+    def particles(self):
+        """Particles in ensemble order (species, supercell, slot) as a dict of arrays."""
+        n = self.num_particles()
+        a = [np.empty(n) for _ in range(7)]
+        sp, sc = np.empty(n, np.int32), np.empty(n, np.int32)
+        self._check(self.lib.pica_download_particles(self.ctx, *[_dp(v) for v in a], _ip(sp), _ip(sc)))
+        return dict(zip(("x", "y", "z", "ux", "uy", "uz", "w"), a), species=sp, supercell=sc)
+
+    def counts(self):
+        c = np.empty(self.nspecies * int(np.prod(self.nsc)), np.int32)
+        self._check(self.lib.pica_get_counts(self.ctx, _ip(c)))
+        return c.reshape(self.nspecies, -1)
+
+    def upload_fields(self, f9):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in f9]
+        ptrs = (C.POINTER(C.c_double) * 9)(*[_dp(a) for a in arrs])
+        self._check(self.lib.pica_upload_fields(self.ctx, ptrs))
+
+    def fields(self):
+        """[ex, ey, ez, bx, by, bz, jx, jy, jz] as (nx, ny, nz) float64 arrays."""
+        out = [np.empty(self.n) for _ in range(9)]
+        ptrs = (C.POINTER(C.c_double) * 9)(*[_dp(a) for a in out])
+        self._check(self.lib.pica_download_fields(self.ctx, ptrs))
+        return out
+
+    # -- operators -------------------------------------------------------------
+    def push_deposit(self):
+        """FieldInterpolator::get + BorisPusher::push + CurrentDepositor::deposit for every particle."""
+        self._check(self.lib.pica_push_deposit(self.ctx))
+
+    def update_b(self, dt):
+        """YeeSolver::updateB(grid, dt) on the periodic grid."""
+        self._check(self.lib.pica_update_b(self.ctx, float(dt)))
+
+    def update_e(self, dt):
+        """YeeSolver::updateE(grid, dt) on the periodic grid."""
+        self._check(self.lib.pica_update_e(self.ctx, float(dt)))
+
+    def migrate(self):
+        """Periodic wrap and supercell re-binning after push_deposit."""
+        self._check(self.lib.pica_migrate(self.ctx))
+
+    def step(self, nsteps=1):
+        self._check(self.lib.pica_step(self.ctx, int(nsteps)))
+
+    # -- diagnostics -----------------------------------------------------------
+    def diagnostics(self, bg_density=0.0):
+        d = PicaDiag()
+        self._check(self.lib.pica_diagnostics(self.ctx, float(bg_density), C.byref(d)))
+        return {k: getattr(d, k) for k in ("field_energy", "kinetic_energy", "total_charge", "gauss_max", "rho_max")}
+
+    def charge_density(self):
+        rho = np.empty(self.n)
+        self._check(self.lib.pica_charge_density(self.ctx, _dp(rho)))
+        return rho
+
+    def field_energy(self):
+        v = C.c_double()
+        self._check(self.lib.pica_field_energy(self.ctx, C.byref(v)))
+        return v.value
+
+    # -- raw device state (host loops that keep the state in host memory) ------
+    def state_slots(self, species=0):
+        return int(self.lib.pica_state_slots(self.ctx, int(species)))
+
+    def state_copy(self, species, comp, host_ptr, to_device):
+        self._check(self.lib.pica_state_copy(self.ctx, int(species), int(comp), C.c_void_p(int(host_ptr)),
+                                             1 if to_device else 0))
+
+
+def plasma_spec(n, h, ppc, sigma_u, weight, seed, species=0, density_mod=0.0, nbeams=1, drift_u=0.0, drift_axis=0):
+    s = PicaPlasmaSpec()
+    for d in range(3):
+        s.n[d], s.h[d] = int(n[d]), float(h[d])
+    s.species, s.ppc, s.density_mod = int(species), float(ppc), float(density_mod)
+    s.drift_u, s.sigma_u, s.weight, s.seed = float(drift_u), float(sigma_u), float(weight), int(seed)
+    s.nbeams, s.drift_axis = int(nbeams), int(drift_axis)
+    return s
+
+
+def generate_plasma(spec, threads=0):
+    """Synthetic plasma on the host (counter-based RNG; independent of thread count)."""
+    lib = load()
+    n = int(lib.pica_plasma_count(C.byref(spec)))
+    if n < 0:
+        raise PicaError(n, "bad plasma spec")
+    a = [np.empty(n) for _ in range(7)]
+    sp = np.empty(n, np.int32)
+    rc = lib.pica_plasma_generate(C.byref(spec), int(threads), *[_dp(v) for v in a], _ip(sp))
+    if rc:
+        raise PicaError(rc, "plasma generation failed")
+    return dict(zip(("x", "y", "z", "ux", "uy", "uz", "w"), a), species=sp)

@@ -1,0 +1,284 @@
+// Yee field update and FP64 diagnostics on the periodic grid.
+//
+// Built with --fmad=false: the FP64 Yee update must round exactly as pica's
+// YeeSolver does (fieldSolver/YeeSolver.h:146-154, 190-195), term for term.
+// Every node is updated from its periodic neighbours, which replaces pica's
+// guard planes and "edge" loops (YeeSolver.h:156-174, 197-212).
+#include <cstdint>
+
+#include "pica_internal.h"
+
+namespace pgb {
+
+namespace {
+
+constexpr double kPiRef = 3.14159265358;  // pica math/Constants.h:10
+
+struct Idx {
+    int64_t o, xm, ym, zm, xp, yp, zp;
+};
+
+__device__ __forceinline__ Idx neighbours(int64_t idx, int nx, int ny, int nz) {
+    const int k = (int)(idx % nz);
+    const int j = (int)((idx / nz) % ny);
+    const int i = (int)(idx / ((int64_t)nz * ny));
+    const int64_t sx = (int64_t)ny * nz, sy = nz;
+    Idx r;
+    r.o = idx;
+    r.xm = idx + (i == 0 ? (int64_t)(nx - 1) * sx : -sx);
+    r.xp = idx + (i == nx - 1 ? -(int64_t)(nx - 1) * sx : sx);
+    r.ym = idx + (j == 0 ? (int64_t)(ny - 1) * sy : -sy);
+    r.yp = idx + (j == ny - 1 ? -(int64_t)(ny - 1) * sy : sy);
+    r.zm = idx + (k == 0 ? nz - 1 : -1);
+    r.zp = idx + (k == nz - 1 ? -(nz - 1) : 1);
+    return r;
+}
+
+// B += c dt curl E terms of YeeSolver.h:190-195 (updateB) with periodic neighbours.
+template <typename R>
+__global__ void __launch_bounds__(256) k_updateB(R* __restrict__ bx, R* __restrict__ by, R* __restrict__ bz,
+                                                 const R* __restrict__ ex, const R* __restrict__ ey,
+                                                 const R* __restrict__ ez, int nx, int ny, int nz, R cx, R cy, R cz) {
+    const int64_t total = (int64_t)nx * ny * nz;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const Idx q = neighbours(idx, nx, ny, nz);
+        const int64_t o = q.o;
+        bx[o] += cz * (ey[o] - ey[q.zm]) - cy * (ez[o] - ez[q.ym]);
+        by[o] += cx * (ez[o] - ez[q.xm]) - cz * (ex[o] - ex[q.zm]);
+        bz[o] += cy * (ex[o] - ex[q.ym]) - cx * (ey[o] - ey[q.xm]);
+    }
+}
+
+// E += -4 pi dt J + c dt curl B, YeeSolver.h:146-154 (updateE) with periodic neighbours.
+template <typename R>
+__global__ void __launch_bounds__(256) k_updateE(R* __restrict__ ex, R* __restrict__ ey, R* __restrict__ ez,
+                                                 const R* __restrict__ bx, const R* __restrict__ by,
+                                                 const R* __restrict__ bz, const R* __restrict__ jx,
+                                                 const R* __restrict__ jy, const R* __restrict__ jz, int nx, int ny,
+                                                 int nz, R cc, R cx, R cy, R cz) {
+    const int64_t total = (int64_t)nx * ny * nz;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const Idx q = neighbours(idx, nx, ny, nz);
+        const int64_t o = q.o;
+        ex[o] += cc * jx[o] + cy * (bz[q.yp] - bz[o]) - cz * (by[q.zp] - by[o]);
+        ey[o] += cc * jy[o] + cz * (bx[q.zp] - bx[o]) - cx * (bz[q.xp] - bz[o]);
+        ez[o] += cc * jz[o] + cx * (by[q.xp] - by[o]) - cy * (bx[q.yp] - bx[o]);
+    }
+}
+
+// Fixed-order block reduction (sum or max) of one double per thread.
+template <bool MAX>
+__device__ __forceinline__ double blockReduce(double v, double* sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) sh[threadIdx.x] = MAX ? fmax(sh[threadIdx.x], sh[threadIdx.x + w]) : sh[threadIdx.x] + sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_sumsq(const R* f0, const R* f1, const R* f2, const R* f3, const R* f4,
+                                               const R* f5, int64_t n, double* partial) {
+    __shared__ double sh[256];
+    double acc = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double a0 = f0[i], a1 = f1[i], a2 = f2[i], a3 = f3[i], a4 = f4[i], a5 = f5[i];
+        acc += a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5;
+    }
+    const double r = blockReduce<false>(acc, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = r;
+}
+
+// Single-block final reduction over `np` partials in a fixed order.
+template <bool MAX>
+__global__ void __launch_bounds__(256) k_final(const double* partial, int np, int stride, int nvals, double* out) {
+    __shared__ double sh[256];
+    for (int v = 0; v < nvals; v++) {
+        double acc = 0.0;
+        for (int i = threadIdx.x; i < np; i += blockDim.x) {
+            const double x = partial[(int64_t)v * stride + i];
+            acc = MAX ? fmax(acc, x) : acc + x;
+        }
+        const double r = blockReduce<MAX>(acc, sh);
+        if (threadIdx.x == 0) out[v] = r;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ double asDouble(const void* p, int64_t i) {
+    return (double)static_cast<const T*>(p)[i];
+}
+
+// Per-supercell kinetic energy and charge (FP64), one block per supercell.
+__global__ void __launch_bounds__(256) k_particleSums(const ParticleSumArgs a, double* partial) {
+    __shared__ double sh[256];
+    const int s = blockIdx.x;
+    double ek = 0.0, q = 0.0;
+    for (int sp = 0; sp < a.nspecies; sp++) {
+        const int64_t start = a.start[sp][s];
+        const int cnt = a.count[sp][s];
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const int64_t o = start + i;
+            double ux, uy, uz, w;
+            if (a.fp64) { ux = asDouble<double>(a.ux[sp], o); uy = asDouble<double>(a.uy[sp], o); uz = asDouble<double>(a.uz[sp], o); w = asDouble<double>(a.w[sp], o); }
+            else { ux = asDouble<float>(a.ux[sp], o); uy = asDouble<float>(a.uy[sp], o); uz = asDouble<float>(a.uz[sp], o); w = asDouble<float>(a.w[sp], o); }
+            const double u2 = ux * ux + uy * uy + uz * uz;
+            ek += w * a.mc2[sp] * (u2 / (1.0 + sqrt(1.0 + u2)));
+            q += a.q[sp] * w;
+        }
+    }
+    const double r0 = blockReduce<false>(ek, sh);
+    const double r1 = blockReduce<false>(q, sh);
+    if (threadIdx.x == 0) { partial[s] = r0; partial[a.nscTot + s] = r1; }
+}
+
+__device__ __forceinline__ void tsc3(double d, double* w) {
+    w[0] = 0.5 * (0.5 - d) * (0.5 - d);
+    w[1] = 0.75 - d * d;
+    w[2] = 0.5 * (0.5 + d) * (0.5 + d);
+}
+
+// Charge density at cell centres (the rho lattice, node m at (m+1/2) h), FP64 atomics.
+__global__ void __launch_bounds__(256) k_rho(const RhoArgs a, double* rho) {
+    const int s = blockIdx.x;
+    const int np = a.shape == PICA_SHAPE_CIC ? 2 : 3;
+    for (int sp = 0; sp < a.nspecies; sp++) {
+        const int64_t start = a.start[sp][s];
+        const int cnt = a.count[sp][s];
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const int64_t o = start + i;
+            int lo[3];
+            double w[3][3];
+            double wt;
+            if (a.fp64) {
+                const double pos[3] = {asDouble<double>(a.p0[sp], o), asDouble<double>(a.p1[sp], o), asDouble<double>(a.p2[sp], o)};
+                wt = asDouble<double>(a.w[sp], o);
+                for (int d = 0; d < 3; d++) {
+                    const double xi = pos[d] * a.invh[d] - 0.5;
+                    if (np == 2) { const int n = (int)floor(xi); w[d][0] = 1.0 - (xi - n); w[d][1] = xi - n; lo[d] = n; }
+                    else { const int n = (int)floor(xi + 0.5); tsc3(xi - n, w[d]); lo[d] = n - 1; }
+                }
+            } else {
+                int c3[3];
+                unpackCell(static_cast<const uint32_t*>(a.p0[sp])[o], c3[0], c3[1], c3[2]);
+                const double off[3] = {asDouble<float>(a.p1[sp], o), asDouble<float>(a.p2[sp], o), asDouble<float>(a.p3[sp], o)};
+                wt = asDouble<float>(a.w[sp], o);
+                for (int d = 0; d < 3; d++) {
+                    if (np == 2) {
+                        const bool hi = off[d] >= 0.5;
+                        const double dd = hi ? off[d] - 0.5 : off[d] + 0.5;
+                        lo[d] = hi ? c3[d] : c3[d] - 1; w[d][0] = 1.0 - dd; w[d][1] = dd;
+                    } else { tsc3(off[d] - 0.5, w[d]); lo[d] = c3[d] - 1; }
+                }
+            }
+            const double v = a.q[sp] * wt * a.norm;
+            for (int ii = 0; ii < np; ii++)
+                for (int jj = 0; jj < np; jj++)
+                    for (int kk = 0; kk < np; kk++) {
+                        int gx = (lo[0] + ii) % a.n[0]; if (gx < 0) gx += a.n[0];
+                        int gy = (lo[1] + jj) % a.n[1]; if (gy < 0) gy += a.n[1];
+                        int gz = (lo[2] + kk) % a.n[2]; if (gz < 0) gz += a.n[2];
+                        atomicAdd(rho + ((int64_t)gx * a.n[1] + gy) * a.n[2] + gz, v * w[0][ii] * w[1][jj] * w[2][kk]);
+                    }
+        }
+    }
+}
+
+// max |div E - 4 pi (rho + bg)| and max |rho|; div E at the cell centre from the
+// face-centred E of pica's lattice (Ex at (i, j+1/2, k+1/2) is the x face of cell (i,j,k)).
+template <typename R>
+__global__ void __launch_bounds__(256) k_gauss(const R* ex, const R* ey, const R* ez, const double* rho, int nx,
+                                               int ny, int nz, double hx, double hy, double hz, double bg,
+                                               double* partial) {
+    __shared__ double sh[256];
+    const int64_t total = (int64_t)nx * ny * nz;
+    double g = 0.0, r = 0.0;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const Idx q = neighbours(idx, nx, ny, nz);
+        const double div = ((double)ex[q.xp] - (double)ex[idx]) / hx + ((double)ey[q.yp] - (double)ey[idx]) / hy +
+                           ((double)ez[q.zp] - (double)ez[idx]) / hz;
+        const double rv = rho[idx];
+        g = fmax(g, fabs(div - 4.0 * kPiRef * (rv + bg)));
+        r = fmax(r, fabs(rv));
+    }
+    const double g0 = blockReduce<true>(g, sh);
+    const double r0 = blockReduce<true>(r, sh);
+    if (threadIdx.x == 0) { partial[blockIdx.x] = g0; partial[kReduceBlocks + blockIdx.x] = r0; }
+}
+
+inline int gridFor(int64_t n) {
+    const int64_t b = (n + 255) / 256;
+    return (int)(b < 152 * 16 ? b : 152 * 16);
+}
+
+}  // namespace
+
+int launchUpdateB(bool fp64, void* const* f, const int* n, const double* c, cudaStream_t s) {
+    const int64_t total = (int64_t)n[0] * n[1] * n[2];
+    if (fp64)
+        k_updateB<double><<<gridFor(total), 256, 0, s>>>((double*)f[3], (double*)f[4], (double*)f[5], (const double*)f[0],
+                                                         (const double*)f[1], (const double*)f[2], n[0], n[1], n[2], c[0], c[1], c[2]);
+    else
+        k_updateB<float><<<gridFor(total), 256, 0, s>>>((float*)f[3], (float*)f[4], (float*)f[5], (const float*)f[0],
+                                                        (const float*)f[1], (const float*)f[2], n[0], n[1], n[2], (float)c[0],
+                                                        (float)c[1], (float)c[2]);
+    return (int)cudaGetLastError();
+}
+
+int launchUpdateE(bool fp64, void* const* f, const int* n, double cc, const double* c, cudaStream_t s) {
+    const int64_t total = (int64_t)n[0] * n[1] * n[2];
+    if (fp64)
+        k_updateE<double><<<gridFor(total), 256, 0, s>>>((double*)f[0], (double*)f[1], (double*)f[2], (const double*)f[3],
+                                                         (const double*)f[4], (const double*)f[5], (const double*)f[6],
+                                                         (const double*)f[7], (const double*)f[8], n[0], n[1], n[2], cc,
+                                                         c[0], c[1], c[2]);
+    else
+        k_updateE<float><<<gridFor(total), 256, 0, s>>>((float*)f[0], (float*)f[1], (float*)f[2], (const float*)f[3],
+                                                        (const float*)f[4], (const float*)f[5], (const float*)f[6],
+                                                        (const float*)f[7], (const float*)f[8], n[0], n[1], n[2], (float)cc,
+                                                        (float)c[0], (float)c[1], (float)c[2]);
+    return (int)cudaGetLastError();
+}
+
+int launchFieldEnergy(bool fp64, void* const* f, int64_t nodes, double* partial, double* out, cudaStream_t s) {
+    if (fp64)
+        k_sumsq<double><<<kReduceBlocks, 256, 0, s>>>((const double*)f[0], (const double*)f[1], (const double*)f[2],
+                                                      (const double*)f[3], (const double*)f[4], (const double*)f[5], nodes, partial);
+    else
+        k_sumsq<float><<<kReduceBlocks, 256, 0, s>>>((const float*)f[0], (const float*)f[1], (const float*)f[2],
+                                                     (const float*)f[3], (const float*)f[4], (const float*)f[5], nodes, partial);
+    k_final<false><<<1, 256, 0, s>>>(partial, kReduceBlocks, 0, 1, out);
+    return (int)cudaGetLastError();
+}
+
+int launchParticleSums(const ParticleSumArgs& a, double* partial, double* out2, cudaStream_t s) {
+    k_particleSums<<<a.nscTot, 256, 0, s>>>(a, partial);
+    k_final<false><<<1, 256, 0, s>>>(partial, a.nscTot, a.nscTot, 2, out2);
+    return (int)cudaGetLastError();
+}
+
+int launchRho(const RhoArgs& a, double* rho, cudaStream_t s) {
+    k_rho<<<a.nscTot, 256, 0, s>>>(a, rho);
+    return (int)cudaGetLastError();
+}
+
+int launchGauss(bool fp64, void* const* f, const double* rho, const int* n, const double* h, double bg,
+                double* partial, double* out2, cudaStream_t s) {
+    if (fp64)
+        k_gauss<double><<<kReduceBlocks, 256, 0, s>>>((const double*)f[0], (const double*)f[1], (const double*)f[2], rho,
+                                                      n[0], n[1], n[2], h[0], h[1], h[2], bg, partial);
+    else
+        k_gauss<float><<<kReduceBlocks, 256, 0, s>>>((const float*)f[0], (const float*)f[1], (const float*)f[2], rho,
+                                                     n[0], n[1], n[2], h[0], h[1], h[2], bg, partial);
+    k_final<true><<<1, 256, 0, s>>>(partial, kReduceBlocks, kReduceBlocks, 2, out2);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace pgb

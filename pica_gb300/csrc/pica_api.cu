@@ -1,0 +1,794 @@
+// C ABI of pica_gb300 (include/pica_gb300.h): context, particle/field transfer,
+// step orchestration and host-side plasma generation.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "pica_internal.h"
+
+using namespace pgb;
+
+namespace {
+
+constexpr double kC = 29979245800.0;     // pica math/Constants.h:11
+constexpr double kPiRef = 3.14159265358; // pica math/Constants.h:10
+
+inline int wrapHost(int a, int n) { a %= n; return a < 0 ? a + n : a; }
+
+struct SpeciesState {
+    void* buf[2][8] = {};
+    int64_t slots[2] = {0, 0};   // allocated slots of each buffer
+    uint8_t* dir = nullptr;
+    int64_t dirSlots = 0;
+    int64_t* d_start = nullptr;
+    int32_t* d_cap = nullptr;
+    int32_t* d_count = nullptr;
+    int32_t* d_nstay = nullptr;
+    int32_t* d_nleave = nullptr;
+    int32_t* d_needed = nullptr;
+    int64_t* d_start2 = nullptr;
+    int32_t* d_cap2 = nullptr;
+    std::vector<int64_t> h_start;
+    std::vector<int32_t> h_cap;
+    int64_t layoutSlots = 0;     // sum of caps of the current layout
+};
+
+}  // namespace
+
+struct pica_ctx {
+    pica_config cfg;
+    bool fp64 = true;
+    int ncomp = 7;
+    size_t compBytes[8] = {};
+    int nsc[3] = {}, nscTot = 0, T[3] = {};
+    cudaStream_t stream = nullptr;
+    void* f[9] = {};
+    SpeciesState sp[kMaxSpecies];
+    int cur = 0;
+    bool pending = false;
+    int* d_flags = nullptr;
+    int* h_flags = nullptr;
+    double* d_red = nullptr;
+    int64_t redCount = 0;
+    double* d_out = nullptr;
+    double* h_out = nullptr;
+    double* d_rho = nullptr;
+    std::string err;
+    int64_t launches = 0;
+    int64_t steps = 0;
+    int threads = 1;
+};
+
+namespace {
+
+int fail(pica_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                               \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? PICA_ERR_OOM : PICA_ERR_CUDA,   \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+    } while (0)
+
+#define CKL(expr)                                                                              \
+    do {                                                                                       \
+        int e_ = (expr);                                                                       \
+        if (e_ != 0)                                                                           \
+            return fail(ctx, PICA_ERR_CUDA, std::string(#expr) + ": " +                        \
+                        cudaGetErrorString((cudaError_t)e_));                                  \
+    } while (0)
+
+int scLinear(const pica_ctx* c, int x, int y, int z) { return (x * c->nsc[1] + y) * c->nsc[2] + z; }
+
+int32_t capacityFor(const pica_ctx* c, int32_t count) {
+    const double sl = c->cfg.slack > 0 ? c->cfg.slack : 0.15;
+    int64_t extra = std::max<int64_t>(32, (int64_t)std::ceil(count * sl));
+    int64_t cap = (count + extra + 31) / 32 * 32;
+    return (int32_t)cap;
+}
+
+void layoutFrom(const pica_ctx* c, const std::vector<int32_t>& counts, std::vector<int64_t>& start,
+                std::vector<int32_t>& cap, int64_t& total) {
+    start.resize(c->nscTot);
+    cap.resize(c->nscTot);
+    total = 0;
+    for (int s = 0; s < c->nscTot; s++) {
+        start[s] = total;
+        cap[s] = capacityFor(c, counts[s]);
+        total += cap[s];
+    }
+}
+
+int ensureBuffer(pica_ctx* ctx, int spi, int b, int64_t slots) {
+    SpeciesState& S = ctx->sp[spi];
+    if (S.slots[b] >= slots) return PICA_OK;
+    for (int k = 0; k < ctx->ncomp; k++) {
+        if (S.buf[b][k]) CK(cudaFree(S.buf[b][k]));
+        S.buf[b][k] = nullptr;
+    }
+    S.slots[b] = 0;
+    for (int k = 0; k < ctx->ncomp; k++) CK(cudaMalloc(&S.buf[b][k], std::max<int64_t>(slots, 1) * ctx->compBytes[k]));
+    S.slots[b] = slots;
+    return PICA_OK;
+}
+
+int ensureDir(pica_ctx* ctx, int spi, int64_t slots) {
+    SpeciesState& S = ctx->sp[spi];
+    if (S.dirSlots >= slots) return PICA_OK;
+    if (S.dir) CK(cudaFree(S.dir));
+    S.dir = nullptr;
+    S.dirSlots = 0;
+    CK(cudaMalloc(&S.dir, std::max<int64_t>(slots, 1)));
+    S.dirSlots = slots;
+    return PICA_OK;
+}
+
+PlainPtrs plainPtrs(pica_ctx* c, int spi, int b) {
+    void* const* p = c->sp[spi].buf[b];
+    return PlainPtrs{(double*)p[0], (double*)p[1], (double*)p[2], (double*)p[3], (double*)p[4], (double*)p[5], (double*)p[6]};
+}
+CellPtrs cellPtrs(pica_ctx* c, int spi, int b) {
+    void* const* p = c->sp[spi].buf[b];
+    return CellPtrs{(uint32_t*)p[0], (float*)p[1], (float*)p[2], (float*)p[3], (float*)p[4], (float*)p[5], (float*)p[6], (float*)p[7]};
+}
+
+// Run fn over [0, n) split into contiguous chunks on `threads` host threads.
+void parallelFor(int threads, int64_t n, const std::function<void(int64_t, int64_t)>& fn) {
+    if (threads <= 1 || n < 65536) { fn(0, n); return; }
+    std::vector<std::thread> th;
+    int64_t chunk = (n + threads - 1) / threads;
+    for (int t = 0; t < threads; t++) {
+        int64_t a = t * chunk, b = std::min(n, a + chunk);
+        if (a >= b) break;
+        th.emplace_back(fn, a, b);
+    }
+    for (auto& t : th) t.join();
+}
+}  // namespace
+
+extern "C" {
+
+int pica_abi_version(void) { return PICA_ABI_VERSION; }
+
+const char* pica_status_string(int s) {
+    switch (s) {
+        case PICA_OK: return "ok";
+        case PICA_ERR_INVALID: return "invalid argument or configuration";
+        case PICA_ERR_CUDA: return "CUDA runtime error";
+        case PICA_ERR_OOM: return "out of memory";
+        case PICA_ERR_OVERFLOW: return "supercell capacity overflow";
+        case PICA_ERR_MIGRATION: return "particle crossed more than one supercell in one step";
+        case PICA_ERR_STATE: return "call out of order";
+        case PICA_ERR_NOT_BUILT: return "combination not built";
+        case PICA_ERR_LIMIT: return "size beyond a fixed limit";
+        default: return "unknown status";
+    }
+}
+
+const char* pica_last_error(pica_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+int64_t pica_launch_count(pica_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int pica_ctx_create(const pica_config* cfg, pica_ctx** out) {
+    pica_ctx* ctx = nullptr;
+    if (!cfg || !out) return PICA_ERR_INVALID;
+    *out = nullptr;
+    if (cfg->form != PICA_FORM_FP64_PLAIN && cfg->form != PICA_FORM_FP32_CELL) return PICA_ERR_INVALID;
+    if (cfg->shape != PICA_SHAPE_CIC && cfg->shape != PICA_SHAPE_TSC) return PICA_ERR_INVALID;
+    if (cfg->deposit != PICA_DEPOSIT_DIRECT && cfg->deposit != PICA_DEPOSIT_ESIRKEPOV) return PICA_ERR_INVALID;
+    if (cfg->nspecies < 1 || cfg->nspecies > kMaxSpecies) return PICA_ERR_INVALID;
+    if (!(cfg->dt > 0)) return PICA_ERR_INVALID;
+    for (int d = 0; d < 3; d++) {
+        if (cfg->n[d] <= 0 || cfg->sc[d] <= 0 || cfg->sc[d] > kMaxS || cfg->n[d] % cfg->sc[d] != 0) return PICA_ERR_INVALID;
+        if (!(cfg->h[d] > 0)) return PICA_ERR_INVALID;
+    }
+    if (cfg->form == PICA_FORM_FP32_CELL && (cfg->n[0] > 2048 || cfg->n[1] > 2048 || cfg->n[2] > 1024)) return PICA_ERR_LIMIT;
+    ctx = new pica_ctx();
+    ctx->cfg = *cfg;
+    ctx->fp64 = cfg->form == PICA_FORM_FP64_PLAIN;
+    ctx->ncomp = ctx->fp64 ? 7 : 8;
+    for (int k = 0; k < 8; k++) ctx->compBytes[k] = ctx->fp64 ? 8 : 4;
+    ctx->nscTot = 1;
+    for (int d = 0; d < 3; d++) {
+        ctx->nsc[d] = cfg->n[d] / cfg->sc[d];
+        ctx->nscTot *= ctx->nsc[d];
+        ctx->T[d] = cfg->sc[d] + 2 * kG + 1;
+    }
+    ctx->threads = cfg->threads > 0 ? cfg->threads : std::max(1u, std::thread::hardware_concurrency());
+    const int64_t nodes = (int64_t)cfg->n[0] * cfg->n[1] * cfg->n[2];
+    const size_t rb = ctx->fp64 ? 8 : 4;
+    int rc = PICA_OK;
+    auto bail = [&](int code) { pica_ctx_destroy(ctx); return code; };
+    for (int c = 0; c < 9; c++) {
+        if (cudaMalloc(&ctx->f[c], nodes * rb) != cudaSuccess) return bail(PICA_ERR_OOM);
+        if (cudaMemset(ctx->f[c], 0, nodes * rb) != cudaSuccess) return bail(PICA_ERR_CUDA);
+    }
+    for (int s = 0; s < cfg->nspecies; s++) {
+        SpeciesState& S = ctx->sp[s];
+        const size_t n = ctx->nscTot;
+        if (cudaMalloc(&S.d_start, n * 8) || cudaMalloc(&S.d_cap, n * 4) || cudaMalloc(&S.d_count, n * 4) ||
+            cudaMalloc(&S.d_nstay, n * 4) || cudaMalloc(&S.d_nleave, n * 4) || cudaMalloc(&S.d_needed, n * 4) ||
+            cudaMalloc(&S.d_start2, n * 8) || cudaMalloc(&S.d_cap2, n * 4))
+            return bail(PICA_ERR_OOM);
+        std::vector<int32_t> zero(n, 0);
+        int64_t total;
+        layoutFrom(ctx, zero, S.h_start, S.h_cap, total);
+        S.layoutSlots = total;
+        if ((rc = ensureBuffer(ctx, s, 0, total)) || (rc = ensureBuffer(ctx, s, 1, total)) || (rc = ensureDir(ctx, s, total)))
+            return bail(rc);
+        if (cudaMemcpy(S.d_start, S.h_start.data(), n * 8, cudaMemcpyHostToDevice) ||
+            cudaMemcpy(S.d_cap, S.h_cap.data(), n * 4, cudaMemcpyHostToDevice) || cudaMemset(S.d_count, 0, n * 4))
+            return bail(PICA_ERR_CUDA);
+    }
+    ctx->redCount = std::max<int64_t>(2 * kReduceBlocks, 2 * (int64_t)ctx->nscTot) + 8;
+    if (cudaMalloc(&ctx->d_flags, 4 * sizeof(int)) || cudaMallocHost(&ctx->h_flags, 4 * sizeof(int)) ||
+        cudaMalloc(&ctx->d_red, ctx->redCount * 8) || cudaMalloc(&ctx->d_out, 8 * 8) || cudaMallocHost(&ctx->h_out, 8 * 8))
+        return bail(PICA_ERR_OOM);
+    cudaMemset(ctx->d_flags, 0, 4 * sizeof(int));
+    if (cudaDeviceSynchronize() != cudaSuccess) return bail(PICA_ERR_CUDA);
+    *out = ctx;
+    return PICA_OK;
+}
+
+int pica_ctx_destroy(pica_ctx* ctx) {
+    if (!ctx) return PICA_ERR_INVALID;
+    cudaDeviceSynchronize();
+    for (auto p : ctx->f) if (p) cudaFree(p);
+    for (auto& S : ctx->sp) {
+        for (auto& b : S.buf) for (auto p : b) if (p) cudaFree(p);
+        for (void* p : {(void*)S.dir, (void*)S.d_start, (void*)S.d_cap, (void*)S.d_count, (void*)S.d_nstay,
+                        (void*)S.d_nleave, (void*)S.d_needed, (void*)S.d_start2, (void*)S.d_cap2})
+            if (p) cudaFree(p);
+    }
+    if (ctx->d_flags) cudaFree(ctx->d_flags);
+    if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+    if (ctx->d_red) cudaFree(ctx->d_red);
+    if (ctx->d_out) cudaFree(ctx->d_out);
+    if (ctx->h_out) cudaFreeHost(ctx->h_out);
+    if (ctx->d_rho) cudaFree(ctx->d_rho);
+    delete ctx;
+    return PICA_OK;
+}
+
+int pica_set_stream(pica_ctx* ctx, void* stream) {
+    if (!ctx) return PICA_ERR_INVALID;
+    ctx->stream = (cudaStream_t)stream;
+    return PICA_OK;
+}
+
+int pica_synchronize(pica_ctx* ctx) {
+    if (!ctx) return PICA_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PICA_OK;
+}
+
+int pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const double* y, const double* z,
+                          const double* ux, const double* uy, const double* uz, const double* w,
+                          const int32_t* species) {
+    if (!ctx || n < 0 || (n > 0 && (!x || !y || !z || !ux || !uy || !uz || !w))) return fail(ctx, PICA_ERR_INVALID, "null array");
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "upload while a migration is pending");
+    CK(cudaStreamSynchronize(ctx->stream));
+    const pica_config& c = ctx->cfg;
+    const int nsp = c.nspecies;
+    double scInv[3], invh[3];
+    for (int d = 0; d < 3; d++) {
+        const double L = (double)c.n[d] * c.h[d];
+        scInv[d] = 1.0 / ((double)c.sc[d] * ((L - 0.0) / (double)c.n[d]));  // EnsembleSupercells.h:31-33
+        invh[d] = 1.0 / c.h[d];
+    }
+    // Route: key = species * nscTot + supercell; FP32 form also converts to cell + offset.
+    std::vector<int32_t> key(n);
+    std::vector<uint32_t> cell(ctx->fp64 ? 0 : n);
+    std::vector<float> off(ctx->fp64 ? 0 : 3 * n);
+    int bad = 0;
+    parallelFor(ctx->threads, n, [&](int64_t a, int64_t b) {
+        for (int64_t i = a; i < b; i++) {
+            const int q = species ? species[i] : 0;
+            if (q < 0 || q >= nsp) { bad = 1; key[i] = 0; continue; }
+            const double p[3] = {x[i], y[i], z[i]};
+            const double uu[4] = {ux[i], uy[i], uz[i], w[i]};
+            bool ok = true;
+            for (int d = 0; d < 3; d++) ok = ok && std::isfinite(p[d]) && p[d] >= 0.0 && p[d] < (double)c.n[d] * c.h[d];
+            for (double v : uu) ok = ok && std::isfinite(v);
+            if (!ok) { bad = 2; key[i] = 0; continue; }
+            int s3[3];
+            if (ctx->fp64) {
+                for (int d = 0; d < 3; d++) {
+                    s3[d] = (int)std::floor((p[d] - 0.0) * scInv[d]);
+                    s3[d] = std::min(std::max(s3[d], 0), ctx->nsc[d] - 1);
+                }
+            } else {
+                int cc[3];
+                for (int d = 0; d < 3; d++) {
+                    const double xi = p[d] * invh[d];
+                    const double fl = std::floor(xi);
+                    cc[d] = (int)fl;
+                    float o = (float)(xi - fl);
+                    if (o >= 1.0f) { o = 0.0f; cc[d] += 1; }
+                    cc[d] = wrapHost(cc[d], c.n[d]);
+                    off[3 * i + d] = o;
+                    s3[d] = cc[d] / c.sc[d];
+                }
+                cell[i] = packCell(cc[0], cc[1], cc[2]);
+            }
+            key[i] = q * ctx->nscTot + scLinear(ctx, s3[0], s3[1], s3[2]);
+        }
+    });
+    if (bad == 1) return fail(ctx, PICA_ERR_INVALID, "species index out of range");
+    if (bad == 2) return fail(ctx, PICA_ERR_INVALID, "non-finite value or position outside [0, n h)");
+    const int64_t nkeys = (int64_t)nsp * ctx->nscTot;
+    std::vector<int64_t> cnt(nkeys + 1, 0);
+    for (int64_t i = 0; i < n; i++) cnt[key[i] + 1]++;
+    // Per species layout.
+    for (int q = 0; q < nsp; q++) {
+        SpeciesState& S = ctx->sp[q];
+        std::vector<int32_t> counts(ctx->nscTot);
+        for (int s = 0; s < ctx->nscTot; s++) counts[s] = (int32_t)cnt[(int64_t)q * ctx->nscTot + s + 1];
+        int64_t total;
+        layoutFrom(ctx, counts, S.h_start, S.h_cap, total);
+        S.layoutSlots = total;
+        int rc;
+        if ((rc = ensureBuffer(ctx, q, 0, total)) || (rc = ensureBuffer(ctx, q, 1, total)) || (rc = ensureDir(ctx, q, total)))
+            return rc;
+        CK(cudaMemcpy(S.d_start, S.h_start.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.d_cap, S.h_cap.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.d_count, counts.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
+    }
+    // Slot of each particle: start of its supercell + rank within the key (stable).
+    std::vector<int64_t> fill(nkeys, 0);
+    std::vector<int64_t> slot(n);
+    for (int64_t i = 0; i < n; i++) {
+        const int32_t k = key[i];
+        const int q = k / ctx->nscTot, s = k % ctx->nscTot;
+        slot[i] = ctx->sp[q].h_start[s] + fill[k]++;
+    }
+    std::vector<int32_t> spOf(n);
+    for (int64_t i = 0; i < n; i++) spOf[i] = key[i] / ctx->nscTot;
+    ctx->cur = 0;
+    for (int q = 0; q < nsp; q++) {
+        SpeciesState& S = ctx->sp[q];
+        const int64_t total = S.layoutSlots;
+        for (int k = 0; k < ctx->ncomp; k++) {
+            std::vector<unsigned char> host(total * ctx->compBytes[k], 0);
+            parallelFor(ctx->threads, n, [&](int64_t a, int64_t b) {
+                for (int64_t i = a; i < b; i++) {
+                    if (spOf[i] != q) continue;
+                    const int64_t o = slot[i];
+                    if (ctx->fp64) {
+                        const double* src[7] = {x, y, z, ux, uy, uz, w};
+                        ((double*)host.data())[o] = src[k][i];
+                    } else if (k == 0) {
+                        ((uint32_t*)host.data())[o] = cell[i];
+                    } else if (k <= 3) {
+                        ((float*)host.data())[o] = off[3 * i + (k - 1)];
+                    } else {
+                        const double* src[4] = {ux, uy, uz, w};
+                        ((float*)host.data())[o] = (float)src[k - 4][i];
+                    }
+                }
+            });
+            CK(cudaMemcpy(S.buf[0][k], host.data(), total * ctx->compBytes[k], cudaMemcpyHostToDevice));
+        }
+    }
+    return PICA_OK;
+}
+
+int64_t pica_num_particles(pica_ctx* ctx) {
+    if (!ctx) return PICA_ERR_INVALID;
+    int64_t total = 0;
+    std::vector<int32_t> counts(ctx->nscTot);
+    for (int q = 0; q < ctx->cfg.nspecies; q++) {
+        if (cudaMemcpy(counts.data(), ctx->sp[q].d_count, ctx->nscTot * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return fail(ctx, PICA_ERR_CUDA, "count download failed");
+        for (int32_t v : counts) total += v;
+    }
+    return total;
+}
+
+int pica_get_counts(pica_ctx* ctx, int32_t* counts) {
+    if (!ctx || !counts) return PICA_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int q = 0; q < ctx->cfg.nspecies; q++)
+        CK(cudaMemcpy(counts + (size_t)q * ctx->nscTot, ctx->sp[q].d_count, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
+    return PICA_OK;
+}
+
+int pica_download_particles(pica_ctx* ctx, double* x, double* y, double* z, double* ux, double* uy, double* uz,
+                            double* w, int32_t* species, int32_t* supercell) {
+    if (!ctx) return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "download while a migration is pending");
+    CK(cudaStreamSynchronize(ctx->stream));
+    const pica_config& c = ctx->cfg;
+    double* out[7] = {x, y, z, ux, uy, uz, w};
+    int64_t o = 0;
+    for (int q = 0; q < c.nspecies; q++) {
+        SpeciesState& S = ctx->sp[q];
+        std::vector<int32_t> counts(ctx->nscTot);
+        CK(cudaMemcpy(counts.data(), S.d_count, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
+        const int64_t total = S.layoutSlots;
+        std::vector<std::vector<unsigned char>> host(ctx->ncomp);
+        for (int k = 0; k < ctx->ncomp; k++) {
+            host[k].resize(total * ctx->compBytes[k]);
+            CK(cudaMemcpy(host[k].data(), S.buf[ctx->cur][k], total * ctx->compBytes[k], cudaMemcpyDeviceToHost));
+        }
+        for (int s = 0; s < ctx->nscTot; s++) {
+            const int64_t st = S.h_start[s];
+            for (int i = 0; i < counts[s]; i++, o++) {
+                const int64_t slot = st + i;
+                if (ctx->fp64) {
+                    for (int k = 0; k < 7; k++)
+                        if (out[k]) out[k][o] = ((double*)host[k].data())[slot];
+                } else {
+                    int cx, cy, cz;
+                    unpackCell(((uint32_t*)host[0].data())[slot], cx, cy, cz);
+                    const float* f[7];
+                    for (int k = 0; k < 7; k++) f[k] = (const float*)host[k + 1].data();
+                    if (x) x[o] = ((double)cx + (double)f[0][slot]) * c.h[0];
+                    if (y) y[o] = ((double)cy + (double)f[1][slot]) * c.h[1];
+                    if (z) z[o] = ((double)cz + (double)f[2][slot]) * c.h[2];
+                    for (int k = 3; k < 7; k++)
+                        if (out[k]) out[k][o] = (double)f[k][slot];
+                }
+                if (species) species[o] = q;
+                if (supercell) supercell[o] = s;
+            }
+        }
+    }
+    return PICA_OK;
+}
+
+int pica_upload_fields(pica_ctx* ctx, const double* const* f9) {
+    if (!ctx || !f9) return PICA_ERR_INVALID;
+    const int64_t nodes = (int64_t)ctx->cfg.n[0] * ctx->cfg.n[1] * ctx->cfg.n[2];
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < 9; c++) {
+        if (!f9[c]) return fail(ctx, PICA_ERR_INVALID, "null field array");
+        if (ctx->fp64) CK(cudaMemcpy(ctx->f[c], f9[c], nodes * 8, cudaMemcpyHostToDevice));
+        else {
+            std::vector<float> tmp(nodes);
+            for (int64_t i = 0; i < nodes; i++) tmp[i] = (float)f9[c][i];
+            CK(cudaMemcpy(ctx->f[c], tmp.data(), nodes * 4, cudaMemcpyHostToDevice));
+        }
+    }
+    return PICA_OK;
+}
+
+int pica_download_fields(pica_ctx* ctx, double* const* f9) {
+    if (!ctx || !f9) return PICA_ERR_INVALID;
+    const int64_t nodes = (int64_t)ctx->cfg.n[0] * ctx->cfg.n[1] * ctx->cfg.n[2];
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < 9; c++) {
+        if (!f9[c]) continue;
+        if (ctx->fp64) CK(cudaMemcpy(f9[c], ctx->f[c], nodes * 8, cudaMemcpyDeviceToHost));
+        else {
+            std::vector<float> tmp(nodes);
+            CK(cudaMemcpy(tmp.data(), ctx->f[c], nodes * 4, cudaMemcpyDeviceToHost));
+            for (int64_t i = 0; i < nodes; i++) f9[c][i] = tmp[i];
+        }
+    }
+    return PICA_OK;
+}
+
+int pica_push_deposit(pica_ctx* ctx) {
+    if (!ctx) return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "push_deposit called twice without migrate");
+    const pica_config& c = ctx->cfg;
+    const int64_t nodes = (int64_t)c.n[0] * c.n[1] * c.n[2];
+    const size_t rb = ctx->fp64 ? 8 : 4;
+    for (int k = 6; k < 9; k++) CK(cudaMemsetAsync(ctx->f[k], 0, nodes * rb, ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_flags, 0, 4 * sizeof(int), ctx->stream));
+    auto fill = [&](auto& a) {
+        for (int d = 0; d < 3; d++) {
+            a.n[d] = c.n[d]; a.S[d] = c.sc[d]; a.nsc[d] = ctx->nsc[d]; a.T[d] = ctx->T[d];
+            a.h[d] = c.h[d]; a.invh[d] = 1.0 / c.h[d]; a.L[d] = (double)c.n[d] * c.h[d];
+            a.scInv[d] = 1.0 / ((double)c.sc[d] * ((a.L[d] - 0.0) / (double)c.n[d]));
+            a.cdth[d] = kC * c.dt / c.h[d];
+        }
+        a.dt = c.dt;
+        a.nspecies = c.nspecies;
+        for (int k = 0; k < 6; k++) a.eb[k] = ctx->f[k];
+        for (int k = 0; k < 3; k++) a.j[k] = ctx->f[6 + k];
+        a.norm = 1.0 / (c.h[0] * c.h[1] * c.h[2]);   // CurrentDepositorYeeGrid.h:203
+        a.flags = ctx->d_flags;
+        for (int q = 0; q < c.nspecies; q++) {
+            SpeciesState& S = ctx->sp[q];
+            auto& sa = a.sp[q];
+            sa.start = S.d_start; sa.cap = S.d_cap; sa.count = S.d_count;
+            sa.nstay = S.d_nstay; sa.nleave = S.d_nleave; sa.dir = S.dir;
+            sa.ec = c.charge[q] * c.dt / (2.0 * c.mass[q] * kC);   // BorisPusher.h:29
+            sa.q = c.charge[q];
+            for (int d = 0; d < 3; d++) sa.kq[d] = -c.charge[q] * (c.h[d] / c.dt);
+            sa.qc = c.charge[q] * kC;
+        }
+    };
+    if (ctx->fp64) {
+        PushArgs<PlainPtrs> a{};
+        fill(a);
+        for (int q = 0; q < c.nspecies; q++) { a.sp[q].in = plainPtrs(ctx, q, ctx->cur); a.sp[q].out = plainPtrs(ctx, q, 1 - ctx->cur); }
+        CKL(launchPushPlain(a, c.shape, c.deposit, ctx->stream));
+    } else {
+        PushArgs<CellPtrs> a{};
+        fill(a);
+        for (int q = 0; q < c.nspecies; q++) { a.sp[q].in = cellPtrs(ctx, q, ctx->cur); a.sp[q].out = cellPtrs(ctx, q, 1 - ctx->cur); }
+        CKL(launchPushCell(a, c.shape, c.deposit, ctx->stream));
+    }
+    ctx->launches++;
+    ctx->pending = true;
+    return PICA_OK;
+}
+
+int pica_update_b(pica_ctx* ctx, double dt) {
+    if (!ctx) return PICA_ERR_INVALID;
+    const pica_config& c = ctx->cfg;
+    double coeff[3];
+    for (int d = 0; d < 3; d++) coeff[d] = (kC * dt) / c.h[d];   // YeeSolver.h:181-182
+    CKL(launchUpdateB(ctx->fp64, ctx->f, c.n, coeff, ctx->stream));
+    ctx->launches++;
+    return PICA_OK;
+}
+
+int pica_update_e(pica_ctx* ctx, double dt) {
+    if (!ctx) return PICA_ERR_INVALID;
+    const pica_config& c = ctx->cfg;
+    double coeff[3];
+    for (int d = 0; d < 3; d++) coeff[d] = (kC * dt) / c.h[d];   // YeeSolver.h:137-138
+    const double cc = -4.0 * kPiRef * dt;                         // YeeSolver.h:135
+    CKL(launchUpdateE(ctx->fp64, ctx->f, c.n, cc, coeff, ctx->stream));
+    ctx->launches++;
+    return PICA_OK;
+}
+
+int pica_migrate(pica_ctx* ctx) {
+    if (!ctx) return PICA_ERR_INVALID;
+    if (!ctx->pending) return fail(ctx, PICA_ERR_STATE, "migrate without push_deposit");
+    const pica_config& c = ctx->cfg;
+    const int other = 1 - ctx->cur;
+    auto fill = [&](auto& a, bool rebuild) {
+        for (int d = 0; d < 3; d++) a.nsc[d] = ctx->nsc[d];
+        a.nspecies = c.nspecies;
+        a.flags = ctx->d_flags;
+        for (int q = 0; q < c.nspecies; q++) {
+            SpeciesState& S = ctx->sp[q];
+            auto& m = a.sp[q];
+            m.start = S.d_start; m.cap = S.d_cap; m.nstay = S.d_nstay; m.nleave = S.d_nleave; m.dir = S.dir;
+            m.count = S.d_count; m.needed = S.d_needed; m.newStart = rebuild ? S.d_start2 : nullptr;
+        }
+    };
+    auto launch = [&](bool rebuild) -> int {
+        if (ctx->fp64) {
+            MigrateArgs<PlainPtrs> a{};
+            fill(a, rebuild);
+            for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = plainPtrs(ctx, q, other); a.sp[q].dst = plainPtrs(ctx, q, ctx->cur); }
+            return launchMigratePlain(a, rebuild, ctx->stream);
+        }
+        MigrateArgs<CellPtrs> a{};
+        fill(a, rebuild);
+        for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = cellPtrs(ctx, q, other); a.sp[q].dst = cellPtrs(ctx, q, ctx->cur); }
+        return launchMigrateCell(a, rebuild, ctx->stream);
+    };
+    CKL(launch(false));
+    ctx->launches++;
+    CK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->pending = false;
+    if (ctx->h_flags[0]) return fail(ctx, ctx->h_flags[0], "a particle crossed more than one supercell in one step");
+    const bool rebalance = c.resort_every > 0 && (ctx->steps + 1) % c.resort_every == 0;
+    if (!ctx->h_flags[1] && !rebalance) {
+        ctx->cur = other;
+        return PICA_OK;
+    }
+    // Rebuild into buffer `cur` with capacities recomputed from stayers + arrivals.
+    for (int q = 0; q < c.nspecies; q++) {
+        SpeciesState& S = ctx->sp[q];
+        std::vector<int32_t> needed(ctx->nscTot);
+        CK(cudaMemcpy(needed.data(), S.d_needed, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
+        std::vector<int64_t> nstart;
+        std::vector<int32_t> ncap;
+        int64_t total;
+        layoutFrom(ctx, needed, nstart, ncap, total);
+        int rc;
+        if ((rc = ensureBuffer(ctx, q, ctx->cur, total))) return rc;
+        CK(cudaMemcpy(S.d_start2, nstart.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.d_cap2, ncap.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
+        S.h_start.swap(nstart);
+        S.h_cap.swap(ncap);
+        S.layoutSlots = total;
+    }
+    CKL(launch(true));
+    ctx->launches++;
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int q = 0; q < c.nspecies; q++) {
+        SpeciesState& S = ctx->sp[q];
+        std::swap(S.d_start, S.d_start2);
+        std::swap(S.d_cap, S.d_cap2);
+        int rc;
+        if ((rc = ensureBuffer(ctx, q, other, S.layoutSlots)) || (rc = ensureDir(ctx, q, S.layoutSlots))) return rc;
+    }
+    return PICA_OK;   // data stays in buffer `cur`
+}
+
+int pica_step(pica_ctx* ctx, int32_t nsteps) {
+    if (!ctx || nsteps < 0) return PICA_ERR_INVALID;
+    const double dt = ctx->cfg.dt;
+    for (int i = 0; i < nsteps; i++) {
+        int rc;
+        if ((rc = pica_push_deposit(ctx))) return rc;
+        if ((rc = pica_update_b(ctx, 0.5 * dt))) return rc;
+        if ((rc = pica_update_e(ctx, dt))) return rc;
+        if ((rc = pica_update_b(ctx, 0.5 * dt))) return rc;
+        if ((rc = pica_migrate(ctx))) return rc;
+        ctx->steps++;
+    }
+    return PICA_OK;
+}
+
+int pica_field_energy(pica_ctx* ctx, double* out) {
+    if (!ctx || !out) return PICA_ERR_INVALID;
+    const pica_config& c = ctx->cfg;
+    const int64_t nodes = (int64_t)c.n[0] * c.n[1] * c.n[2];
+    CKL(launchFieldEnergy(ctx->fp64, ctx->f, nodes, ctx->d_red, ctx->d_out, ctx->stream));
+    ctx->launches += 2;
+    CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *out = ctx->h_out[0] * (c.h[0] * c.h[1] * c.h[2]) / (8.0 * kPiRef);
+    return PICA_OK;
+}
+
+static int buildRho(pica_ctx* ctx) {
+    const pica_config& c = ctx->cfg;
+    const int64_t nodes = (int64_t)c.n[0] * c.n[1] * c.n[2];
+    if (!ctx->d_rho) CK(cudaMalloc(&ctx->d_rho, nodes * 8));
+    CK(cudaMemsetAsync(ctx->d_rho, 0, nodes * 8, ctx->stream));
+    RhoArgs r{};
+    r.fp64 = ctx->fp64; r.shape = c.shape; r.nspecies = c.nspecies; r.nscTot = ctx->nscTot;
+    for (int d = 0; d < 3; d++) { r.n[d] = c.n[d]; r.S[d] = c.sc[d]; r.nsc[d] = ctx->nsc[d]; r.invh[d] = 1.0 / c.h[d]; }
+    r.norm = 1.0 / (c.h[0] * c.h[1] * c.h[2]);
+    for (int q = 0; q < c.nspecies; q++) {
+        void* const* b = ctx->sp[q].buf[ctx->cur];
+        r.p0[q] = b[0]; r.p1[q] = b[1]; r.p2[q] = b[2]; r.p3[q] = ctx->fp64 ? nullptr : b[3];
+        r.w[q] = ctx->fp64 ? b[6] : b[7];
+        r.start[q] = ctx->sp[q].d_start; r.count[q] = ctx->sp[q].d_count; r.q[q] = c.charge[q];
+    }
+    CKL(launchRho(r, ctx->d_rho, ctx->stream));
+    ctx->launches++;
+    return PICA_OK;
+}
+
+int pica_charge_density(pica_ctx* ctx, double* rho) {
+    if (!ctx || !rho) return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "charge density while a migration is pending");
+    int rc = buildRho(ctx);
+    if (rc) return rc;
+    const int64_t nodes = (int64_t)ctx->cfg.n[0] * ctx->cfg.n[1] * ctx->cfg.n[2];
+    CK(cudaMemcpyAsync(rho, ctx->d_rho, nodes * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PICA_OK;
+}
+
+int pica_diagnostics(pica_ctx* ctx, double bg, pica_diag* out) {
+    if (!ctx || !out) return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "diagnostics while a migration is pending");
+    const pica_config& c = ctx->cfg;
+    std::memset(out, 0, sizeof(*out));
+    int rc = pica_field_energy(ctx, &out->field_energy);
+    if (rc) return rc;
+    ParticleSumArgs a{};
+    a.fp64 = ctx->fp64; a.nspecies = c.nspecies; a.nscTot = ctx->nscTot;
+    for (int q = 0; q < c.nspecies; q++) {
+        void* const* b = ctx->sp[q].buf[ctx->cur];
+        const int o = ctx->fp64 ? 3 : 4;
+        a.ux[q] = b[o]; a.uy[q] = b[o + 1]; a.uz[q] = b[o + 2]; a.w[q] = b[o + 3];
+        a.start[q] = ctx->sp[q].d_start; a.count[q] = ctx->sp[q].d_count;
+        a.mc2[q] = c.mass[q] * kC * kC; a.q[q] = c.charge[q];
+    }
+    CKL(launchParticleSums(a, ctx->d_red, ctx->d_out, ctx->stream));
+    ctx->launches += 2;
+    if ((rc = buildRho(ctx))) return rc;
+    CKL(launchGauss(ctx->fp64, ctx->f, ctx->d_rho, c.n, c.h, bg, ctx->d_red, ctx->d_out + 2, ctx->stream));
+    ctx->launches += 2;
+    CK(cudaMemcpyAsync(ctx->h_out, ctx->d_out, 4 * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    out->kinetic_energy = ctx->h_out[0];
+    out->total_charge = ctx->h_out[1];
+    out->gauss_max = ctx->h_out[2];
+    out->rho_max = ctx->h_out[3];
+    return PICA_OK;
+}
+
+int64_t pica_state_slots(pica_ctx* ctx, int32_t species) {
+    if (!ctx || species < 0 || species >= ctx->cfg.nspecies) return PICA_ERR_INVALID;
+    return ctx->sp[species].layoutSlots;
+}
+
+int pica_state_copy(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device) {
+    if (!ctx || !host || species < 0 || species >= ctx->cfg.nspecies || comp < 0 || comp >= ctx->ncomp)
+        return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "state copy while a migration is pending");
+    SpeciesState& S = ctx->sp[species];
+    const size_t bytes = S.layoutSlots * ctx->compBytes[comp];
+    if (to_device) CK(cudaMemcpyAsync(S.buf[ctx->cur][comp], host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    else CK(cudaMemcpyAsync(host, S.buf[ctx->cur][comp], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return PICA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host-side synthetic plasma.  Counter-based random numbers (SplitMix64 finaliser
+// of seed, cell, particle and draw index), so the result does not depend on the
+// thread count.  Positions uniform in the cell; u = drift + N(0, sigma) per
+// component (Box-Muller).
+// ---------------------------------------------------------------------------
+static inline uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static inline double uni(uint64_t seed, int64_t cell, int64_t p, int draw) {
+    const uint64_t key = ((uint64_t)cell << 24) ^ ((uint64_t)p << 4) ^ (uint64_t)draw;
+    return (double)(mix64(mix64(seed) ^ key) >> 11) * 0x1.0p-53;
+}
+static inline double normal(uint64_t seed, int64_t cell, int64_t p, int draw) {
+    const double u1 = 1.0 - uni(seed, cell, p, draw), u2 = uni(seed, cell, p, draw + 1);
+    return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2);
+}
+static inline int cellCount(const pica_plasma_spec* s, int i) {
+    const double f = 1.0 + s->density_mod * std::cos(2.0 * 3.14159265358979323846 * (i + 0.5) / s->n[0]);
+    return (int)std::lround(s->ppc * f);
+}
+
+int64_t pica_plasma_count(const pica_plasma_spec* s) {
+    if (!s || s->n[0] <= 0 || s->n[1] <= 0 || s->n[2] <= 0 || s->ppc < 0) return PICA_ERR_INVALID;
+    int64_t total = 0;
+    for (int i = 0; i < s->n[0]; i++) total += (int64_t)cellCount(s, i) * s->n[1] * s->n[2];
+    return total;
+}
+
+int pica_plasma_generate(const pica_plasma_spec* s, int32_t threads, double* x, double* y, double* z, double* ux,
+                         double* uy, double* uz, double* w, int32_t* species) {
+    if (pica_plasma_count(s) < 0 || !x || !y || !z || !ux || !uy || !uz || !w) return PICA_ERR_INVALID;
+    const int nx = s->n[0], ny = s->n[1], nz = s->n[2];
+    std::vector<int64_t> planeStart(nx + 1, 0);
+    for (int i = 0; i < nx; i++) planeStart[i + 1] = planeStart[i] + (int64_t)cellCount(s, i) * ny * nz;
+    const int nthreads = threads > 0 ? threads : std::max(1u, std::thread::hardware_concurrency());
+    auto work = [&](int i0, int i1) {
+        for (int i = i0; i < i1; i++) {
+            const int per = cellCount(s, i);
+            int64_t o = planeStart[i];
+            for (int j = 0; j < ny; j++)
+                for (int k = 0; k < nz; k++) {
+                    const int64_t cell = ((int64_t)i * ny + j) * nz + k;
+                    for (int p = 0; p < per; p++, o++) {
+                        x[o] = ((double)i + uni(s->seed, cell, p, 0)) * s->h[0];
+                        y[o] = ((double)j + uni(s->seed, cell, p, 1)) * s->h[1];
+                        z[o] = ((double)k + uni(s->seed, cell, p, 2)) * s->h[2];
+                        double u3[3] = {s->sigma_u * normal(s->seed, cell, p, 3), s->sigma_u * normal(s->seed, cell, p, 5),
+                                        s->sigma_u * normal(s->seed, cell, p, 7)};
+                        if (s->nbeams == 2) u3[s->drift_axis] += (p % 2 == 0) ? s->drift_u : -s->drift_u;
+                        else u3[s->drift_axis] += s->drift_u;
+                        ux[o] = u3[0]; uy[o] = u3[1]; uz[o] = u3[2];
+                        w[o] = s->weight;
+                        if (species) species[o] = s->species;
+                    }
+                }
+        }
+    };
+    std::vector<std::thread> th;
+    const int chunk = (nx + nthreads - 1) / nthreads;
+    for (int t = 0; t < nthreads; t++) {
+        const int a = t * chunk, b = std::min(nx, a + chunk);
+        if (a >= b) break;
+        th.emplace_back(work, a, b);
+    }
+    for (auto& t : th) t.join();
+    return PICA_OK;
+}
+
+}  // extern "C"

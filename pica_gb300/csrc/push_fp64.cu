@@ -1,0 +1,37 @@
+// FP64 plain form: push and migration kernels.  Compiled with --fmad=false so
+// every double expression rounds as pica's C++ does (no contraction).
+#include "push_kernels.cuh"
+
+namespace pgb {
+
+namespace {
+template <int SHAPE, int DEP>
+int launchOne(const PushArgs<PlainPtrs>& a, cudaStream_t s) {
+    const int TT = a.T[0] * a.T[1] * a.T[2];
+    const size_t smem = (size_t)9 * TT * sizeof(double);
+    auto k = k_push<true, SHAPE, DEP>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
+    k<<<nscTot, kPushThreads, smem, s>>>(a);
+    return (int)cudaGetLastError();
+}
+}  // namespace
+
+int launchPushPlain(const PushArgs<PlainPtrs>& a, int shape, int dep, cudaStream_t s) {
+    if (shape == PICA_SHAPE_CIC && dep == PICA_DEPOSIT_DIRECT) return launchOne<PICA_SHAPE_CIC, PICA_DEPOSIT_DIRECT>(a, s);
+    if (shape == PICA_SHAPE_CIC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchOne<PICA_SHAPE_CIC, PICA_DEPOSIT_ESIRKEPOV>(a, s);
+    if (shape == PICA_SHAPE_TSC && dep == PICA_DEPOSIT_DIRECT) return launchOne<PICA_SHAPE_TSC, PICA_DEPOSIT_DIRECT>(a, s);
+    if (shape == PICA_SHAPE_TSC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchOne<PICA_SHAPE_TSC, PICA_DEPOSIT_ESIRKEPOV>(a, s);
+    return -1;
+}
+
+int launchMigratePlain(const MigrateArgs<PlainPtrs>& a, bool rebuild, cudaStream_t s) {
+    const int64_t nscTot = (int64_t)a.nsc[0] * a.nsc[1] * a.nsc[2];
+    const int blocks = (int)((nscTot * 32 + 255) / 256);
+    if (rebuild) k_migrate<PlainPtrs, true><<<blocks, 256, 0, s>>>(a);
+    else k_migrate<PlainPtrs, false><<<blocks, 256, 0, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace pgb

@@ -1,0 +1,73 @@
+"""CPU checks of the C ABI library: it builds, loads, exports every declared
+symbol, and its host-only routines (plasma generation) behave.  No device work."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+import pica_gb300
+from pica_gb300 import _lib, workloads
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+
+
+def declared_functions():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fn)).read()
+            names |= set(re.findall(r"\b(pica_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    declared = declared_functions()
+    assert len(declared) >= 25
+    for name in declared:
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, name
+    assert lib.pica_abi_version() == 1
+    assert lib.pica_status_string(-5).decode().startswith("particle crossed")
+
+
+def test_config_struct_layout_matches_header():
+    # pica_config: 3 int32 + 3 int32 + 3 double + double + 4 int32 + 4 double + 4 double + double + 2 int32
+    assert C.sizeof(_lib.PicaConfig) == 4 * 6 + 8 * 4 + 4 * 4 + 8 * 8 + 8 + 4 * 2
+    assert C.sizeof(_lib.PicaDiag) == 8 * 8
+
+
+def test_plasma_generation_is_thread_count_independent():
+    spec = pica_gb300.plasma_spec((6, 5, 4), (1e-3, 1e-3, 1e-3), 9, 0.05, 2.0, seed=7)
+    a = pica_gb300.generate_plasma(spec, threads=1)
+    b = pica_gb300.generate_plasma(spec, threads=5)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert len(a["x"]) == 6 * 5 * 4 * 9
+    # positions in their cell, cell-major order
+    cell = (np.floor(a["x"] / 1e-3).astype(int) * 5 + np.floor(a["y"] / 1e-3).astype(int)) * 4 + np.floor(a["z"] / 1e-3).astype(int)
+    assert np.all(np.diff(cell) >= 0)
+    assert abs(np.std(np.concatenate([a["ux"], a["uy"], a["uz"]])) - 0.05) < 0.01
+
+
+def test_density_modulation_and_beams():
+    spec = pica_gb300.plasma_spec((16, 2, 2), (1.0, 1.0, 1.0), 100, 0.01, 1.0, seed=3, density_mod=0.9, nbeams=2,
+                                  drift_u=0.2, drift_axis=0)
+    p = pica_gb300.generate_plasma(spec)
+    per_plane = np.bincount(np.floor(p["x"]).astype(int), minlength=16) // 4
+    expected = np.round(100 * (1 + 0.9 * np.cos(2 * np.pi * (np.arange(16) + 0.5) / 16))).astype(int)
+    assert np.array_equal(per_plane, expected)
+    assert per_plane.min() >= 10 and per_plane.max() <= 190
+    assert abs(np.mean(np.abs(p["ux"])) - 0.2) < 0.01
+
+
+def test_workload_sizes():
+    c2 = workloads.config2()
+    n = c2["sim"]["n"]
+    assert n == (128, 128, 128) and c2["specs"][0].ppc == 100
+    assert int(np.prod(n)) * 100 == 209715200
+    members = workloads.batched_members()
+    assert len(members) == 64
+    edges = [m["sim"]["n"][0] for m in members]
+    assert min(edges) >= 32 and max(edges) <= 96 and all(e % 4 == 0 for e in edges)

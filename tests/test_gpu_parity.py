@@ -1,0 +1,228 @@
+"""GPU parity tests: the CUDA library (through the C ABI) against the golden
+fixtures made by pica's own headers and against the oracle restatement.
+
+Tolerances (written per test): FP64 plain form within 1e-12 relative (the only
+difference is the order of the J sums: shared-memory and global atomics);
+integer results (per-supercell counts, migration order, supercell of every
+particle) exactly equal.  FP32 form against the FP32 oracle: 1e-4 on
+particle momenta and fields (FMA contraction and atomic order differ)."""
+import numpy as np
+import pytest
+
+import pica_gb300 as pg
+from oracle import pic_oracle as po
+from tests.helpers import load_golden, particle_args, periodic_err, rel_err, species_of, thermal_inputs
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+
+
+def gpu_sim(n, sc, h, dt, **kw):
+    return pg.Simulation(n, h, dt, supercell=sc, **kw)
+
+
+def compare_particles(pg_, po_, L, tol_x, tol_u):
+    assert np.array_equal(pg_["supercell"], po_["supercell"])
+    assert np.array_equal(pg_["species"], po_["species"])
+    for d, k in enumerate(("x", "y", "z")):
+        assert periodic_err(pg_[k], po_[k], L[d]) < tol_x, k
+    for k in ("ux", "uy", "uz"):
+        assert rel_err(pg_[k], po_[k]) < tol_u, k
+    assert np.array_equal(pg_["w"], po_["w"]) or rel_err(pg_["w"], po_["w"]) < 1e-7
+
+
+@pytest.mark.parametrize("name", ["cic_direct_8cube", "cic_direct_2species"])
+def test_fp64_matches_reference_golden(name):
+    g = load_golden(name)
+    n, sc, h = tuple(g["n"]), tuple(g["sc"]), tuple(g["h"])
+    s = gpu_sim(n, sc, h, float(g["dt"]), species=species_of(g))
+    s.upload_particles(g["in_x"], g["in_y"], g["in_z"], g["in_ux"], g["in_uy"], g["in_uz"], g["in_w"], g["in_species"])
+    s.upload_fields(list(g["in_fields"]))
+    for st in range(int(g["steps"])):
+        s.step(1)
+        assert np.array_equal(s.counts(), g["counts"][st]), st
+    p = s.particles()
+    ref = {k: g["out_" + k] for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species", "supercell")}
+    L = [n[d] * h[d] for d in range(3)]
+    compare_particles(p, ref, L, FP64_TOL, FP64_TOL)
+    f = s.fields()
+    for c in range(9):
+        assert rel_err(f[c], g["out_fields"][c]) < FP64_TOL, c
+
+
+def run_pair(n, sc, d, steps, form, shape, deposit, species=(pg.ELECTRON,), fields=None, slack=0.15):
+    s = gpu_sim(n, sc, d["h"], d["dt"], form=form, shape=shape, deposit=deposit, species=species, slack=slack)
+    o = po.Oracle(n, sc, d["h"], d["dt"], form=form, shape=shape, deposit=deposit, species=species)
+    s.upload_particles(*particle_args(d))
+    o.load(*particle_args(d))
+    f9 = fields if fields is not None else [np.zeros(n)] * 9
+    s.upload_fields(f9)
+    o.set_fields(f9)
+    for _ in range(steps):
+        s.step(1)
+        o.step(1)
+        assert np.array_equal(s.counts(), o.counts())
+    return s, o
+
+
+@pytest.mark.parametrize("shape,deposit", [(pg.SHAPE_CIC, pg.DEPOSIT_DIRECT), (pg.SHAPE_CIC, pg.DEPOSIT_ESIRKEPOV),
+                                           (pg.SHAPE_TSC, pg.DEPOSIT_DIRECT), (pg.SHAPE_TSC, pg.DEPOSIT_ESIRKEPOV)])
+def test_fp64_forms_match_oracle(shape, deposit):
+    n, sc = (12, 8, 16), (4, 2, 4)
+    d = thermal_inputs(n, 5, seed=21, u_sigma=0.1, hscale=(1.0, 1.2, 0.8), nspecies=2)
+    rng = np.random.default_rng(2)
+    fields = [2e3 * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3
+    species = (pg.ELECTRON, (pg.ELECTRON_MASS * 100.0, -pg.ELECTRON_CHARGE))
+    s, o = run_pair(n, sc, d, 6, pg.FORM_FP64_PLAIN, shape, deposit, species=species, fields=fields)
+    L = [n[k] * d["h"][k] for k in range(3)]
+    compare_particles(s.particles(), o.particles(), L, FP64_TOL, FP64_TOL)
+    fs, fo = s.fields(), o.get_fields()
+    for c in range(9):
+        assert rel_err(fs[c], fo[c]) < FP64_TOL, c
+
+
+def test_fp64_thermal_32cube_100_steps():
+    """The plain FP64 32^3 x 50 ppc electron plasma (CIC, Boris, direct, supercell 2^3) for 100 steps."""
+    from pica_gb300 import workloads
+    wl = workloads.config1()
+    p = pg.generate_plasma(wl["specs"][0])
+    sim = wl["sim"]
+    s = pg.Simulation(**sim)
+    o = po.Oracle(sim["n"], sim["supercell"], sim["h"], sim["dt"])
+    args = [p[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w")] + [p["species"]]
+    s.upload_particles(*args)
+    o.load(*args)
+    zeros = [np.zeros(sim["n"])] * 9
+    s.upload_fields(zeros)
+    o.set_fields(zeros)
+    for chunk in range(10):
+        s.step(10)
+        o.step(10)
+        assert np.array_equal(s.counts(), o.counts()), chunk
+    L = [sim["n"][k] * sim["h"][k] for k in range(3)]
+    compare_particles(s.particles(), o.particles(), L, FP64_TOL, FP64_TOL)
+    fs, fo = s.fields(), o.get_fields()
+    for c in range(9):
+        assert rel_err(fs[c], fo[c]) < FP64_TOL, c
+
+
+@pytest.mark.parametrize("shape,deposit", [(pg.SHAPE_CIC, pg.DEPOSIT_DIRECT), (pg.SHAPE_CIC, pg.DEPOSIT_ESIRKEPOV),
+                                           (pg.SHAPE_TSC, pg.DEPOSIT_DIRECT), (pg.SHAPE_TSC, pg.DEPOSIT_ESIRKEPOV)])
+def test_fp32_cell_form_matches_oracle(shape, deposit):
+    n, sc = (16, 8, 8), (4, 4, 2)
+    d = thermal_inputs(n, 6, seed=31, u_sigma=0.1)
+    s, o = run_pair(n, sc, d, 5, pg.FORM_FP32_CELL, shape, deposit)
+    ps, pr = s.particles(), o.particles()
+    L = [n[k] * d["h"][k] for k in range(3)]
+    assert np.array_equal(ps["supercell"], pr["supercell"])
+    for k, key in enumerate(("x", "y", "z")):
+        assert periodic_err(ps[key], pr[key], L[k]) < 1e-6
+    for key in ("ux", "uy", "uz"):
+        assert rel_err(ps[key], pr[key]) < 1e-4
+    fs, fo = s.fields(), o.get_fields()
+    for c in range(9):
+        assert rel_err(fs[c], fo[c]) < 1e-4, c
+
+
+def test_fp64_yee_update_bit_exact():
+    """With no particles the step is YeeSolver only: bit-exact against the oracle."""
+    n = (8, 12, 6)
+    d = thermal_inputs(n, 1, seed=1)
+    rng = np.random.default_rng(4)
+    f9 = [rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3
+    s = gpu_sim(n, (2, 2, 2), d["h"], d["dt"])
+    o = po.Oracle(n, (2, 2, 2), d["h"], d["dt"])
+    s.upload_fields(f9)
+    o.set_fields(f9)
+    s.step(3)
+    o.step(3)
+    fs, fo = s.fields(), o.get_fields()
+    for c in range(9):
+        assert np.array_equal(fs[c], fo[c]), c
+
+
+def test_migration_overflow_rebuild_keeps_order():
+    """A cold beam concentrates particles into a supercell with no spare room: the
+    in-place append overflows, the layout is rebuilt, and the order stays canonical."""
+    n, sc = (16, 4, 4), (2, 2, 2)
+    d = thermal_inputs(n, 2, seed=41, u_sigma=1e-4)
+    # Pack 120 particles near the +x face of supercell x=0 moving +x fast: supercell x=1 gets all.
+    h = d["h"]
+    m = 120
+    rng = np.random.default_rng(5)
+    x = np.concatenate([d["x"], (1.97 + 0.02 * rng.random(m)) * h[0]])
+    y = np.concatenate([d["y"], 0.5 * h[1] + 0 * rng.random(m)])
+    z = np.concatenate([d["z"], 0.5 * h[2] + rng.random(m) * h[2]])
+    ux = np.concatenate([d["ux"], np.full(m, 3.0)])
+    uy = np.concatenate([d["uy"], np.zeros(m)])
+    uz = np.concatenate([d["uz"], np.zeros(m)])
+    w = np.concatenate([d["w"], np.full(m, d["w"][0])])
+    sp = np.zeros(len(x), np.int32)
+    dd = dict(h=h, dt=d["dt"], x=x, y=y, z=z, ux=ux, uy=uy, uz=uz, w=w, species=sp)
+    s, o = run_pair(n, sc, dd, 4, pg.FORM_FP64_PLAIN, pg.SHAPE_CIC, pg.DEPOSIT_DIRECT, slack=1e-9)
+    L = [n[k] * h[k] for k in range(3)]
+    compare_particles(s.particles(), o.particles(), L, FP64_TOL, FP64_TOL)
+
+
+def test_resort_cadence_rebalances_without_changing_results():
+    n, sc = (8, 8, 8), (2, 2, 2)
+    d = thermal_inputs(n, 4, seed=12, u_sigma=0.2)
+    out = []
+    for every in (0, 2):
+        s = gpu_sim(n, sc, d["h"], d["dt"], form=pg.FORM_FP32_CELL, deposit=pg.DEPOSIT_ESIRKEPOV, resort_every=every)
+        s.upload_particles(*particle_args(d))
+        s.upload_fields([np.zeros(n)] * 9)
+        s.step(5)
+        out.append((s.particles(), s.counts()))
+    assert np.array_equal(out[0][1], out[1][1])
+    for k in ("x", "ux", "supercell"):
+        assert np.array_equal(out[0][0][k], out[1][0][k]), k
+
+
+def test_diagnostics_match_oracle():
+    n, sc = (8, 8, 8), (4, 4, 4)
+    d = thermal_inputs(n, 6, seed=7)
+    for form in (pg.FORM_FP64_PLAIN, pg.FORM_FP32_CELL):
+        s, o = run_pair(n, sc, d, 3, form, pg.SHAPE_TSC, pg.DEPOSIT_ESIRKEPOV)
+        bg = 4.80320427e-10 * 1e18
+        ds, do = s.diagnostics(bg), o.diagnostics(bg)
+        tol = 1e-12 if form == pg.FORM_FP64_PLAIN else 1e-4
+        for k in ("field_energy", "kinetic_energy", "total_charge", "gauss_max", "rho_max"):
+            assert abs(ds[k] - do[k]) <= tol * abs(do[k]), (form, k, ds[k], do[k])
+        assert rel_err(s.charge_density(), o.charge_density()) < tol
+
+
+def test_upload_download_roundtrip_and_order():
+    n, sc = (8, 8, 8), (2, 4, 2)
+    d = thermal_inputs(n, 3, seed=17, nspecies=2)
+    s = gpu_sim(n, sc, d["h"], d["dt"], species=(pg.ELECTRON, pg.ELECTRON))
+    o = po.Oracle(n, sc, d["h"], d["dt"], species=(pg.ELECTRON, pg.ELECTRON))
+    s.upload_particles(*particle_args(d))
+    o.load(*particle_args(d))
+    p, q = s.particles(), o.particles()
+    for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species", "supercell"):
+        assert np.array_equal(p[k], q[k]), k
+    assert np.array_equal(s.counts(), o.counts())
+
+
+def test_error_paths_do_not_fault():
+    n = (8, 8, 8)
+    d = thermal_inputs(n, 2, seed=3)
+    s = gpu_sim(n, (2, 2, 2), d["h"], d["dt"])
+    s.upload_particles(*particle_args(d))
+    s.push_deposit()
+    with pytest.raises(pg.PicaError) as e:
+        s.push_deposit()
+    assert e.value.status == -6
+    s.migrate()
+    # A time step far above the Courant limit moves a relativistic particle across
+    # more than one supercell: reported as an error, no device fault.
+    s2 = gpu_sim(n, (1, 1, 1), d["h"], 40 * d["h"][0] / 2.9979e10)
+    s2.upload_particles([0.5 * d["h"][0]], [0.5 * d["h"][1]], [0.5 * d["h"][2]], [50.0], [0.0], [0.0], [1.0])
+    with pytest.raises(pg.PicaError) as e:
+        s2.step(1)
+    assert e.value.status == -5
+    # The context stays usable.
+    s.step(2)
+    assert s.num_particles() == len(d["x"])

@@ -1,0 +1,170 @@
+"""CPU tests of the oracle: pinned to pica's own headers and to the golden
+fixtures, plus known answers for the parts pica does not have (TSC,
+Esirkepov charge conservation, Boris gyration, E x B drift)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pic_oracle as po
+from tests.helpers import C, E, ME, load_golden, rel_err, species_of, thermal_inputs
+
+REFERENCE_AVAILABLE = os.path.isdir("/root/reference/include/pica") or os.path.exists(po.REF_SO)
+
+
+def run_fixture(kind, g):
+    o = po.Oracle(tuple(g["n"]), tuple(g["sc"]), tuple(g["h"]), float(g["dt"]), species=species_of(g), kind=kind)
+    o.load(g["in_x"], g["in_y"], g["in_z"], g["in_ux"], g["in_uy"], g["in_uz"], g["in_w"], g["in_species"])
+    o.set_fields(list(g["in_fields"]))
+    counts, migs = [], []
+    for s in range(int(g["steps"])):
+        o.step(1)
+        counts.append(o.counts())
+        m = o.migrations()
+        migs.append(np.concatenate([np.full((len(m), 1), s, np.int32), m], axis=1))
+    return o, np.stack(counts), np.concatenate(migs)
+
+
+@pytest.mark.parametrize("name", ["cic_direct_8cube", "cic_direct_2species"])
+def test_port_reproduces_golden_bit_exactly(name):
+    g = load_golden(name)
+    o, counts, migs = run_fixture("port", g)
+    p = o.particles()
+    for k in ("x", "y", "z", "ux", "uy", "uz", "w"):
+        assert np.array_equal(p[k], g["out_" + k]), k
+    assert np.array_equal(p["supercell"], g["out_supercell"])
+    assert np.array_equal(p["species"], g["out_species"])
+    f = o.get_fields()
+    for c in range(9):
+        assert np.array_equal(f[c], g["out_fields"][c]), c
+    assert np.array_equal(counts, g["counts"])
+    assert np.array_equal(migs, g["migrations"])
+
+
+@pytest.mark.skipif(not REFERENCE_AVAILABLE, reason="pica sources not mounted here")
+@pytest.mark.parametrize("n,sc,ppc,steps", [((8, 8, 8), (2, 2, 2), 6, 3),
+                                            ((64, 4, 4), (2, 2, 2), 2, 3),   # supercell origin m=62: trunc(m h / h) = 61
+                                            ((12, 8, 6), (3, 4, 2), 4, 3)])
+def test_port_matches_reference_headers(n, sc, ppc, steps):
+    po.build(reference=True)
+    d = thermal_inputs(n, ppc, seed=11, u_sigma=0.1)
+    res = []
+    for kind in ("port", "reference"):
+        o = po.Oracle(n, sc, d["h"], d["dt"], kind=kind)
+        o.load(d["x"], d["y"], d["z"], d["ux"], d["uy"], d["uz"], d["w"])
+        rng = np.random.default_rng(3)
+        o.set_fields([1e3 * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3)
+        o.step(steps)
+        res.append((o.particles(), o.get_fields(), o.counts(), o.migrations()))
+    (pa, fa, ca, ma), (pb, fb, cb, mb) = res
+    for k in ("x", "y", "z", "ux", "uy", "uz", "w"):
+        assert np.array_equal(pa[k], pb[k]), k
+    for c in range(9):
+        assert np.array_equal(fa[c], fb[c]), c
+    assert np.array_equal(ca, cb) and np.array_equal(ma, mb)
+
+
+def div_faces(jx, jy, jz, h):
+    return ((np.roll(jx, -1, 0) - jx) / h[0] + (np.roll(jy, -1, 1) - jy) / h[1] + (np.roll(jz, -1, 2) - jz) / h[2])
+
+
+@pytest.mark.parametrize("form,tol", [(po.FORM_FP64_PLAIN, 1e-12), (po.FORM_FP32_CELL, 2e-6)])
+@pytest.mark.parametrize("shape", [po.SHAPE_CIC, po.SHAPE_TSC])
+def test_esirkepov_continuity(form, tol, shape):
+    """(rho^{n+1} - rho^n)/dt + div J^{n+1/2} = 0 on the cell-centred lattice."""
+    n = (8, 8, 8)
+    d = thermal_inputs(n, 6, seed=5, u_sigma=0.2)
+    o = po.Oracle(n, (4, 4, 4), d["h"], d["dt"], form=form, shape=shape, deposit=po.DEPOSIT_ESIRKEPOV)
+    o.load(d["x"], d["y"], d["z"], d["ux"], d["uy"], d["uz"], d["w"])
+    rng = np.random.default_rng(9)
+    o.set_fields([5e3 * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3)
+    for _ in range(3):
+        r0 = o.charge_density()
+        o.step(1)
+        r1 = o.charge_density()
+        f = o.get_fields()
+        res = (r1 - r0) / d["dt"] + div_faces(f[6], f[7], f[8], d["h"])
+        scale = np.max(np.abs(r0)) / d["dt"]
+        assert np.max(np.abs(res)) / scale < tol
+
+
+def single_particle(u0, e, b, steps, form=po.FORM_FP64_PLAIN, n=(8, 8, 8)):
+    """One particle of negligible weight in uniform fields (self-fields ~1e-30 of the applied ones)."""
+    h0 = 1e-3
+    dt = 0.5 * h0 / (C * np.sqrt(3))
+    o = po.Oracle(n, (4, 4, 4), (h0, h0, h0), dt, form=form, deposit=po.DEPOSIT_ESIRKEPOV, shape=po.SHAPE_TSC)
+    x0 = 4.3 * h0
+    o.load([x0], [x0], [x0], [u0[0]], [u0[1]], [u0[2]], [1e-30])
+    o.set_fields([np.full(n, e[0]), np.full(n, e[1]), np.full(n, e[2]), np.full(n, b[0]), np.full(n, b[1]),
+                  np.full(n, b[2])] + [np.zeros(n)] * 3)
+    traj = []
+    for _ in range(steps):
+        o.step(1)
+        p = o.particles()
+        traj.append([p[k][0] for k in ("x", "y", "z", "ux", "uy", "uz")])
+    return np.array(traj), dt, h0
+
+
+def test_boris_gyration_known_answer():
+    """Uniform B: |u| is conserved and the phase advances by 2 atan(|t|) per step (BorisPusher.h:33-43)."""
+    b = 3.0e4
+    u0 = np.array([0.1, 0.0, 0.0])
+    traj, dt, _ = single_particle(u0, (0, 0, 0), (0, 0, b), 40)
+    u = traj[:, 3:]
+    assert np.max(np.abs(np.linalg.norm(u, axis=1) - 0.1)) < 1e-14
+    gamma = np.sqrt(1 + 0.01)
+    t = (E * dt / (2 * ME * C)) * b / gamma
+    phase = np.unwrap(np.arctan2(u[:, 1], u[:, 0]))
+    expected = -2 * np.arctan(t) * np.arange(1, 41)   # rotation sense of the Boris map for t along z
+    assert np.max(np.abs(phase - expected)) < 1e-12
+
+
+def test_exb_drift():
+    """E x B drift c E x B / B^2 of a non-relativistic electron, averaged over whole gyro-periods."""
+    b = 1.0e5
+    e_y = 1.0e2   # v_d = c E/B = 3e7 cm/s << c
+    traj, dt, _ = single_particle(np.zeros(3), (0, e_y, 0), (0, 0, b), 2000, n=(64, 64, 8))
+    omega = abs(E) * b / (ME * C)
+    period = int(round(2 * np.pi / omega / dt))
+    k = (len(traj) // period) * period
+    vx = np.diff(np.unwrap(traj[:k + 1, 0], period=64 * 1e-3)) / dt
+    vd = C * e_y / b
+    assert abs(np.mean(vx[:k]) - vd) / vd < 2e-3
+
+
+@pytest.mark.parametrize("shape", [po.SHAPE_CIC, po.SHAPE_TSC])
+def test_fp32_form_tracks_fp64(shape):
+    """The FP32 cell form follows the FP64 form within single-precision error over a few steps."""
+    n = (8, 8, 8)
+    d = thermal_inputs(n, 4, seed=8)
+    out = []
+    for form in (po.FORM_FP64_PLAIN, po.FORM_FP32_CELL):
+        o = po.Oracle(n, (4, 4, 4), d["h"], d["dt"], form=form, shape=shape, deposit=po.DEPOSIT_ESIRKEPOV)
+        o.load(d["x"], d["y"], d["z"], d["ux"], d["uy"], d["uz"], d["w"])
+        o.set_fields([np.zeros(n)] * 9)
+        o.step(5)
+        out.append((o.particles(), o.get_fields(), o.counts()))
+    (p64, f64, c64), (p32, f32, c32) = out
+    assert np.array_equal(c64, c32)
+    assert rel_err(p32["ux"], p64["ux"]) < 1e-4
+    for c in range(9):
+        assert rel_err(f32[c], f64[c]) < 1e-3
+
+
+def test_diagnostics_conservation():
+    """Total charge is exact; field + kinetic energy of a thermal plasma drifts little over 20 steps."""
+    n = (8, 8, 8)
+    d = thermal_inputs(n, 8, seed=4)
+    o = po.Oracle(n, (4, 4, 4), d["h"], d["dt"], shape=po.SHAPE_TSC, deposit=po.DEPOSIT_ESIRKEPOV)
+    o.load(d["x"], d["y"], d["z"], d["ux"], d["uy"], d["uz"], d["w"])
+    o.set_fields([np.zeros(n)] * 9)
+    bg = -E * 1e18
+    d0 = o.diagnostics(bg)
+    o.step(20)
+    d1 = o.diagnostics(bg)
+    assert d1["total_charge"] == pytest.approx(d0["total_charge"], rel=1e-14)
+    e0 = d0["field_energy"] + d0["kinetic_energy"]
+    e1 = d1["field_energy"] + d1["kinetic_energy"]
+    assert abs(e1 - e0) / e0 < 2e-2
+    # Esirkepov keeps div E - 4 pi rho at its initial value.
+    assert abs(d1["gauss_max"] - d0["gauss_max"]) / d0["gauss_max"] < 0.5
