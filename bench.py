@@ -1,0 +1,357 @@
+#!/usr/bin/env python
+"""Throughput of pica's particle-in-cell step on GB300.
+
+Workload (default): the FP32 precision form of the thermal electron plasma,
+128^3 cells x 100 electrons/cell (2.1e8 particles), TSC form factor,
+Esirkepov deposition, supercell 4^3, seeded synthetic input generated on the
+host.  One "step" = gather + Boris push + Esirkepov deposit of every particle,
+the Yee update (B half step, E step, B half step) and supercell migration.
+
+Printed (rank 0, one JSON line): particle-steps/s with device-resident state
+(`value`), the same through the C ABI with the particle state copied from and
+to pinned host memory every step (`e2e`), the push kernel against the HBM
+roofline, the FP64 plain form of the same workload, and the oracle
+restatement timed on this machine's host cores (`cpu_baseline`).
+
+`--impl reference` times the CPU implementation of the same step instead
+(the oracle restatement built from this tree, all host cores).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300, FP32 vs FP64 form at stated error; % HBM peak"
+UNIT = "particle-steps/s"
+BYTES_PER_PARTICLE_FP32 = 60   # cell 4 + offsets 12 + u 12, read and written, + weight read
+BYTES_PER_PARTICLE_FP64 = 104  # x 24 + u 24, read and written, + weight read
+PUSH_GRID_BYTES_PER_CELL_FP32 = 36  # E/B gather 6 words + J write 3 words, FP32
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--edge", type=int, default=128, help="grid edge (cells); 128 is the reference workload")
+    return ap.parse_args()
+
+
+def measured_hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic_per_particle():
+    """DRAM bytes per particle of the push kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "push_fp32_tsc_esirkepov.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_particle:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        time.sleep(0.2)
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(edge, form):
+    import pica_gb300 as pg
+    from pica_gb300 import workloads
+
+    wl = workloads.thermal(n=(edge, edge, edge), ppc=100, supercell=(4, 4, 4), form=form, shape=pg.SHAPE_TSC,
+                           deposit=pg.DEPOSIT_ESIRKEPOV, steps=1000)
+    return wl
+
+
+def cpu_sample(args, steps=None, seconds=None):
+    """Oracle restatement of the same step on a 32^3-cell block of the workload (same ppc,
+    supercell, form factor and deposition), all host cores.  Returns (value, cores, sample)."""
+    import pica_gb300 as pg
+    from oracle import pic_oracle as po
+
+    from pica_gb300 import workloads
+
+    edge = 32
+    wl = make_workload(edge, pg.FORM_FP32_CELL)
+    p = pg.generate_plasma(wl["specs"][0])
+    sim = wl["sim"]
+    cores = os.cpu_count() or 1
+    o = po.Oracle(sim["n"], sim["supercell"], sim["h"], sim["dt"], form=po.FORM_FP32_CELL, shape=po.SHAPE_TSC,
+                  deposit=po.DEPOSIT_ESIRKEPOV, threads=cores)
+    o.load(p["x"], p["y"], p["z"], p["ux"], p["uy"], p["uz"], p["w"], p["species"])
+    o.set_fields([np.zeros(sim["n"])] * 9)
+    npart = len(p["x"])
+    t = time.perf_counter()
+    o.step(1)
+    t1 = time.perf_counter() - t
+    if steps is None:
+        steps = int(max(1, min(50, math.ceil((seconds or 12.0) / max(t1, 1e-3)))))
+    t = time.perf_counter()
+    o.step(steps)
+    el = time.perf_counter() - t
+    del workloads
+    sample = (f"{edge}^3 cells x 100 ppc ({npart} electrons), TSC, Esirkepov, supercell 4^3, FP32 cell form, "
+              f"{steps} steps, oracle restatement (pica has no TSC/Esirkepov), OpenMP {cores} threads")
+    return npart * steps / el, cores, sample, el
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    # warm-up steps then exactly K timed steps of the CPU step on the bounded sample
+    import pica_gb300 as pg  # noqa: F401  (host-side plasma generator only)
+    value, cores, sample, el = cpu_sample(args, steps=args.steps + args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / (args.steps + args.warmup),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": f"thermal electron plasma {args.edge}^3 x 100 ppc, TSC, Esirkepov, supercell 4^3 "
+                               f"(CPU step on a 32^3 block of it)", "parallelism": "OpenMP over supercells"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    import pica_gb300 as pg
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---------------- FP32 form, device-resident ----------------
+    wl = make_workload(args.edge, pg.FORM_FP32_CELL)
+    spec = wl["specs"][0]
+    spec.seed = spec.seed + rank          # independent replica per rank (weak scaling)
+    parts = pg.generate_plasma(spec)
+    npart = len(parts["x"])
+    ncells = int(np.prod(wl["sim"]["n"]))
+    sim = pg.Simulation(**wl["sim"])
+    stream = torch.cuda.current_stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.upload_particles(*[parts[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w")], parts["species"])
+    sim.upload_fields([np.zeros(wl["sim"]["n"])] * 9)
+    dt = wl["sim"]["dt"]
+
+    def one_step(ev0=None, ev1=None):
+        if ev0 is not None:
+            ev0.record(stream)
+        sim.push_deposit()
+        if ev1 is not None:
+            ev1.record(stream)
+        sim.update_b(0.5 * dt)
+        sim.update_e(dt)
+        sim.update_b(0.5 * dt)
+        sim.migrate()
+
+    for _ in range(args.warmup):
+        one_step()
+    barrier()
+    K = args.steps
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = sim.launch_count()
+    with ClockSampler(local) as clk:
+        barrier()
+        t_start.record(stream)
+        for k in range(K):
+            one_step(*evs[k])
+        t_end.record(stream)
+        barrier()
+    launches = sim.launch_count() - launches0
+    elapsed = t_start.elapsed_time(t_end) / 1e3
+    push_ms = [a.elapsed_time(b) for a, b in evs]
+    if dist is not None:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * npart * K / elapsed
+    push_avg = float(np.mean(push_ms)) / 1e3
+    peak, peak_kind = measured_hbm_peak()
+    alg_bytes = BYTES_PER_PARTICLE_FP32 * npart + PUSH_GRID_BYTES_PER_CELL_FP32 * ncells
+    achieved = alg_bytes / push_avg / 1e9
+    tpp = profiled_traffic_per_particle()
+    roofline = {"bound": "hbm", "kernel": "k_push<fp32, TSC, Esirkepov>", "achieved": achieved, "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None if tpp is None else tpp * npart,
+                "algorithmic_bytes_per_launch": alg_bytes, "push_ms": 1e3 * push_avg,
+                "step_fraction_in_push": push_avg * K / elapsed}
+    step_alg = BYTES_PER_PARTICLE_FP32 * npart + 120 * ncells
+    clocks = clk.summary()
+
+    # ---------------- e2e through the C ABI with host buffers ----------------
+    e2e = None
+    if rank == 0 or True:
+        comps = 8
+        slots = sim.state_slots(0)
+        host = [torch.empty(slots * 4, dtype=torch.uint8, pin_memory=True) for _ in range(comps)]
+        for c in range(comps):
+            sim.state_copy(0, c, host[c].data_ptr(), False)
+        torch.cuda.synchronize()
+        h2d = d2h = 0
+        te0, te1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        w0 = time.perf_counter()
+        te0.record(stream)
+        for _ in range(args.e2e_steps):
+            if sim.state_slots(0) != slots:
+                break
+            for c in range(comps):
+                sim.state_copy(0, c, host[c].data_ptr(), True)
+            h2d += slots * 4 * comps
+            one_step()
+            if sim.state_slots(0) != slots:
+                break
+            for c in range(comps):
+                sim.state_copy(0, c, host[c].data_ptr(), False)
+            d2h += slots * 4 * comps
+        te1.record(stream)
+        barrier()
+        wall = time.perf_counter() - w0
+        e_el = te0.elapsed_time(te1) / 1e3
+        e2e = {"value": world * npart * args.e2e_steps / max(e_el, wall), "unit": UNIT,
+               "h2d_bytes_per_step": h2d // max(1, args.e2e_steps), "d2h_bytes_per_step": d2h // max(1, args.e2e_steps),
+               "steps": args.e2e_steps, "path": "pica_state_copy (pinned host) -> pica_push_deposit/update_b/update_e/"
+                                                 "update_b/migrate -> pica_state_copy"}
+        del host
+    sim.close()
+    del sim
+    torch.cuda.synchronize()
+
+    # ---------------- FP64 plain form of the same workload ----------------
+    fp64 = None
+    if args.fp64_steps > 0:
+        wl64 = make_workload(args.edge, pg.FORM_FP64_PLAIN)
+        s64 = pg.Simulation(**wl64["sim"])
+        s64.set_stream(stream.cuda_stream)
+        s64.upload_particles(*[parts[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w")], parts["species"])
+        s64.upload_fields([np.zeros(wl64["sim"]["n"])] * 9)
+        s64.step(1)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        s64.step(args.fp64_steps)
+        b.record(stream)
+        torch.cuda.synchronize()
+        el64 = a.elapsed_time(b) / 1e3
+        fp64 = {"value": npart * args.fp64_steps / el64, "ms_per_step": 1e3 * el64 / args.fp64_steps,
+                "steps": args.fp64_steps, "dtype": "fp64", "form": "FP64 plain (absolute positions)"}
+        s64.close()
+
+    if rank != 0:
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, cores, sample, _ = cpu_sample(args, seconds=args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": 1e3 * elapsed / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": f"thermal electron plasma {args.edge}^3 cells x 100 ppc ({npart} electrons per GPU), "
+                               "FP32 cell+offset form, TSC, Esirkepov, supercell 4^3, Boris, periodic",
+                   "particles_per_gpu": npart, "cells": ncells, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (particle state %.1f GB)" % (npart * 32 / 1e9)},
+        "roofline": roofline,
+        "step_hbm_frac": step_alg / (elapsed / K) / 1e9 / peak,
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+        "fp64_form": fp64, "fp32_over_fp64": (value / world / fp64["value"]) if fp64 else None,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,248 @@
+// pica_gb300.hpp -- header-only C++ mirror of pica's hot-path classes over the
+// pica_gb300 C ABI (pica_gb300.h).
+//
+// pica's host loop constructs a YeeGrid, an EnsembleSupercells of
+// ParticleArraySoA<Particle3d>, a BorisPusher, and per supercell a
+// FieldInterpolatorCICSupercell and a CurrentDepositorCICSupercell, then calls
+// get / push / deposit per particle and YeeSolver::updateB/updateE per step.
+// Here the same names stand for device-resident objects and each operator
+// acts on every particle at once:
+//
+//   pica:                                            pica_gb300:
+//   YeeGrid<Three,double> grid(origin, step, size)   Simulation sim(config); auto& grid = sim.grid();
+//   grid.ex(i,j,k) = v                               grid.ex(i,j,k) = v; ...; grid.upload();
+//   EnsembleSupercells<PA> ens(min, max, N, S)        auto& ens = sim.ensemble();
+//   ens.add(particle)                                 ens.add(particle); ...; ens.upload();
+//   BorisPusher<Particle3d,double> pusher(dt)         (dt and ParticleTypes are in the config)
+//   for each supercell, particle: fi.get; pusher.push;  pushSupercells(sim);      // one call
+//     cd.deposit; ~cd                                 ens.migrate();
+//   YeeSolver().updateB(grid, dt)                      YeeSolver().updateB(grid, dt);
+//
+// Errors: every call that fails throws pica_gb300::Error (status + message);
+// the C ABI itself never throws.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "pica_gb300.h"
+
+namespace pica_gb300 {
+
+struct FP3 {
+    double x = 0, y = 0, z = 0;
+    FP3() = default;
+    FP3(double a, double b, double c) : x(a), y(b), z(c) {}
+};
+struct Int3 {
+    int x = 0, y = 0, z = 0;
+    Int3() = default;
+    Int3(int a, int b, int c) : x(a), y(b), z(c) {}
+};
+
+// Constants of pica math/Constants.h:10-14 (CGS, pi truncated as in pica).
+namespace constants {
+const double pi = 3.14159265358;
+const double c = 29979245800.0;
+const double electronCharge = -4.80320427e-10;
+const double electronMass = 9.10938215e-28;
+}  // namespace constants
+
+// One entry of pica's ParticleTypes table (particles/Particle.h:21-31).
+struct ParticleType {
+    double mass, charge;
+};
+
+// Particle<Three> with normalised momentum p = u/(m c) (particles/Particle.h:34-112).
+struct Particle3d {
+    FP3 position, p;
+    double factor = 1.0;
+    short typeIndex = 0;
+};
+
+class Error : public std::runtime_error {
+public:
+    Error(int status, const std::string& msg) : std::runtime_error(msg), status(status) {}
+    int status;
+};
+
+enum class Form { FP64Plain = PICA_FORM_FP64_PLAIN, FP32Cell = PICA_FORM_FP32_CELL };
+enum class Shape { CIC = PICA_SHAPE_CIC, TSC = PICA_SHAPE_TSC };
+enum class Depositor { Direct = PICA_DEPOSIT_DIRECT, Esirkepov = PICA_DEPOSIT_ESIRKEPOV };
+
+struct Config {
+    Int3 numCells{32, 32, 32};
+    Int3 numCellsPerSupercell{2, 2, 2};
+    FP3 step{1, 1, 1};
+    double dt = 1;
+    Form form = Form::FP64Plain;
+    Shape shape = Shape::CIC;
+    Depositor depositor = Depositor::Direct;
+    std::vector<ParticleType> types{{constants::electronMass, constants::electronCharge}};
+    double slack = 0.15;
+    int resortEvery = 0;
+};
+
+class Simulation;
+class YeeSolver;
+
+// Host mirror of the device grid: pica's YeeGrid accessors on host arrays,
+// moved to / from the device with upload() / download().
+class YeeGrid {
+public:
+    double& ex(int i, int j, int k) { return f_[0][idx(i, j, k)]; }
+    double& ey(int i, int j, int k) { return f_[1][idx(i, j, k)]; }
+    double& ez(int i, int j, int k) { return f_[2][idx(i, j, k)]; }
+    double& bx(int i, int j, int k) { return f_[3][idx(i, j, k)]; }
+    double& by(int i, int j, int k) { return f_[4][idx(i, j, k)]; }
+    double& bz(int i, int j, int k) { return f_[5][idx(i, j, k)]; }
+    double& jx(int i, int j, int k) { return f_[6][idx(i, j, k)]; }
+    double& jy(int i, int j, int k) { return f_[7][idx(i, j, k)]; }
+    double& jz(int i, int j, int k) { return f_[8][idx(i, j, k)]; }
+    Int3 getSize() const { return n_; }
+    FP3 getStep() const { return h_; }
+    FP3 getOrigin() const { return FP3(0, 0, 0); }
+    inline void upload();
+    inline void download();
+
+private:
+    friend class Simulation;
+    friend class YeeSolver;
+    size_t idx(int i, int j, int k) const { return ((size_t)i * n_.y + j) * n_.z + k; }
+    pica_ctx* ctx_ = nullptr;
+    Int3 n_;
+    FP3 h_;
+    std::array<std::vector<double>, 9> f_;
+};
+
+// Host staging of the device ensemble: add() collects particles, upload()
+// routes them to supercells (EnsembleSupercells::add, EnsembleSupercells.h:41-45).
+class EnsembleSupercells {
+public:
+    void add(const Particle3d& p) {
+        x_.push_back(p.position.x); y_.push_back(p.position.y); z_.push_back(p.position.z);
+        ux_.push_back(p.p.x); uy_.push_back(p.p.y); uz_.push_back(p.p.z);
+        w_.push_back(p.factor); t_.push_back(p.typeIndex);
+    }
+    inline void upload();
+    // All particles in ensemble order (type, supercell, slot).
+    inline std::vector<Particle3d> particles() const;
+    inline std::vector<int32_t> counts() const;
+    Int3 getNumSupercells() const { return nsc_; }
+    Int3 getNumCellsPerSupercell() const { return S_; }
+    inline void migrate();
+
+private:
+    friend class Simulation;
+    pica_ctx* ctx_ = nullptr;
+    int ntypes_ = 1;
+    Int3 nsc_, S_;
+    std::vector<double> x_, y_, z_, ux_, uy_, uz_, w_;
+    std::vector<int32_t> t_;
+};
+
+inline void check(pica_ctx* ctx, int rc) {
+    if (rc != PICA_OK) throw Error(rc, std::string(pica_status_string(rc)) + ": " + (ctx ? pica_last_error(ctx) : ""));
+}
+
+class Simulation {
+public:
+    explicit Simulation(const Config& c) {
+        pica_config cfg{};
+        cfg.n[0] = c.numCells.x; cfg.n[1] = c.numCells.y; cfg.n[2] = c.numCells.z;
+        cfg.sc[0] = c.numCellsPerSupercell.x; cfg.sc[1] = c.numCellsPerSupercell.y; cfg.sc[2] = c.numCellsPerSupercell.z;
+        cfg.h[0] = c.step.x; cfg.h[1] = c.step.y; cfg.h[2] = c.step.z;
+        cfg.dt = c.dt;
+        cfg.form = (int32_t)c.form; cfg.shape = (int32_t)c.shape; cfg.deposit = (int32_t)c.depositor;
+        cfg.nspecies = (int32_t)c.types.size();
+        for (size_t i = 0; i < c.types.size() && i < 4; i++) { cfg.mass[i] = c.types[i].mass; cfg.charge[i] = c.types[i].charge; }
+        cfg.slack = c.slack;
+        cfg.resort_every = c.resortEvery;
+        check(nullptr, pica_ctx_create(&cfg, &ctx_));
+        dt_ = c.dt;
+        grid_.ctx_ = ctx_; grid_.n_ = c.numCells; grid_.h_ = c.step;
+        const size_t nodes = (size_t)c.numCells.x * c.numCells.y * c.numCells.z;
+        for (auto& a : grid_.f_) a.assign(nodes, 0.0);
+        ens_.ctx_ = ctx_; ens_.ntypes_ = cfg.nspecies; ens_.S_ = c.numCellsPerSupercell;
+        ens_.nsc_ = Int3(c.numCells.x / c.numCellsPerSupercell.x, c.numCells.y / c.numCellsPerSupercell.y,
+                         c.numCells.z / c.numCellsPerSupercell.z);
+    }
+    ~Simulation() { if (ctx_) pica_ctx_destroy(ctx_); }
+    Simulation(const Simulation&) = delete;
+    Simulation& operator=(const Simulation&) = delete;
+
+    YeeGrid& grid() { return grid_; }
+    EnsembleSupercells& ensemble() { return ens_; }
+    pica_ctx* handle() { return ctx_; }
+    double dt() const { return dt_; }
+    void setStream(void* cudaStream) { check(ctx_, pica_set_stream(ctx_, cudaStream)); }
+    // One full step: push + deposit, B(dt/2), E(dt), B(dt/2), migrate.
+    void step(int n = 1) { check(ctx_, pica_step(ctx_, n)); }
+    pica_diag diagnostics(double bgDensity = 0.0) {
+        pica_diag d{};
+        check(ctx_, pica_diagnostics(ctx_, bgDensity, &d));
+        return d;
+    }
+
+private:
+    pica_ctx* ctx_ = nullptr;
+    double dt_ = 0;
+    YeeGrid grid_;
+    EnsembleSupercells ens_;
+};
+
+void YeeGrid::upload() {
+    const double* p[9];
+    for (int c = 0; c < 9; c++) p[c] = f_[c].data();
+    check(ctx_, pica_upload_fields(ctx_, p));
+}
+void YeeGrid::download() {
+    double* p[9];
+    for (int c = 0; c < 9; c++) p[c] = f_[c].data();
+    check(ctx_, pica_download_fields(ctx_, p));
+}
+
+void EnsembleSupercells::upload() {
+    check(ctx_, pica_upload_particles(ctx_, (int64_t)w_.size(), x_.data(), y_.data(), z_.data(), ux_.data(),
+                                      uy_.data(), uz_.data(), w_.data(), t_.data()));
+    x_.clear(); y_.clear(); z_.clear(); ux_.clear(); uy_.clear(); uz_.clear(); w_.clear(); t_.clear();
+}
+std::vector<Particle3d> EnsembleSupercells::particles() const {
+    const int64_t n = pica_num_particles(ctx_);
+    if (n < 0) check(ctx_, (int)n);
+    std::vector<double> a[7];
+    for (auto& v : a) v.resize(n);
+    std::vector<int32_t> t(n), s(n);
+    check(ctx_, pica_download_particles(ctx_, a[0].data(), a[1].data(), a[2].data(), a[3].data(), a[4].data(),
+                                        a[5].data(), a[6].data(), t.data(), s.data()));
+    std::vector<Particle3d> out(n);
+    for (int64_t i = 0; i < n; i++) {
+        out[i].position = FP3(a[0][i], a[1][i], a[2][i]);
+        out[i].p = FP3(a[3][i], a[4][i], a[5][i]);
+        out[i].factor = a[6][i];
+        out[i].typeIndex = (short)t[i];
+    }
+    return out;
+}
+std::vector<int32_t> EnsembleSupercells::counts() const {
+    std::vector<int32_t> c((size_t)ntypes_ * nsc_.x * nsc_.y * nsc_.z);
+    check(ctx_, pica_get_counts(ctx_, c.data()));
+    return c;
+}
+void EnsembleSupercells::migrate() { check(ctx_, pica_migrate(ctx_)); }
+
+// pica YeeSolver (fieldSolver/YeeSolver.h:11-38) on the periodic device grid.
+class YeeSolver {
+public:
+    void updateE(YeeGrid& g, double dt) { check(g.ctx_, pica_update_e(g.ctx_, dt)); }
+    void updateB(YeeGrid& g, double dt) { check(g.ctx_, pica_update_b(g.ctx_, dt)); }
+};
+
+// FieldInterpolator::get + BorisPusher::push + CurrentDepositor::deposit for
+// every particle of every supercell (the supercell loop of a pica host loop).
+inline void pushSupercells(Simulation& sim) { check(sim.handle(), pica_push_deposit(sim.handle())); }
+
+}  // namespace pica_gb300

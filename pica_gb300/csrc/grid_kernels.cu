@@ -68,6 +68,19 @@ __global__ void __launch_bounds__(256) k_updateE(R* __restrict__ ex, R* __restri
     }
 }
 
+// J = Jacc * scale (one rounding from the exact integer sum), and clear Jacc for the next deposit.
+template <typename R>
+__global__ void __launch_bounds__(256) k_convertJ(R* __restrict__ jx, R* __restrict__ jy, R* __restrict__ jz,
+                                                  unsigned long long* __restrict__ ax, unsigned long long* __restrict__ ay,
+                                                  unsigned long long* __restrict__ az, int64_t n, double scale) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        jx[i] = (R)((double)(long long)ax[i] * scale);
+        jy[i] = (R)((double)(long long)ay[i] * scale);
+        jz[i] = (R)((double)(long long)az[i] * scale);
+        ax[i] = 0ull; ay[i] = 0ull; az[i] = 0ull;
+    }
+}
+
 // Fixed-order block reduction (sum or max) of one double per thread.
 template <bool MAX>
 __device__ __forceinline__ double blockReduce(double v, double* sh) {
@@ -219,6 +232,17 @@ inline int gridFor(int64_t n) {
 }
 
 }  // namespace
+
+int launchConvertJ(bool fp64, void* const* j, unsigned long long* const* a, int64_t nodes, double scale,
+                   cudaStream_t s) {
+    if (fp64)
+        k_convertJ<double><<<gridFor(nodes), 256, 0, s>>>((double*)j[0], (double*)j[1], (double*)j[2], a[0], a[1], a[2],
+                                                          nodes, scale);
+    else
+        k_convertJ<float><<<gridFor(nodes), 256, 0, s>>>((float*)j[0], (float*)j[1], (float*)j[2], a[0], a[1], a[2],
+                                                         nodes, scale);
+    return (int)cudaGetLastError();
+}
 
 int launchUpdateB(bool fp64, void* const* f, const int* n, const double* c, cudaStream_t s) {
     const int64_t total = (int64_t)n[0] * n[1] * n[2];

@@ -58,6 +58,9 @@ struct pica_ctx {
     double* d_out = nullptr;
     double* h_out = nullptr;
     double* d_rho = nullptr;
+    unsigned long long* jacc[3] = {};
+    double kmax = 1.0;      // power of two bounding |q w| max(c, h/dt) (sets the J fixed-point unit)
+    int jfrac = 40;         // fraction bits of the J fixed point (see pica_internal.h)
     std::string err;
     int64_t launches = 0;
     int64_t steps = 0;
@@ -106,6 +109,21 @@ void layoutFrom(const pica_ctx* c, const std::vector<int32_t>& counts, std::vect
         cap[s] = capacityFor(c, counts[s]);
         total += cap[s];
     }
+}
+
+// Fraction bits of the J fixed point for the current layout: a node can receive one
+// contribution per particle of every supercell whose tile covers it.
+void updateJFrac(pica_ctx* ctx) {
+    int64_t maxCaps = 0;
+    for (int q = 0; q < ctx->cfg.nspecies; q++) {
+        int32_t m = 0;
+        for (int32_t v : ctx->sp[q].h_cap) m = std::max(m, v);
+        maxCaps += m;
+    }
+    int64_t cover = 1;
+    for (int d = 0; d < 3; d++) cover *= (ctx->cfg.sc[d] + 2 * kG + 1 + ctx->cfg.sc[d] - 1) / ctx->cfg.sc[d];
+    const double worst = (double)cover * (double)std::max<int64_t>(maxCaps, 1) + 1.0;
+    ctx->jfrac = std::min(kJFracBitsMax, 62 - (int)std::ceil(std::log2(worst)));
 }
 
 int ensureBuffer(pica_ctx* ctx, int spi, int b, int64_t slots) {
@@ -211,6 +229,10 @@ int pica_ctx_create(const pica_config* cfg, pica_ctx** out) {
         if (cudaMalloc(&ctx->f[c], nodes * rb) != cudaSuccess) return bail(PICA_ERR_OOM);
         if (cudaMemset(ctx->f[c], 0, nodes * rb) != cudaSuccess) return bail(PICA_ERR_CUDA);
     }
+    for (int c = 0; c < 3; c++) {
+        if (cudaMalloc(&ctx->jacc[c], nodes * 8) != cudaSuccess) return bail(PICA_ERR_OOM);
+        if (cudaMemset(ctx->jacc[c], 0, nodes * 8) != cudaSuccess) return bail(PICA_ERR_CUDA);
+    }
     for (int s = 0; s < cfg->nspecies; s++) {
         SpeciesState& S = ctx->sp[s];
         const size_t n = ctx->nscTot;
@@ -242,6 +264,7 @@ int pica_ctx_destroy(pica_ctx* ctx) {
     if (!ctx) return PICA_ERR_INVALID;
     cudaDeviceSynchronize();
     for (auto p : ctx->f) if (p) cudaFree(p);
+    for (auto p : ctx->jacc) if (p) cudaFree(p);
     for (auto& S : ctx->sp) {
         for (auto& b : S.buf) for (auto p : b) if (p) cudaFree(p);
         for (void* p : {(void*)S.dir, (void*)S.d_start, (void*)S.d_cap, (void*)S.d_count, (void*)S.d_nstay,
@@ -324,6 +347,16 @@ int pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const doubl
     });
     if (bad == 1) return fail(ctx, PICA_ERR_INVALID, "species index out of range");
     if (bad == 2) return fail(ctx, PICA_ERR_INVALID, "non-finite value or position outside [0, n h)");
+    // Fixed-point unit of the J accumulators: kmax = 2^ceil(log2 max |q w| max(c, h/dt)).
+    {
+        double hmax = std::max(std::max(c.h[0], c.h[1]), c.h[2]);
+        double vmax = std::max(kC, hmax / c.dt), bound = 0.0;
+        for (int64_t i = 0; i < n; i++) {
+            const int q = species ? species[i] : 0;
+            bound = std::max(bound, std::fabs(c.charge[q] * w[i]) * vmax);
+        }
+        ctx->kmax = bound > 0 ? std::ldexp(1.0, (int)std::ceil(std::log2(bound))) : 1.0;
+    }
     const int64_t nkeys = (int64_t)nsp * ctx->nscTot;
     std::vector<int64_t> cnt(nkeys + 1, 0);
     for (int64_t i = 0; i < n; i++) cnt[key[i] + 1]++;
@@ -342,6 +375,7 @@ int pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const doubl
         CK(cudaMemcpy(S.d_cap, S.h_cap.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S.d_count, counts.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
     }
+    updateJFrac(ctx);
     // Slot of each particle: start of its supercell + rank within the key (stable).
     std::vector<int64_t> fill(nkeys, 0);
     std::vector<int64_t> slot(n);
@@ -482,9 +516,9 @@ int pica_push_deposit(pica_ctx* ctx) {
     if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "push_deposit called twice without migrate");
     const pica_config& c = ctx->cfg;
     const int64_t nodes = (int64_t)c.n[0] * c.n[1] * c.n[2];
-    const size_t rb = ctx->fp64 ? 8 : 4;
-    for (int k = 6; k < 9; k++) CK(cudaMemsetAsync(ctx->f[k], 0, nodes * rb, ctx->stream));
     CK(cudaMemsetAsync(ctx->d_flags, 0, 4 * sizeof(int), ctx->stream));
+    if (ctx->fp64)
+        for (int k = 6; k < 9; k++) CK(cudaMemsetAsync(ctx->f[k], 0, nodes * 8, ctx->stream));
     auto fill = [&](auto& a) {
         for (int d = 0; d < 3; d++) {
             a.n[d] = c.n[d]; a.S[d] = c.sc[d]; a.nsc[d] = ctx->nsc[d]; a.T[d] = ctx->T[d];
@@ -495,7 +529,8 @@ int pica_push_deposit(pica_ctx* ctx) {
         a.dt = c.dt;
         a.nspecies = c.nspecies;
         for (int k = 0; k < 6; k++) a.eb[k] = ctx->f[k];
-        for (int k = 0; k < 3; k++) a.j[k] = ctx->f[6 + k];
+        for (int k = 0; k < 3; k++) { a.jacc[k] = ctx->jacc[k]; a.j[k] = ctx->f[6 + k]; }
+        a.invUnit = std::ldexp(1.0, ctx->jfrac) / ctx->kmax;
         a.norm = 1.0 / (c.h[0] * c.h[1] * c.h[2]);   // CurrentDepositorYeeGrid.h:203
         a.flags = ctx->d_flags;
         for (int q = 0; q < c.nspecies; q++) {
@@ -521,6 +556,12 @@ int pica_push_deposit(pica_ctx* ctx) {
         CKL(launchPushCell(a, c.shape, c.deposit, ctx->stream));
     }
     ctx->launches++;
+    if (!ctx->fp64) {
+        // J = sum / h^3 (CurrentDepositorYeeGrid.h:203), from the exact fixed-point sums.
+        const double scale = (ctx->kmax * std::ldexp(1.0, -ctx->jfrac)) * (1.0 / (c.h[0] * c.h[1] * c.h[2]));
+        CKL(launchConvertJ(false, ctx->f + 6, ctx->jacc, nodes, scale, ctx->stream));
+        ctx->launches++;
+    }
     ctx->pending = true;
     return PICA_OK;
 }
@@ -579,8 +620,9 @@ int pica_migrate(pica_ctx* ctx) {
     CK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->pending = false;
+    ctx->steps++;
     if (ctx->h_flags[0]) return fail(ctx, ctx->h_flags[0], "a particle crossed more than one supercell in one step");
-    const bool rebalance = c.resort_every > 0 && (ctx->steps + 1) % c.resort_every == 0;
+    const bool rebalance = c.resort_every > 0 && ctx->steps % c.resort_every == 0;
     if (!ctx->h_flags[1] && !rebalance) {
         ctx->cur = other;
         return PICA_OK;
@@ -602,6 +644,7 @@ int pica_migrate(pica_ctx* ctx) {
         S.h_cap.swap(ncap);
         S.layoutSlots = total;
     }
+    updateJFrac(ctx);
     CKL(launch(true));
     ctx->launches++;
     CK(cudaStreamSynchronize(ctx->stream));
@@ -625,7 +668,6 @@ int pica_step(pica_ctx* ctx, int32_t nsteps) {
         if ((rc = pica_update_e(ctx, dt))) return rc;
         if ((rc = pica_update_b(ctx, 0.5 * dt))) return rc;
         if ((rc = pica_migrate(ctx))) return rc;
-        ctx->steps++;
     }
     return PICA_OK;
 }

@@ -26,6 +26,14 @@ constexpr int kMaxSpecies = 4;
 constexpr int kG = 2;      // tile guard: a supercell tile starts at node m - 2
 constexpr int kMaxS = 8;   // largest supported supercell edge (tile edge S + 5)
 constexpr int kPushThreads = 256;
+// FP32 form: current is accumulated in 64-bit two's-complement fixed point: one unit =
+// kmax * 2^-F, where kmax (a power of two) bounds |q w| max(c, h/dt) over the
+// particles, so every contribution is at most 2^F units.  F (at most 48) is
+// chosen from the layout so that the largest number of contributions one node
+// can receive in a step (all particles of the supercells whose tiles cover
+// it) times 2^F stays below 2^62.  Integer sums are exact and independent of
+// the order of the atomic adds, so the deposit is deterministic.
+constexpr int kJFracBitsMax = 48;
 
 // Packed FP32-form cell index: x (11 bits) | y (11 bits) | z (10 bits).
 __host__ __device__ inline uint32_t packCell(int x, int y, int z) {
@@ -65,8 +73,10 @@ struct PushArgs {
     double h[3], invh[3], L[3], scInv[3], dt;
     double cdth[3];     // c dt / h (FP32 form position update in cell units)
     const void* eb[6];  // ex ey ez bx by bz (Real)
-    void* j[3];         // jx jy jz (Real)
-    double norm;        // 1 / (hx hy hz)
+    unsigned long long* jacc[3];  // FP32 form: J accumulators, fixed point (unit kmax * 2^-F)
+    double invUnit;     // FP32 form: 2^F / kmax, current contribution -> fixed-point units
+    void* j[3];         // FP64 form: jx jy jz (double), summed with FP64 atomics
+    double norm;        // FP64 form: 1 / (hx hy hz)
     int* flags;         // flags[0]: error code (0 = ok)
     SpeciesArgs<P> sp[kMaxSpecies];
 };
@@ -100,6 +110,9 @@ int launchMigratePlain(const MigrateArgs<PlainPtrs>& a, bool rebuild, cudaStream
 int launchMigrateCell(const MigrateArgs<CellPtrs>& a, bool rebuild, cudaStream_t s);
 
 // Grid launchers (grid_kernels.cu).  `fp64` selects double vs float arrays.
+// J = Jacc * scale (Real), then Jacc = 0.
+int launchConvertJ(bool fp64, void* const* j, unsigned long long* const* jacc, int64_t nodes, double scale,
+                   cudaStream_t s);
 int launchUpdateB(bool fp64, void* const* f, const int* n, const double* coeff, cudaStream_t s);
 int launchUpdateE(bool fp64, void* const* f, const int* n, double cc, const double* coeff, cudaStream_t s);
 // Field energy: sum over nodes of sum_c f_c^2 (FP64) into *out (device); partial: scratch of

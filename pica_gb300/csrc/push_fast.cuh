@@ -1,0 +1,446 @@
+// FP32 cell-form push kernel specialised for charge-conserving (Esirkepov)
+// deposition, built around the supercell's particles being stored in cell
+// order (they are generated that way and kept so by the periodic in-supercell
+// sort):
+//
+//  * A warp owns a contiguous segment of 32*K particles of its supercell; lane
+//    l handles the K consecutive particles lK .. lK+K-1, so a lane rarely
+//    changes cell and the warp's lanes mostly share one or two cells.
+//  * Particles that stay in their cell (about 96% per step for a thermal
+//    plasma at half the Courant step) have old and new shapes on the same
+//    3 (TSC) or 2 (CIC) rho-lattice nodes per dimension, so their Esirkepov
+//    current lives on a fixed small window of faces (54 values for TSC, 12
+//    for CIC).  Each lane sums its particles' window contributions in
+//    registers; at the end of the segment the warp reduces the windows of
+//    lanes that share a cell with a transposed shuffle reduction (each lane
+//    ends with 2 of the 64 padded sums) and issues at most two 64-bit integer
+//    shared-memory atomics per lane.  Compared with one atomic per
+//    contribution per particle this removes the 32-way same-address
+//    serialisation of the shared-memory atomics.
+//  * Particles whose window changes are queued in shared memory and deposited
+//    after the chunk, densely, on the general 4- (TSC) or 3-node (CIC) window.
+//  * Outputs wait in shared memory until one block-wide prefix per chunk gives
+//    their stable rank, so the ensemble order matches the general kernel.
+#pragma once
+
+#include "push_kernels.cuh"
+
+namespace pgb {
+
+// Sum NV (<= 64, padded to 64) per-lane values over the warp: lane l returns the
+// sums of values 2l and 2l+1 in s0, s1.  Values of lanes with take == false
+// count as zero.  62 shuffles per lane.
+template <int NV>
+__device__ __forceinline__ void warpTransposeSum(const float* v, bool take, int lane, float& s0, float& s1) {
+    float x[32];
+    // round 0 (partner lane ^ 16): keep the half selected by lane bit 4.
+    {
+        const bool hi = (lane >> 4) & 1;
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+            const float a = (k < NV && take) ? v[k] : 0.0f;
+            const float b = (k + 32 < NV && take) ? v[k + 32] : 0.0f;
+            const float send = hi ? a : b;
+            const float keep = hi ? b : a;
+            x[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+    }
+#pragma unroll
+    for (int r = 1; r < 5; r++) {
+        const int half = 32 >> r, mask = 16 >> r;
+        const bool hi = (lane >> (4 - r)) & 1;
+#pragma unroll
+        for (int k = 0; k < half; k++) {
+            const float send = hi ? x[k] : x[k + half];
+            const float keep = hi ? x[k + half] : x[k];
+            x[k] = keep + __shfl_xor_sync(0xffffffffu, send, mask);
+        }
+    }
+    s0 = x[0];
+    s1 = x[1];
+}
+
+// Tile address of window contribution j for the stay-in-cell Esirkepov window
+// starting at tile node b (per dimension).  TSC: NWn = 3 nodes, 2 faces;
+// CIC: NWn = 2 nodes, 1 face.  Layout: Jx (faces x NWn x NWn), then Jy, then Jz.
+template <int NWn>
+__device__ __forceinline__ unsigned long long* windowAddr(unsigned long long* jt, int TT, int T1, int T2, const int* b,
+                                                          int j) {
+    constexpr int F = NWn - 1;            // faces per dimension
+    constexpr int per = F * NWn * NWn;    // contributions per component
+    const int c = j / per, r = j - c * per;
+    int o[3];
+    if (c == 0) { o[0] = r / (NWn * NWn) + 1; o[1] = (r / NWn) % NWn; o[2] = r % NWn; }
+    else if (c == 1) { o[0] = r / (F * NWn); o[1] = (r / NWn) % F + 1; o[2] = r % NWn; }
+    else { o[0] = r / (NWn * F); o[1] = (r / F) % NWn; o[2] = r % F + 1; }
+    return jt + c * TT + ((b[0] + o[0]) * T1 + (b[1] + o[1])) * T2 + (b[2] + o[2]);
+}
+
+// Boris rotation of BorisPusher.h:33-43 in FP32 with the hardware reciprocal
+// square root and fast division (a few ulp; the FP32 form is checked against
+// the FP32 oracle within 1e-4).  Returns 1/gamma of the new u.
+__device__ __forceinline__ float borisFast(float ec, const float* eb, float* u) {
+    const float em[3] = {eb[0] * ec, eb[1] * ec, eb[2] * ec};
+    const float um[3] = {u[0] + em[0], u[1] + em[1], u[2] + em[2]};
+    const float tc = ec * rsqrtf(1.0f + (um[0] * um[0] + um[1] * um[1] + um[2] * um[2]));
+    const float t[3] = {eb[3] * tc, eb[4] * tc, eb[5] * tc};
+    const float up[3] = {um[0] + (um[1] * t[2] - um[2] * t[1]), um[1] + (um[2] * t[0] - um[0] * t[2]),
+                         um[2] + (um[0] * t[1] - um[1] * t[0])};
+    const float sc = __fdividef(2.0f, 1.0f + (t[0] * t[0] + t[1] * t[1] + t[2] * t[2]));
+    const float s[3] = {t[0] * sc, t[1] * sc, t[2] * sc};
+    u[0] = um[0] + (up[1] * s[2] - up[2] * s[1]) + em[0];
+    u[1] = um[1] + (up[2] * s[0] - up[0] * s[2]) + em[1];
+    u[2] = um[2] + (up[0] * s[1] - up[1] * s[0]) + em[2];
+    return rsqrtf(1.0f + (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
+}
+
+constexpr int kQWords = 11;  // queued window change: o[3], on[3], kq[3], packed lc, packed ln
+
+// Esirkepov deposit of a particle whose rho-lattice window changes (old shape on
+// nodes lo0.., new on lo1..): general NWn+1-node window with per-lane atomics.
+template <int SHAPE>
+__device__ __forceinline__ void generalWindow(unsigned long long* jt, int TT, int T1, int T2, const float* o,
+                                              const float* on, const int* lc, const int* ln, const float* kq) {
+    constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;
+    constexpr int NW4 = NWn + 1;
+    float s0[3][NW4], s1[3][NW4];
+    int b[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        float w0[NWn], w1[NWn];
+        int lo0, lo1;
+        if constexpr (SHAPE == PICA_SHAPE_TSC) {
+            tscWeights(o[d] - 0.5f, w0);
+            tscWeights(on[d] - 0.5f, w1);
+            lo0 = lc[d] - 1;
+            lo1 = ln[d] - 1;
+        } else {
+            const bool h0 = o[d] >= 0.5f, h1 = on[d] >= 0.5f;
+            const float d0 = h0 ? o[d] - 0.5f : o[d] + 0.5f, d1 = h1 ? on[d] - 0.5f : on[d] + 0.5f;
+            w0[0] = 1.0f - d0; w0[1] = d0;
+            w1[0] = 1.0f - d1; w1[1] = d1;
+            lo0 = h0 ? lc[d] : lc[d] - 1;
+            lo1 = h1 ? ln[d] : ln[d] - 1;
+        }
+        const int base = min(lo0, lo1);
+        placeShape<float, NW4, NWn>(s0[d], lo0, base, w0);
+        placeShape<float, NW4, NWn>(s1[d], lo1, base, w1);
+        b[d] = base + kG;
+    }
+    esirkepov<float, NW4>(jt, jt + TT, jt + 2 * TT, T1, T2, b, s0, s1, kq);
+}
+
+template <int SHAPE, int K, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __grid_constant__ PushArgs<CellPtrs> a) {
+    constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;   // stay-in-cell window nodes per dimension
+    constexpr int NV = 3 * (NWn - 1) * NWn * NWn;          // 54 (TSC) or 12 (CIC)
+    constexpr int kWarps = THREADS / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int kQueue = THREADS * K / 8;   // window-changing particles queued per chunk
+    __shared__ int s_cnt[2][kWarps];
+    __shared__ int s_base[2];
+    __shared__ int s_nq;
+    __shared__ float sQueue[kQueue * kQWords];
+
+    const int T1 = a.T[1], T2 = a.T[2], TT = a.T[0] * T1 * T2;
+    unsigned long long* jt = reinterpret_cast<unsigned long long*>(smem_raw);
+    float* eb = reinterpret_cast<float*>(jt + 3 * TT);
+    uint32_t* sOut = reinterpret_cast<uint32_t*>(eb + 6 * TT);     // [warp][K][8][32]
+    uint8_t* sCode = reinterpret_cast<uint8_t*>(sOut + kWarps * K * 8 * 32);  // [warp][K][32]
+    if (threadIdx.x == 0) s_nq = 0;
+    const int s = blockIdx.x;
+    int sc[3];
+    sc[2] = s % a.nsc[2];
+    sc[1] = (s / a.nsc[2]) % a.nsc[1];
+    sc[0] = s / (a.nsc[1] * a.nsc[2]);
+    const int m[3] = {sc[0] * a.S[0], sc[1] * a.S[1], sc[2] * a.S[2]};
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+    for (int t = threadIdx.x; t < 6 * TT; t += blockDim.x) {
+        const int c = t / TT, r = t - c * TT;
+        const int i = r / (T1 * T2), jj = (r / T2) % T1, k = r % T2;
+        const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
+        eb[t] = static_cast<const float*>(a.eb[c])[((int64_t)gx * a.n[1] + gy) * a.n[2] + gz];
+    }
+    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) jt[t] = 0ull;
+    const float invU = (float)a.invUnit;
+    const float cdth[3] = {(float)a.cdth[0], (float)a.cdth[1], (float)a.cdth[2]};
+    bool bad = false;
+    __syncthreads();
+
+    for (int spi = 0; spi < a.nspecies; spi++) {
+        const SpeciesArgs<CellPtrs>& sa = a.sp[spi];
+        const int64_t start = sa.start[s];
+        const int cap = sa.cap[s];
+        const int count = sa.count[s];
+        const float ec = (float)sa.ec;
+        const float kqs[3] = {(float)sa.kq[0] * invU, (float)sa.kq[1] * invU, (float)sa.kq[2] * invU};
+        if (threadIdx.x == 0) { s_base[0] = 0; s_base[1] = 0; }
+        __syncthreads();
+        for (int chunk = 0; chunk < count; chunk += THREADS * K) {
+            const int seg = chunk + warp * 32 * K;
+            float acc[NV];
+#pragma unroll
+            for (int k = 0; k < NV; k++) acc[k] = 0.0f;
+            int accKey = -1;
+            // Outputs wait in this warp's shared-memory slice until the stable rank is known.
+            uint32_t* so = sOut + (size_t)warp * K * 8 * 32;
+            unsigned stayBits = 0u, leaveBits = 0u;   // bit it: this lane's particle it stays / leaves
+#pragma unroll 1
+            for (int it = 0; it < K; it++) {
+                const int i = seg + lane * K + it;
+                const bool act = i < count;
+                int code = 13;
+                if (act) {
+                    const int64_t slot = start + i;
+                    int c3[3];
+                    unpackCell(sa.in.cell[slot], c3[0], c3[1], c3[2]);
+                    const int lc[3] = {c3[0] - m[0], c3[1] - m[1], c3[2] - m[2]};
+                    const float o[3] = {sa.in.ox[slot], sa.in.oy[slot], sa.in.oz[slot]};
+                    float u[3] = {sa.in.ux[slot], sa.in.uy[slot], sa.in.uz[slot]};
+                    const float wgt = sa.in.w[slot];
+                    float eb6[6];
+                    if constexpr (SHAPE == PICA_SHAPE_CIC) {
+                        int bc[3], bs[3];
+                        float wc[3][2], ws[3][2];
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            bc[d] = lc[d] + kG; wc[d][0] = 1.0f - o[d]; wc[d][1] = o[d];
+                            const bool hi = o[d] >= 0.5f;
+                            const float dd = hi ? o[d] - 0.5f : o[d] + 0.5f;
+                            bs[d] = (hi ? lc[d] : lc[d] - 1) + kG; ws[d][0] = 1.0f - dd; ws[d][1] = dd;
+                        }
+#pragma unroll
+                        for (int comp = 0; comp < 6; comp++) {
+                            int t0[3];
+#pragma unroll
+                            for (int d = 0; d < 3; d++) t0[d] = stag(comp, d) ? bs[d] : bc[d];
+                            eb6[comp] = gatherSep<float, 2>(eb + comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
+                                                            stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2]);
+                        }
+                    } else {
+                        int bc[3], bs[3];
+                        float wc[3][3], ws[3][3];
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            const bool hi = o[d] >= 0.5f;
+                            bc[d] = lc[d] + (hi ? 1 : 0) - 1 + kG; tscWeights(hi ? o[d] - 1.0f : o[d], wc[d]);
+                            bs[d] = lc[d] - 1 + kG; tscWeights(o[d] - 0.5f, ws[d]);
+                        }
+#pragma unroll
+                        for (int comp = 0; comp < 6; comp++) {
+                            int t0[3];
+#pragma unroll
+                            for (int d = 0; d < 3; d++) t0[d] = stag(comp, d) ? bs[d] : bc[d];
+                            eb6[comp] = gatherSep<float, 3>(eb + comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
+                                                            stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2]);
+                        }
+                    }
+                    const float ig = borisFast(ec, eb6, u);
+                    int ln[3];
+                    float on[3];
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        float onew = o[d] + (u[d] * ig) * cdth[d];
+                        const float fl = floorf(onew);
+                        ln[d] = lc[d] + (int)fl;
+                        onew = onew - fl;
+                        if (onew >= 1.0f) { onew -= 1.0f; ln[d] += 1; }
+                        on[d] = onew;
+                    }
+                    bool inRange = true;
+#pragma unroll
+                    for (int d = 0; d < 3; d++)
+                        inRange = inRange && ln[d] >= -1 && ln[d] <= a.S[d] && abs(ln[d] - lc[d]) <= 1 &&
+                                  on[d] >= 0.0f && on[d] < 1.0f;
+                    if (!inRange) {
+                        bad = true;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) { ln[d] = lc[d]; on[d] = o[d]; }
+                    }
+                    const float kq[3] = {kqs[0] * wgt, kqs[1] * wgt, kqs[2] * wgt};
+                    // Old and new shapes on the rho lattice: TSC nodes lc-1..lc+1 (weights of o-1/2);
+                    // CIC nodes base, base+1 with base = lc or lc-1 by o >= 1/2.
+                    int lo0[3], lo1[3];
+                    float w0[3][NWn], w1[3][NWn];
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        if constexpr (SHAPE == PICA_SHAPE_TSC) {
+                            tscWeights(o[d] - 0.5f, w0[d]);
+                            tscWeights(on[d] - 0.5f, w1[d]);
+                            lo0[d] = lc[d] - 1;
+                            lo1[d] = ln[d] - 1;
+                        } else {
+                            const bool h0 = o[d] >= 0.5f, h1 = on[d] >= 0.5f;
+                            const float d0 = h0 ? o[d] - 0.5f : o[d] + 0.5f, d1 = h1 ? on[d] - 0.5f : on[d] + 0.5f;
+                            w0[d][0] = 1.0f - d0; w0[d][1] = d0;
+                            w1[d][0] = 1.0f - d1; w1[d][1] = d1;
+                            lo0[d] = h0 ? lc[d] : lc[d] - 1;
+                            lo1[d] = h1 ? ln[d] : ln[d] - 1;
+                        }
+                    }
+                    const bool sameWindow = inRange && lo0[0] == lo1[0] && lo0[1] == lo1[1] && lo0[2] == lo1[2];
+                    if (sameWindow) {
+                        const int key = ((lo0[0] + 4) << 16) | ((lo0[1] + 4) << 8) | (lo0[2] + 4);
+                        if (key != accKey) {
+                            if (accKey >= 0) {
+                                const int b[3] = {(accKey >> 16) - 4 + kG, ((accKey >> 8) & 0xff) - 4 + kG, (accKey & 0xff) - 4 + kG};
+#pragma unroll
+                                for (int j = 0; j < NV; j++)
+                                    if (acc[j] != 0.0f) addQ(windowAddr<NWn>(jt, TT, T1, T2, b, j), acc[j]);
+                            }
+#pragma unroll
+                            for (int j = 0; j < NV; j++) acc[j] = 0.0f;
+                            accKey = key;
+                        }
+                        // a = S0, dd = S1 - S0; p = a + d/2, q = a/2 + d/3; yz = a_y p_z + d_y q_z.
+                        float aa[3][NWn], dd[3][NWn], pp[3][NWn], qq[3][NWn];
+#pragma unroll
+                        for (int d = 0; d < 3; d++)
+#pragma unroll
+                            for (int k = 0; k < NWn; k++) {
+                                aa[d][k] = w0[d][k];
+                                dd[d][k] = w1[d][k] - w0[d][k];
+                                pp[d][k] = aa[d][k] + 0.5f * dd[d][k];
+                                qq[d][k] = 0.5f * aa[d][k] + (float)kThird * dd[d][k];
+                            }
+                        // e[d][f]: -(q w) h_d/dt times the running sum of dd over faces 0..f.
+                        float e[3][NWn - 1];
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            float run = 0.0f;
+#pragma unroll
+                            for (int f = 0; f < NWn - 1; f++) { run += dd[d][f]; e[d][f] = kq[d] * run; }
+                        }
+                        constexpr int P = (NWn - 1) * NWn * NWn;
+#pragma unroll
+                        for (int f = 0; f < NWn - 1; f++)
+#pragma unroll
+                            for (int y = 0; y < NWn; y++)
+#pragma unroll
+                                for (int z = 0; z < NWn; z++) {
+                                    acc[f * NWn * NWn + y * NWn + z] += e[0][f] * (aa[1][y] * pp[2][z] + dd[1][y] * qq[2][z]);
+                                    acc[P + y * (NWn - 1) * NWn + f * NWn + z] += e[1][f] * (aa[0][y] * pp[2][z] + dd[0][y] * qq[2][z]);
+                                    acc[2 * P + y * NWn * (NWn - 1) + z * (NWn - 1) + f] += e[2][f] * (aa[0][y] * pp[1][z] + dd[0][y] * qq[1][z]);
+                                }
+                    } else if (inRange) {
+                        // Window changes: queue the particle for the general window pass after the chunk.
+                        const int qi = atomicAdd(&s_nq, 1);
+                        if (qi < kQueue) {
+                            float* e = sQueue + qi * kQWords;
+#pragma unroll
+                            for (int d = 0; d < 3; d++) {
+                                e[d] = o[d]; e[3 + d] = on[d]; e[6 + d] = kq[d];
+                            }
+                            e[9] = __int_as_float(((lc[0] + 4) << 16) | ((lc[1] + 4) << 8) | (lc[2] + 4));
+                            e[10] = __int_as_float(((ln[0] + 4) << 16) | ((ln[1] + 4) << 8) | (ln[2] + 4));
+                        } else {
+                            generalWindow<SHAPE>(jt, TT, T1, T2, o, on, lc, ln, kq);
+                        }
+                    }
+                    int gc[3], nsc3[3];
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        gc[d] = wrapi(m[d] + ln[d], a.n[d]);
+                        nsc3[d] = gc[d] / a.S[d];
+                    }
+                    code = dirCode(sc, nsc3, a.nsc, bad);
+                    uint32_t* q = so + it * 8 * 32 + lane;
+                    q[0] = packCell(gc[0], gc[1], gc[2]);
+                    q[32] = __float_as_uint(on[0]); q[64] = __float_as_uint(on[1]); q[96] = __float_as_uint(on[2]);
+                    q[128] = __float_as_uint(u[0]); q[160] = __float_as_uint(u[1]); q[192] = __float_as_uint(u[2]);
+                    q[224] = __float_as_uint(wgt);
+                    sCode[(warp * K + it) * 32 + lane] = (uint8_t)code;
+                }
+                stayBits |= (act && code == 13 ? 1u : 0u) << it;
+                leaveBits |= (act && code != 13 ? 1u : 0u) << it;
+            }
+            // Reduce the stay-in-cell windows of lanes that share a window (up to two groups),
+            // then flush what remains lane by lane.
+            bool pending = accKey >= 0;
+#pragma unroll 1
+            for (int g = 0; g < 2; g++) {
+                const unsigned live = __ballot_sync(0xffffffffu, pending);
+                if (!live) break;
+                const int ref = __shfl_sync(0xffffffffu, accKey, __ffs(live) - 1);
+                const bool mine = pending && accKey == ref;
+                float s0v, s1v;
+                warpTransposeSum<NV>(acc, mine, lane, s0v, s1v);
+                const int b[3] = {(ref >> 16) - 4 + kG, ((ref >> 8) & 0xff) - 4 + kG, (ref & 0xff) - 4 + kG};
+                if (2 * lane < NV && s0v != 0.0f) addQ(windowAddr<NWn>(jt, TT, T1, T2, b, 2 * lane), s0v);
+                if (2 * lane + 1 < NV && s1v != 0.0f) addQ(windowAddr<NWn>(jt, TT, T1, T2, b, 2 * lane + 1), s1v);
+                if (mine) pending = false;
+            }
+            if (pending) {
+                const int b[3] = {(accKey >> 16) - 4 + kG, ((accKey >> 8) & 0xff) - 4 + kG, (accKey & 0xff) - 4 + kG};
+#pragma unroll
+                for (int j = 0; j < NV; j++)
+                    if (acc[j] != 0.0f) addQ(windowAddr<NWn>(jt, TT, T1, T2, b, j), acc[j]);
+            }
+            // Stable partition of the chunk: stayers packed from the front, leavers from the back,
+            // in particle order (lane-major within the warp, warp-major within the chunk).
+            const int myS = __popc(stayBits), myL = __popc(leaveBits);
+            int exS = myS, exL = myL;   // inclusive lane scan
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int ts = __shfl_up_sync(0xffffffffu, exS, d), tl = __shfl_up_sync(0xffffffffu, exL, d);
+                if (lane >= d) { exS += ts; exL += tl; }
+            }
+            if (lane == 31) { s_cnt[0][warp] = exS; s_cnt[1][warp] = exL; }
+            exS -= myS;
+            exL -= myL;
+            __syncthreads();
+            // Window changes queued by this chunk (all lanes, dense).
+            const int nq = min(s_nq, kQueue);
+            for (int qi = threadIdx.x; qi < nq; qi += THREADS) {
+                const float* e = sQueue + qi * kQWords;
+                const int k0 = __float_as_int(e[9]), k1 = __float_as_int(e[10]);
+                const int lc[3] = {(k0 >> 16) - 4, ((k0 >> 8) & 0xff) - 4, (k0 & 0xff) - 4};
+                const int ln[3] = {(k1 >> 16) - 4, ((k1 >> 8) & 0xff) - 4, (k1 & 0xff) - 4};
+                generalWindow<SHAPE>(jt, TT, T1, T2, e, e + 3, lc, ln, e + 6);
+            }
+            int rs = s_base[0] + exS, rl = s_base[1] + exL;
+            for (int w = 0; w < warp; w++) { rs += s_cnt[0][w]; rl += s_cnt[1][w]; }
+#pragma unroll 1
+            for (int it = 0; it < K; it++) {
+                const bool st = (stayBits >> it) & 1, lv = (leaveBits >> it) & 1;
+                if (st || lv) {
+                    int64_t o;
+                    if (st) o = start + rs++;
+                    else {
+                        o = start + cap - 1 - (rl++);
+                        sa.dir[o] = sCode[(warp * K + it) * 32 + lane];
+                    }
+                    const uint32_t* q = so + it * 8 * 32 + lane;
+                    sa.out.cell[o] = q[0];
+                    sa.out.ox[o] = __uint_as_float(q[32]); sa.out.oy[o] = __uint_as_float(q[64]);
+                    sa.out.oz[o] = __uint_as_float(q[96]);
+                    sa.out.ux[o] = __uint_as_float(q[128]); sa.out.uy[o] = __uint_as_float(q[160]);
+                    sa.out.uz[o] = __uint_as_float(q[192]);
+                    sa.out.w[o] = __uint_as_float(q[224]);
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int w = 0; w < kWarps; w++) { s_base[0] += s_cnt[0][w]; s_base[1] += s_cnt[1][w]; }
+                s_nq = 0;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) { sa.nstay[s] = s_base[0]; sa.nleave[s] = s_base[1]; }
+        __syncthreads();
+    }
+    if (bad) atomicExch(a.flags, PICA_ERR_MIGRATION);
+    __syncthreads();
+    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) {
+        const unsigned long long v = jt[t];
+        if (v != 0ull) {
+            const int c = t / TT, r = t - c * TT;
+            const int i = r / (T1 * T2), jj = (r / T2) % T1, k = r % T2;
+            const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
+            atomicAdd(a.jacc[c] + ((int64_t)gx * a.n[1] + gy) * a.n[2] + gz, v);
+        }
+    }
+}
+
+}  // namespace pgb

@@ -1,5 +1,5 @@
 // FP32 cell form: push and migration kernels (FMA contraction allowed).
-#include "push_kernels.cuh"
+#include "push_fast.cuh"
 
 namespace pgb {
 
@@ -7,7 +7,7 @@ namespace {
 template <int SHAPE, int DEP>
 int launchOne(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     const int TT = a.T[0] * a.T[1] * a.T[2];
-    const size_t smem = (size_t)9 * TT * sizeof(float);
+    const size_t smem = (size_t)6 * TT * sizeof(float) + (size_t)3 * TT * sizeof(unsigned long long);
     auto k = k_push<false, SHAPE, DEP>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
@@ -17,7 +17,23 @@ int launchOne(const PushArgs<CellPtrs>& a, cudaStream_t s) {
 }
 }  // namespace
 
+template <int SHAPE>
+int launchEsirkepov(const PushArgs<CellPtrs>& a, cudaStream_t s) {
+    const int TT = a.T[0] * a.T[1] * a.T[2];
+    constexpr int K = 8, THREADS = 128, MINB = 3;
+    const size_t smem = (size_t)6 * TT * sizeof(float) + (size_t)3 * TT * sizeof(unsigned long long) +
+                        (size_t)(THREADS / 32) * K * 32 * (8 * sizeof(uint32_t) + 1);
+    auto k = k_push_cell_esirkepov<SHAPE, K, THREADS, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
+    k<<<nscTot, THREADS, smem, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
 int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int dep, cudaStream_t s) {
+    if (shape == PICA_SHAPE_TSC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchEsirkepov<PICA_SHAPE_TSC>(a, s);
+    if (shape == PICA_SHAPE_CIC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchEsirkepov<PICA_SHAPE_CIC>(a, s);
     if (shape == PICA_SHAPE_CIC && dep == PICA_DEPOSIT_DIRECT) return launchOne<PICA_SHAPE_CIC, PICA_DEPOSIT_DIRECT>(a, s);
     if (shape == PICA_SHAPE_CIC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchOne<PICA_SHAPE_CIC, PICA_DEPOSIT_ESIRKEPOV>(a, s);
     if (shape == PICA_SHAPE_TSC && dep == PICA_DEPOSIT_DIRECT) return launchOne<PICA_SHAPE_TSC, PICA_DEPOSIT_DIRECT>(a, s);

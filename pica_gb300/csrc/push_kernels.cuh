@@ -5,8 +5,9 @@
 //
 // One CTA owns one supercell.  It stages the E/B tile of nodes [m-2, m+S+3)
 // per dimension (periodic) into shared memory, accumulates the supercell's
-// current in a shared-memory tile of the same extent, and adds the tile to
-// the global J once (periodic) at the end -- the GPU form of pica's
+// current in a shared-memory tile of the same extent (64-bit fixed point,
+// native integer shared-memory atomics), and adds the tile to the global
+// accumulator once (periodic) at the end -- the GPU form of pica's
 // FieldInterpolatorCICSupercell / CurrentDepositorCICSupercell pair
 // (fieldInterpolation/FieldInterpolatorYeeGrid.h:188-283,
 //  currentDeposition/CurrentDepositorYeeGrid.h:168-264).
@@ -43,6 +44,15 @@ __device__ __forceinline__ void tscWeights(R d, R* w) {
     w[2] = h * (h + d) * (h + d);
 }
 
+// Add one current contribution to a tile node.  FP32 form: the contribution is
+// already scaled to fixed-point units and is added as a 64-bit integer (exact,
+// order-independent).  FP64 form: plain FP64 add, so the FP64 result differs
+// from pica's only by the order of the sums.
+__device__ __forceinline__ void addQ(unsigned long long* p, float scaled) {
+    atomicAdd(p, (unsigned long long)__float2ll_rn(scaled));
+}
+__device__ __forceinline__ void addQ(double* p, double v) { atomicAdd(p, v); }
+
 // Separable W^3-point gather: sum_i wx_i sum_j wy_j (sum_k wz_k F), left to right.
 template <typename R, int W>
 __device__ __forceinline__ R gatherSep(const R* tile, int T1, int T2, const int* t0, const R* wx, const R* wy,
@@ -64,17 +74,17 @@ __device__ __forceinline__ R gatherSep(const R* tile, int T1, int T2, const int*
     return r;
 }
 
-template <typename R, int W>
-__device__ __forceinline__ void scatterSep(R* tile, int T1, int T2, const int* t0, const R* wx, const R* wy,
+template <typename R, int W, typename A>
+__device__ __forceinline__ void scatterSep(A* tile, int T1, int T2, const int* t0, const R* wx, const R* wy,
                                            const R* wz, R v) {
 #pragma unroll
     for (int i = 0; i < W; i++)
 #pragma unroll
         for (int j = 0; j < W; j++) {
-            R* row = tile + ((t0[0] + i) * T1 + (t0[1] + j)) * T2 + t0[2];
+            A* row = tile + ((t0[0] + i) * T1 + (t0[1] + j)) * T2 + t0[2];
             R vij = (v * wx[i]) * wy[j];
 #pragma unroll
-            for (int k = 0; k < W; k++) atomicAdd(row + k, vij * wz[k]);
+            for (int k = 0; k < W; k++) addQ(row + k, vij * wz[k]);
         }
 }
 
@@ -93,14 +103,14 @@ __device__ __forceinline__ void cicScatterRef(double* t, int T1, int T2, const i
     double* p = t + (b[0] * T1 + b[1]) * T2 + b[2];
     const int sy = T2, sx = T1 * T2;
     const double cx = c[0], cy = c[1], cz = c[2];
-    atomicAdd(p, (1.0 - cx) * (1.0 - cy) * (1.0 - cz) * v);
-    atomicAdd(p + 1, (1.0 - cx) * (1.0 - cy) * cz * v);
-    atomicAdd(p + sy, (1.0 - cx) * cy * (1.0 - cz) * v);
-    atomicAdd(p + sy + 1, (1.0 - cx) * cy * cz * v);
-    atomicAdd(p + sx, cx * (1.0 - cy) * (1.0 - cz) * v);
-    atomicAdd(p + sx + 1, cx * (1.0 - cy) * cz * v);
-    atomicAdd(p + sx + sy, cx * cy * (1.0 - cz) * v);
-    atomicAdd(p + sx + sy + 1, cx * cy * cz * v);
+    addQ(p, (1.0 - cx) * (1.0 - cy) * (1.0 - cz) * v);
+    addQ(p + 1, (1.0 - cx) * (1.0 - cy) * cz * v);
+    addQ(p + sy, (1.0 - cx) * cy * (1.0 - cz) * v);
+    addQ(p + sy + 1, (1.0 - cx) * cy * cz * v);
+    addQ(p + sx, cx * (1.0 - cy) * (1.0 - cz) * v);
+    addQ(p + sx + 1, cx * (1.0 - cy) * cz * v);
+    addQ(p + sx + sy, cx * cy * (1.0 - cz) * v);
+    addQ(p + sx + sy + 1, cx * cy * cz * v);
 }
 
 // Boris rotation of BorisPusher.h:33-43 on normalised momentum u; returns 1/gamma
@@ -125,8 +135,8 @@ __device__ __forceinline__ R boris(R ec, const R* eb, R* u) {
 // cell centres, J on faces.  s0/s1: old/new shape in an NW-node window of the
 // rho lattice starting at tile index b; k: -(q w) h_d / dt.  Jx of the face
 // between window nodes i and i+1 is pica Jx node b_x + i + 1.
-template <typename R, int NW>
-__device__ __forceinline__ void esirkepov(R* jx, R* jy, R* jz, int T1, int T2, const int* b, const R (*s0)[NW],
+template <typename R, int NW, typename A>
+__device__ __forceinline__ void esirkepov(A* jx, A* jy, A* jz, int T1, int T2, const int* b, const R (*s0)[NW],
                                           const R (*s1)[NW], const R* k) {
     R ds[3][NW];
 #pragma unroll
@@ -143,7 +153,7 @@ __device__ __forceinline__ void esirkepov(R* jx, R* jy, R* jz, int T1, int T2, c
 #pragma unroll
             for (int i = 0; i < NW - 1; i++) {
                 acc = acc + ds[0][i] * yz;
-                atomicAdd(jx + ((b[0] + i + 1) * T1 + (b[1] + j)) * T2 + (b[2] + l), acc * k[0]);
+                addQ(jx + ((b[0] + i + 1) * T1 + (b[1] + j)) * T2 + (b[2] + l), acc * k[0]);
             }
         }
 #pragma unroll
@@ -155,7 +165,7 @@ __device__ __forceinline__ void esirkepov(R* jx, R* jy, R* jz, int T1, int T2, c
 #pragma unroll
             for (int j = 0; j < NW - 1; j++) {
                 acc = acc + ds[1][j] * xz;
-                atomicAdd(jy + ((b[0] + i) * T1 + (b[1] + j + 1)) * T2 + (b[2] + l), acc * k[1]);
+                addQ(jy + ((b[0] + i) * T1 + (b[1] + j + 1)) * T2 + (b[2] + l), acc * k[1]);
             }
         }
 #pragma unroll
@@ -167,17 +177,22 @@ __device__ __forceinline__ void esirkepov(R* jx, R* jy, R* jz, int T1, int T2, c
 #pragma unroll
             for (int l = 0; l < NW - 1; l++) {
                 acc = acc + ds[2][l] * xy;
-                atomicAdd(jz + ((b[0] + i) * T1 + (b[1] + j)) * T2 + (b[2] + l + 1), acc * k[2]);
+                addQ(jz + ((b[0] + i) * T1 + (b[1] + j)) * T2 + (b[2] + l + 1), acc * k[2]);
             }
         }
 }
 
+// s[lo - base + k] = w[k] in an NW window, written with selects so s stays in registers.
 template <typename R, int NW, int P>
 __device__ __forceinline__ void placeShape(R* s, int lo, int base, const R* w) {
+    const int off = lo - base;
 #pragma unroll
-    for (int i = 0; i < NW; i++) s[i] = R(0);
+    for (int i = 0; i < NW; i++) {
+        R v = R(0);
 #pragma unroll
-    for (int i = 0; i < P; i++) s[lo - base + i] = w[i];
+        for (int k = 0; k < P; k++) v = (i - off == k) ? w[k] : v;
+        s[i] = v;
+    }
 }
 
 // Direction code of a supercell move, (dx+1)*9 + (dy+1)*3 + (dz+1); 13 = stay.
@@ -208,16 +223,17 @@ __device__ __forceinline__ void copyParticle(const CellPtrs& s, int64_t i, const
 // ---------------------------------------------------------------------------
 template <bool PLAIN, int SHAPE, int DEP>
 __global__ void __launch_bounds__(kPushThreads)
-k_push(const PushArgs<typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::type> a) {
+k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::type> a) {
     using R = typename std::conditional<PLAIN, double, float>::type;
     using P = typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::type;
+    using A = typename std::conditional<PLAIN, double, unsigned long long>::type;  // J tile accumulator
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_cnt[2][kPushThreads / 32];
     __shared__ int s_base[2];
 
     const int T1 = a.T[1], T2 = a.T[2], TT = a.T[0] * T1 * T2;
-    R* eb = reinterpret_cast<R*>(smem_raw);
-    R* jt = eb + 6 * TT;
+    A* jt = reinterpret_cast<A*>(smem_raw);
+    R* eb = reinterpret_cast<R*>(jt + 3 * TT);
     const int s = blockIdx.x;
     int sc[3];
     sc[2] = s % a.nsc[2];
@@ -233,7 +249,7 @@ k_push(const PushArgs<typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::typ
         const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
         eb[t] = static_cast<const R*>(a.eb[c])[((int64_t)gx * a.n[1] + gy) * a.n[2] + gz];
     }
-    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) jt[t] = R(0);
+    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) jt[t] = A(0);
 
     // pica supercell index math (FieldInterpolatorYeeGrid.h:197-205): tile index t of
     // the reference maps to node trunc(minPos/h) - 1 + t, i.e. our tile index t + off.
@@ -246,9 +262,10 @@ k_push(const PushArgs<typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::typ
         nos[d] = no[d] + 0.5;
         off[d] = ((int)(minPos / a.h[d]) - 1) - (m[d] - kG);
     }
-    R* jx = jt;
-    R* jy = jt + TT;
-    R* jz = jt + 2 * TT;
+    A* jx = jt;
+    A* jy = jt + TT;
+    A* jz = jt + 2 * TT;
+    const R invU = (R)a.invUnit;
     bool bad = false;
     __syncthreads();
 
@@ -490,7 +507,7 @@ k_push(const PushArgs<typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::typ
 #pragma unroll
                         for (int d = 0; d < 3; d++) { ln[d] = lc[d]; on[d] = o[d]; }
                     } else if constexpr (DEP == PICA_DEPOSIT_DIRECT) {
-                        const float qcw = (float)sa.qc * wgt;
+                        const float qcw = (float)sa.qc * wgt * invU;
                         const float cur[3] = {(u[0] * ig) * qcw, (u[1] * ig) * qcw, (u[2] * ig) * qcw};
                         if constexpr (SHAPE == PICA_SHAPE_CIC) {
                             int bc[3], bs[3];
@@ -529,7 +546,8 @@ k_push(const PushArgs<typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::typ
                             }
                         }
                     } else {
-                        const float kq[3] = {(float)sa.kq[0] * wgt, (float)sa.kq[1] * wgt, (float)sa.kq[2] * wgt};
+                        const float kq[3] = {(float)sa.kq[0] * wgt * invU, (float)sa.kq[1] * wgt * invU,
+                                             (float)sa.kq[2] * wgt * invU};
                         int b[3];
                         if constexpr (SHAPE == PICA_SHAPE_CIC) {
                             float s0[3][3], s1[3][3];
@@ -605,15 +623,18 @@ k_push(const PushArgs<typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::typ
     }
     if (bad) atomicExch(a.flags, PICA_ERR_MIGRATION);
     __syncthreads();
-    // Flush the supercell's J tile to the grid: J += tile / h^3 (CurrentDepositorYeeGrid.h:201-213).
-    const R norm = (R)a.norm;
+    // Flush the supercell's tile once (periodic).  FP64: J += tile / h^3 as
+    // CurrentDepositorYeeGrid.h:201-213; FP32: into the fixed-point accumulator,
+    // the 1/h^3 is applied when J is formed from the exact sums.
     for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) {
-        const R v = jt[t];
-        if (v != R(0)) {
+        const A v = jt[t];
+        if (v != A(0)) {
             const int c = t / TT, r = t - c * TT;
             const int i = r / (T1 * T2), jj = (r / T2) % T1, k = r % T2;
             const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
-            atomicAdd(static_cast<R*>(a.j[c]) + ((int64_t)gx * a.n[1] + gy) * a.n[2] + gz, v * norm);
+            const int64_t node = ((int64_t)gx * a.n[1] + gy) * a.n[2] + gz;
+            if constexpr (PLAIN) atomicAdd(static_cast<double*>(a.j[c]) + node, v * a.norm);
+            else atomicAdd(a.jacc[c] + node, v);
         }
     }
 }
@@ -624,7 +645,7 @@ k_push(const PushArgs<typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::typ
 // source's slot order).  REBUILD copies stayers + arrivals into a new layout.
 // ---------------------------------------------------------------------------
 template <class P, bool REBUILD>
-__global__ void __launch_bounds__(256) k_migrate(const MigrateArgs<P> a) {
+__global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ MigrateArgs<P> a) {
     const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
     const int d = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
