@@ -207,6 +207,10 @@ inline void placeShape(R* s, int lo, int base, const R* w) {
 // ----------------------------------------------------------------------------
 // Particle stores.
 // ----------------------------------------------------------------------------
+// Dead slots (left by particles that moved to another supercell) are marked
+// x = -1e300 (FP64 form; positions are never below -L, even before the
+// periodic wrap) or cx = -1 (FP32 form).
+const double kDeadX = -1.0e300;
 struct PlainStore {  // FP64 absolute positions, normalised momentum u = p/(mc)
     std::vector<double> x, y, z, ux, uy, uz, w;
     size_t size() const { return w.size(); }
@@ -215,6 +219,11 @@ struct PlainStore {  // FP64 absolute positions, normalised momentum u = p/(mc)
         x.push_back(s.x[i]); y.push_back(s.y[i]); z.push_back(s.z[i]);
         ux.push_back(s.ux[i]); uy.push_back(s.uy[i]); uz.push_back(s.uz[i]); w.push_back(s.w[i]);
     }
+    void set(size_t k, const PlainStore& s, size_t i) {
+        x[k] = s.x[i]; y[k] = s.y[i]; z[k] = s.z[i]; ux[k] = s.ux[i]; uy[k] = s.uy[i]; uz[k] = s.uz[i]; w[k] = s.w[i];
+    }
+    bool alive(size_t i) const { return x[i] > -1.0e299; }
+    void kill(size_t i) { x[i] = kDeadX; }
 };
 struct CellStore {  // FP32 form: integer cell + FP32 offset in [0,1)
     std::vector<int32_t> cx, cy, cz;
@@ -226,6 +235,12 @@ struct CellStore {  // FP32 form: integer cell + FP32 offset in [0,1)
         ox.push_back(s.ox[i]); oy.push_back(s.oy[i]); oz.push_back(s.oz[i]);
         ux.push_back(s.ux[i]); uy.push_back(s.uy[i]); uz.push_back(s.uz[i]); w.push_back(s.w[i]);
     }
+    void set(size_t k, const CellStore& s, size_t i) {
+        cx[k] = s.cx[i]; cy[k] = s.cy[i]; cz[k] = s.cz[i]; ox[k] = s.ox[i]; oy[k] = s.oy[i]; oz[k] = s.oz[i];
+        ux[k] = s.ux[i]; uy[k] = s.uy[i]; uz[k] = s.uz[i]; w[k] = s.w[i];
+    }
+    bool alive(size_t i) const { return cx[i] >= 0; }
+    void kill(size_t i) { cx[i] = -1; }
 };
 
 struct Migration { int32_t sp, src, slot, dst; };
@@ -257,6 +272,7 @@ struct SimBase {
         if (c.threads > 0) omp_set_num_threads(c.threads);
 #endif
     }
+    int steps = 0;
     int scLinear(int sx, int sy, int sz) const { return (sx * nsc[1] + sy) * nsc[2] + sz; }
     void scCoords(int s, int* sxyz) const {
         sxyz[2] = s % nsc[2]; sxyz[1] = (s / nsc[2]) % nsc[1]; sxyz[0] = s / (nsc[1] * nsc[2]);
@@ -299,7 +315,46 @@ struct Sim : SimBase {
     void step();
     void pushSupercell(int s, R* jt);
     void migrate();
+    void resort();   // drop dead slots and sort every supercell by cell (stable)
 };
+
+// Local cell of particle i of supercell s: (lx*Sy + ly)*Sz + lz, the sort key.
+inline int cellKey(const SimBase& S, const PlainStore& st, size_t i, const int* m) {
+    const double p[3] = {st.x[i], st.y[i], st.z[i]};
+    int l[3];
+    for (int d = 0; d < 3; d++) {
+        l[d] = (int)std::floor(p[d] * S.invh[d]) - m[d];
+        l[d] = std::min(std::max(l[d], 0), S.cfg.sc[d] - 1);
+    }
+    return (l[0] * S.cfg.sc[1] + l[1]) * S.cfg.sc[2] + l[2];
+}
+inline int cellKey(const SimBase& S, const CellStore& st, size_t i, const int* m) {
+    return ((st.cx[i] - m[0]) * S.cfg.sc[1] + (st.cy[i] - m[1])) * S.cfg.sc[2] + (st.cz[i] - m[2]);
+}
+
+// Live particles of st in (cell, slot) order.
+template <typename Store>
+Store sortedByCell(const SimBase& S, const Store& st, int s) {
+    int sxyz[3]; S.scCoords(s, sxyz);
+    const int m[3] = {sxyz[0] * S.cfg.sc[0], sxyz[1] * S.cfg.sc[1], sxyz[2] * S.cfg.sc[2]};
+    std::vector<std::pair<int, size_t>> key;
+    for (size_t i = 0; i < st.size(); i++)
+        if (st.alive(i)) key.push_back({cellKey(S, st, i, m), i});
+    std::stable_sort(key.begin(), key.end(), [](const std::pair<int, size_t>& a, const std::pair<int, size_t>& b) {
+        return a.first < b.first;
+    });
+    Store out;
+    for (auto& k : key) out.append(st, k.second);
+    return out;
+}
+
+template <typename R, typename Store>
+void Sim<R, Store>::resort() {
+    for (auto& v : parts) {
+#pragma omp parallel for schedule(dynamic, 8)
+        for (int s = 0; s < nscTot; s++) v[s] = sortedByCell(*this, v[s], s);
+    }
+}
 
 // ---- plain FP64 form helpers ------------------------------------------------
 template <>
@@ -320,6 +375,7 @@ int Sim<double, PlainStore>::load(int64_t n, const double* x, const double* y, c
         st.x.push_back(x[i]); st.y.push_back(y[i]); st.z.push_back(z[i]);
         st.ux.push_back(ux[i]); st.uy.push_back(uy[i]); st.uz.push_back(uz[i]); st.w.push_back(w[i]);
     }
+    resort();
     return 0;
 }
 
@@ -347,6 +403,7 @@ int Sim<float, CellStore>::load(int64_t n, const double* x, const double* y, con
         st.ux.push_back((float)ux[i]); st.uy.push_back((float)uy[i]); st.uz.push_back((float)uz[i]);
         st.w.push_back((float)w[i]);
     }
+    resort();
     return 0;
 }
 
@@ -430,6 +487,7 @@ void Sim<double, PlainStore>::pushSupercell(int s, double* jt) {
         const double ec = eCoeff[sp];
         const double q = c.charge[sp];
         for (size_t p = 0; p < st.size(); p++) {
+            if (!st.alive(p)) continue;
             double pos[3] = {st.x[p], st.y[p], st.z[p]};
             double eb[6];
             if (cic) {
@@ -567,6 +625,7 @@ void Sim<float, CellStore>::pushSupercell(int s, float* jt) {
         for (int d = 0; d < 3; d++) kqs[d] = (float)(-c.charge[sp] * (c.h[d] / c.dt));
         const float qc = (float)(c.charge[sp] * kC);
         for (size_t p = 0; p < st.size(); p++) {
+            if (!st.alive(p)) continue;
             int lc[3] = {st.cx[p] - m[0], st.cy[p] - m[1], st.cz[p] - m[2]};
             float o[3] = {st.ox[p], st.oy[p], st.oz[p]};
             float eb[6];
@@ -687,6 +746,7 @@ inline void newSupercell(const SimBase& S, const CellStore& st, size_t p, int* o
 }
 inline void wrapPositions(const SimBase& S, PlainStore& st) {
     for (size_t p = 0; p < st.size(); p++) {
+        if (!st.alive(p)) continue;
         double* v[3] = {&st.x[p], &st.y[p], &st.z[p]};
         for (int d = 0; d < 3; d++) {
             if (*v[d] < 0.0) *v[d] += S.L[d];
@@ -701,41 +761,52 @@ void Sim<R, Store>::migrate() {
     migrations.clear();
     for (int sp = 0; sp < cfg.nspecies; sp++) {
         std::vector<Store>& sc = parts[sp];
-        std::vector<std::vector<int8_t>> dirs(nscTot);
+        std::vector<std::vector<int8_t>> dirs(nscTot);   // -1: dead slot
 #pragma omp parallel for schedule(dynamic, 8)
         for (int s = 0; s < nscTot; s++) {
             wrapPositions(*this, sc[s]);
             int o[3]; scCoords(s, o);
-            dirs[s].resize(sc[s].size());
+            dirs[s].assign(sc[s].size(), -1);
             for (size_t p = 0; p < sc[s].size(); p++) {
+                if (!sc[s].alive(p)) continue;
                 int nw[3]; newSupercell(*this, sc[s], p, nw);
                 dirs[s][p] = (int8_t)dirCode(o, nw);
             }
         }
         for (int s = 0; s < nscTot; s++)
             for (size_t p = 0; p < sc[s].size(); p++)
-                if (dirs[s][p] != 13) {
+                if (dirs[s][p] >= 0 && dirs[s][p] != 13) {
                     int ds[3], o[3]; dirDelta(dirs[s][p], ds); scCoords(s, o);
                     int dst = scLinear(wrapi(o[0] + ds[0], nsc[0]), wrapi(o[1] + ds[1], nsc[1]), wrapi(o[2] + ds[2], nsc[2]));
                     migrations.push_back({sp, s, (int32_t)p, dst});
                 }
-        // Each destination: its stayers in slot order, then arrivals by direction code, each in source-slot order.
+        // Each destination: this step's own leavers leave holes (ascending slots); arrivals
+        // in canonical order (direction code, then source slot) fill the holes, then append.
         std::vector<Store> next(nscTot);
 #pragma omp parallel for schedule(dynamic, 8)
         for (int d = 0; d < nscTot; d++) {
+            next[d] = sc[d];
+            std::vector<size_t> holes;
             for (size_t p = 0; p < sc[d].size(); p++)
-                if (dirs[d][p] == 13) next[d].append(sc[d], p);
+                if (dirs[d][p] >= 0 && dirs[d][p] != 13) { holes.push_back(p); next[d].kill(p); }
             int dc[3]; scCoords(d, dc);
+            size_t k = 0;
             for (int dir = 0; dir < 27; dir++) {
                 if (dir == 13) continue;
                 int ds[3]; dirDelta(dir, ds);
                 int src = scLinear(wrapi(dc[0] - ds[0], nsc[0]), wrapi(dc[1] - ds[1], nsc[1]), wrapi(dc[2] - ds[2], nsc[2]));
                 for (size_t p = 0; p < sc[src].size(); p++)
-                    if (dirs[src][p] == dir) next[d].append(sc[src], p);
+                    if (dirs[src][p] == dir) {
+                        if (k < holes.size()) next[d].set(holes[k], sc[src], p);
+                        else next[d].append(sc[src], p);
+                        k++;
+                    }
             }
         }
         sc.swap(next);
     }
+    steps++;
+    if (cfg.resort_every > 0 && steps % cfg.resort_every == 0) resort();
 }
 
 template <typename R, typename Store>
@@ -790,6 +861,7 @@ void depositRho(const SimBase& S, const std::vector<std::vector<PlainStore>>& pa
     for (int sp = 0; sp < c.nspecies; sp++)
         for (auto& st : parts[sp])
             for (size_t p = 0; p < st.size(); p++) {
+                if (!st.alive(p)) continue;
                 double pos[3] = {st.x[p], st.y[p], st.z[p]};
                 int lo[3]; double w[3][3]; int np = c.shape == ORC_SHAPE_CIC ? 2 : 3;
                 for (int d = 0; d < 3; d++) {
@@ -812,6 +884,7 @@ void depositRho(const SimBase& S, const std::vector<std::vector<CellStore>>& par
     for (int sp = 0; sp < c.nspecies; sp++)
         for (auto& st : parts[sp])
             for (size_t p = 0; p < st.size(); p++) {
+                if (!st.alive(p)) continue;
                 int cc[3] = {st.cx[p], st.cy[p], st.cz[p]};
                 double o[3] = {st.ox[p], st.oy[p], st.oz[p]};
                 int lo[3]; double w[3][3]; int np = c.shape == ORC_SHAPE_CIC ? 2 : 3;
@@ -835,6 +908,7 @@ inline double kinetic(const SimBase& S, const std::vector<std::vector<PlainStore
     for (int sp = 0; sp < S.cfg.nspecies; sp++)
         for (auto& st : parts[sp])
             for (size_t p = 0; p < st.size(); p++) {
+                if (!st.alive(p)) continue;
                 double u2 = st.ux[p] * st.ux[p] + st.uy[p] * st.uy[p] + st.uz[p] * st.uz[p];
                 e += st.w[p] * S.cfg.mass[sp] * kC * kC * (u2 / (1.0 + std::sqrt(1.0 + u2)));
             }
@@ -845,6 +919,7 @@ inline double kinetic(const SimBase& S, const std::vector<std::vector<CellStore>
     for (int sp = 0; sp < S.cfg.nspecies; sp++)
         for (auto& st : parts[sp])
             for (size_t p = 0; p < st.size(); p++) {
+                if (!st.alive(p)) continue;
                 double ux = st.ux[p], uy = st.uy[p], uz = st.uz[p];
                 double u2 = ux * ux + uy * uy + uz * uz;
                 e += (double)st.w[p] * S.cfg.mass[sp] * kC * kC * (u2 / (1.0 + std::sqrt(1.0 + u2)));
@@ -881,10 +956,16 @@ int setFields(S* s, const double* const* f9) {
     s->grid.fill(0, 6);
     return 0;
 }
+template <typename Store>
+int64_t aliveCount(const Store& st) {
+    int64_t n = 0;
+    for (size_t p = 0; p < st.size(); p++) n += st.alive(p) ? 1 : 0;
+    return n;
+}
 template <typename S>
 int getCounts(S* s, int32_t* counts) {
     for (int sp = 0; sp < s->cfg.nspecies; sp++)
-        for (int k = 0; k < s->nscTot; k++) counts[(size_t)sp * s->nscTot + k] = (int32_t)s->parts[sp][k].size();
+        for (int k = 0; k < s->nscTot; k++) counts[(size_t)sp * s->nscTot + k] = (int32_t)aliveCount(s->parts[sp][k]);
     return 0;
 }
 template <typename S>
@@ -965,8 +1046,8 @@ int64_t orc_num_particles(void* sim) {
     Handle* h = (Handle*)sim;
     if (!h) return -1;
     int64_t n = 0;
-    if (h->plain) { for (auto& v : h->plain->parts) for (auto& s : v) n += s.size(); }
-    else { for (auto& v : h->cell->parts) for (auto& s : v) n += s.size(); }
+    if (h->plain) { for (auto& v : h->plain->parts) for (auto& s : v) n += aliveCount(s); }
+    else { for (auto& v : h->cell->parts) for (auto& s : v) n += aliveCount(s); }
     return n;
 }
 
@@ -980,11 +1061,13 @@ int orc_get_particles(void* sim, double* x, double* y, double* z, double* ux, do
         for (int sp = 0; sp < s->cfg.nspecies; sp++)
             for (int k = 0; k < s->nscTot; k++) {
                 const PlainStore& st = s->parts[sp][k];
-                for (size_t p = 0; p < st.size(); p++, o++) {
+                for (size_t p = 0; p < st.size(); p++) {
+                    if (!st.alive(p)) continue;
                     x[o] = st.x[p]; y[o] = st.y[p]; z[o] = st.z[p];
                     ux[o] = st.ux[p]; uy[o] = st.uy[p]; uz[o] = st.uz[p]; w[o] = st.w[p];
                     if (species) species[o] = sp;
                     if (supercell) supercell[o] = k;
+                    o++;
                 }
             }
     } else {
@@ -992,13 +1075,15 @@ int orc_get_particles(void* sim, double* x, double* y, double* z, double* ux, do
         for (int sp = 0; sp < s->cfg.nspecies; sp++)
             for (int k = 0; k < s->nscTot; k++) {
                 const CellStore& st = s->parts[sp][k];
-                for (size_t p = 0; p < st.size(); p++, o++) {
+                for (size_t p = 0; p < st.size(); p++) {
+                    if (!st.alive(p)) continue;
                     x[o] = ((double)st.cx[p] + (double)st.ox[p]) * s->cfg.h[0];
                     y[o] = ((double)st.cy[p] + (double)st.oy[p]) * s->cfg.h[1];
                     z[o] = ((double)st.cz[p] + (double)st.oz[p]) * s->cfg.h[2];
                     ux[o] = st.ux[p]; uy[o] = st.uy[p]; uz[o] = st.uz[p]; w[o] = st.w[p];
                     if (species) species[o] = sp;
                     if (supercell) supercell[o] = k;
+                    o++;
                 }
             }
     }
@@ -1014,10 +1099,12 @@ int orc_get_particles_cell(void* sim, int32_t* cell, float* ox, float* oy, float
     for (int sp = 0; sp < s->cfg.nspecies; sp++)
         for (int k = 0; k < s->nscTot; k++) {
             const CellStore& st = s->parts[sp][k];
-            for (size_t p = 0; p < st.size(); p++, o++) {
+            for (size_t p = 0; p < st.size(); p++) {
+                if (!st.alive(p)) continue;
                 cell[o] = (st.cx[p] * s->cfg.n[1] + st.cy[p]) * s->cfg.n[2] + st.cz[p];
                 ox[o] = st.ox[p]; oy[o] = st.oy[p]; oz[o] = st.oz[p];
                 ux[o] = st.ux[p]; uy[o] = st.uy[p]; uz[o] = st.uz[p]; w[o] = st.w[p];
+                o++;
             }
         }
     return 0;
@@ -1069,7 +1156,7 @@ int orc_diagnostics(void* sim, double bg, orc_diag* out) {
         out->kinetic_energy = kinetic(*b, s->parts);
         depositRho<double>(*b, s->parts, r);
         out->gauss_max = gaussResidual(s, r, bg, &out->rho_max);
-        for (int sp = 0; sp < c.nspecies; sp++) for (auto& st : s->parts[sp]) for (double w : st.w) out->total_charge += c.charge[sp] * w;
+        for (int sp = 0; sp < c.nspecies; sp++) for (auto& st : s->parts[sp]) for (size_t p = 0; p < st.size(); p++) if (st.alive(p)) out->total_charge += c.charge[sp] * st.w[p];
     } else {
         auto* s = h->cell;
         for (int comp = 0; comp < 6; comp++)
@@ -1078,7 +1165,7 @@ int orc_diagnostics(void* sim, double bg, orc_diag* out) {
         out->kinetic_energy = kinetic(*b, s->parts);
         depositRho<float>(*b, s->parts, r);
         out->gauss_max = gaussResidual(s, r, bg, &out->rho_max);
-        for (int sp = 0; sp < c.nspecies; sp++) for (auto& st : s->parts[sp]) for (float w : st.w) out->total_charge += c.charge[sp] * (double)w;
+        for (int sp = 0; sp < c.nspecies; sp++) for (auto& st : s->parts[sp]) for (size_t p = 0; p < st.size(); p++) if (st.alive(p)) out->total_charge += c.charge[sp] * (double)st.w[p];
     }
     out->field_energy = fe * vol / (8.0 * kPi);
     return 0;

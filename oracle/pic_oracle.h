@@ -12,6 +12,17 @@
  *            FP64 absolute-position form and FP32 cell+offset form).
  *   ref_*  : oracle/ref_harness.cpp, a driver around pica's own headers
  *            (FP64, CIC, direct deposition only); it pins the restatement.
+ *
+ * Ensemble order (both implement it identically):
+ *   - load: particles are routed to supercells and, within a supercell, put
+ *     in cell order (stable: local cell (lx*Sy + ly)*Sz + lz, then input order);
+ *   - step: a particle that leaves its supercell leaves a dead slot behind;
+ *     each destination receives its arrivals in canonical order (direction
+ *     code 0..26 of the move, then source slot) into the slots its own
+ *     leavers vacated in this step (ascending), then appended at the end;
+ *   - every resort_every steps: each supercell drops its dead slots and is
+ *     re-sorted by cell (stable).
+ * Downloads list the live particles in slot order.
  */
 #ifndef PICA_ORACLE_H
 #define PICA_ORACLE_H
@@ -38,7 +49,7 @@ typedef struct orc_config {
     double mass[4];      /* g                                            */
     double charge[4];    /* statC                                        */
     int32_t threads;     /* OpenMP threads, 0 = runtime default          */
-    int32_t pad_;
+    int32_t resort_every;/* compact + sort each supercell by cell every k steps (0 = never) */
 } orc_config;
 
 /* Diagnostics, all FP64 sums (see orc_diagnostics). */

@@ -25,7 +25,7 @@ class OrcConfig(C.Structure):
     _fields_ = [
         ("n", C.c_int32 * 3), ("sc", C.c_int32 * 3), ("h", C.c_double * 3), ("dt", C.c_double),
         ("form", C.c_int32), ("shape", C.c_int32), ("deposit", C.c_int32), ("nspecies", C.c_int32),
-        ("mass", C.c_double * 4), ("charge", C.c_double * 4), ("threads", C.c_int32), ("pad_", C.c_int32),
+        ("mass", C.c_double * 4), ("charge", C.c_double * 4), ("threads", C.c_int32), ("resort_every", C.c_int32),
     ]
 
 
@@ -90,7 +90,7 @@ class Oracle:
     """One CPU simulation.  kind = "port" (restatement) or "reference" (pica headers)."""
 
     def __init__(self, n, sc, h, dt, form=FORM_FP64_PLAIN, shape=SHAPE_CIC, deposit=DEPOSIT_DIRECT,
-                 species=((9.10938215e-28, -4.80320427e-10),), threads=0, kind="port"):
+                 species=((9.10938215e-28, -4.80320427e-10),), threads=0, kind="port", resort_every=0):
         self.lib, self.p = _lib(kind)
         cfg = OrcConfig()
         for d in range(3):
@@ -100,6 +100,7 @@ class Oracle:
         for i, (m, q) in enumerate(species):
             cfg.mass[i], cfg.charge[i] = m, q
         cfg.threads = threads
+        cfg.resort_every = int(resort_every)
         self.cfg = cfg
         self.n = tuple(int(v) for v in n)
         self.nsc = tuple(int(n[d]) // int(sc[d]) for d in range(3))

@@ -18,8 +18,9 @@
  *   - periodic J guard fold, YeeSolver::updateB(dt/2), updateE(dt),
  *     updateB(dt/2) with periodic E/B guard fills;
  *   - periodic position wrap and supercell migration in the canonical order
- *     (stayers in slot order, then arrivals by direction code 0..26, each in
- *     source-slot order).
+ *     described in pic_oracle.h (dead slots marked x = -1e300; arrivals by
+ *     direction code, then source slot, fill this step's holes, then append),
+ *     and every resort_every steps a stable re-sort of each supercell by cell.
  */
 #include "pica/math/Constants.h"
 #include "pica/math/Vectors.h"
@@ -34,6 +35,7 @@
 
 #include "pic_oracle.h"
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -66,7 +68,40 @@ struct RefSim {
 
     ~RefSim() { delete grid; for (auto e : ens) delete e; }
 
+    int steps = 0;
     int scLinear(Int3 c) const { return (c.x * nsc.y + c.y) * nsc.z + c.z; }
+    // Dead slots carry x = -1e300 (positions never go below -L, even before the wrap).
+    static bool alive(PArray::ConstParticleRef p) { return p.getPosition().x > -1.0e299; }
+    // Local cell of a particle in supercell s: (lx*Sy + ly)*Sz + lz.
+    int cellKey(PArray::ConstParticleRef p, Int3 sc) const {
+        FP3 x = p.getPosition();
+        int l[3];
+        for (int d = 0; d < 3; d++) {
+            l[d] = (int)std::floor(x[d] * (1.0 / h[d])) - sc[d] * S[d];
+            l[d] = std::min(std::max(l[d], 0), S[d] - 1);
+        }
+        return (l[0] * S.y + l[1]) * S.z + l[2];
+    }
+    // Drop dead slots and sort each supercell by cell (stable).
+    void resort() {
+        const int nscTot = nsc.x * nsc.y * nsc.z;
+        for (auto e : ens) {
+#pragma omp parallel for schedule(dynamic, 8)
+            for (int s = 0; s < nscTot; s++) {
+                Int3 c = scCoords(s);
+                PArray& arr = e->getParticles(c);
+                const PArray& carr = arr;
+                std::vector<std::pair<int, int>> key;
+                for (int p = 0; p < arr.size(); p++)
+                    if (alive(carr[p])) key.push_back({cellKey(carr[p], c), p});
+                std::stable_sort(key.begin(), key.end(),
+                                 [](const std::pair<int, int>& a, const std::pair<int, int>& b) { return a.first < b.first; });
+                PArray out;
+                for (auto& k : key) out.pushBack(carr[k.second]);
+                arr = out;
+            }
+        }
+    }
     Int3 scCoords(int s) const { return Int3(s / (nsc.y * nsc.z), (s / nsc.z) % nsc.y, s % nsc.z); }
 
     void init(const orc_config& c) {
@@ -154,6 +189,7 @@ struct RefSim {
                 const double q = cfg.charge[sp];
                 for (int p = 0; p < arr.size(); p++) {
                     PArray::ParticleRef ref = arr[p];
+                    if (!alive(ref)) continue;
                     FP3 e, b;
                     fi.get(ref.getPosition(), e, b);
                     pusher.push(&ref, e, b);
@@ -177,15 +213,16 @@ struct RefSim {
         const int nscTot = nsc.x * nsc.y * nsc.z;
         for (int sp = 0; sp < cfg.nspecies; sp++) {
             Ensemble& e = *ens[sp];
-            std::vector<std::vector<int>> dirs(nscTot);
+            std::vector<std::vector<int>> dirs(nscTot);   // -1: dead slot
             int localErr = 0;
 #pragma omp parallel for schedule(dynamic, 8) reduction(min : localErr)
             for (int s = 0; s < nscTot; s++) {
                 Int3 o = scCoords(s);
                 PArray& arr = e.getParticles(o);
-                dirs[s].resize(arr.size());
+                dirs[s].assign(arr.size(), -1);
                 for (int p = 0; p < arr.size(); p++) {
                     PArray::ParticleRef ref = arr[p];
+                    if (!alive(ref)) continue;
                     FP3 x = ref.getPosition();
                     for (int d = 0; d < 3; d++) {
                         if (x[d] < 0.0) x[d] += L[d];
@@ -209,7 +246,7 @@ struct RefSim {
                 Int3 o = scCoords(s);
                 for (int p = 0; p < (int)dirs[s].size(); p++) {
                     int code = dirs[s][p];
-                    if (code == 13) continue;
+                    if (code < 0 || code == 13) continue;
                     Int3 ds(code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1);
                     int dst = scLinear(Int3(wrapi(o.x + ds.x, nsc.x), wrapi(o.y + ds.y, nsc.y), wrapi(o.z + ds.z, nsc.z)));
                     migrations.push_back({sp, s, p, dst});
@@ -219,20 +256,42 @@ struct RefSim {
 #pragma omp parallel for schedule(dynamic, 8)
             for (int d = 0; d < nscTot; d++) {
                 Int3 dc = scCoords(d);
-                PArray& own = e.getParticles(dc);
-                for (int p = 0; p < own.size(); p++)
-                    if (dirs[d][p] == 13) next[d].pushBack(own[p]);
+                next[d] = e.getParticles(dc);
+                std::vector<int> holes;
+                for (int p = 0; p < (int)dirs[d].size(); p++)
+                    if (dirs[d][p] >= 0 && dirs[d][p] != 13) {
+                        holes.push_back(p);
+                        PArray::ParticleRef r = next[d][p];
+                        FP3 x = r.getPosition();
+                        x.x = -1.0e300;
+                        r.setPosition(x);
+                    }
+                size_t k = 0;
                 for (int code = 0; code < 27; code++) {
                     if (code == 13) continue;
                     Int3 ds(code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1);
                     int src = scLinear(Int3(wrapi(dc.x - ds.x, nsc.x), wrapi(dc.y - ds.y, nsc.y), wrapi(dc.z - ds.z, nsc.z)));
-                    PArray& arr = e.getParticles(scCoords(src));
+                    const PArray& arr = e.getParticles(scCoords(src));
                     for (int p = 0; p < arr.size(); p++)
-                        if (dirs[src][p] == code) next[d].pushBack(arr[p]);
+                        if (dirs[src][p] == code) {
+                            if (k < holes.size()) {
+                                PArray::ParticleRef r = next[d][holes[k]];
+                                PArray::ConstParticleRef a = arr[p];
+                                r.setPosition(a.getPosition());
+                                r.setP(a.getP());
+                                r.setFactor(a.getFactor());
+                                r.setType(a.getType());
+                            } else {
+                                next[d].pushBack(arr[p]);
+                            }
+                            k++;
+                        }
                 }
             }
             for (int s = 0; s < nscTot; s++) e.getParticles(scCoords(s)) = next[s];
         }
+        steps++;
+        if (cfg.resort_every > 0 && steps % cfg.resort_every == 0) resort();
     }
 };
 
@@ -268,6 +327,7 @@ int ref_load(void* sim, int64_t n, const double* x, const double* y, const doubl
         Int3 c = s->supercellOf(*s->ens[sp], tmp[0]);
         s->ens[sp]->getParticles(c).pushBack(p);
     }
+    s->resort();
     return 0;
 }
 
@@ -319,7 +379,11 @@ int64_t ref_num_particles(void* sim) {
     if (!s) return -1;
     int64_t n = 0;
     int nscTot = s->nsc.x * s->nsc.y * s->nsc.z;
-    for (auto e : s->ens) for (int k = 0; k < nscTot; k++) n += e->getParticles(s->scCoords(k)).size();
+    for (auto e : s->ens)
+        for (int k = 0; k < nscTot; k++) {
+            const PArray& arr = e->getParticles(s->scCoords(k));
+            for (int p = 0; p < arr.size(); p++) n += RefSim::alive(arr[p]) ? 1 : 0;
+        }
     return n;
 }
 
@@ -332,13 +396,15 @@ int ref_get_particles(void* sim, double* x, double* y, double* z, double* ux, do
     for (int sp = 0; sp < s->cfg.nspecies; sp++)
         for (int k = 0; k < nscTot; k++) {
             PArray& arr = s->ens[sp]->getParticles(s->scCoords(k));
-            for (int p = 0; p < arr.size(); p++, o++) {
+            for (int p = 0; p < arr.size(); p++) {
                 PArray::ConstParticleRef r = ((const PArray&)arr)[p];
+                if (!RefSim::alive(r)) continue;
                 FP3 pos = r.getPosition(), u = r.getP();
                 x[o] = pos.x; y[o] = pos.y; z[o] = pos.z;
                 ux[o] = u.x; uy[o] = u.y; uz[o] = u.z; w[o] = r.getFactor();
                 if (species) species[o] = sp;
                 if (supercell) supercell[o] = k;
+                o++;
             }
         }
     return 0;
@@ -349,7 +415,12 @@ int ref_get_counts(void* sim, int32_t* counts) {
     if (!s) return -1;
     int nscTot = s->nsc.x * s->nsc.y * s->nsc.z;
     for (int sp = 0; sp < s->cfg.nspecies; sp++)
-        for (int k = 0; k < nscTot; k++) counts[(size_t)sp * nscTot + k] = s->ens[sp]->getParticles(s->scCoords(k)).size();
+        for (int k = 0; k < nscTot; k++) {
+            const PArray& arr = s->ens[sp]->getParticles(s->scCoords(k));
+            int32_t n = 0;
+            for (int p = 0; p < arr.size(); p++) n += RefSim::alive(arr[p]) ? 1 : 0;
+            counts[(size_t)sp * nscTot + k] = n;
+        }
     return 0;
 }
 

@@ -138,6 +138,9 @@ __global__ void __launch_bounds__(256) k_particleSums(const ParticleSumArgs a, d
         const int cnt = a.count[sp][s];
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
             const int64_t o = start + i;
+            if (a.fp64 ? !aliveX(static_cast<const double*>(a.key[sp])[o])
+                       : static_cast<const uint32_t*>(a.key[sp])[o] == kDeadCell)
+                continue;
             double ux, uy, uz, w;
             if (a.fp64) { ux = asDouble<double>(a.ux[sp], o); uy = asDouble<double>(a.uy[sp], o); uz = asDouble<double>(a.uz[sp], o); w = asDouble<double>(a.w[sp], o); }
             else { ux = asDouble<float>(a.ux[sp], o); uy = asDouble<float>(a.uy[sp], o); uz = asDouble<float>(a.uz[sp], o); w = asDouble<float>(a.w[sp], o); }
@@ -166,6 +169,9 @@ __global__ void __launch_bounds__(256) k_rho(const RhoArgs a, double* rho) {
         const int cnt = a.count[sp][s];
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
             const int64_t o = start + i;
+            if (a.fp64 ? !aliveX(static_cast<const double*>(a.p0[sp])[o])
+                       : static_cast<const uint32_t*>(a.p0[sp])[o] == kDeadCell)
+                continue;
             int lo[3];
             double w[3][3];
             double wt;

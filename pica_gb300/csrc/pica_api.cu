@@ -7,6 +7,7 @@
 #include <functional>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "pica_internal.h"
@@ -21,18 +22,23 @@ constexpr double kPiRef = 3.14159265358; // pica math/Constants.h:10
 inline int wrapHost(int a, int n) { a %= n; return a < 0 ? a + n : a; }
 
 struct SpeciesState {
-    void* buf[2][8] = {};
+    void* buf[2][8] = {};        // A = buf[cur], B = buf[1 - cur]
     int64_t slots[2] = {0, 0};   // allocated slots of each buffer
-    uint8_t* dir = nullptr;
-    int64_t dirSlots = 0;
+    uint8_t* dir = nullptr;      // direction code per slot
+    int32_t* llist = nullptr;    // leaver slots per supercell (at [start, start + nleave))
+    int64_t slotArrays = 0;      // allocated entries of dir / llist
+    void* outbox[8] = {};        // overflow rebuild: leavers gathered per source supercell
+    int64_t outSlots = 0;
     int64_t* d_start = nullptr;
     int32_t* d_cap = nullptr;
-    int32_t* d_count = nullptr;
-    int32_t* d_nstay = nullptr;
+    int32_t* d_count = nullptr;  // used slots, dead ones included
+    int32_t* d_alive = nullptr;  // live particles
     int32_t* d_nleave = nullptr;
     int32_t* d_needed = nullptr;
+    int32_t* d_neededAlive = nullptr;
     int64_t* d_start2 = nullptr;
     int32_t* d_cap2 = nullptr;
+    int64_t* d_outOff = nullptr;
     std::vector<int64_t> h_start;
     std::vector<int32_t> h_cap;
     int64_t layoutSlots = 0;     // sum of caps of the current layout
@@ -61,6 +67,7 @@ struct pica_ctx {
     unsigned long long* jacc[3] = {};
     double kmax = 1.0;      // power of two bounding |q w| max(c, h/dt) (sets the J fixed-point unit)
     int jfrac = 40;         // fraction bits of the J fixed point (see pica_internal.h)
+    int tileSplit = 16;     // low bits of the split shared-memory tile sums (FP32 form)
     std::string err;
     int64_t launches = 0;
     int64_t steps = 0;
@@ -123,7 +130,12 @@ void updateJFrac(pica_ctx* ctx) {
     int64_t cover = 1;
     for (int d = 0; d < 3; d++) cover *= (ctx->cfg.sc[d] + 2 * kG + 1 + ctx->cfg.sc[d] - 1) / ctx->cfg.sc[d];
     const double worst = (double)cover * (double)std::max<int64_t>(maxCaps, 1) + 1.0;
-    ctx->jfrac = std::min(kJFracBitsMax, 62 - (int)std::ceil(std::log2(worst)));
+    // Shared-memory tile: a node receives at most one contribution per particle of
+    // its supercell (all species): low part L bits summed unsigned, high part signed,
+    // each sum below 2^31: L = 31 - b and F <= 62 - 2b with b = bits(largest count).
+    const int b = (int)std::ceil(std::log2((double)std::max<int64_t>(maxCaps, 1) + 1.0));
+    ctx->tileSplit = 31 - b;
+    ctx->jfrac = std::min(std::min(kJFracBitsMax, 62 - (int)std::ceil(std::log2(worst))), 62 - 2 * b);
 }
 
 int ensureBuffer(pica_ctx* ctx, int spi, int b, int64_t slots) {
@@ -139,15 +151,42 @@ int ensureBuffer(pica_ctx* ctx, int spi, int b, int64_t slots) {
     return PICA_OK;
 }
 
-int ensureDir(pica_ctx* ctx, int spi, int64_t slots) {
+int ensureSlotArrays(pica_ctx* ctx, int spi, int64_t slots) {
     SpeciesState& S = ctx->sp[spi];
-    if (S.dirSlots >= slots) return PICA_OK;
+    if (S.slotArrays >= slots) return PICA_OK;
     if (S.dir) CK(cudaFree(S.dir));
+    if (S.llist) CK(cudaFree(S.llist));
     S.dir = nullptr;
-    S.dirSlots = 0;
+    S.llist = nullptr;
+    S.slotArrays = 0;
     CK(cudaMalloc(&S.dir, std::max<int64_t>(slots, 1)));
-    S.dirSlots = slots;
+    CK(cudaMalloc(&S.llist, std::max<int64_t>(slots, 1) * 4));
+    S.slotArrays = slots;
     return PICA_OK;
+}
+
+int ensureOutbox(pica_ctx* ctx, int spi, int64_t slots) {
+    SpeciesState& S = ctx->sp[spi];
+    if (S.outSlots >= slots) return PICA_OK;
+    for (int k = 0; k < ctx->ncomp; k++) {
+        if (S.outbox[k]) CK(cudaFree(S.outbox[k]));
+        S.outbox[k] = nullptr;
+    }
+    S.outSlots = 0;
+    for (int k = 0; k < ctx->ncomp; k++) CK(cudaMalloc(&S.outbox[k], std::max<int64_t>(slots, 1) * ctx->compBytes[k]));
+    S.outSlots = slots;
+    return PICA_OK;
+}
+
+template <class P>
+P ptrsOf(void* const* p);
+template <>
+PlainPtrs ptrsOf<PlainPtrs>(void* const* p) {
+    return PlainPtrs{(double*)p[0], (double*)p[1], (double*)p[2], (double*)p[3], (double*)p[4], (double*)p[5], (double*)p[6]};
+}
+template <>
+CellPtrs ptrsOf<CellPtrs>(void* const* p) {
+    return CellPtrs{(uint32_t*)p[0], (float*)p[1], (float*)p[2], (float*)p[3], (float*)p[4], (float*)p[5], (float*)p[6], (float*)p[7]};
 }
 
 PlainPtrs plainPtrs(pica_ctx* c, int spi, int b) {
@@ -237,17 +276,20 @@ int pica_ctx_create(const pica_config* cfg, pica_ctx** out) {
         SpeciesState& S = ctx->sp[s];
         const size_t n = ctx->nscTot;
         if (cudaMalloc(&S.d_start, n * 8) || cudaMalloc(&S.d_cap, n * 4) || cudaMalloc(&S.d_count, n * 4) ||
-            cudaMalloc(&S.d_nstay, n * 4) || cudaMalloc(&S.d_nleave, n * 4) || cudaMalloc(&S.d_needed, n * 4) ||
-            cudaMalloc(&S.d_start2, n * 8) || cudaMalloc(&S.d_cap2, n * 4))
+            cudaMalloc(&S.d_alive, n * 4) || cudaMalloc(&S.d_nleave, n * 4) || cudaMalloc(&S.d_needed, n * 4) ||
+            cudaMalloc(&S.d_neededAlive, n * 4) || cudaMalloc(&S.d_start2, n * 8) || cudaMalloc(&S.d_cap2, n * 4) ||
+            cudaMalloc(&S.d_outOff, n * 8))
             return bail(PICA_ERR_OOM);
         std::vector<int32_t> zero(n, 0);
         int64_t total;
         layoutFrom(ctx, zero, S.h_start, S.h_cap, total);
         S.layoutSlots = total;
-        if ((rc = ensureBuffer(ctx, s, 0, total)) || (rc = ensureBuffer(ctx, s, 1, total)) || (rc = ensureDir(ctx, s, total)))
+        if ((rc = ensureBuffer(ctx, s, 0, total)) || (rc = ensureBuffer(ctx, s, 1, total)) ||
+            (rc = ensureSlotArrays(ctx, s, total)))
             return bail(rc);
         if (cudaMemcpy(S.d_start, S.h_start.data(), n * 8, cudaMemcpyHostToDevice) ||
-            cudaMemcpy(S.d_cap, S.h_cap.data(), n * 4, cudaMemcpyHostToDevice) || cudaMemset(S.d_count, 0, n * 4))
+            cudaMemcpy(S.d_cap, S.h_cap.data(), n * 4, cudaMemcpyHostToDevice) || cudaMemset(S.d_count, 0, n * 4) ||
+            cudaMemset(S.d_alive, 0, n * 4) || cudaMemset(S.d_nleave, 0, n * 4))
             return bail(PICA_ERR_CUDA);
     }
     ctx->redCount = std::max<int64_t>(2 * kReduceBlocks, 2 * (int64_t)ctx->nscTot) + 8;
@@ -267,8 +309,10 @@ int pica_ctx_destroy(pica_ctx* ctx) {
     for (auto p : ctx->jacc) if (p) cudaFree(p);
     for (auto& S : ctx->sp) {
         for (auto& b : S.buf) for (auto p : b) if (p) cudaFree(p);
-        for (void* p : {(void*)S.dir, (void*)S.d_start, (void*)S.d_cap, (void*)S.d_count, (void*)S.d_nstay,
-                        (void*)S.d_nleave, (void*)S.d_needed, (void*)S.d_start2, (void*)S.d_cap2})
+        for (auto p : S.outbox) if (p) cudaFree(p);
+        for (void* p : {(void*)S.dir, (void*)S.llist, (void*)S.d_start, (void*)S.d_cap, (void*)S.d_count,
+                        (void*)S.d_alive, (void*)S.d_nleave, (void*)S.d_needed, (void*)S.d_neededAlive,
+                        (void*)S.d_start2, (void*)S.d_cap2, (void*)S.d_outOff})
             if (p) cudaFree(p);
     }
     if (ctx->d_flags) cudaFree(ctx->d_flags);
@@ -307,8 +351,11 @@ int pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const doubl
         scInv[d] = 1.0 / ((double)c.sc[d] * ((L - 0.0) / (double)c.n[d]));  // EnsembleSupercells.h:31-33
         invh[d] = 1.0 / c.h[d];
     }
-    // Route: key = species * nscTot + supercell; FP32 form also converts to cell + offset.
-    std::vector<int32_t> key(n);
+    // Route: key = species * nscTot + supercell and the local cell inside the supercell
+    // (particles are stored by supercell, then cell, stably); FP32 form also converts
+    // to cell + offset.
+    const int S3 = c.sc[0] * c.sc[1] * c.sc[2];
+    std::vector<int32_t> key(n), lcell(n);
     std::vector<uint32_t> cell(ctx->fp64 ? 0 : n);
     std::vector<float> off(ctx->fp64 ? 0 : 3 * n);
     int bad = 0;
@@ -323,10 +370,12 @@ int pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const doubl
             for (double v : uu) ok = ok && std::isfinite(v);
             if (!ok) { bad = 2; key[i] = 0; continue; }
             int s3[3];
+            int l3[3];
             if (ctx->fp64) {
                 for (int d = 0; d < 3; d++) {
                     s3[d] = (int)std::floor((p[d] - 0.0) * scInv[d]);
                     s3[d] = std::min(std::max(s3[d], 0), ctx->nsc[d] - 1);
+                    l3[d] = std::min(std::max((int)std::floor(p[d] * invh[d]) - s3[d] * c.sc[d], 0), c.sc[d] - 1);
                 }
             } else {
                 int cc[3];
@@ -339,10 +388,12 @@ int pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const doubl
                     cc[d] = wrapHost(cc[d], c.n[d]);
                     off[3 * i + d] = o;
                     s3[d] = cc[d] / c.sc[d];
+                    l3[d] = cc[d] - s3[d] * c.sc[d];
                 }
                 cell[i] = packCell(cc[0], cc[1], cc[2]);
             }
             key[i] = q * ctx->nscTot + scLinear(ctx, s3[0], s3[1], s3[2]);
+            lcell[i] = (l3[0] * c.sc[1] + l3[1]) * c.sc[2] + l3[2];
         }
     });
     if (bad == 1) return fail(ctx, PICA_ERR_INVALID, "species index out of range");
@@ -369,21 +420,29 @@ int pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const doubl
         layoutFrom(ctx, counts, S.h_start, S.h_cap, total);
         S.layoutSlots = total;
         int rc;
-        if ((rc = ensureBuffer(ctx, q, 0, total)) || (rc = ensureBuffer(ctx, q, 1, total)) || (rc = ensureDir(ctx, q, total)))
+        if ((rc = ensureBuffer(ctx, q, 0, total)) || (rc = ensureBuffer(ctx, q, 1, total)) ||
+            (rc = ensureSlotArrays(ctx, q, total)))
             return rc;
         CK(cudaMemcpy(S.d_start, S.h_start.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S.d_cap, S.h_cap.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S.d_count, counts.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.d_alive, counts.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemset(S.d_nleave, 0, ctx->nscTot * 4));
     }
     updateJFrac(ctx);
-    // Slot of each particle: start of its supercell + rank within the key (stable).
-    std::vector<int64_t> fill(nkeys, 0);
-    std::vector<int64_t> slot(n);
-    for (int64_t i = 0; i < n; i++) {
-        const int32_t k = key[i];
-        const int q = k / ctx->nscTot, s = k % ctx->nscTot;
-        slot[i] = ctx->sp[q].h_start[s] + fill[k]++;
+    // Slot of each particle: start of its supercell + its rank by (local cell, input order).
+    std::vector<int64_t> base2((size_t)nkeys * S3 + 1, 0);
+    for (int64_t i = 0; i < n; i++) base2[(size_t)key[i] * S3 + lcell[i] + 1]++;
+    for (int64_t k = 0; k < nkeys; k++) {
+        int64_t run = ctx->sp[k / ctx->nscTot].h_start[k % ctx->nscTot];
+        for (int l = 0; l < S3; l++) {
+            const int64_t c2 = base2[(size_t)k * S3 + l + 1];
+            base2[(size_t)k * S3 + l] = run;
+            run += c2;
+        }
     }
+    std::vector<int64_t> slot(n);
+    for (int64_t i = 0; i < n; i++) slot[i] = base2[(size_t)key[i] * S3 + lcell[i]]++;
     std::vector<int32_t> spOf(n);
     for (int64_t i = 0; i < n; i++) spOf[i] = key[i] / ctx->nscTot;
     ctx->cur = 0;
@@ -419,8 +478,9 @@ int64_t pica_num_particles(pica_ctx* ctx) {
     if (!ctx) return PICA_ERR_INVALID;
     int64_t total = 0;
     std::vector<int32_t> counts(ctx->nscTot);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ctx, PICA_ERR_CUDA, "synchronize failed");
     for (int q = 0; q < ctx->cfg.nspecies; q++) {
-        if (cudaMemcpy(counts.data(), ctx->sp[q].d_count, ctx->nscTot * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        if (cudaMemcpy(counts.data(), ctx->sp[q].d_alive, ctx->nscTot * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
             return fail(ctx, PICA_ERR_CUDA, "count download failed");
         for (int32_t v : counts) total += v;
     }
@@ -431,7 +491,7 @@ int pica_get_counts(pica_ctx* ctx, int32_t* counts) {
     if (!ctx || !counts) return PICA_ERR_INVALID;
     CK(cudaStreamSynchronize(ctx->stream));
     for (int q = 0; q < ctx->cfg.nspecies; q++)
-        CK(cudaMemcpy(counts + (size_t)q * ctx->nscTot, ctx->sp[q].d_count, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(counts + (size_t)q * ctx->nscTot, ctx->sp[q].d_alive, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
     return PICA_OK;
 }
 
@@ -455,8 +515,11 @@ int pica_download_particles(pica_ctx* ctx, double* x, double* y, double* z, doub
         }
         for (int s = 0; s < ctx->nscTot; s++) {
             const int64_t st = S.h_start[s];
-            for (int i = 0; i < counts[s]; i++, o++) {
+            for (int i = 0; i < counts[s]; i++) {
                 const int64_t slot = st + i;
+                if (ctx->fp64 ? !aliveX(((double*)host[0].data())[slot])
+                              : ((uint32_t*)host[0].data())[slot] == kDeadCell)
+                    continue;
                 if (ctx->fp64) {
                     for (int k = 0; k < 7; k++)
                         if (out[k]) out[k][o] = ((double*)host[k].data())[slot];
@@ -473,6 +536,7 @@ int pica_download_particles(pica_ctx* ctx, double* x, double* y, double* z, doub
                 }
                 if (species) species[o] = q;
                 if (supercell) supercell[o] = s;
+                o++;
             }
         }
     }
@@ -531,13 +595,14 @@ int pica_push_deposit(pica_ctx* ctx) {
         for (int k = 0; k < 6; k++) a.eb[k] = ctx->f[k];
         for (int k = 0; k < 3; k++) { a.jacc[k] = ctx->jacc[k]; a.j[k] = ctx->f[6 + k]; }
         a.invUnit = std::ldexp(1.0, ctx->jfrac) / ctx->kmax;
+        a.tileSplit = ctx->tileSplit;
         a.norm = 1.0 / (c.h[0] * c.h[1] * c.h[2]);   // CurrentDepositorYeeGrid.h:203
         a.flags = ctx->d_flags;
         for (int q = 0; q < c.nspecies; q++) {
             SpeciesState& S = ctx->sp[q];
             auto& sa = a.sp[q];
             sa.start = S.d_start; sa.cap = S.d_cap; sa.count = S.d_count;
-            sa.nstay = S.d_nstay; sa.nleave = S.d_nleave; sa.dir = S.dir;
+            sa.nleave = S.d_nleave; sa.llist = S.llist; sa.dir = S.dir;
             sa.ec = c.charge[q] * c.dt / (2.0 * c.mass[q] * kC);   // BorisPusher.h:29
             sa.q = c.charge[q];
             for (int d = 0; d < 3; d++) sa.kq[d] = -c.charge[q] * (c.h[d] / c.dt);
@@ -547,12 +612,12 @@ int pica_push_deposit(pica_ctx* ctx) {
     if (ctx->fp64) {
         PushArgs<PlainPtrs> a{};
         fill(a);
-        for (int q = 0; q < c.nspecies; q++) { a.sp[q].in = plainPtrs(ctx, q, ctx->cur); a.sp[q].out = plainPtrs(ctx, q, 1 - ctx->cur); }
+        for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = plainPtrs(ctx, q, ctx->cur); a.sp[q].out = plainPtrs(ctx, q, 1 - ctx->cur); }
         CKL(launchPushPlain(a, c.shape, c.deposit, ctx->stream));
     } else {
         PushArgs<CellPtrs> a{};
         fill(a);
-        for (int q = 0; q < c.nspecies; q++) { a.sp[q].in = cellPtrs(ctx, q, ctx->cur); a.sp[q].out = cellPtrs(ctx, q, 1 - ctx->cur); }
+        for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = cellPtrs(ctx, q, ctx->cur); a.sp[q].out = cellPtrs(ctx, q, 1 - ctx->cur); }
         CKL(launchPushCell(a, c.shape, c.deposit, ctx->stream));
     }
     ctx->launches++;
@@ -587,75 +652,141 @@ int pica_update_e(pica_ctx* ctx, double dt) {
     return PICA_OK;
 }
 
+}  // extern "C"
+
+// Upload a new layout (start/cap per supercell) into the *2 arrays; returns its slot total.
+static int stageLayout(pica_ctx* ctx, int q, const std::vector<int32_t>& counts, int64_t& total) {
+    SpeciesState& S = ctx->sp[q];
+    std::vector<int64_t> nstart;
+    std::vector<int32_t> ncap;
+    layoutFrom(ctx, counts, nstart, ncap, total);
+    CK(cudaMemcpy(S.d_start2, nstart.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(S.d_cap2, ncap.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
+    S.h_start.swap(nstart);
+    S.h_cap.swap(ncap);
+    S.layoutSlots = total;
+    return PICA_OK;
+}
+
+template <class P>
+static int migrateImpl(pica_ctx* ctx) {
+    const pica_config& c = ctx->cfg;
+    const int A = ctx->cur, B = 1 - ctx->cur;
+    auto args = [&](MigrateArgs<P>& a) {
+        for (int d = 0; d < 3; d++) { a.nsc[d] = ctx->nsc[d]; a.S[d] = c.sc[d]; a.invh[d] = 1.0 / c.h[d]; }
+        a.nspecies = c.nspecies;
+        a.flags = ctx->d_flags;
+        int32_t maxCap = 0;
+        for (int q = 0; q < c.nspecies; q++) {
+            SpeciesState& S = ctx->sp[q];
+            for (int32_t v : S.h_cap) maxCap = std::max(maxCap, v);
+            auto& m = a.sp[q];
+            m.a = ptrsOf<P>(S.buf[A]); m.b = ptrsOf<P>(S.buf[B]); m.dst = ptrsOf<P>(S.buf[B]);
+            m.outbox = ptrsOf<P>(S.outbox);
+            m.start = S.d_start; m.cap = S.d_cap; m.count = S.d_count; m.alive = S.d_alive;
+            m.nleave = S.d_nleave; m.llist = S.llist; m.dir = S.dir;
+            m.needed = S.d_needed; m.neededAlive = S.d_neededAlive;
+            m.newStart = S.d_start2; m.outOff = S.d_outOff;
+        }
+        a.bitmapWords = (maxCap + 31) / 32;
+    };
+    MigrateArgs<P> a{};
+    args(a);
+    if ((size_t)a.bitmapWords * 4 > 200 * 1024) return fail(ctx, PICA_ERR_LIMIT, "supercell capacity too large for the leaver sort");
+    auto launch = [&](MigrateArgs<P>& m, int stage) -> int {
+        if constexpr (std::is_same<P, PlainPtrs>::value) return launchMigratePlain(m, stage, ctx->stream);
+        else return launchMigrateCell(m, stage, ctx->stream);
+    };
+    CKL(launch(a, kSortLeavers));
+    CKL(launch(a, kCountArrivals));
+    ctx->launches += 2;
+    CK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_flags[0]) return fail(ctx, ctx->h_flags[0], "a particle crossed more than one supercell in one step");
+    if (!ctx->h_flags[1]) {
+        CKL(launch(a, kFill));
+        ctx->launches++;
+    } else {
+        // Overflow: gather the leavers into the outbox (B is then free), rebuild A + arrivals
+        // into B with capacities for the new counts, and swap.
+        for (int q = 0; q < c.nspecies; q++) {
+            SpeciesState& S = ctx->sp[q];
+            std::vector<int32_t> nl(ctx->nscTot), needed(ctx->nscTot);
+            CK(cudaMemcpy(nl.data(), S.d_nleave, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
+            std::vector<int64_t> off(ctx->nscTot);
+            int64_t tot = 0;
+            for (int k = 0; k < ctx->nscTot; k++) { off[k] = tot; tot += nl[k]; }
+            int rc;
+            if ((rc = ensureOutbox(ctx, q, tot))) return rc;
+            CK(cudaMemcpy(S.d_outOff, off.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice));
+        }
+        args(a);
+        CKL(launch(a, kGatherOutbox));
+        ctx->launches++;
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (int q = 0; q < c.nspecies; q++) {
+            SpeciesState& S = ctx->sp[q];
+            std::vector<int32_t> needed(ctx->nscTot);
+            CK(cudaMemcpy(needed.data(), S.d_needed, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
+            int64_t total;
+            int rc;
+            if ((rc = stageLayout(ctx, q, needed, total)) || (rc = ensureBuffer(ctx, q, B, total))) return rc;
+        }
+        args(a);   // buffer B may have been reallocated
+        CKL(launch(a, kRebuild));
+        ctx->launches++;
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (int q = 0; q < c.nspecies; q++) {
+            SpeciesState& S = ctx->sp[q];
+            std::swap(S.d_start, S.d_start2);
+            std::swap(S.d_cap, S.d_cap2);
+            int rc;
+            if ((rc = ensureBuffer(ctx, q, A, S.layoutSlots)) || (rc = ensureSlotArrays(ctx, q, S.layoutSlots))) return rc;
+        }
+        ctx->cur = B;
+        updateJFrac(ctx);
+    }
+    ctx->steps++;
+    if (c.resort_every > 0 && ctx->steps % c.resort_every == 0) {
+        // Compact every supercell and sort it by cell into the other buffer, with
+        // capacities recomputed from the live counts.
+        const int A2 = ctx->cur, B2 = 1 - ctx->cur;
+        for (int q = 0; q < c.nspecies; q++) {
+            SpeciesState& S = ctx->sp[q];
+            std::vector<int32_t> alive(ctx->nscTot);
+            CK(cudaStreamSynchronize(ctx->stream));
+            CK(cudaMemcpy(alive.data(), S.d_alive, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
+            int64_t total;
+            int rc;
+            if ((rc = stageLayout(ctx, q, alive, total)) || (rc = ensureBuffer(ctx, q, B2, total)) ||
+                (rc = ensureSlotArrays(ctx, q, total)))
+                return rc;
+        }
+        MigrateArgs<P> r{};
+        args(r);   // a = current buffer A2, dst = B2
+        CKL(launch(r, kResort));
+        ctx->launches++;
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (int q = 0; q < c.nspecies; q++) {
+            SpeciesState& S = ctx->sp[q];
+            std::swap(S.d_start, S.d_start2);
+            std::swap(S.d_cap, S.d_cap2);
+            int rc;
+            if ((rc = ensureBuffer(ctx, q, A2, S.layoutSlots))) return rc;
+        }
+        ctx->cur = B2;
+        updateJFrac(ctx);
+    }
+    return PICA_OK;
+}
+
+extern "C" {
+
 int pica_migrate(pica_ctx* ctx) {
     if (!ctx) return PICA_ERR_INVALID;
     if (!ctx->pending) return fail(ctx, PICA_ERR_STATE, "migrate without push_deposit");
-    const pica_config& c = ctx->cfg;
-    const int other = 1 - ctx->cur;
-    auto fill = [&](auto& a, bool rebuild) {
-        for (int d = 0; d < 3; d++) a.nsc[d] = ctx->nsc[d];
-        a.nspecies = c.nspecies;
-        a.flags = ctx->d_flags;
-        for (int q = 0; q < c.nspecies; q++) {
-            SpeciesState& S = ctx->sp[q];
-            auto& m = a.sp[q];
-            m.start = S.d_start; m.cap = S.d_cap; m.nstay = S.d_nstay; m.nleave = S.d_nleave; m.dir = S.dir;
-            m.count = S.d_count; m.needed = S.d_needed; m.newStart = rebuild ? S.d_start2 : nullptr;
-        }
-    };
-    auto launch = [&](bool rebuild) -> int {
-        if (ctx->fp64) {
-            MigrateArgs<PlainPtrs> a{};
-            fill(a, rebuild);
-            for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = plainPtrs(ctx, q, other); a.sp[q].dst = plainPtrs(ctx, q, ctx->cur); }
-            return launchMigratePlain(a, rebuild, ctx->stream);
-        }
-        MigrateArgs<CellPtrs> a{};
-        fill(a, rebuild);
-        for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = cellPtrs(ctx, q, other); a.sp[q].dst = cellPtrs(ctx, q, ctx->cur); }
-        return launchMigrateCell(a, rebuild, ctx->stream);
-    };
-    CKL(launch(false));
-    ctx->launches++;
-    CK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
     ctx->pending = false;
-    ctx->steps++;
-    if (ctx->h_flags[0]) return fail(ctx, ctx->h_flags[0], "a particle crossed more than one supercell in one step");
-    const bool rebalance = c.resort_every > 0 && ctx->steps % c.resort_every == 0;
-    if (!ctx->h_flags[1] && !rebalance) {
-        ctx->cur = other;
-        return PICA_OK;
-    }
-    // Rebuild into buffer `cur` with capacities recomputed from stayers + arrivals.
-    for (int q = 0; q < c.nspecies; q++) {
-        SpeciesState& S = ctx->sp[q];
-        std::vector<int32_t> needed(ctx->nscTot);
-        CK(cudaMemcpy(needed.data(), S.d_needed, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
-        std::vector<int64_t> nstart;
-        std::vector<int32_t> ncap;
-        int64_t total;
-        layoutFrom(ctx, needed, nstart, ncap, total);
-        int rc;
-        if ((rc = ensureBuffer(ctx, q, ctx->cur, total))) return rc;
-        CK(cudaMemcpy(S.d_start2, nstart.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(S.d_cap2, ncap.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
-        S.h_start.swap(nstart);
-        S.h_cap.swap(ncap);
-        S.layoutSlots = total;
-    }
-    updateJFrac(ctx);
-    CKL(launch(true));
-    ctx->launches++;
-    CK(cudaStreamSynchronize(ctx->stream));
-    for (int q = 0; q < c.nspecies; q++) {
-        SpeciesState& S = ctx->sp[q];
-        std::swap(S.d_start, S.d_start2);
-        std::swap(S.d_cap, S.d_cap2);
-        int rc;
-        if ((rc = ensureBuffer(ctx, q, other, S.layoutSlots)) || (rc = ensureDir(ctx, q, S.layoutSlots))) return rc;
-    }
-    return PICA_OK;   // data stays in buffer `cur`
+    return ctx->fp64 ? migrateImpl<PlainPtrs>(ctx) : migrateImpl<CellPtrs>(ctx);
 }
 
 int pica_step(pica_ctx* ctx, int32_t nsteps) {
@@ -728,6 +859,7 @@ int pica_diagnostics(pica_ctx* ctx, double bg, pica_diag* out) {
         void* const* b = ctx->sp[q].buf[ctx->cur];
         const int o = ctx->fp64 ? 3 : 4;
         a.ux[q] = b[o]; a.uy[q] = b[o + 1]; a.uz[q] = b[o + 2]; a.w[q] = b[o + 3];
+        a.key[q] = b[0];
         a.start[q] = ctx->sp[q].d_start; a.count[q] = ctx->sp[q].d_count;
         a.mc2[q] = c.mass[q] * kC * kC; a.q[q] = c.charge[q];
     }

@@ -4,15 +4,18 @@
 //   fields  : 9 arrays (ex ey ez bx by bz jx jy jz) of N^3 Real, z fastest,
 //             index (i*ny + j)*nz + k -- pica's Array3d layout without guards
 //             (periodicity is handled by index wrap in every kernel).
-//   particles, per species: two SoA buffers A/B of `slots` entries.  Supercell
-//             s owns slots [start[s], start[s] + cap[s]); its count[s] live
-//             particles are packed at the front, in ensemble order.
-//             FP64 plain form : x y z ux uy uz w            (double, 56 B)
-//             FP32 cell form  : cell(uint32 packed) ox oy oz ux uy uz w (4 B each, 32 B)
-//             The push kernel reads buffer `cur` and writes the other one:
-//             stayers packed at the front of the supercell's range, leavers
-//             packed backwards from its end with a direction byte each; the
-//             migrate kernel then appends arrivals after the stayers in place.
+//   particles, per species: SoA buffers A (current) and B (side buffer) of
+//             `slots` entries.  Supercell s owns slots [start[s], start[s] +
+//             cap[s]); slots [0, count[s]) of it are used, some of them dead.
+//             FP64 plain form : x y z ux uy uz w            (double, 56 B; dead: x = -1e300)
+//             FP32 cell form  : cell(uint32 packed) ox oy oz ux uy uz w (4 B each, 32 B;
+//                               dead: cell = 0xFFFFFFFF)
+//   A step: the push kernel updates A in place; a particle that leaves its
+//   supercell is copied to B at its own slot index, its slot in A becomes
+//   dead and the slot joins the supercell's leaver list.  Migration fills
+//   each destination's fresh holes with its arrivals (canonical order), then
+//   appends.  Every resort_every steps each supercell is compacted and
+//   sorted by cell into B, and A and B swap.
 #pragma once
 
 #include <cstdint>
@@ -51,15 +54,21 @@ struct CellPtrs {   // FP32 cell form particle SoA
     float *ox, *oy, *oz, *ux, *uy, *uz, *w;
 };
 
+// Dead-slot markers.
+constexpr double kDeadX = -1.0e300;          // FP64 form: x of a dead slot
+constexpr uint32_t kDeadCell = 0xFFFFFFFFu;  // FP32 form: cell of a dead slot
+__host__ __device__ inline bool aliveX(double x) { return x > -1.0e299; }
+
 template <class P>
 struct SpeciesArgs {
-    P in, out;
+    P buf;             // A: updated in place
+    P out;             // B: leaver copies at their own slot index
     const int64_t* start;
     const int32_t* cap;
     const int32_t* count;
-    int32_t* nstay;
-    int32_t* nleave;
-    uint8_t* dir;      // direction byte per slot of the output buffer
+    int32_t* nleave;   // leavers per supercell (this step)
+    int32_t* llist;    // leaver slots, list of supercell s at [start[s], start[s] + nleave[s])
+    uint8_t* dir;      // direction code per slot (valid for leavers)
     double ec;         // q dt / (2 m c)   (BorisPusher.h:29)
     double q;          // charge
     double kq[3];      // -q h_d / dt      (Esirkepov current factor per unit weight)
@@ -75,6 +84,7 @@ struct PushArgs {
     const void* eb[6];  // ex ey ez bx by bz (Real)
     unsigned long long* jacc[3];  // FP32 form: J accumulators, fixed point (unit kmax * 2^-F)
     double invUnit;     // FP32 form: 2^F / kmax, current contribution -> fixed-point units
+    int tileSplit;      // FP32 form: low bits L of the split shared-memory tile sums
     void* j[3];         // FP64 form: jx jy jz (double), summed with FP64 atomics
     double norm;        // FP64 form: 1 / (hx hy hz)
     int* flags;         // flags[0]: error code (0 = ok)
@@ -83,22 +93,29 @@ struct PushArgs {
 
 template <class P>
 struct MigrateSpecies {
-    P buf;                  // the buffer written by the push kernel
-    P dst;                  // rebuild destination (new layout)
+    P a;                    // A (current)
+    P b;                    // B (leaver copies at their slot index)
+    P dst;                  // rebuild / resort destination (new layout)
+    P outbox;               // rebuild: leaver copies gathered per source supercell
     const int64_t* start;
     const int32_t* cap;
-    const int32_t* nstay;
+    int32_t* count;         // used slots (incl. dead)
+    int32_t* alive;         // live particles
     const int32_t* nleave;
+    int32_t* llist;
     const uint8_t* dir;
-    int32_t* count;         // in-place migrate: new counts
-    int32_t* needed;        // stayers + arrivals (always written)
-    const int64_t* newStart;// rebuild: new layout starts
+    int32_t* needed;        // count after migration
+    int32_t* neededAlive;   // live particles after migration
+    const int64_t* newStart;// rebuild / resort: new layout
+    const int64_t* outOff;  // rebuild: first outbox entry of each source supercell
 };
 
 template <class P>
 struct MigrateArgs {
-    int nsc[3];
+    int nsc[3], S[3];
     int nspecies;
+    double invh[3];         // FP64 resort: local cell from x
+    int bitmapWords;        // leaver sort: 32-bit words covering the largest count
     int* flags;             // flags[0] error code, flags[1] overflow
     MigrateSpecies<P> sp[kMaxSpecies];
 };
@@ -106,8 +123,10 @@ struct MigrateArgs {
 // Push launchers (push_fp64.cu / push_fp32.cu).  Return cudaError_t as int.
 int launchPushPlain(const PushArgs<PlainPtrs>& a, int shape, int deposit, cudaStream_t s);
 int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int deposit, cudaStream_t s);
-int launchMigratePlain(const MigrateArgs<PlainPtrs>& a, bool rebuild, cudaStream_t s);
-int launchMigrateCell(const MigrateArgs<CellPtrs>& a, bool rebuild, cudaStream_t s);
+// Migration stages.
+enum MigrateStage { kSortLeavers = 0, kCountArrivals = 1, kFill = 2, kGatherOutbox = 3, kRebuild = 4, kResort = 5 };
+int launchMigratePlain(const MigrateArgs<PlainPtrs>& a, int stage, cudaStream_t s);
+int launchMigrateCell(const MigrateArgs<CellPtrs>& a, int stage, cudaStream_t s);
 
 // Grid launchers (grid_kernels.cu).  `fp64` selects double vs float arrays.
 // J = Jacc * scale (Real), then Jacc = 0.
@@ -123,6 +142,7 @@ int launchFieldEnergy(bool fp64, void* const* f, int64_t nodes, double* partial,
 struct ParticleSumArgs {
     bool fp64;
     int nspecies, nscTot;
+    const void* key[kMaxSpecies];   // x (FP64) or packed cell (FP32): dead-slot test
     const void* ux[kMaxSpecies];
     const void* uy[kMaxSpecies];
     const void* uz[kMaxSpecies];

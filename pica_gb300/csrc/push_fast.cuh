@@ -17,10 +17,12 @@
 //    shared-memory atomics per lane.  Compared with one atomic per
 //    contribution per particle this removes the 32-way same-address
 //    serialisation of the shared-memory atomics.
-//  * Particles whose window changes are queued in shared memory and deposited
-//    after the chunk, densely, on the general 4- (TSC) or 3-node (CIC) window.
-//  * Outputs wait in shared memory until one block-wide prefix per chunk gives
-//    their stable rank, so the ensemble order matches the general kernel.
+//  * Particles whose window changes are queued in a per-warp shared-memory
+//    queue and deposited densely on the general 4- (TSC) or 3-node (CIC)
+//    window when it fills and at the end.
+//  * Stayers are written back in place; leavers go to the side buffer at
+//    their own slot (see pica_internal.h), so the kernel needs no block-wide
+//    synchronisation between the tile staging and the final tile flush.
 #pragma once
 
 #include "push_kernels.cuh"
@@ -64,8 +66,7 @@ __device__ __forceinline__ void warpTransposeSum(const float* v, bool take, int 
 // starting at tile node b (per dimension).  TSC: NWn = 3 nodes, 2 faces;
 // CIC: NWn = 2 nodes, 1 face.  Layout: Jx (faces x NWn x NWn), then Jy, then Jz.
 template <int NWn>
-__device__ __forceinline__ unsigned long long* windowAddr(unsigned long long* jt, int TT, int T1, int T2, const int* b,
-                                                          int j) {
+__device__ __forceinline__ int windowIdx(int TT, int T1, int T2, const int* b, int j) {
     constexpr int F = NWn - 1;            // faces per dimension
     constexpr int per = F * NWn * NWn;    // contributions per component
     const int c = j / per, r = j - c * per;
@@ -73,7 +74,7 @@ __device__ __forceinline__ unsigned long long* windowAddr(unsigned long long* jt
     if (c == 0) { o[0] = r / (NWn * NWn) + 1; o[1] = (r / NWn) % NWn; o[2] = r % NWn; }
     else if (c == 1) { o[0] = r / (F * NWn); o[1] = (r / NWn) % F + 1; o[2] = r % NWn; }
     else { o[0] = r / (NWn * F); o[1] = (r / F) % NWn; o[2] = r % F + 1; }
-    return jt + c * TT + ((b[0] + o[0]) * T1 + (b[1] + o[1])) * T2 + (b[2] + o[2]);
+    return c * TT + ((b[0] + o[0]) * T1 + (b[1] + o[1])) * T2 + (b[2] + o[2]);
 }
 
 // Boris rotation of BorisPusher.h:33-43 in FP32 with the hardware reciprocal
@@ -99,7 +100,7 @@ constexpr int kQWords = 11;  // queued window change: o[3], on[3], kq[3], packed
 // Esirkepov deposit of a particle whose rho-lattice window changes (old shape on
 // nodes lo0.., new on lo1..): general NWn+1-node window with per-lane atomics.
 template <int SHAPE>
-__device__ __forceinline__ void generalWindow(unsigned long long* jt, int TT, int T1, int T2, const float* o,
+__device__ __forceinline__ void generalWindow(const FixTile& jt, int TT, int T1, int T2, const float* o,
                                               const float* on, const int* lc, const int* ln, const float* kq) {
     constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;
     constexpr int NW4 = NWn + 1;
@@ -127,27 +128,37 @@ __device__ __forceinline__ void generalWindow(unsigned long long* jt, int TT, in
         placeShape<float, NW4, NWn>(s1[d], lo1, base, w1);
         b[d] = base + kG;
     }
-    esirkepov<float, NW4>(jt, jt + TT, jt + 2 * TT, T1, T2, b, s0, s1, kq);
+    esirkepov<float, NW4>(jt, TT, T1, T2, b, s0, s1, kq);
+}
+
+// Deposit the queued window changes of one warp (lanes take entries).
+template <int SHAPE>
+__device__ __forceinline__ void drainQueue(const float* q, int nq, const FixTile& jt, int TT, int T1, int T2) {
+    for (int k = threadIdx.x & 31; k < nq; k += 32) {
+        const float* e = q + k * kQWords;
+        const int k0 = __float_as_int(e[9]), k1 = __float_as_int(e[10]);
+        const int lc[3] = {(k0 >> 16) - 4, ((k0 >> 8) & 0xff) - 4, (k0 & 0xff) - 4};
+        const int ln[3] = {(k1 >> 16) - 4, ((k1 >> 8) & 0xff) - 4, (k1 & 0xff) - 4};
+        generalWindow<SHAPE>(jt, TT, T1, T2, e, e + 3, lc, ln, e + 6);
+    }
 }
 
 template <int SHAPE, int K, int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __grid_constant__ PushArgs<CellPtrs> a) {
-    constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;   // stay-in-cell window nodes per dimension
+    constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;   // stay-in-window nodes per dimension
     constexpr int NV = 3 * (NWn - 1) * NWn * NWn;          // 54 (TSC) or 12 (CIC)
     constexpr int kWarps = THREADS / 32;
+    constexpr int kQ = 64;                                 // queued window changes per warp
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int kQueue = THREADS * K / 8;   // window-changing particles queued per chunk
-    __shared__ int s_cnt[2][kWarps];
-    __shared__ int s_base[2];
-    __shared__ int s_nq;
-    __shared__ float sQueue[kQueue * kQWords];
+    __shared__ int s_nleave;
+    __shared__ float sQueue[kWarps][kQ * kQWords];
 
     const int T1 = a.T[1], T2 = a.T[2], TT = a.T[0] * T1 * T2;
-    unsigned long long* jt = reinterpret_cast<unsigned long long*>(smem_raw);
-    float* eb = reinterpret_cast<float*>(jt + 3 * TT);
-    uint32_t* sOut = reinterpret_cast<uint32_t*>(eb + 6 * TT);     // [warp][K][8][32]
-    uint8_t* sCode = reinterpret_cast<uint8_t*>(sOut + kWarps * K * 8 * 32);  // [warp][K][32]
-    if (threadIdx.x == 0) s_nq = 0;
+    FixTile jt;
+    jt.lo = reinterpret_cast<unsigned int*>(smem_raw);
+    jt.hi = reinterpret_cast<int*>(jt.lo + 3 * TT);
+    jt.L = a.tileSplit;
+    float* eb = reinterpret_cast<float*>(jt.hi + 3 * TT);
     const int s = blockIdx.x;
     int sc[3];
     sc[2] = s % a.nsc[2];
@@ -155,6 +166,8 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
     sc[0] = s / (a.nsc[1] * a.nsc[2]);
     const int m[3] = {sc[0] * a.S[0], sc[1] * a.S[1], sc[2] * a.S[2]};
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    float* myQ = sQueue[warp];
 
     for (int t = threadIdx.x; t < 6 * TT; t += blockDim.x) {
         const int c = t / TT, r = t - c * TT;
@@ -162,43 +175,41 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
         const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
         eb[t] = static_cast<const float*>(a.eb[c])[((int64_t)gx * a.n[1] + gy) * a.n[2] + gz];
     }
-    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) jt[t] = 0ull;
+    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) { jt.lo[t] = 0u; jt.hi[t] = 0; }
     const float invU = (float)a.invUnit;
     const float cdth[3] = {(float)a.cdth[0], (float)a.cdth[1], (float)a.cdth[2]};
     bool bad = false;
+    int nq = 0;   // entries in this warp's queue (warp-uniform)
     __syncthreads();
 
     for (int spi = 0; spi < a.nspecies; spi++) {
         const SpeciesArgs<CellPtrs>& sa = a.sp[spi];
         const int64_t start = sa.start[s];
-        const int cap = sa.cap[s];
         const int count = sa.count[s];
         const float ec = (float)sa.ec;
         const float kqs[3] = {(float)sa.kq[0] * invU, (float)sa.kq[1] * invU, (float)sa.kq[2] * invU};
-        if (threadIdx.x == 0) { s_base[0] = 0; s_base[1] = 0; }
+        if (threadIdx.x == 0) s_nleave = 0;
         __syncthreads();
-        for (int chunk = 0; chunk < count; chunk += THREADS * K) {
-            const int seg = chunk + warp * 32 * K;
+        const int nseg = (count + 32 * K - 1) / (32 * K);
+        for (int seg = warp; seg < nseg; seg += kWarps) {
             float acc[NV];
 #pragma unroll
             for (int k = 0; k < NV; k++) acc[k] = 0.0f;
             int accKey = -1;
-            // Outputs wait in this warp's shared-memory slice until the stable rank is known.
-            uint32_t* so = sOut + (size_t)warp * K * 8 * 32;
-            unsigned stayBits = 0u, leaveBits = 0u;   // bit it: this lane's particle it stays / leaves
 #pragma unroll 1
             for (int it = 0; it < K; it++) {
-                const int i = seg + lane * K + it;
-                const bool act = i < count;
-                int code = 13;
+                const int i = seg * 32 * K + lane * K + it;
+                const int64_t slot = start + i;
+                const bool act = i < count && sa.buf.cell[slot] != kDeadCell;
+                bool needQ = false;
+                float qe[kQWords];
                 if (act) {
-                    const int64_t slot = start + i;
                     int c3[3];
-                    unpackCell(sa.in.cell[slot], c3[0], c3[1], c3[2]);
+                    unpackCell(sa.buf.cell[slot], c3[0], c3[1], c3[2]);
                     const int lc[3] = {c3[0] - m[0], c3[1] - m[1], c3[2] - m[2]};
-                    const float o[3] = {sa.in.ox[slot], sa.in.oy[slot], sa.in.oz[slot]};
-                    float u[3] = {sa.in.ux[slot], sa.in.uy[slot], sa.in.uz[slot]};
-                    const float wgt = sa.in.w[slot];
+                    const float o[3] = {sa.buf.ox[slot], sa.buf.oy[slot], sa.buf.oz[slot]};
+                    float u[3] = {sa.buf.ux[slot], sa.buf.uy[slot], sa.buf.uz[slot]};
+                    const float wgt = sa.buf.w[slot];
                     float eb6[6];
                     if constexpr (SHAPE == PICA_SHAPE_CIC) {
                         int bc[3], bs[3];
@@ -287,7 +298,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
                                 const int b[3] = {(accKey >> 16) - 4 + kG, ((accKey >> 8) & 0xff) - 4 + kG, (accKey & 0xff) - 4 + kG};
 #pragma unroll
                                 for (int j = 0; j < NV; j++)
-                                    if (acc[j] != 0.0f) addQ(windowAddr<NWn>(jt, TT, T1, T2, b, j), acc[j]);
+                                    jt.add(windowIdx<NWn>(TT, T1, T2, b, j), acc[j]);
                             }
 #pragma unroll
                             for (int j = 0; j < NV; j++) acc[j] = 0.0f;
@@ -324,19 +335,11 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
                                     acc[2 * P + y * NWn * (NWn - 1) + z * (NWn - 1) + f] += e[2][f] * (aa[0][y] * pp[1][z] + dd[0][y] * qq[1][z]);
                                 }
                     } else if (inRange) {
-                        // Window changes: queue the particle for the general window pass after the chunk.
-                        const int qi = atomicAdd(&s_nq, 1);
-                        if (qi < kQueue) {
-                            float* e = sQueue + qi * kQWords;
+                        needQ = true;
 #pragma unroll
-                            for (int d = 0; d < 3; d++) {
-                                e[d] = o[d]; e[3 + d] = on[d]; e[6 + d] = kq[d];
-                            }
-                            e[9] = __int_as_float(((lc[0] + 4) << 16) | ((lc[1] + 4) << 8) | (lc[2] + 4));
-                            e[10] = __int_as_float(((ln[0] + 4) << 16) | ((ln[1] + 4) << 8) | (ln[2] + 4));
-                        } else {
-                            generalWindow<SHAPE>(jt, TT, T1, T2, o, on, lc, ln, kq);
-                        }
+                        for (int d = 0; d < 3; d++) { qe[d] = o[d]; qe[3 + d] = on[d]; qe[6 + d] = kq[d]; }
+                        qe[9] = __int_as_float(((lc[0] + 4) << 16) | ((lc[1] + 4) << 8) | (lc[2] + 4));
+                        qe[10] = __int_as_float(((ln[0] + 4) << 16) | ((ln[1] + 4) << 8) | (ln[2] + 4));
                     }
                     int gc[3], nsc3[3];
 #pragma unroll
@@ -344,22 +347,42 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
                         gc[d] = wrapi(m[d] + ln[d], a.n[d]);
                         nsc3[d] = gc[d] / a.S[d];
                     }
-                    code = dirCode(sc, nsc3, a.nsc, bad);
-                    uint32_t* q = so + it * 8 * 32 + lane;
-                    q[0] = packCell(gc[0], gc[1], gc[2]);
-                    q[32] = __float_as_uint(on[0]); q[64] = __float_as_uint(on[1]); q[96] = __float_as_uint(on[2]);
-                    q[128] = __float_as_uint(u[0]); q[160] = __float_as_uint(u[1]); q[192] = __float_as_uint(u[2]);
-                    q[224] = __float_as_uint(wgt);
-                    sCode[(warp * K + it) * 32 + lane] = (uint8_t)code;
+                    const int code = dirCode(sc, nsc3, a.nsc, bad);
+                    // Stayers in place (the weight does not change); a leaver goes to the side
+                    // buffer at its own slot, its slot dies and joins the leaver list.
+                    const CellPtrs& o2 = code == 13 ? sa.buf : sa.out;
+                    o2.cell[slot] = packCell(gc[0], gc[1], gc[2]);
+                    o2.ox[slot] = on[0]; o2.oy[slot] = on[1]; o2.oz[slot] = on[2];
+                    o2.ux[slot] = u[0]; o2.uy[slot] = u[1]; o2.uz[slot] = u[2];
+                    if (code != 13) {
+                        o2.w[slot] = wgt;
+                        sa.dir[slot] = (uint8_t)code;
+                        sa.llist[start + atomicAdd(&s_nleave, 1)] = i;
+                        sa.buf.cell[slot] = kDeadCell;
+                    }
                 }
-                stayBits |= (act && code == 13 ? 1u : 0u) << it;
-                leaveBits |= (act && code != 13 ? 1u : 0u) << it;
+                // Queue window changes (warp-cooperative; drain when full).
+                const unsigned qm = __ballot_sync(0xffffffffu, needQ);
+                if (qm) {
+                    if (nq + __popc(qm) > kQ) {
+                        drainQueue<SHAPE>(myQ, nq, jt, TT, T1, T2);
+                        nq = 0;
+                        __syncwarp();
+                    }
+                    if (needQ) {
+                        float* e = myQ + (nq + __popc(qm & lt)) * kQWords;
+#pragma unroll
+                        for (int k = 0; k < kQWords; k++) e[k] = qe[k];
+                    }
+                    nq += __popc(qm);
+                    __syncwarp();
+                }
             }
-            // Reduce the stay-in-cell windows of lanes that share a window (up to two groups),
+            // Reduce the stay-in-window sums of lanes sharing a window (up to three groups),
             // then flush what remains lane by lane.
             bool pending = accKey >= 0;
 #pragma unroll 1
-            for (int g = 0; g < 2; g++) {
+            for (int g = 0; g < 3; g++) {
                 const unsigned live = __ballot_sync(0xffffffffu, pending);
                 if (!live) break;
                 const int ref = __shfl_sync(0xffffffffu, accKey, __ffs(live) - 1);
@@ -367,73 +390,26 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
                 float s0v, s1v;
                 warpTransposeSum<NV>(acc, mine, lane, s0v, s1v);
                 const int b[3] = {(ref >> 16) - 4 + kG, ((ref >> 8) & 0xff) - 4 + kG, (ref & 0xff) - 4 + kG};
-                if (2 * lane < NV && s0v != 0.0f) addQ(windowAddr<NWn>(jt, TT, T1, T2, b, 2 * lane), s0v);
-                if (2 * lane + 1 < NV && s1v != 0.0f) addQ(windowAddr<NWn>(jt, TT, T1, T2, b, 2 * lane + 1), s1v);
+                if (2 * lane < NV) jt.add(windowIdx<NWn>(TT, T1, T2, b, 2 * lane), s0v);
+                if (2 * lane + 1 < NV) jt.add(windowIdx<NWn>(TT, T1, T2, b, 2 * lane + 1), s1v);
                 if (mine) pending = false;
             }
             if (pending) {
                 const int b[3] = {(accKey >> 16) - 4 + kG, ((accKey >> 8) & 0xff) - 4 + kG, (accKey & 0xff) - 4 + kG};
 #pragma unroll
                 for (int j = 0; j < NV; j++)
-                    if (acc[j] != 0.0f) addQ(windowAddr<NWn>(jt, TT, T1, T2, b, j), acc[j]);
+                    jt.add(windowIdx<NWn>(TT, T1, T2, b, j), acc[j]);
             }
-            // Stable partition of the chunk: stayers packed from the front, leavers from the back,
-            // in particle order (lane-major within the warp, warp-major within the chunk).
-            const int myS = __popc(stayBits), myL = __popc(leaveBits);
-            int exS = myS, exL = myL;   // inclusive lane scan
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const int ts = __shfl_up_sync(0xffffffffu, exS, d), tl = __shfl_up_sync(0xffffffffu, exL, d);
-                if (lane >= d) { exS += ts; exL += tl; }
-            }
-            if (lane == 31) { s_cnt[0][warp] = exS; s_cnt[1][warp] = exL; }
-            exS -= myS;
-            exL -= myL;
-            __syncthreads();
-            // Window changes queued by this chunk (all lanes, dense).
-            const int nq = min(s_nq, kQueue);
-            for (int qi = threadIdx.x; qi < nq; qi += THREADS) {
-                const float* e = sQueue + qi * kQWords;
-                const int k0 = __float_as_int(e[9]), k1 = __float_as_int(e[10]);
-                const int lc[3] = {(k0 >> 16) - 4, ((k0 >> 8) & 0xff) - 4, (k0 & 0xff) - 4};
-                const int ln[3] = {(k1 >> 16) - 4, ((k1 >> 8) & 0xff) - 4, (k1 & 0xff) - 4};
-                generalWindow<SHAPE>(jt, TT, T1, T2, e, e + 3, lc, ln, e + 6);
-            }
-            int rs = s_base[0] + exS, rl = s_base[1] + exL;
-            for (int w = 0; w < warp; w++) { rs += s_cnt[0][w]; rl += s_cnt[1][w]; }
-#pragma unroll 1
-            for (int it = 0; it < K; it++) {
-                const bool st = (stayBits >> it) & 1, lv = (leaveBits >> it) & 1;
-                if (st || lv) {
-                    int64_t o;
-                    if (st) o = start + rs++;
-                    else {
-                        o = start + cap - 1 - (rl++);
-                        sa.dir[o] = sCode[(warp * K + it) * 32 + lane];
-                    }
-                    const uint32_t* q = so + it * 8 * 32 + lane;
-                    sa.out.cell[o] = q[0];
-                    sa.out.ox[o] = __uint_as_float(q[32]); sa.out.oy[o] = __uint_as_float(q[64]);
-                    sa.out.oz[o] = __uint_as_float(q[96]);
-                    sa.out.ux[o] = __uint_as_float(q[128]); sa.out.uy[o] = __uint_as_float(q[160]);
-                    sa.out.uz[o] = __uint_as_float(q[192]);
-                    sa.out.w[o] = __uint_as_float(q[224]);
-                }
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                for (int w = 0; w < kWarps; w++) { s_base[0] += s_cnt[0][w]; s_base[1] += s_cnt[1][w]; }
-                s_nq = 0;
-            }
-            __syncthreads();
         }
-        if (threadIdx.x == 0) { sa.nstay[s] = s_base[0]; sa.nleave[s] = s_base[1]; }
+        __syncthreads();
+        if (threadIdx.x == 0) sa.nleave[s] = s_nleave;
         __syncthreads();
     }
+    drainQueue<SHAPE>(myQ, nq, jt, TT, T1, T2);
     if (bad) atomicExch(a.flags, PICA_ERR_MIGRATION);
     __syncthreads();
     for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) {
-        const unsigned long long v = jt[t];
+        const unsigned long long v = (unsigned long long)jt.node(t);
         if (v != 0ull) {
             const int c = t / TT, r = t - c * TT;
             const int i = r / (T1 * T2), jj = (r / T2) % T1, k = r % T2;

@@ -10,6 +10,7 @@ int launchOne(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     const size_t smem = (size_t)6 * TT * sizeof(float) + (size_t)3 * TT * sizeof(unsigned long long);
     auto k = k_push<false, SHAPE, DEP>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return (int)e;
     const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
     k<<<nscTot, kPushThreads, smem, s>>>(a);
@@ -25,6 +26,7 @@ int launchEsirkepov(const PushArgs<CellPtrs>& a, cudaStream_t s) {
                         (size_t)(THREADS / 32) * K * 32 * (8 * sizeof(uint32_t) + 1);
     auto k = k_push_cell_esirkepov<SHAPE, K, THREADS, MINB>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return (int)e;
     const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
     k<<<nscTot, THREADS, smem, s>>>(a);
@@ -41,11 +43,26 @@ int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int dep, cudaStream_t
     return -1;
 }
 
-int launchMigrateCell(const MigrateArgs<CellPtrs>& a, bool rebuild, cudaStream_t s) {
+int launchMigrateCell(const MigrateArgs<CellPtrs>& a, int stage, cudaStream_t s) {
     const int64_t nscTot = (int64_t)a.nsc[0] * a.nsc[1] * a.nsc[2];
-    const int blocks = (int)((nscTot * 32 + 255) / 256);
-    if (rebuild) k_migrate<CellPtrs, true><<<blocks, 256, 0, s>>>(a);
-    else k_migrate<CellPtrs, false><<<blocks, 256, 0, s>>>(a);
+    const int warpBlocks = (int)((nscTot * 32 + 255) / 256);
+    switch (stage) {
+        case kSortLeavers: {
+            const size_t smem = (size_t)a.bitmapWords * sizeof(unsigned int);
+            if (smem > 48 * 1024) {
+                const cudaError_t e = cudaFuncSetAttribute(k_sortLeavers<CellPtrs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) return (int)e;
+            }
+            k_sortLeavers<CellPtrs><<<(int)nscTot, 128, smem, s>>>(a);
+            break;
+        }
+        case kCountArrivals: k_migrate<CellPtrs, kCountArrivals><<<warpBlocks, 256, 0, s>>>(a); break;
+        case kFill: k_migrate<CellPtrs, kFill><<<warpBlocks, 256, 0, s>>>(a); break;
+        case kGatherOutbox: k_migrate<CellPtrs, kGatherOutbox><<<warpBlocks, 256, 0, s>>>(a); break;
+        case kRebuild: k_migrate<CellPtrs, kRebuild><<<warpBlocks, 256, 0, s>>>(a); break;
+        case kResort: k_resort<CellPtrs><<<(int)((nscTot + 3) / 4), 128, 0, s>>>(a); break;
+        default: return (int)cudaErrorInvalidValue;
+    }
     return (int)cudaGetLastError();
 }
 

@@ -11,6 +11,7 @@ int launchOne(const PushArgs<PlainPtrs>& a, cudaStream_t s) {
     const size_t smem = (size_t)9 * TT * sizeof(double);
     auto k = k_push<true, SHAPE, DEP>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return (int)e;
     const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
     k<<<nscTot, kPushThreads, smem, s>>>(a);
@@ -26,11 +27,26 @@ int launchPushPlain(const PushArgs<PlainPtrs>& a, int shape, int dep, cudaStream
     return -1;
 }
 
-int launchMigratePlain(const MigrateArgs<PlainPtrs>& a, bool rebuild, cudaStream_t s) {
+int launchMigratePlain(const MigrateArgs<PlainPtrs>& a, int stage, cudaStream_t s) {
     const int64_t nscTot = (int64_t)a.nsc[0] * a.nsc[1] * a.nsc[2];
-    const int blocks = (int)((nscTot * 32 + 255) / 256);
-    if (rebuild) k_migrate<PlainPtrs, true><<<blocks, 256, 0, s>>>(a);
-    else k_migrate<PlainPtrs, false><<<blocks, 256, 0, s>>>(a);
+    const int warpBlocks = (int)((nscTot * 32 + 255) / 256);
+    switch (stage) {
+        case kSortLeavers: {
+            const size_t smem = (size_t)a.bitmapWords * sizeof(unsigned int);
+            if (smem > 48 * 1024) {
+                const cudaError_t e = cudaFuncSetAttribute(k_sortLeavers<PlainPtrs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) return (int)e;
+            }
+            k_sortLeavers<PlainPtrs><<<(int)nscTot, 128, smem, s>>>(a);
+            break;
+        }
+        case kCountArrivals: k_migrate<PlainPtrs, kCountArrivals><<<warpBlocks, 256, 0, s>>>(a); break;
+        case kFill: k_migrate<PlainPtrs, kFill><<<warpBlocks, 256, 0, s>>>(a); break;
+        case kGatherOutbox: k_migrate<PlainPtrs, kGatherOutbox><<<warpBlocks, 256, 0, s>>>(a); break;
+        case kRebuild: k_migrate<PlainPtrs, kRebuild><<<warpBlocks, 256, 0, s>>>(a); break;
+        case kResort: k_resort<PlainPtrs><<<(int)((nscTot + 3) / 4), 128, 0, s>>>(a); break;
+        default: return (int)cudaErrorInvalidValue;
+    }
     return (int)cudaGetLastError();
 }
 

@@ -44,14 +44,32 @@ __device__ __forceinline__ void tscWeights(R d, R* w) {
     w[2] = h * (h + d) * (h + d);
 }
 
-// Add one current contribution to a tile node.  FP32 form: the contribution is
-// already scaled to fixed-point units and is added as a 64-bit integer (exact,
-// order-independent).  FP64 form: plain FP64 add, so the FP64 result differs
-// from pica's only by the order of the sums.
-__device__ __forceinline__ void addQ(unsigned long long* p, float scaled) {
-    atomicAdd(p, (unsigned long long)__float2ll_rn(scaled));
-}
-__device__ __forceinline__ void addQ(double* p, double v) { atomicAdd(p, v); }
+// Current tiles in shared memory.  FP32 form: each node keeps the exact
+// integer (fixed-point) sum split into a low part (the low L bits of every
+// contribution, summed as unsigned 32-bit) and a high part (the rest, summed
+// as signed 32-bit), both with native 32-bit shared-memory atomics; L and the
+// fraction bits are chosen so that neither part can overflow for the largest
+// supercell (see the host).  The 64-bit node sum is hi * 2^L + lo.  Integer
+// sums are exact, so the result does not depend on the order of the adds.
+// FP64 form: plain FP64 adds, so the FP64 result differs from pica's only by
+// the order of the sums.
+struct FixTile {
+    unsigned int* lo;
+    int* hi;
+    int L;
+    __device__ __forceinline__ void add(int idx, float scaled) const {
+        const long long v = __float2ll_rn(scaled);
+        if (v != 0) {
+            atomicAdd(lo + idx, (unsigned int)(v & ((1ll << L) - 1)));
+            atomicAdd(hi + idx, (int)(v >> L));
+        }
+    }
+    __device__ __forceinline__ long long node(int idx) const { return ((long long)hi[idx] << L) + (long long)lo[idx]; }
+};
+struct DblTile {
+    double* p;
+    __device__ __forceinline__ void add(int idx, double v) const { atomicAdd(p + idx, v); }
+};
 
 // Separable W^3-point gather: sum_i wx_i sum_j wy_j (sum_k wz_k F), left to right.
 template <typename R, int W>
@@ -74,17 +92,17 @@ __device__ __forceinline__ R gatherSep(const R* tile, int T1, int T2, const int*
     return r;
 }
 
-template <typename R, int W, typename A>
-__device__ __forceinline__ void scatterSep(A* tile, int T1, int T2, const int* t0, const R* wx, const R* wy,
-                                           const R* wz, R v) {
+template <typename R, int W, typename Tile>
+__device__ __forceinline__ void scatterSep(const Tile& tile, int off, int T1, int T2, const int* t0, const R* wx,
+                                           const R* wy, const R* wz, R v) {
 #pragma unroll
     for (int i = 0; i < W; i++)
 #pragma unroll
         for (int j = 0; j < W; j++) {
-            A* row = tile + ((t0[0] + i) * T1 + (t0[1] + j)) * T2 + t0[2];
+            const int row = off + ((t0[0] + i) * T1 + (t0[1] + j)) * T2 + t0[2];
             R vij = (v * wx[i]) * wy[j];
 #pragma unroll
-            for (int k = 0; k < W; k++) addQ(row + k, vij * wz[k]);
+            for (int k = 0; k < W; k++) tile.add(row + k, vij * wz[k]);
         }
 }
 
@@ -99,18 +117,19 @@ __device__ __forceinline__ double cicGatherRef(const double* t, int T1, int T2, 
            p[sx + sy] * cx * cy * (1.0 - cz) + p[sx + sy + 1] * cx * cy * cz;
 }
 // pica's CIC 8-point deposit, CurrentDepositorYeeGrid.h:254-261 (same factor order).
-__device__ __forceinline__ void cicScatterRef(double* t, int T1, int T2, const int* b, const double* c, double v) {
-    double* p = t + (b[0] * T1 + b[1]) * T2 + b[2];
+__device__ __forceinline__ void cicScatterRef(const DblTile& t, int off, int T1, int T2, const int* b, const double* c,
+                                              double v) {
+    const int p = off + (b[0] * T1 + b[1]) * T2 + b[2];
     const int sy = T2, sx = T1 * T2;
     const double cx = c[0], cy = c[1], cz = c[2];
-    addQ(p, (1.0 - cx) * (1.0 - cy) * (1.0 - cz) * v);
-    addQ(p + 1, (1.0 - cx) * (1.0 - cy) * cz * v);
-    addQ(p + sy, (1.0 - cx) * cy * (1.0 - cz) * v);
-    addQ(p + sy + 1, (1.0 - cx) * cy * cz * v);
-    addQ(p + sx, cx * (1.0 - cy) * (1.0 - cz) * v);
-    addQ(p + sx + 1, cx * (1.0 - cy) * cz * v);
-    addQ(p + sx + sy, cx * cy * (1.0 - cz) * v);
-    addQ(p + sx + sy + 1, cx * cy * cz * v);
+    t.add(p, (1.0 - cx) * (1.0 - cy) * (1.0 - cz) * v);
+    t.add(p + 1, (1.0 - cx) * (1.0 - cy) * cz * v);
+    t.add(p + sy, (1.0 - cx) * cy * (1.0 - cz) * v);
+    t.add(p + sy + 1, (1.0 - cx) * cy * cz * v);
+    t.add(p + sx, cx * (1.0 - cy) * (1.0 - cz) * v);
+    t.add(p + sx + 1, cx * (1.0 - cy) * cz * v);
+    t.add(p + sx + sy, cx * cy * (1.0 - cz) * v);
+    t.add(p + sx + sy + 1, cx * cy * cz * v);
 }
 
 // Boris rotation of BorisPusher.h:33-43 on normalised momentum u; returns 1/gamma
@@ -135,8 +154,8 @@ __device__ __forceinline__ R boris(R ec, const R* eb, R* u) {
 // cell centres, J on faces.  s0/s1: old/new shape in an NW-node window of the
 // rho lattice starting at tile index b; k: -(q w) h_d / dt.  Jx of the face
 // between window nodes i and i+1 is pica Jx node b_x + i + 1.
-template <typename R, int NW, typename A>
-__device__ __forceinline__ void esirkepov(A* jx, A* jy, A* jz, int T1, int T2, const int* b, const R (*s0)[NW],
+template <typename R, int NW, typename Tile>
+__device__ __forceinline__ void esirkepov(const Tile& jt, int TT, int T1, int T2, const int* b, const R (*s0)[NW],
                                           const R (*s1)[NW], const R* k) {
     R ds[3][NW];
 #pragma unroll
@@ -153,7 +172,7 @@ __device__ __forceinline__ void esirkepov(A* jx, A* jy, A* jz, int T1, int T2, c
 #pragma unroll
             for (int i = 0; i < NW - 1; i++) {
                 acc = acc + ds[0][i] * yz;
-                addQ(jx + ((b[0] + i + 1) * T1 + (b[1] + j)) * T2 + (b[2] + l), acc * k[0]);
+                jt.add(((b[0] + i + 1) * T1 + (b[1] + j)) * T2 + (b[2] + l), acc * k[0]);
             }
         }
 #pragma unroll
@@ -165,7 +184,7 @@ __device__ __forceinline__ void esirkepov(A* jx, A* jy, A* jz, int T1, int T2, c
 #pragma unroll
             for (int j = 0; j < NW - 1; j++) {
                 acc = acc + ds[1][j] * xz;
-                addQ(jy + ((b[0] + i) * T1 + (b[1] + j + 1)) * T2 + (b[2] + l), acc * k[1]);
+                jt.add(TT + ((b[0] + i) * T1 + (b[1] + j + 1)) * T2 + (b[2] + l), acc * k[1]);
             }
         }
 #pragma unroll
@@ -177,7 +196,7 @@ __device__ __forceinline__ void esirkepov(A* jx, A* jy, A* jz, int T1, int T2, c
 #pragma unroll
             for (int l = 0; l < NW - 1; l++) {
                 acc = acc + ds[2][l] * xy;
-                addQ(jz + ((b[0] + i) * T1 + (b[1] + j)) * T2 + (b[2] + l + 1), acc * k[2]);
+                jt.add(2 * TT + ((b[0] + i) * T1 + (b[1] + j)) * T2 + (b[2] + l + 1), acc * k[2]);
             }
         }
 }
@@ -209,6 +228,11 @@ __device__ __forceinline__ int dirCode(const int* o, const int* nw, const int* n
     return code;
 }
 
+__device__ __forceinline__ bool aliveAt(const PlainPtrs& p, int64_t i) { return aliveX(p.x[i]); }
+__device__ __forceinline__ bool aliveAt(const CellPtrs& p, int64_t i) { return p.cell[i] != kDeadCell; }
+__device__ __forceinline__ void killAt(const PlainPtrs& p, int64_t i) { p.x[i] = kDeadX; }
+__device__ __forceinline__ void killAt(const CellPtrs& p, int64_t i) { p.cell[i] = kDeadCell; }
+
 __device__ __forceinline__ void copyParticle(const PlainPtrs& s, int64_t i, const PlainPtrs& d, int64_t j) {
     d.x[j] = s.x[i]; d.y[j] = s.y[i]; d.z[j] = s.z[i];
     d.ux[j] = s.ux[i]; d.uy[j] = s.uy[i]; d.uz[j] = s.uz[i]; d.w[j] = s.w[i];
@@ -226,22 +250,30 @@ __global__ void __launch_bounds__(kPushThreads)
 k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::type> a) {
     using R = typename std::conditional<PLAIN, double, float>::type;
     using P = typename std::conditional<PLAIN, PlainPtrs, CellPtrs>::type;
-    using A = typename std::conditional<PLAIN, double, unsigned long long>::type;  // J tile accumulator
+
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int s_cnt[2][kPushThreads / 32];
-    __shared__ int s_base[2];
+    __shared__ int s_nleave;
 
     const int T1 = a.T[1], T2 = a.T[2], TT = a.T[0] * T1 * T2;
-    A* jt = reinterpret_cast<A*>(smem_raw);
-    R* eb = reinterpret_cast<R*>(jt + 3 * TT);
+    // J tile (3 components x TT nodes) then the E/B tile (6 x TT).
+    using Tile = typename std::conditional<PLAIN, DblTile, FixTile>::type;
+    Tile jt;
+    R* eb;
+    if constexpr (PLAIN) {
+        jt.p = reinterpret_cast<double*>(smem_raw);
+        eb = reinterpret_cast<R*>(jt.p + 3 * TT);
+    } else {
+        jt.lo = reinterpret_cast<unsigned int*>(smem_raw);
+        jt.hi = reinterpret_cast<int*>(jt.lo + 3 * TT);
+        jt.L = a.tileSplit;
+        eb = reinterpret_cast<R*>(jt.hi + 3 * TT);
+    }
     const int s = blockIdx.x;
     int sc[3];
     sc[2] = s % a.nsc[2];
     sc[1] = (s / a.nsc[2]) % a.nsc[1];
     sc[0] = s / (a.nsc[1] * a.nsc[2]);
     const int m[3] = {sc[0] * a.S[0], sc[1] * a.S[1], sc[2] * a.S[2]};
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-
     // Stage the E/B tile (periodic) and clear the J tile.
     for (int t = threadIdx.x; t < 6 * TT; t += blockDim.x) {
         const int c = t / TT, r = t - c * TT;
@@ -249,7 +281,10 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
         const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
         eb[t] = static_cast<const R*>(a.eb[c])[((int64_t)gx * a.n[1] + gy) * a.n[2] + gz];
     }
-    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) jt[t] = A(0);
+    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) {
+        if constexpr (PLAIN) jt.p[t] = 0.0;
+        else { jt.lo[t] = 0u; jt.hi[t] = 0; }
+    }
 
     // pica supercell index math (FieldInterpolatorYeeGrid.h:197-205): tile index t of
     // the reference maps to node trunc(minPos/h) - 1 + t, i.e. our tile index t + off.
@@ -262,9 +297,6 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
         nos[d] = no[d] + 0.5;
         off[d] = ((int)(minPos / a.h[d]) - 1) - (m[d] - kG);
     }
-    A* jx = jt;
-    A* jy = jt + TT;
-    A* jz = jt + 2 * TT;
     const R invU = (R)a.invUnit;
     bool bad = false;
     __syncthreads();
@@ -272,27 +304,24 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
     for (int spi = 0; spi < a.nspecies; spi++) {
         const SpeciesArgs<P>& sa = a.sp[spi];
         const int64_t start = sa.start[s];
-        const int cap = sa.cap[s];
         const int count = sa.count[s];
         const R ec = (R)sa.ec;
-        if (threadIdx.x == 0) { s_base[0] = 0; s_base[1] = 0; }
+        if (threadIdx.x == 0) s_nleave = 0;
         __syncthreads();
-        for (int base = 0; base < count; base += blockDim.x) {
-            const int i = base + threadIdx.x;
-            const bool act = i < count;
-            int code = 13;
+        for (int i = threadIdx.x; i < count; i += blockDim.x) {
             const int64_t slot = start + i;
-            // New particle state (written after the rank computation).
-            R nu[3], nw8 = R(0);
+            if (!aliveAt(sa.buf, slot)) continue;
+            int code = 13;
+            R nu[3];
             double npos[3];
             uint32_t ncell = 0;
             float no3[3];
-            if (act) {
+            {
                 R u[3], eb6[6], wgt;
                 if constexpr (PLAIN) {
-                    const double pos[3] = {sa.in.x[slot], sa.in.y[slot], sa.in.z[slot]};
-                    u[0] = sa.in.ux[slot]; u[1] = sa.in.uy[slot]; u[2] = sa.in.uz[slot];
-                    wgt = sa.in.w[slot];
+                    const double pos[3] = {sa.buf.x[slot], sa.buf.y[slot], sa.buf.z[slot]};
+                    u[0] = sa.buf.ux[slot]; u[1] = sa.buf.uy[slot]; u[2] = sa.buf.uz[slot];
+                    wgt = sa.buf.w[slot];
                     if constexpr (SHAPE == PICA_SHAPE_CIC) {
                         int ic[3], is[3];
                         double cc[3], cs[3];
@@ -373,7 +402,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                     b[d] = (stag(comp, d) ? is[d] : ic[d]) + off[d];
                                     w[d] = stag(comp, d) ? cs[d] : cc[d];
                                 }
-                                cicScatterRef(jt + comp * TT, T1, T2, b, w, cur[comp]);
+                                cicScatterRef(jt, comp * TT, T1, T2, b, w, cur[comp]);
                             }
                         } else {
                             int nc[3], ns[3];
@@ -390,7 +419,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 int t0[3];
 #pragma unroll
                                 for (int d = 0; d < 3; d++) t0[d] = (stag(comp, d) ? ns[d] : nc[d]) - 1 - (m[d] - kG);
-                                scatterSep<double, 3>(jt + comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
+                                scatterSep<double, 3>(jt, comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
                                                       stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2], cur[comp]);
                             }
                         }
@@ -411,7 +440,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 placeShape<double, 3, 2>(s1[d], n1, lo, w1);
                                 b[d] = lo - (m[d] - kG);
                             }
-                            esirkepov<double, 3>(jx, jy, jz, T1, T2, b, s0, s1, kq);
+                            esirkepov<double, 3>(jt, TT, T1, T2, b, s0, s1, kq);
                         } else {
                             double s0[3][4], s1[3][4];
 #pragma unroll
@@ -426,7 +455,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 placeShape<double, 4, 3>(s1[d], n1 - 1, lo, w1);
                                 b[d] = lo - (m[d] - kG);
                             }
-                            esirkepov<double, 4>(jx, jy, jz, T1, T2, b, s0, s1, kq);
+                            esirkepov<double, 4>(jt, TT, T1, T2, b, s0, s1, kq);
                         }
                     }
                     // Periodic wrap and new supercell (EnsembleSupercells.h:54-57, floor, clamped).
@@ -444,11 +473,11 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                 } else {
                     // FP32 cell form.
                     int c3[3];
-                    unpackCell(sa.in.cell[slot], c3[0], c3[1], c3[2]);
+                    unpackCell(sa.buf.cell[slot], c3[0], c3[1], c3[2]);
                     const int lc[3] = {c3[0] - m[0], c3[1] - m[1], c3[2] - m[2]};
-                    const float o[3] = {sa.in.ox[slot], sa.in.oy[slot], sa.in.oz[slot]};
-                    u[0] = sa.in.ux[slot]; u[1] = sa.in.uy[slot]; u[2] = sa.in.uz[slot];
-                    wgt = sa.in.w[slot];
+                    const float o[3] = {sa.buf.ox[slot], sa.buf.oy[slot], sa.buf.oz[slot]};
+                    u[0] = sa.buf.ux[slot]; u[1] = sa.buf.uy[slot]; u[2] = sa.buf.uz[slot];
+                    wgt = sa.buf.w[slot];
                     if constexpr (SHAPE == PICA_SHAPE_CIC) {
                         int bc[3], bs[3];
                         float wc[3][2], ws[3][2];
@@ -524,7 +553,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 int t0[3];
 #pragma unroll
                                 for (int d = 0; d < 3; d++) t0[d] = stag(comp, d) ? bs[d] : bc[d];
-                                scatterSep<float, 2>(jt + comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
+                                scatterSep<float, 2>(jt, comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
                                                      stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2], cur[comp]);
                             }
                         } else {
@@ -541,7 +570,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 int t0[3];
 #pragma unroll
                                 for (int d = 0; d < 3; d++) t0[d] = stag(comp, d) ? bs[d] : bc[d];
-                                scatterSep<float, 3>(jt + comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
+                                scatterSep<float, 3>(jt, comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
                                                      stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2], cur[comp]);
                             }
                         }
@@ -562,7 +591,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 placeShape<float, 3, 2>(s1[d], n1, lo, w1);
                                 b[d] = lo + kG;
                             }
-                            esirkepov<float, 3>(jx, jy, jz, T1, T2, b, s0, s1, kq);
+                            esirkepov<float, 3>(jt, TT, T1, T2, b, s0, s1, kq);
                         } else {
                             float s0[3][4], s1[3][4];
 #pragma unroll
@@ -575,7 +604,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 placeShape<float, 4, 3>(s1[d], ln[d] - 1, lo, w1);
                                 b[d] = lo + kG;
                             }
-                            esirkepov<float, 4>(jx, jy, jz, T1, T2, b, s0, s1, kq);
+                            esirkepov<float, 4>(jt, TT, T1, T2, b, s0, s1, kq);
                         }
                     }
                     int gc[3], nsc3[3];
@@ -589,36 +618,25 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                     code = dirCode(sc, nsc3, a.nsc, bad);
                 }
                 nu[0] = u[0]; nu[1] = u[1]; nu[2] = u[2];
-                nw8 = wgt;
             }
-            // Stable partition: stayers packed from the front, leavers from the back.
-            const bool stay = act && code == 13, leave = act && code != 13;
-            const unsigned ms = __ballot_sync(0xffffffffu, stay), ml = __ballot_sync(0xffffffffu, leave);
-            if (lane == 0) { s_cnt[0][warp] = __popc(ms); s_cnt[1][warp] = __popc(ml); }
-            __syncthreads();
-            int rs = s_base[0], rl = s_base[1];
-            for (int w = 0; w < warp; w++) { rs += s_cnt[0][w]; rl += s_cnt[1][w]; }
-            const unsigned lt = (1u << lane) - 1u;
-            if (act) {
-                int64_t o;
-                if (stay) o = start + rs + __popc(ms & lt);
-                else {
-                    o = start + cap - 1 - (rl + __popc(ml & lt));
-                    sa.dir[o] = (uint8_t)code;
-                }
-                if constexpr (PLAIN) {
-                    sa.out.x[o] = npos[0]; sa.out.y[o] = npos[1]; sa.out.z[o] = npos[2];
-                } else {
-                    sa.out.cell[o] = ncell; sa.out.ox[o] = no3[0]; sa.out.oy[o] = no3[1]; sa.out.oz[o] = no3[2];
-                }
-                sa.out.ux[o] = nu[0]; sa.out.uy[o] = nu[1]; sa.out.uz[o] = nu[2]; sa.out.w[o] = nw8;
+            // Stayers are updated in place (the weight does not change); a leaver is copied to
+            // the side buffer at its own slot, its slot dies and joins the leaver list.
+            const P& o = code == 13 ? sa.buf : sa.out;
+            if constexpr (PLAIN) {
+                o.x[slot] = npos[0]; o.y[slot] = npos[1]; o.z[slot] = npos[2];
+            } else {
+                o.cell[slot] = ncell; o.ox[slot] = no3[0]; o.oy[slot] = no3[1]; o.oz[slot] = no3[2];
             }
-            __syncthreads();
-            if (threadIdx.x == 0)
-                for (int w = 0; w < nwarps; w++) { s_base[0] += s_cnt[0][w]; s_base[1] += s_cnt[1][w]; }
-            __syncthreads();
+            o.ux[slot] = nu[0]; o.uy[slot] = nu[1]; o.uz[slot] = nu[2];
+            if (code != 13) {
+                o.w[slot] = sa.buf.w[slot];
+                sa.dir[slot] = (uint8_t)code;
+                sa.llist[start + atomicAdd(&s_nleave, 1)] = i;
+                killAt(sa.buf, slot);
+            }
         }
-        if (threadIdx.x == 0) { sa.nstay[s] = s_base[0]; sa.nleave[s] = s_base[1]; }
+        __syncthreads();
+        if (threadIdx.x == 0) sa.nleave[s] = s_nleave;
         __syncthreads();
     }
     if (bad) atomicExch(a.flags, PICA_ERR_MIGRATION);
@@ -627,73 +645,219 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
     // CurrentDepositorYeeGrid.h:201-213; FP32: into the fixed-point accumulator,
     // the 1/h^3 is applied when J is formed from the exact sums.
     for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) {
-        const A v = jt[t];
-        if (v != A(0)) {
+        double vd = 0.0;
+        long long vq = 0;
+        if constexpr (PLAIN) vd = jt.p[t];
+        else vq = jt.node(t);
+        if (vd != 0.0 || vq != 0) {
             const int c = t / TT, r = t - c * TT;
             const int i = r / (T1 * T2), jj = (r / T2) % T1, k = r % T2;
             const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
             const int64_t node = ((int64_t)gx * a.n[1] + gy) * a.n[2] + gz;
-            if constexpr (PLAIN) atomicAdd(static_cast<double*>(a.j[c]) + node, v * a.norm);
-            else atomicAdd(a.jacc[c] + node, v);
+            if constexpr (PLAIN) atomicAdd(static_cast<double*>(a.j[c]) + node, vd * a.norm);
+            else atomicAdd(a.jacc[c] + node, (unsigned long long)vq);
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// Migration: one warp per destination supercell.  Arrivals are appended after
-// the destination's stayers in canonical order (direction code 0..26, then the
-// source's slot order).  REBUILD copies stayers + arrivals into a new layout.
+// Migration kernels.  A step's leaver lists (slots, in arbitrary order) are
+// sorted, then each destination supercell (one warp) takes its arrivals in
+// canonical order -- direction code 0..26, then source slot -- into the holes
+// its own leavers left (ascending), then appends.  The arrivals are counted
+// first so that a capacity overflow is known before anything is written.
 // ---------------------------------------------------------------------------
-template <class P, bool REBUILD>
+__device__ __forceinline__ int neighbour(const int* nsc, const int* dc, int code) {
+    const int ds[3] = {code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1};
+    return (wrapi(dc[0] - ds[0], nsc[0]) * nsc[1] + wrapi(dc[1] - ds[1], nsc[1])) * nsc[2] + wrapi(dc[2] - ds[2], nsc[2]);
+}
+
+// Sort each supercell's leaver list ascending with a bitmap over its slots (one CTA per supercell).
+template <class P>
+__global__ void __launch_bounds__(128) k_sortLeavers(const __grid_constant__ MigrateArgs<P> a) {
+    extern __shared__ unsigned int bits[];
+    const int s = blockIdx.x;
+    const int lane = threadIdx.x & 31;
+    for (int spi = 0; spi < a.nspecies; spi++) {
+        const MigrateSpecies<P>& sa = a.sp[spi];
+        const int n = sa.nleave[s];
+        if (n <= 1) continue;   // uniform across the block
+        const int64_t start = sa.start[s];
+        const int nw = (sa.count[s] + 31) / 32;
+        for (int w = threadIdx.x; w < nw; w += blockDim.x) bits[w] = 0u;
+        __syncthreads();
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const int slot = sa.llist[start + k];
+            atomicOr(&bits[slot >> 5], 1u << (slot & 31));
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int base = 0;
+            for (int w0 = 0; w0 < nw; w0 += 32) {
+                const int w = w0 + lane;
+                unsigned b = w < nw ? bits[w] : 0u;
+                const int c = __popc(b);
+                int incl = c;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, d);
+                    if (lane >= d) incl += t;
+                }
+                int pos = base + incl - c;
+                while (b) {
+                    const int bit = __ffs(b) - 1;
+                    sa.llist[start + pos++] = w * 32 + bit;
+                    b &= b - 1u;
+                }
+                base += __shfl_sync(0xffffffffu, incl, 31);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Arrivals of destination d, walked in canonical order; fn(k, srcSupercell, srcSlot, r)
+// is called by the matching lane with k the arrival's rank at d and r its index in the
+// source's leaver list.  Returns the number of arrivals.
+template <class P, class F>
+__device__ __forceinline__ int forArrivals(const MigrateArgs<P>& a, const MigrateSpecies<P>& sa, int d, F&& fn) {
+    const int lane = threadIdx.x & 31;
+    const int dc[3] = {d / (a.nsc[1] * a.nsc[2]), (d / a.nsc[2]) % a.nsc[1], d % a.nsc[2]};
+    const unsigned lt = (1u << lane) - 1u;
+    int pos = 0;
+    for (int code = 0; code < 27; code++) {
+        if (code == 13) continue;
+        const int src = neighbour(a.nsc, dc, code);
+        const int L = sa.nleave[src];
+        if (L == 0) continue;
+        const int64_t sst = sa.start[src];
+        for (int r0 = 0; r0 < L; r0 += 32) {
+            const int r = r0 + lane;
+            int slot = -1;
+            bool match = false;
+            if (r < L) {
+                slot = sa.llist[sst + r];
+                match = sa.dir[sst + slot] == code;
+            }
+            const unsigned mk = __ballot_sync(0xffffffffu, match);
+            if (match) fn(pos + __popc(mk & lt), src, slot, r);
+            pos += __popc(mk);
+        }
+    }
+    return pos;
+}
+
+template <class P, int STAGE>
 __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ MigrateArgs<P> a) {
     const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
     const int d = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (d >= nscTot) return;
-    const int dc[3] = {d / (a.nsc[1] * a.nsc[2]), (d / a.nsc[2]) % a.nsc[1], d % a.nsc[2]};
-    const unsigned lt = (1u << lane) - 1u;
+    if (STAGE == kFill && a.flags[1] != 0) return;   // overflow: the rebuild path runs instead
     for (int spi = 0; spi < a.nspecies; spi++) {
         const MigrateSpecies<P>& sa = a.sp[spi];
         const int64_t start = sa.start[d];
-        const int nstay = sa.nstay[d];
-        const int limit = sa.cap[d] - sa.nleave[d];
-        int64_t dstBase = start;
-        if constexpr (REBUILD) {
-            dstBase = sa.newStart[d];
-            for (int i = lane; i < nstay; i += 32) copyParticle(sa.buf, start + i, sa.dst, dstBase + i);
-        }
-        int pos = nstay;
-        bool over = false;
-        for (int code = 0; code < 27; code++) {
-            if (code == 13) continue;
-            const int ds[3] = {code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1};
-            const int src = (wrapi(dc[0] - ds[0], a.nsc[0]) * a.nsc[1] + wrapi(dc[1] - ds[1], a.nsc[1])) * a.nsc[2] +
-                            wrapi(dc[2] - ds[2], a.nsc[2]);
-            const int L = sa.nleave[src];
-            if (L == 0) continue;
-            const int64_t tail = sa.start[src] + sa.cap[src] - 1;
-            for (int r0 = 0; r0 < L; r0 += 32) {
-                const int r = r0 + lane;
-                const bool match = r < L && sa.dir[tail - r] == code;
-                const unsigned mk = __ballot_sync(0xffffffffu, match);
-                if (match) {
-                    const int dst = pos + __popc(mk & lt);
-                    if constexpr (REBUILD) copyParticle(sa.buf, tail - r, sa.dst, dstBase + dst);
-                    else {
-                        if (dst < limit) copyParticle(sa.buf, tail - r, sa.buf, start + dst);
-                        else over = true;
-                    }
-                }
-                pos += __popc(mk);
+        const int nh = sa.nleave[d];
+        const int cnt = sa.count[d];
+        int arrivals;
+        if constexpr (STAGE == kCountArrivals) {
+            arrivals = forArrivals(a, sa, d, [](int, int, int, int) {});
+            if (lane == 0) {
+                const int need = cnt + max(0, arrivals - nh);
+                sa.needed[d] = need;
+                sa.neededAlive[d] = sa.alive[d] - nh + arrivals;
+                if (need > sa.cap[d]) atomicExch(a.flags + 1, 1);
             }
+        } else if constexpr (STAGE == kFill) {
+            arrivals = forArrivals(a, sa, d, [&](int k, int src, int slot, int) {
+                const int target = k < nh ? sa.llist[start + k] : cnt + (k - nh);
+                copyParticle(sa.b, sa.start[src] + slot, sa.a, start + target);
+            });
+            if (lane == 0) { sa.count[d] = cnt + max(0, arrivals - nh); sa.alive[d] = sa.alive[d] - nh + arrivals; }
+        } else if constexpr (STAGE == kGatherOutbox) {
+            const int64_t off = sa.outOff[d];
+            for (int k = lane; k < nh; k += 32) copyParticle(sa.b, start + sa.llist[start + k], sa.outbox, off + k);
+        } else if constexpr (STAGE == kRebuild) {
+            const int64_t ns = sa.newStart[d];
+            for (int i = lane; i < cnt; i += 32) copyParticle(sa.a, start + i, sa.dst, ns + i);
+            __syncwarp();
+            arrivals = forArrivals(a, sa, d, [&](int k, int src, int, int r) {
+                const int target = k < nh ? sa.llist[start + k] : cnt + (k - nh);
+                copyParticle(sa.outbox, sa.outOff[src] + r, sa.dst, ns + target);
+            });
+            if (lane == 0) { sa.count[d] = cnt + max(0, arrivals - nh); sa.alive[d] = sa.alive[d] - nh + arrivals; }
         }
-        if (lane == 0) {
-            sa.needed[d] = pos;
-            if constexpr (REBUILD) sa.count[d] = pos;
-            else if (pos <= limit) sa.count[d] = pos;
+    }
+}
+
+// Local cell (lx*Sy + ly)*Sz + lz of a live particle of supercell with origin cell m.
+__device__ __forceinline__ int localCell(const PlainPtrs& p, int64_t i, const int* m, const int* S, const double* invh) {
+    const double x[3] = {p.x[i], p.y[i], p.z[i]};
+    int l[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) l[d] = min(max((int)floor(x[d] * invh[d]) - m[d], 0), S[d] - 1);
+    return (l[0] * S[1] + l[1]) * S[2] + l[2];
+}
+__device__ __forceinline__ int localCell(const CellPtrs& p, int64_t i, const int* m, const int* S, const double*) {
+    int c[3];
+    unpackCell(p.cell[i], c[0], c[1], c[2]);
+    return ((c[0] - m[0]) * S[1] + (c[1] - m[1])) * S[2] + (c[2] - m[2]);
+}
+
+// Compact each supercell (drop dead slots) and sort it by cell, stably, into the new
+// layout of buffer dst.  One warp per supercell; 512 cell bins per warp in shared memory.
+template <class P>
+__global__ void __launch_bounds__(128) k_resort(const __grid_constant__ MigrateArgs<P> a) {
+    __shared__ int bins[4][512];
+    const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int d = blockIdx.x * 4 + warp;
+    if (d >= nscTot) return;
+    int* b = bins[warp];
+    const int nb = a.S[0] * a.S[1] * a.S[2];
+    const int dc[3] = {d / (a.nsc[1] * a.nsc[2]), (d / a.nsc[2]) % a.nsc[1], d % a.nsc[2]};
+    const int m[3] = {dc[0] * a.S[0], dc[1] * a.S[1], dc[2] * a.S[2]};
+    const unsigned lt = (1u << lane) - 1u;
+    for (int spi = 0; spi < a.nspecies; spi++) {
+        const MigrateSpecies<P>& sa = a.sp[spi];
+        const int64_t start = sa.start[d], ns = sa.newStart[d];
+        const int cnt = sa.count[d];
+        for (int k = lane; k < nb; k += 32) b[k] = 0;
+        __syncwarp();
+        for (int i = lane; i < cnt; i += 32)
+            if (aliveAt(sa.a, start + i)) atomicAdd(&b[localCell(sa.a, start + i, m, a.S, a.invh)], 1);
+        __syncwarp();
+        // exclusive scan of the bins: 16 consecutive bins per lane
+        {
+            int loc[16], sum = 0;
+#pragma unroll
+            for (int k = 0; k < 16; k++) { const int j = lane * 16 + k; loc[k] = j < nb ? b[j] : 0; sum += loc[k]; }
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            int run = incl - sum;
+#pragma unroll
+            for (int k = 0; k < 16; k++) { const int j = lane * 16 + k; if (j < nb) b[j] = run; run += loc[k]; }
         }
-        over = __any_sync(0xffffffffu, over);
-        if (over && lane == 0) atomicExch(a.flags + 1, 1);
+        __syncwarp();
+        for (int i0 = 0; i0 < cnt; i0 += 32) {
+            const int i = i0 + lane;
+            const int key = (i < cnt && aliveAt(sa.a, start + i)) ? localCell(sa.a, start + i, m, a.S, a.invh) : -1;
+            const unsigned grp = __match_any_sync(0xffffffffu, key);
+            int base = 0;
+            if (key >= 0) base = b[key];
+            __syncwarp();
+            if (key >= 0) {
+                copyParticle(sa.a, start + i, sa.dst, ns + base + __popc(grp & lt));
+                if (lane == __ffs(grp) - 1) b[key] = base + __popc(grp);
+            }
+            __syncwarp();
+        }
+        if (lane == 0) sa.count[d] = sa.alive[d];
+        __syncwarp();
     }
 }
 

@@ -24,7 +24,7 @@ ME = 9.10938215e-28
 PI = 3.14159265358
 
 
-def case(name, n, sc, ppc, steps, seed, species=((ME, E),), field_amp=0.0, u_sigma=0.05):
+def case(name, n, sc, ppc, steps, seed, species=((ME, E),), field_amp=0.0, u_sigma=0.05, resort_every=0):
     rng = np.random.default_rng(seed)
     n0 = 1e18
     wp = np.sqrt(4 * PI * n0 * E * E / ME)
@@ -38,7 +38,7 @@ def case(name, n, sc, ppc, steps, seed, species=((ME, E),), field_amp=0.0, u_sig
     w = np.full(len(pos), n0 * np.prod(hh) / ppc) * (1.0 + 0.1 * rng.random(len(pos)))
     sp = rng.integers(0, len(species), len(pos)).astype(np.int32)
     f9 = [field_amp * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3
-    o = Oracle(n, sc, hh, dt, species=species, kind="reference")
+    o = Oracle(n, sc, hh, dt, species=species, kind="reference", resort_every=resort_every)
     o.load(pos[:, 0], pos[:, 1], pos[:, 2], u[:, 0], u[:, 1], u[:, 2], w, sp)
     o.set_fields(f9)
     counts, migs = [], []
@@ -51,7 +51,7 @@ def case(name, n, sc, ppc, steps, seed, species=((ME, E),), field_amp=0.0, u_sig
     f = o.get_fields()
     out = os.path.join(HERE, name + ".npz")
     np.savez_compressed(
-        out, n=np.array(n), sc=np.array(sc), h=np.array(hh), dt=dt, steps=steps,
+        out, n=np.array(n), sc=np.array(sc), h=np.array(hh), dt=dt, steps=steps, resort_every=resort_every,
         mass=np.array([m for m, _ in species]), charge=np.array([q for _, q in species]),
         in_x=pos[:, 0], in_y=pos[:, 1], in_z=pos[:, 2], in_ux=u[:, 0], in_uy=u[:, 1], in_uz=u[:, 2], in_w=w,
         in_species=sp, in_fields=np.stack(f9),
@@ -66,4 +66,4 @@ if __name__ == "__main__":
     case("cic_direct_8cube", (8, 8, 8), (2, 2, 2), 4, 5, seed=1)
     # Non-cubic grid and supercell, two species, non-zero initial E and B.
     case("cic_direct_2species", (8, 12, 16), (2, 2, 4), 3, 4, seed=2,
-         species=((ME, E), (ME * 4.0, -E)), field_amp=2.0e3, u_sigma=0.08)
+         species=((ME, E), (ME * 4.0, -E)), field_amp=2.0e3, u_sigma=0.08, resort_every=2)

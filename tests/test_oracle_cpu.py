@@ -13,7 +13,8 @@ REFERENCE_AVAILABLE = os.path.isdir("/root/reference/include/pica") or os.path.e
 
 
 def run_fixture(kind, g):
-    o = po.Oracle(tuple(g["n"]), tuple(g["sc"]), tuple(g["h"]), float(g["dt"]), species=species_of(g), kind=kind)
+    o = po.Oracle(tuple(g["n"]), tuple(g["sc"]), tuple(g["h"]), float(g["dt"]), species=species_of(g), kind=kind,
+                  resort_every=int(g["resort_every"]))
     o.load(g["in_x"], g["in_y"], g["in_z"], g["in_ux"], g["in_uy"], g["in_uz"], g["in_w"], g["in_species"])
     o.set_fields(list(g["in_fields"]))
     counts, migs = [], []
@@ -42,15 +43,15 @@ def test_port_reproduces_golden_bit_exactly(name):
 
 
 @pytest.mark.skipif(not REFERENCE_AVAILABLE, reason="pica sources not mounted here")
-@pytest.mark.parametrize("n,sc,ppc,steps", [((8, 8, 8), (2, 2, 2), 6, 3),
-                                            ((64, 4, 4), (2, 2, 2), 2, 3),   # supercell origin m=62: trunc(m h / h) = 61
-                                            ((12, 8, 6), (3, 4, 2), 4, 3)])
-def test_port_matches_reference_headers(n, sc, ppc, steps):
+@pytest.mark.parametrize("n,sc,ppc,steps,resort", [((8, 8, 8), (2, 2, 2), 6, 3, 0),
+                                                   ((64, 4, 4), (2, 2, 2), 2, 3, 2),  # origin m=62: trunc(m h / h) = 61
+                                                   ((12, 8, 6), (3, 4, 2), 4, 5, 2)])
+def test_port_matches_reference_headers(n, sc, ppc, steps, resort):
     po.build(reference=True)
     d = thermal_inputs(n, ppc, seed=11, u_sigma=0.1)
     res = []
     for kind in ("port", "reference"):
-        o = po.Oracle(n, sc, d["h"], d["dt"], kind=kind)
+        o = po.Oracle(n, sc, d["h"], d["dt"], kind=kind, resort_every=resort)
         o.load(d["x"], d["y"], d["z"], d["ux"], d["uy"], d["uz"], d["w"])
         rng = np.random.default_rng(3)
         o.set_fields([1e3 * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3)
