@@ -143,7 +143,12 @@ __device__ __forceinline__ void drainQueue(const float* q, int nq, const FixTile
     }
 }
 
-template <int SHAPE, int K, int THREADS, int MINB>
+// Wrap a cell index that is at most one period out of range.
+__device__ __forceinline__ int wrapNear(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+// SC > 0: cubic supercells of edge SC known at compile time (tile strides become
+// constants); SC == 0: edges read from the arguments.
+template <int SHAPE, int K, int THREADS, int MINB, int SC>
 __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __grid_constant__ PushArgs<CellPtrs> a) {
     constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;   // stay-in-window nodes per dimension
     constexpr int NV = 3 * (NWn - 1) * NWn * NWn;          // 54 (TSC) or 12 (CIC)
@@ -153,7 +158,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
     __shared__ int s_nleave;
     __shared__ float sQueue[kWarps][kQ * kQWords];
 
-    const int T1 = a.T[1], T2 = a.T[2], TT = a.T[0] * T1 * T2;
+    const int T1 = SC ? SC + 2 * kG + 1 : a.T[1], T2 = SC ? SC + 2 * kG + 1 : a.T[2];
+    const int TT = (SC ? SC + 2 * kG + 1 : a.T[0]) * T1 * T2;
+    const int Sx = SC ? SC : a.S[0], Sy = SC ? SC : a.S[1], Sz = SC ? SC : a.S[2];
+    const int Sv[3] = {Sx, Sy, Sz};
     FixTile jt;
     jt.lo = reinterpret_cast<unsigned int*>(smem_raw);
     jt.hi = reinterpret_cast<int*>(jt.lo + 3 * TT);
@@ -164,7 +172,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
     sc[2] = s % a.nsc[2];
     sc[1] = (s / a.nsc[2]) % a.nsc[1];
     sc[0] = s / (a.nsc[1] * a.nsc[2]);
-    const int m[3] = {sc[0] * a.S[0], sc[1] * a.S[1], sc[2] * a.S[2]};
+    const int m[3] = {sc[0] * Sx, sc[1] * Sy, sc[2] * Sz};
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
     float* myQ = sQueue[warp];
@@ -262,7 +270,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
                     bool inRange = true;
 #pragma unroll
                     for (int d = 0; d < 3; d++)
-                        inRange = inRange && ln[d] >= -1 && ln[d] <= a.S[d] && abs(ln[d] - lc[d]) <= 1 &&
+                        inRange = inRange && ln[d] >= -1 && ln[d] <= Sv[d] && abs(ln[d] - lc[d]) <= 1 &&
                                   on[d] >= 0.0f && on[d] < 1.0f;
                     if (!inRange) {
                         bad = true;
@@ -341,11 +349,15 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
                         qe[9] = __int_as_float(((lc[0] + 4) << 16) | ((lc[1] + 4) << 8) | (lc[2] + 4));
                         qe[10] = __int_as_float(((ln[0] + 4) << 16) | ((ln[1] + 4) << 8) | (ln[2] + 4));
                     }
+                    // New cell (periodic) and the move's direction code, from the wrapped
+                    // supercell coordinates (with one or two supercells along a dimension
+                    // the periodic +1 and -1 neighbours coincide; dirCode resolves that
+                    // the same way the oracle does).
                     int gc[3], nsc3[3];
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
-                        gc[d] = wrapi(m[d] + ln[d], a.n[d]);
-                        nsc3[d] = gc[d] / a.S[d];
+                        gc[d] = wrapNear(m[d] + ln[d], a.n[d]);
+                        nsc3[d] = gc[d] / Sv[d];
                     }
                     const int code = dirCode(sc, nsc3, a.nsc, bad);
                     // Stayers in place (the weight does not change); a leaver goes to the side

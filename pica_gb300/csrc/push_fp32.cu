@@ -18,19 +18,26 @@ int launchOne(const PushArgs<CellPtrs>& a, cudaStream_t s) {
 }
 }  // namespace
 
-template <int SHAPE>
-int launchEsirkepov(const PushArgs<CellPtrs>& a, cudaStream_t s) {
+template <int SHAPE, int SC>
+int launchEsirkepovS(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     const int TT = a.T[0] * a.T[1] * a.T[2];
     constexpr int K = 8, THREADS = 128, MINB = 3;
-    const size_t smem = (size_t)6 * TT * sizeof(float) + (size_t)3 * TT * sizeof(unsigned long long) +
-                        (size_t)(THREADS / 32) * K * 32 * (8 * sizeof(uint32_t) + 1);
-    auto k = k_push_cell_esirkepov<SHAPE, K, THREADS, MINB>;
+    const size_t smem = (size_t)6 * TT * sizeof(float) + (size_t)3 * TT * 2 * sizeof(uint32_t);
+    auto k = k_push_cell_esirkepov<SHAPE, K, THREADS, MINB, SC>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return (int)e;
     const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
     k<<<nscTot, THREADS, smem, s>>>(a);
     return (int)cudaGetLastError();
+}
+
+template <int SHAPE>
+int launchEsirkepov(const PushArgs<CellPtrs>& a, cudaStream_t s) {
+    const bool cubic = a.S[0] == a.S[1] && a.S[1] == a.S[2];
+    if (cubic && a.S[0] == 4) return launchEsirkepovS<SHAPE, 4>(a, s);
+    if (cubic && a.S[0] == 2) return launchEsirkepovS<SHAPE, 2>(a, s);
+    return launchEsirkepovS<SHAPE, 0>(a, s);
 }
 
 int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int dep, cudaStream_t s) {
