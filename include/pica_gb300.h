@@ -113,6 +113,10 @@ int         pica_synchronize(pica_ctx* ctx);
 const char* pica_last_error(pica_ctx* ctx);
 /* Kernels this context has launched since creation (for launch accounting). */
 int64_t     pica_launch_count(pica_ctx* ctx);
+/* Launch shape of the FP32 charge-conserving push kernel (no counterpart in pica,
+ * which has no GPU path): 0..count-1, chosen by pica_gb300.autotune. */
+int         pica_set_variant(pica_ctx* ctx, int32_t variant);
+int         pica_get_variant(pica_ctx* ctx, int32_t* variant, int32_t* count);
 
 /* Particles.  Replaces EnsembleSupercells::add (EnsembleSupercells.h:41-45) for
  * every particle: particles are routed to supercells by

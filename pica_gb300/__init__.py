@@ -100,6 +100,15 @@ class Simulation:
     def launch_count(self):
         return int(self.lib.pica_launch_count(self.ctx))
 
+    def set_variant(self, variant):
+        """Launch shape of the FP32 charge-conserving push kernel (see pica_gb300.autotune)."""
+        self._check(self.lib.pica_set_variant(self.ctx, int(variant)))
+
+    def variant(self):
+        v, n = C.c_int32(), C.c_int32()
+        self._check(self.lib.pica_get_variant(self.ctx, C.byref(v), C.byref(n)))
+        return v.value, n.value
+
     # -- data ----------------------------------------------------------------
     def upload_particles(self, x, y, z, ux, uy, uz, w, species=None):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z, ux, uy, uz, w)]

@@ -45,6 +45,8 @@ SIGNATURES = {
     "pica_synchronize": (C.c_int, [_vp]),
     "pica_last_error": (C.c_char_p, [_vp]),
     "pica_launch_count": (_i64, [_vp]),
+    "pica_set_variant": (C.c_int, [_vp, _i32]),
+    "pica_get_variant": (C.c_int, [_vp, _ip, _ip]),
     "pica_upload_particles": (C.c_int, [_vp, _i64] + [_dp] * 7 + [_ip]),
     "pica_num_particles": (_i64, [_vp]),
     "pica_download_particles": (C.c_int, [_vp] + [_dp] * 7 + [_ip, _ip]),

@@ -1,0 +1,77 @@
+"""Autotuner for the supercell PIC step.
+
+Three knobs change speed but not results (the FP32 deposit sums are exact, so
+every choice gives the same particles and fields bit for bit):
+
+* the launch variant of the FP32 charge-conserving push kernel (particles per
+  lane, CTAs per SM) -- ``tune_variant`` times each on the live simulation;
+* the in-supercell resort cadence (how often each supercell is compacted and
+  re-sorted by cell, which keeps the warps of the push kernel on one cell);
+* the supercell edge (tile size against particles per CTA).
+
+``tune_config`` searches the last two on a sample of the workload (a block of
+the grid with the same particles per cell) through a caller-supplied factory
+and caches the answer in a JSON file keyed by grid, particles per cell, form,
+shape and depositor.
+"""
+import json
+import os
+import time
+
+DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "pica_gb300", "autotune.json")
+
+
+def _timed_steps(sim, steps):
+    sim.synchronize()
+    t = time.perf_counter()
+    sim.step(steps)
+    sim.synchronize()
+    return (time.perf_counter() - t) / steps
+
+
+def tune_variant(sim, steps=2):
+    """Time every launch variant for `steps` steps (the simulation advances by
+    variants x (steps + 1) steps) and keep the fastest.  Returns {variant: s/step}."""
+    _, count = sim.variant()
+    times = {}
+    for v in range(count):
+        sim.set_variant(v)
+        sim.step(1)  # first launch of a variant sets its attributes
+        times[v] = _timed_steps(sim, steps)
+    best = min(times, key=times.get)
+    sim.set_variant(best)
+    return times
+
+
+def config_key(n, ppc, form, shape, deposit):
+    return f"{n[0]}x{n[1]}x{n[2]}|ppc={ppc}|form={form}|shape={shape}|deposit={deposit}"
+
+
+def tune_config(make_sim, key, supercells=((4, 4, 4), (2, 2, 2)), cadences=(4, 8, 16), steps=4, cache=DEFAULT_CACHE):
+    """make_sim(supercell, resort_every) -> Simulation with particles and fields loaded
+    (a sample of the workload).  Returns the best {"supercell", "resort_every",
+    "variant", "s_per_step"} and stores it in `cache` under `key`."""
+    if cache and os.path.exists(cache):
+        with open(cache) as f:
+            known = json.load(f)
+        if key in known:
+            return known[key]
+    else:
+        known = {}
+    best = None
+    for sc in supercells:
+        for every in cadences:
+            sim = make_sim(sc, every)
+            vt = tune_variant(sim, steps=1)
+            v = min(vt, key=vt.get)
+            sim.set_variant(v)
+            t = _timed_steps(sim, steps)
+            sim.close()
+            if best is None or t < best["s_per_step"]:
+                best = {"supercell": list(sc), "resort_every": every, "variant": v, "s_per_step": t}
+    if cache:
+        os.makedirs(os.path.dirname(cache), exist_ok=True)
+        known[key] = best
+        with open(cache, "w") as f:
+            json.dump(known, f, indent=1)
+    return best

@@ -68,6 +68,7 @@ struct pica_ctx {
     double kmax = 1.0;      // power of two bounding |q w| max(c, h/dt) (sets the J fixed-point unit)
     int jfrac = 40;         // fraction bits of the J fixed point (see pica_internal.h)
     int tileSplit = 16;     // low bits of the split shared-memory tile sums (FP32 form)
+    int variant = 0;        // launch variant of the FP32 Esirkepov push kernel
     std::string err;
     int64_t launches = 0;
     int64_t steps = 0;
@@ -322,6 +323,19 @@ int pica_ctx_destroy(pica_ctx* ctx) {
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
     if (ctx->d_rho) cudaFree(ctx->d_rho);
     delete ctx;
+    return PICA_OK;
+}
+
+int pica_set_variant(pica_ctx* ctx, int32_t variant) {
+    if (!ctx || variant < 0 || variant >= kPushVariants) return fail(ctx, PICA_ERR_INVALID, "no such push variant");
+    ctx->variant = variant;
+    return PICA_OK;
+}
+
+int pica_get_variant(pica_ctx* ctx, int32_t* variant, int32_t* count) {
+    if (!ctx) return PICA_ERR_INVALID;
+    if (variant) *variant = ctx->variant;
+    if (count) *count = kPushVariants;
     return PICA_OK;
 }
 
@@ -618,7 +632,7 @@ int pica_push_deposit(pica_ctx* ctx) {
         PushArgs<CellPtrs> a{};
         fill(a);
         for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = cellPtrs(ctx, q, ctx->cur); a.sp[q].out = cellPtrs(ctx, q, 1 - ctx->cur); }
-        CKL(launchPushCell(a, c.shape, c.deposit, ctx->stream));
+        CKL(launchPushCell(a, c.shape, c.deposit, ctx->variant, ctx->stream));
     }
     ctx->launches++;
     if (!ctx->fp64) {

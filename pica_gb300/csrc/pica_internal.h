@@ -122,7 +122,9 @@ struct MigrateArgs {
 
 // Push launchers (push_fp64.cu / push_fp32.cu).  Return cudaError_t as int.
 int launchPushPlain(const PushArgs<PlainPtrs>& a, int shape, int deposit, cudaStream_t s);
-int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int deposit, cudaStream_t s);
+// variant: launch shape of the FP32 Esirkepov kernel (0..kPushVariants-1), see push_fp32.cu.
+constexpr int kPushVariants = 4;
+int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int deposit, int variant, cudaStream_t s);
 // Migration stages.
 enum MigrateStage { kSortLeavers = 0, kCountArrivals = 1, kFill = 2, kGatherOutbox = 3, kRebuild = 4, kResort = 5 };
 int launchMigratePlain(const MigrateArgs<PlainPtrs>& a, int stage, cudaStream_t s);

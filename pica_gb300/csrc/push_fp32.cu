@@ -18,10 +18,9 @@ int launchOne(const PushArgs<CellPtrs>& a, cudaStream_t s) {
 }
 }  // namespace
 
-template <int SHAPE, int SC>
-int launchEsirkepovS(const PushArgs<CellPtrs>& a, cudaStream_t s) {
+template <int SHAPE, int SC, int K, int THREADS, int MINB>
+int launchEsirkepovV(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     const int TT = a.T[0] * a.T[1] * a.T[2];
-    constexpr int K = 8, THREADS = 128, MINB = 3;
     const size_t smem = (size_t)6 * TT * sizeof(float) + (size_t)3 * TT * 2 * sizeof(uint32_t);
     auto k = k_push_cell_esirkepov<SHAPE, K, THREADS, MINB, SC>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -32,17 +31,31 @@ int launchEsirkepovS(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     return (int)cudaGetLastError();
 }
 
-template <int SHAPE>
-int launchEsirkepov(const PushArgs<CellPtrs>& a, cudaStream_t s) {
-    const bool cubic = a.S[0] == a.S[1] && a.S[1] == a.S[2];
-    if (cubic && a.S[0] == 4) return launchEsirkepovS<SHAPE, 4>(a, s);
-    if (cubic && a.S[0] == 2) return launchEsirkepovS<SHAPE, 2>(a, s);
-    return launchEsirkepovS<SHAPE, 0>(a, s);
+// Launch variants of the Esirkepov kernel.  All keep K = 8 particles per lane, so the
+// particles summed together in registers (and hence every rounding) are the same and
+// the variants give bit-identical results; they differ in CTA size and occupancy:
+// 0: 128 threads, >= 3 CTAs/SM   1: 128 threads, >= 2 CTAs/SM
+// 2: 64 threads, >= 6 CTAs/SM    3: 256 threads, >= 1 CTA/SM.
+template <int SHAPE, int SC>
+int launchEsirkepovS(const PushArgs<CellPtrs>& a, int variant, cudaStream_t s) {
+    switch (variant) {
+        case 1: return launchEsirkepovV<SHAPE, SC, 8, 128, 2>(a, s);
+        case 2: return launchEsirkepovV<SHAPE, SC, 8, 64, 6>(a, s);
+        case 3: return launchEsirkepovV<SHAPE, SC, 8, 256, 1>(a, s);
+        default: return launchEsirkepovV<SHAPE, SC, 8, 128, 3>(a, s);
+    }
 }
 
-int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int dep, cudaStream_t s) {
-    if (shape == PICA_SHAPE_TSC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchEsirkepov<PICA_SHAPE_TSC>(a, s);
-    if (shape == PICA_SHAPE_CIC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchEsirkepov<PICA_SHAPE_CIC>(a, s);
+template <int SHAPE>
+int launchEsirkepov(const PushArgs<CellPtrs>& a, int variant, cudaStream_t s) {
+    const bool cubic = a.S[0] == a.S[1] && a.S[1] == a.S[2];
+    if (cubic && a.S[0] == 4) return launchEsirkepovS<SHAPE, 4>(a, variant, s);
+    return launchEsirkepovS<SHAPE, 0>(a, variant, s);
+}
+
+int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int dep, int variant, cudaStream_t s) {
+    if (shape == PICA_SHAPE_TSC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchEsirkepov<PICA_SHAPE_TSC>(a, variant, s);
+    if (shape == PICA_SHAPE_CIC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchEsirkepov<PICA_SHAPE_CIC>(a, variant, s);
     if (shape == PICA_SHAPE_CIC && dep == PICA_DEPOSIT_DIRECT) return launchOne<PICA_SHAPE_CIC, PICA_DEPOSIT_DIRECT>(a, s);
     if (shape == PICA_SHAPE_CIC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchOne<PICA_SHAPE_CIC, PICA_DEPOSIT_ESIRKEPOV>(a, s);
     if (shape == PICA_SHAPE_TSC && dep == PICA_DEPOSIT_DIRECT) return launchOne<PICA_SHAPE_TSC, PICA_DEPOSIT_DIRECT>(a, s);

@@ -255,3 +255,40 @@ def test_error_paths_do_not_fault():
     # The context stays usable.
     s.step(2)
     assert s.num_particles() == len(d["x"])
+
+
+@pytest.mark.parametrize("shape", [pg.SHAPE_CIC, pg.SHAPE_TSC])
+def test_push_variants_give_identical_results(shape):
+    """Every launch variant of the FP32 charge-conserving push kernel gives the same
+    particles and fields bit for bit (the J sums are exact integers)."""
+    n, sc = (16, 8, 8), (4, 4, 4)
+    d = thermal_inputs(n, 10, seed=77, u_sigma=0.2)
+    out = []
+    _, count = gpu_sim(n, sc, d["h"], d["dt"], form=pg.FORM_FP32_CELL).variant()
+    for v in range(count):
+        s = gpu_sim(n, sc, d["h"], d["dt"], form=pg.FORM_FP32_CELL, shape=shape, deposit=pg.DEPOSIT_ESIRKEPOV,
+                    resort_every=3)
+        s.set_variant(v)
+        s.upload_particles(*particle_args(d))
+        s.upload_fields([np.zeros(n)] * 9)
+        s.step(6)
+        out.append((s.particles(), s.fields()))
+    for p, f in out[1:]:
+        for k in ("x", "y", "z", "ux", "uy", "uz", "w", "supercell"):
+            assert np.array_equal(p[k], out[0][0][k]), k
+        for c in range(9):
+            assert np.array_equal(f[c], out[0][1][c]), c
+
+
+def test_autotune_picks_a_variant():
+    from pica_gb300 import autotune
+    n = (16, 16, 16)
+    d = thermal_inputs(n, 8, seed=5)
+    s = gpu_sim(n, (4, 4, 4), d["h"], d["dt"], form=pg.FORM_FP32_CELL, shape=pg.SHAPE_TSC,
+                deposit=pg.DEPOSIT_ESIRKEPOV, resort_every=4)
+    s.upload_particles(*particle_args(d))
+    s.upload_fields([np.zeros(n)] * 9)
+    times = autotune.tune_variant(s, steps=1)
+    assert len(times) == s.variant()[1]
+    assert s.variant()[0] == min(times, key=times.get)
+    assert s.num_particles() == len(d["x"])
