@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--edge", type=int, default=128, help="grid edge (cells); 128 is the reference workload")
     ap.add_argument("--resort-every", type=int, default=8, help="in-supercell cell sort cadence (steps)")
+    ap.add_argument("--variant", type=int, default=-1, help="push-kernel launch variant (-1: autotune)")
     return ap.parse_args()
 
 
@@ -234,7 +235,11 @@ def main():
 
     # Launch variant of the push kernel chosen on this workload (part of the warm-up).
     from pica_gb300 import autotune
-    tune = autotune.tune_variant(sim, steps=1)
+    if args.variant < 0:
+        tune = autotune.tune_variant(sim, steps=1)
+    else:
+        sim.set_variant(args.variant)
+        tune = {}
     for _ in range(args.warmup):
         one_step()
     barrier()

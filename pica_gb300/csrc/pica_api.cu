@@ -131,12 +131,14 @@ void updateJFrac(pica_ctx* ctx) {
     int64_t cover = 1;
     for (int d = 0; d < 3; d++) cover *= (ctx->cfg.sc[d] + 2 * kG + 1 + ctx->cfg.sc[d] - 1) / ctx->cfg.sc[d];
     const double worst = (double)cover * (double)std::max<int64_t>(maxCaps, 1) + 1.0;
-    // Shared-memory tile: a node receives at most one contribution per particle of
-    // its supercell (all species): low part L bits summed unsigned, high part signed,
-    // each sum below 2^31: L = 31 - b and F <= 62 - 2b with b = bits(largest count).
+    // Shared-memory tile: a node receives at most one addition per particle of its
+    // supercell (all species), each below 2^F in magnitude.  With maxCaps < 2^b the
+    // unsigned low part (L bits per addition) stays below 2^32 for L <= 32 - b, and
+    // the signed high part, |sum floor(v / 2^L)| <= 2^(F+b-L) + 2^b, below 2^31 for
+    // F <= 29 + L - b.  L <= 23 keeps the split exact in FP32 (FixTile::add).
     const int b = (int)std::ceil(std::log2((double)std::max<int64_t>(maxCaps, 1) + 1.0));
-    ctx->tileSplit = 31 - b;
-    ctx->jfrac = std::min(std::min(kJFracBitsMax, 62 - (int)std::ceil(std::log2(worst))), 62 - 2 * b);
+    ctx->tileSplit = std::min(31 - b, 23);
+    ctx->jfrac = std::min(std::min(kJFracBitsMax, 62 - (int)std::ceil(std::log2(worst))), 29 + ctx->tileSplit - b);
 }
 
 int ensureBuffer(pica_ctx* ctx, int spi, int b, int64_t slots) {

@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
     FixTile jt;
     jt.lo = reinterpret_cast<unsigned int*>(smem_raw);
     jt.hi = reinterpret_cast<int*>(jt.lo + 3 * TT);
-    jt.L = a.tileSplit;
+    jt.setSplit(a.tileSplit);
     float* eb = reinterpret_cast<float*>(jt.hi + 3 * TT);
     const int s = blockIdx.x;
     int sc[3];

@@ -56,12 +56,27 @@ __device__ __forceinline__ void tscWeights(R d, R* w) {
 struct FixTile {
     unsigned int* lo;
     int* hi;
-    int L;
+    int L;       // low-part bits, 1..23
+    float up;    // 2^L
+    float down;  // 2^-L
+    __device__ __forceinline__ void setSplit(int bits) {
+        L = bits;
+        up = __int_as_float((127 + bits) << 23);
+        down = __int_as_float((127 - bits) << 23);
+    }
+    // Adds v = round-to-nearest-even(scaled) as hi*2^L + lo, lo in [0, 2^L), with
+    // 32-bit operations only (a 64-bit float-to-integer conversion runs on the
+    // FP64 pipe, which is narrow on this part).  r = rint(scaled) is an integer
+    // m*2^e with |m| < 2^24; h = floor(r 2^-L) is exact, and r - h 2^L is a
+    // multiple of 2^e below 2^L <= 2^23, hence exact in FP32 and recovered from
+    // the mantissa of (l + 2^23).
     __device__ __forceinline__ void add(int idx, float scaled) const {
-        const long long v = __float2ll_rn(scaled);
-        if (v != 0) {
-            atomicAdd(lo + idx, (unsigned int)(v & ((1ll << L) - 1)));
-            atomicAdd(hi + idx, (int)(v >> L));
+        const float r = rintf(scaled);
+        if (r != 0.f) {
+            const float h = floorf(r * down);
+            const float l = fmaf(-h, up, r);
+            atomicAdd(lo + idx, __float_as_uint(l + 8388608.0f) - 0x4B000000u);
+            atomicAdd(hi + idx, __float2int_rz(h));
         }
     }
     __device__ __forceinline__ long long node(int idx) const { return ((long long)hi[idx] << L) + (long long)lo[idx]; }
@@ -265,7 +280,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
     } else {
         jt.lo = reinterpret_cast<unsigned int*>(smem_raw);
         jt.hi = reinterpret_cast<int*>(jt.lo + 3 * TT);
-        jt.L = a.tileSplit;
+        jt.setSplit(a.tileSplit);
         eb = reinterpret_cast<R*>(jt.hi + 3 * TT);
     }
     const int s = blockIdx.x;
