@@ -164,6 +164,22 @@ int     pica_charge_density(pica_ctx* ctx, double* rho);
 /* Field energy sum over the grid (FP64, deterministic two-pass reduction). */
 int     pica_field_energy(pica_ctx* ctx, double* out);
 
+/* Field energy of six caller-owned device arrays (ex ey ez bx by bz, Array3d
+ * order, n[0] x n[1] x n[2] nodes, double if fp64 else float) with no context
+ * and no allocation, for callers that must not allocate: a diagnostics hook
+ * beside a live step (cudaMalloc and cudaFree synchronise the device), an
+ * application whose memory pool has reserved the device, or a component that
+ * owns its fields but has no pica context.  The scratch is one static device
+ * array of 16384 partial sums (128 KB), so grids above 512^3 = 134,217,728
+ * nodes return PICA_ERR_LIMIT.  The first call on each device looks the
+ * scratch address up (cudaGetSymbolAddress) with that device current: make it
+ * before any stream capture.  Calls that can overlap on the GPU (other streams,
+ * other host threads) race on the one scratch: serialise them.  Runs on
+ * `stream` (a cudaStream_t, 0 for the legacy stream) and synchronises it.
+ * No counterpart in the reference. */
+int     pica_field_energy_noalloc(const void* const* fields, int32_t fp64, const int32_t* n, const double* h,
+                                  void* stream, double* out);
+
 /* Device state, for host loops that keep the particle state in host memory
  * between steps: raw copies of the current particle buffer (the device
  * layout, slot arrays of pica_state_slots() entries per species and

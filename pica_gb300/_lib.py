@@ -61,6 +61,7 @@ SIGNATURES = {
     "pica_diagnostics": (C.c_int, [_vp, C.c_double, C.POINTER(PicaDiag)]),
     "pica_charge_density": (C.c_int, [_vp, _dp]),
     "pica_field_energy": (C.c_int, [_vp, _dp]),
+    "pica_field_energy_noalloc": (C.c_int, [C.POINTER(_vp), _i32, _ip, _dp, _vp, _dp]),
     "pica_state_slots": (_i64, [_vp, _i32]),
     "pica_state_copy": (C.c_int, [_vp, _i32, _i32, _vp, _i32]),
     "pica_plasma_count": (_i64, [C.POINTER(PicaPlasmaSpec)]),

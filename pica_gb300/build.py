@@ -22,6 +22,7 @@ UNITS = [
     ("push_fp64.cu", ["--fmad=false"]),
     ("push_fp32.cu", []),
     ("grid_kernels.cu", ["--fmad=false"]),
+    ("noalloc.cu", ["--fmad=false"]),
 ]
 
 
