@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--edge", type=int, default=128, help="grid edge (cells); 128 is the reference workload")
     ap.add_argument("--resort-every", type=int, default=8, help="in-supercell cell sort cadence (steps)")
     ap.add_argument("--variant", type=int, default=-1, help="push-kernel launch variant (-1: autotune)")
+    ap.add_argument("--validate-steps", type=int, default=1000,
+                    help="steps of the FP32-vs-FP64 error run on a 32^3 block (0: skip)")
     return ap.parse_args()
 
 
@@ -349,6 +351,12 @@ def main():
                 "steps": args.fp64_steps, "dtype": "fp64", "form": "FP64 plain (absolute positions)"}
         s64.close()
 
+    # ---------------- FP32 form against the FP64 plain form (error metrics) ----------------
+    errors = None
+    if args.validate_steps > 0 and rank == 0:
+        from pica_gb300 import validate
+        errors = validate.compare_forms(n=(32, 32, 32), ppc=100, steps=args.validate_steps, every=20)
+
     if rank != 0:
         if dist is not None:
             dist.barrier()
@@ -370,6 +378,7 @@ def main():
         "step_hbm_frac": step_alg / (elapsed / K) / 1e9 / peak,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
         "fp64_form": fp64, "fp32_over_fp64": (value / world / fp64["value"]) if fp64 else None,
+        "fp32_vs_fp64_errors": errors,
         "tuning": {"push_variant": sim_variant, "variant_s_per_step": {str(k): v for k, v in tune.items()},
                    "resort_every": args.resort_every},
     }

@@ -1,13 +1,18 @@
 """Autotuner for the supercell PIC step.
 
-Three knobs change speed but not results (the FP32 deposit sums are exact, so
-every choice gives the same particles and fields bit for bit):
+Three knobs change speed:
 
-* the launch variant of the FP32 charge-conserving push kernel (particles per
-  lane, CTAs per SM) -- ``tune_variant`` times each on the live simulation;
+* the launch variant of the FP32 charge-conserving push kernel (CTA size and
+  CTAs per SM) -- ``tune_variant`` times each on the live simulation.  Every
+  variant sums the same particles in the same order, so the results are the same
+  bit for bit;
 * the in-supercell resort cadence (how often each supercell is compacted and
   re-sorted by cell, which keeps the warps of the push kernel on one cell);
 * the supercell edge (tile size against particles per CTA).
+
+The last two change the order of particles within a supercell and hence the
+FP32 rounding of the pre-summed window currents (results agree to FP32 rounding,
+not bit for bit).
 
 ``tune_config`` searches the last two on a sample of the workload (a block of
 the grid with the same particles per cell) through a caller-supplied factory

@@ -4,63 +4,33 @@
 // sort):
 //
 //  * A warp owns a contiguous segment of 32*K particles of its supercell; lane
-//    l handles the K consecutive particles lK .. lK+K-1, so a lane rarely
-//    changes cell and the warp's lanes mostly share one or two cells.
-//  * Particles that stay in their cell (about 96% per step for a thermal
-//    plasma at half the Courant step) have old and new shapes on the same
-//    3 (TSC) or 2 (CIC) rho-lattice nodes per dimension, so their Esirkepov
-//    current lives on a fixed small window of faces (54 values for TSC, 12
-//    for CIC).  Each lane sums its particles' window contributions in
-//    registers; at the end of the segment the warp reduces the windows of
-//    lanes that share a cell with a transposed shuffle reduction (each lane
-//    ends with 2 of the 64 padded sums) and issues at most two 64-bit integer
-//    shared-memory atomics per lane.  Compared with one atomic per
-//    contribution per particle this removes the 32-way same-address
-//    serialisation of the shared-memory atomics.
+//    l handles the K consecutive particles lK .. lK+K-1 (the next one's data is
+//    loaded one iteration ahead), so a lane rarely changes cell and the warp's
+//    lanes mostly share one or two cells.
+//  * Particles that keep their rho-lattice window (the cell for TSC; about 96%
+//    per step for a thermal plasma at half the Courant step) deposit on a fixed
+//    small window of faces (54 values for TSC, 12 for CIC).  Each lane sums
+//    its particles' window contributions in registers, keyed by the window.
+//    When a lane meets a particle of another window it parks its sums in a
+//    spare row of the warp's shared-memory reduction area.  At the end of the
+//    segment every lane writes its sums to its own row, and the warp adds the
+//    rows of each window in a fixed order (lane rows, then park rows in the
+//    order they were taken): lane t sums values t and t+32 over the rows and
+//    issues one fixed-point shared-memory atomic per value.  The order depends
+//    only on the particle data, so the result is reproducible bit for bit.
 //  * Particles whose window changes are queued in a per-warp shared-memory
-//    queue and deposited densely on the general 4- (TSC) or 3-node (CIC)
-//    window when it fills and at the end.
+//    ring and deposited on the general 4- (TSC) or 3-node (CIC) window, 32 at a
+//    time (one per lane), by one out-of-line routine.
 //  * Stayers are written back in place; leavers go to the side buffer at
 //    their own slot (see pica_internal.h), so the kernel needs no block-wide
 //    synchronisation between the tile staging and the final tile flush.
+//  * The E/B tile holds only the nodes that the gather reads, m-1 .. m+S+1
+//    per dimension; the current tile spans m-2 .. m+S+2 (general windows).
 #pragma once
 
 #include "push_kernels.cuh"
 
 namespace pgb {
-
-// Sum NV (<= 64, padded to 64) per-lane values over the warp: lane l returns the
-// sums of values 2l and 2l+1 in s0, s1.  Values of lanes with take == false
-// count as zero.  62 shuffles per lane.
-template <int NV>
-__device__ __forceinline__ void warpTransposeSum(const float* v, bool take, int lane, float& s0, float& s1) {
-    float x[32];
-    // round 0 (partner lane ^ 16): keep the half selected by lane bit 4.
-    {
-        const bool hi = (lane >> 4) & 1;
-#pragma unroll
-        for (int k = 0; k < 32; k++) {
-            const float a = (k < NV && take) ? v[k] : 0.0f;
-            const float b = (k + 32 < NV && take) ? v[k + 32] : 0.0f;
-            const float send = hi ? a : b;
-            const float keep = hi ? b : a;
-            x[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-        }
-    }
-#pragma unroll
-    for (int r = 1; r < 5; r++) {
-        const int half = 32 >> r, mask = 16 >> r;
-        const bool hi = (lane >> (4 - r)) & 1;
-#pragma unroll
-        for (int k = 0; k < half; k++) {
-            const float send = hi ? x[k] : x[k + half];
-            const float keep = hi ? x[k + half] : x[k];
-            x[k] = keep + __shfl_xor_sync(0xffffffffu, send, mask);
-        }
-    }
-    s0 = x[0];
-    s1 = x[1];
-}
 
 // Tile address of window contribution j for the stay-in-cell Esirkepov window
 // starting at tile node b (per dimension).  TSC: NWn = 3 nodes, 2 faces;
@@ -99,8 +69,8 @@ constexpr int kQWords = 11;  // queued window change: o[3], on[3], kq[3], packed
 
 // Esirkepov deposit of a particle whose rho-lattice window changes (old shape on
 // nodes lo0.., new on lo1..): general NWn+1-node window with per-lane atomics.
-template <int SHAPE>
-__device__ __forceinline__ void generalWindow(const FixTile& jt, int TT, int T1, int T2, const float* o,
+template <int SHAPE, typename Tile>
+__device__ __forceinline__ void generalWindow(const Tile& jt, int TT, int T1, int T2, const float* o,
                                               const float* on, const int* lc, const int* ln, const float* kq) {
     constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;
     constexpr int NW4 = NWn + 1;
@@ -131,20 +101,92 @@ __device__ __forceinline__ void generalWindow(const FixTile& jt, int TT, int T1,
     esirkepov<float, NW4>(jt, TT, T1, T2, b, s0, s1, kq);
 }
 
-// Deposit the queued window changes of one warp (lanes take entries).
-template <int SHAPE>
-__device__ __forceinline__ void drainQueue(const float* q, int nq, const FixTile& jt, int TT, int T1, int T2) {
-    for (int k = threadIdx.x & 31; k < nq; k += 32) {
-        const float* e = q + k * kQWords;
-        const int k0 = __float_as_int(e[9]), k1 = __float_as_int(e[10]);
-        const int lc[3] = {(k0 >> 16) - 4, ((k0 >> 8) & 0xff) - 4, (k0 & 0xff) - 4};
-        const int ln[3] = {(k1 >> 16) - 4, ((k1 >> 8) & 0xff) - 4, (k1 & 0xff) - 4};
-        generalWindow<SHAPE>(jt, TT, T1, T2, e, e + 3, lc, ln, e + 6);
+// Fixed-point tile addressed by shared-window byte addresses, for code that is
+// not inlined into the kernel (the compiler then no longer knows that the tile
+// is in shared memory): same arithmetic as FixTile::add.
+struct FixTileS {
+    unsigned lo, hi;
+    float up, down;
+    __device__ __forceinline__ void add(int idx, float scaled) const {
+        const float r = rintf(scaled);
+        if (r != 0.f) {
+            const float h = floorf(r * down);
+            const float l = fmaf(-h, up, r);
+            const unsigned lu = __float_as_uint(l + 8388608.0f) - 0x4B000000u;
+            const int hv = __float2int_rz(h);
+            asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(lo + 4u * (unsigned)idx), "r"(lu) : "memory");
+            asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(hi + 4u * (unsigned)idx), "r"(hv) : "memory");
+        }
     }
+};
+
+constexpr int kRing = 64;  // queued window changes per warp (ring)
+
+// Deposit n <= 32 queued window changes of one warp starting at ring entry head,
+// one per lane.  Out of line: one copy of the general-window code serves every
+// call site.
+template <int SHAPE>
+__device__ __noinline__ void drainRing(unsigned ring, int head, int n, FixTileS jt, int TT, int T1, int T2) {
+    const int k = threadIdx.x & 31;
+    if (k >= n) return;
+    const unsigned e = ring + 4u * (unsigned)(((head + k) & (kRing - 1)) * kQWords);
+    float v[kQWords];
+#pragma unroll
+    for (int w = 0; w < kQWords; w++) asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v[w]) : "r"(e + 4u * w) : "memory");
+    const int k0 = __float_as_int(v[9]), k1 = __float_as_int(v[10]);
+    const int lc[3] = {(k0 >> 16) - 4, ((k0 >> 8) & 0xff) - 4, (k0 & 0xff) - 4};
+    const int ln[3] = {(k1 >> 16) - 4, ((k1 >> 8) & 0xff) - 4, (k1 & 0xff) - 4};
+    generalWindow<SHAPE>(jt, TT, T1, T2, v, v + 3, lc, ln, v + 6);
 }
 
 // Wrap a cell index that is at most one period out of range.
 __device__ __forceinline__ int wrapNear(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+// Rows of a warp's reduction area: 32 lane rows and kPark rows for sums parked
+// when a lane changes window; odd, so that the column reads are conflict-free.
+constexpr int kRedRows = 41;
+
+// Add up, per window key, the rows of a warp's reduction area (value j of row r
+// at red[j * kRedRows + r]; keys[r] < 0: empty) and deposit the sums: lane t
+// sums values t and t + 32 over the member rows, lane rows first, then the np
+// park rows, in ascending order.
+template <int NWn, int NV>
+__device__ __forceinline__ void reduceRows(const float* red, const int* keys, int np, const FixTile& jt, int TT,
+                                           int T1, int T2, int lane) {
+    const int kl = keys[lane];
+    const int kp = lane < np ? keys[32 + lane] : -1;
+    unsigned pendL = __ballot_sync(0xffffffffu, kl >= 0);
+    unsigned pendP = __ballot_sync(0xffffffffu, kp >= 0);
+    const float* c0 = red + lane * kRedRows;
+    const float* c1 = red + (lane + 32) * kRedRows;
+    while (pendL | pendP) {
+        const int ref = pendL ? __shfl_sync(0xffffffffu, kl, __ffs(pendL) - 1)
+                              : __shfl_sync(0xffffffffu, kp, __ffs(pendP) - 1);
+        const unsigned mL = __ballot_sync(0xffffffffu, kl == ref) & pendL;
+        const unsigned mP = __ballot_sync(0xffffffffu, kp == ref) & pendP;
+        pendL &= ~mL;
+        pendP &= ~mP;
+        float s0 = 0.0f, s1 = 0.0f;
+        for (unsigned m = mL; m; m &= m - 1) {
+            const int r = __ffs(m) - 1;
+            if (lane < NV) s0 += c0[r];
+            if (lane + 32 < NV) s1 += c1[r];
+        }
+        for (unsigned m = mP; m; m &= m - 1) {
+            const int r = 32 + __ffs(m) - 1;
+            if (lane < NV) s0 += c0[r];
+            if (lane + 32 < NV) s1 += c1[r];
+        }
+        const int b[3] = {(ref >> 16) - 4 + kG, ((ref >> 8) & 0xff) - 4 + kG, (ref & 0xff) - 4 + kG};
+        if (lane < NV) jt.add(windowIdx<NWn>(TT, T1, T2, b, lane), s0);
+        if (lane + 32 < NV) jt.add(windowIdx<NWn>(TT, T1, T2, b, lane + 32), s1);
+    }
+}
+
+// Dynamic shared memory of k_push_cell_esirkepov, in 4-byte words.
+__host__ __device__ constexpr int64_t esirkepovSmemWords(int TT, int ETT, int warps, int nv) {
+    return 6ll * TT + 6ll * ETT + (int64_t)warps * (kRing * kQWords + nv * kRedRows + kRedRows);
+}
 
 // SC > 0: cubic supercells of edge SC known at compile time (tile strides become
 // constants); SC == 0: edges read from the arguments.
@@ -153,41 +195,52 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
     constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;   // stay-in-window nodes per dimension
     constexpr int NV = 3 * (NWn - 1) * NWn * NWn;          // 54 (TSC) or 12 (CIC)
     constexpr int kWarps = THREADS / 32;
-    constexpr int kQ = 64;                                 // queued window changes per warp
+    constexpr int kPark = kRedRows - 32;
+    constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_nleave;
-    __shared__ float sQueue[kWarps][kQ * kQWords];
 
+    // Current tile: origin m - kG, edges S + 2kG + 1.  E/B tile: origin m - 1, edges S + 3.
     const int T1 = SC ? SC + 2 * kG + 1 : a.T[1], T2 = SC ? SC + 2 * kG + 1 : a.T[2];
     const int TT = (SC ? SC + 2 * kG + 1 : a.T[0]) * T1 * T2;
     const int Sx = SC ? SC : a.S[0], Sy = SC ? SC : a.S[1], Sz = SC ? SC : a.S[2];
+    const int E1 = Sy + 3, E2 = Sz + 3, ETT = (Sx + 3) * E1 * E2;
     const int Sv[3] = {Sx, Sy, Sz};
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
     FixTile jt;
     jt.lo = reinterpret_cast<unsigned int*>(smem_raw);
     jt.hi = reinterpret_cast<int*>(jt.lo + 3 * TT);
     jt.setSplit(a.tileSplit);
     float* eb = reinterpret_cast<float*>(jt.hi + 3 * TT);
+    float* ring = eb + 6 * ETT + warp * (kRing * kQWords);
+    float* red = eb + 6 * ETT + kWarps * (kRing * kQWords) + warp * (NV * kRedRows);
+    int* keys = reinterpret_cast<int*>(eb + 6 * ETT + kWarps * (kRing * kQWords + NV * kRedRows)) + warp * kRedRows;
+    FixTileS jts;
+    jts.lo = (unsigned)__cvta_generic_to_shared(jt.lo);
+    jts.hi = (unsigned)__cvta_generic_to_shared(jt.hi);
+    jts.up = jt.up;
+    jts.down = jt.down;
+    const unsigned ringS = (unsigned)__cvta_generic_to_shared(ring);
+
     const int s = blockIdx.x;
     int sc[3];
     sc[2] = s % a.nsc[2];
     sc[1] = (s / a.nsc[2]) % a.nsc[1];
     sc[0] = s / (a.nsc[1] * a.nsc[2]);
     const int m[3] = {sc[0] * Sx, sc[1] * Sy, sc[2] * Sz};
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const unsigned lt = (1u << lane) - 1u;
-    float* myQ = sQueue[warp];
 
-    for (int t = threadIdx.x; t < 6 * TT; t += blockDim.x) {
-        const int c = t / TT, r = t - c * TT;
-        const int i = r / (T1 * T2), jj = (r / T2) % T1, k = r % T2;
-        const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
+    for (int t = threadIdx.x; t < 6 * ETT; t += THREADS) {
+        const int c = t / ETT, r = t - c * ETT;
+        const int i = r / (E1 * E2), jj = (r / E2) % E1, k = r % E2;
+        const int gx = wrapi(m[0] - 1 + i, a.n[0]), gy = wrapi(m[1] - 1 + jj, a.n[1]), gz = wrapi(m[2] - 1 + k, a.n[2]);
         eb[t] = static_cast<const float*>(a.eb[c])[((int64_t)gx * a.n[1] + gy) * a.n[2] + gz];
     }
-    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) { jt.lo[t] = 0u; jt.hi[t] = 0; }
+    for (int t = threadIdx.x; t < 3 * TT; t += THREADS) { jt.lo[t] = 0u; jt.hi[t] = 0; }
     const float invU = (float)a.invUnit;
     const float cdth[3] = {(float)a.cdth[0], (float)a.cdth[1], (float)a.cdth[2]};
     bool bad = false;
-    int nq = 0;   // entries in this warp's queue (warp-uniform)
+    int qHead = 0, qN = 0;   // this warp's ring of queued window changes (warp-uniform)
     __syncthreads();
 
     for (int spi = 0; spi < a.nspecies; spi++) {
@@ -204,37 +257,98 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
 #pragma unroll
             for (int k = 0; k < NV; k++) acc[k] = 0.0f;
             int accKey = -1;
+            int nPark = 0;   // warp-uniform
+            const int i0 = seg * 32 * K + lane * K;
+            // Particle data one iteration ahead.
+            uint32_t pc = kDeadCell;
+            float po[3] = {0.f, 0.f, 0.f}, pu[3] = {0.f, 0.f, 0.f}, pw = 0.f;
+            if (i0 < count) {
+                const int64_t sl = start + i0;
+                pc = sa.buf.cell[sl];
+                po[0] = sa.buf.ox[sl]; po[1] = sa.buf.oy[sl]; po[2] = sa.buf.oz[sl];
+                pu[0] = sa.buf.ux[sl]; pu[1] = sa.buf.uy[sl]; pu[2] = sa.buf.uz[sl];
+                pw = sa.buf.w[sl];
+            }
 #pragma unroll 1
             for (int it = 0; it < K; it++) {
-                const int i = seg * 32 * K + lane * K + it;
+                const int i = i0 + it;
                 const int64_t slot = start + i;
-                const bool act = i < count && sa.buf.cell[slot] != kDeadCell;
+                const uint32_t cellv = pc;
+                const float o[3] = {po[0], po[1], po[2]};
+                float u[3] = {pu[0], pu[1], pu[2]};
+                const float wgt = pw;
+                if (it + 1 < K && i + 1 < count) {
+                    const int64_t sl = slot + 1;
+                    pc = sa.buf.cell[sl];
+                    po[0] = sa.buf.ox[sl]; po[1] = sa.buf.oy[sl]; po[2] = sa.buf.oz[sl];
+                    pu[0] = sa.buf.ux[sl]; pu[1] = sa.buf.uy[sl]; pu[2] = sa.buf.uz[sl];
+                    pw = sa.buf.w[sl];
+                }
+                const bool act = i < count && cellv != kDeadCell;
+                int lc[3] = {0, 0, 0};
+                int key = -1;
+                if (act) {
+                    int c3[3];
+                    unpackCell(cellv, c3[0], c3[1], c3[2]);
+                    int lw[3];
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        lc[d] = c3[d] - m[d];
+                        lw[d] = SHAPE == PICA_SHAPE_TSC ? lc[d] - 1 : (o[d] >= 0.5f ? lc[d] : lc[d] - 1);
+                    }
+                    key = ((lw[0] + 4) << 16) | ((lw[1] + 4) << 8) | (lw[2] + 4);
+                }
+                // A lane meeting another window parks its sums (or, when the park rows
+                // are used up, the warp deposits every row now and starts afresh).
+                const bool sw = act && key != accKey;
+                const bool park = sw && accKey >= 0;
+                const unsigned pm = __ballot_sync(FULL, park);
+                if (pm) {
+                    if (nPark + __popc(pm) > kPark) {
+#pragma unroll
+                        for (int j = 0; j < NV; j++) red[j * kRedRows + lane] = acc[j];
+                        keys[lane] = accKey;
+                        __syncwarp();
+                        reduceRows<NWn, NV>(red, keys, nPark, jt, TT, T1, T2, lane);
+                        __syncwarp();
+#pragma unroll
+                        for (int j = 0; j < NV; j++) acc[j] = 0.0f;
+                        nPark = 0;
+                    } else {
+                        if (park) {
+                            const int row = 32 + nPark + __popc(pm & lt);
+#pragma unroll
+                            for (int j = 0; j < NV; j++) red[j * kRedRows + row] = acc[j];
+                            keys[row] = accKey;
+                        }
+                        nPark += __popc(pm);
+                    }
+                }
+                if (sw) {
+#pragma unroll
+                    for (int j = 0; j < NV; j++) acc[j] = 0.0f;
+                    accKey = key;
+                }
                 bool needQ = false;
                 float qe[kQWords];
                 if (act) {
-                    int c3[3];
-                    unpackCell(sa.buf.cell[slot], c3[0], c3[1], c3[2]);
-                    const int lc[3] = {c3[0] - m[0], c3[1] - m[1], c3[2] - m[2]};
-                    const float o[3] = {sa.buf.ox[slot], sa.buf.oy[slot], sa.buf.oz[slot]};
-                    float u[3] = {sa.buf.ux[slot], sa.buf.uy[slot], sa.buf.uz[slot]};
-                    const float wgt = sa.buf.w[slot];
                     float eb6[6];
                     if constexpr (SHAPE == PICA_SHAPE_CIC) {
                         int bc[3], bs[3];
                         float wc[3][2], ws[3][2];
 #pragma unroll
                         for (int d = 0; d < 3; d++) {
-                            bc[d] = lc[d] + kG; wc[d][0] = 1.0f - o[d]; wc[d][1] = o[d];
+                            bc[d] = lc[d] + 1; wc[d][0] = 1.0f - o[d]; wc[d][1] = o[d];
                             const bool hi = o[d] >= 0.5f;
                             const float dd = hi ? o[d] - 0.5f : o[d] + 0.5f;
-                            bs[d] = (hi ? lc[d] : lc[d] - 1) + kG; ws[d][0] = 1.0f - dd; ws[d][1] = dd;
+                            bs[d] = hi ? lc[d] + 1 : lc[d]; ws[d][0] = 1.0f - dd; ws[d][1] = dd;
                         }
 #pragma unroll
                         for (int comp = 0; comp < 6; comp++) {
                             int t0[3];
 #pragma unroll
                             for (int d = 0; d < 3; d++) t0[d] = stag(comp, d) ? bs[d] : bc[d];
-                            eb6[comp] = gatherSep<float, 2>(eb + comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
+                            eb6[comp] = gatherSep<float, 2>(eb + comp * ETT, E1, E2, t0, stag(comp, 0) ? ws[0] : wc[0],
                                                             stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2]);
                         }
                     } else {
@@ -243,15 +357,15 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
 #pragma unroll
                         for (int d = 0; d < 3; d++) {
                             const bool hi = o[d] >= 0.5f;
-                            bc[d] = lc[d] + (hi ? 1 : 0) - 1 + kG; tscWeights(hi ? o[d] - 1.0f : o[d], wc[d]);
-                            bs[d] = lc[d] - 1 + kG; tscWeights(o[d] - 0.5f, ws[d]);
+                            bc[d] = lc[d] + (hi ? 1 : 0); tscWeights(hi ? o[d] - 1.0f : o[d], wc[d]);
+                            bs[d] = lc[d]; tscWeights(o[d] - 0.5f, ws[d]);
                         }
 #pragma unroll
                         for (int comp = 0; comp < 6; comp++) {
                             int t0[3];
 #pragma unroll
                             for (int d = 0; d < 3; d++) t0[d] = stag(comp, d) ? bs[d] : bc[d];
-                            eb6[comp] = gatherSep<float, 3>(eb + comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
+                            eb6[comp] = gatherSep<float, 3>(eb + comp * ETT, E1, E2, t0, stag(comp, 0) ? ws[0] : wc[0],
                                                             stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2]);
                         }
                     }
@@ -300,18 +414,6 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
                     }
                     const bool sameWindow = inRange && lo0[0] == lo1[0] && lo0[1] == lo1[1] && lo0[2] == lo1[2];
                     if (sameWindow) {
-                        const int key = ((lo0[0] + 4) << 16) | ((lo0[1] + 4) << 8) | (lo0[2] + 4);
-                        if (key != accKey) {
-                            if (accKey >= 0) {
-                                const int b[3] = {(accKey >> 16) - 4 + kG, ((accKey >> 8) & 0xff) - 4 + kG, (accKey & 0xff) - 4 + kG};
-#pragma unroll
-                                for (int j = 0; j < NV; j++)
-                                    jt.add(windowIdx<NWn>(TT, T1, T2, b, j), acc[j]);
-                            }
-#pragma unroll
-                            for (int j = 0; j < NV; j++) acc[j] = 0.0f;
-                            accKey = key;
-                        }
                         // a = S0, dd = S1 - S0; p = a + d/2, q = a/2 + d/3; yz = a_y p_z + d_y q_z.
                         float aa[3][NWn], dd[3][NWn], pp[3][NWn], qq[3][NWn];
 #pragma unroll
@@ -373,54 +475,40 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
                         sa.buf.cell[slot] = kDeadCell;
                     }
                 }
-                // Queue window changes (warp-cooperative; drain when full).
-                const unsigned qm = __ballot_sync(0xffffffffu, needQ);
+                // Queue window changes in the ring; deposit 32 at a time (one per lane).
+                const unsigned qm = __ballot_sync(FULL, needQ);
                 if (qm) {
-                    if (nq + __popc(qm) > kQ) {
-                        drainQueue<SHAPE>(myQ, nq, jt, TT, T1, T2);
-                        nq = 0;
-                        __syncwarp();
-                    }
                     if (needQ) {
-                        float* e = myQ + (nq + __popc(qm & lt)) * kQWords;
+                        float* e = ring + ((qHead + qN + __popc(qm & lt)) & (kRing - 1)) * kQWords;
 #pragma unroll
                         for (int k = 0; k < kQWords; k++) e[k] = qe[k];
                     }
-                    nq += __popc(qm);
+                    qN += __popc(qm);
                     __syncwarp();
+                    if (qN >= 32) {
+                        drainRing<SHAPE>(ringS, qHead, 32, jts, TT, T1, T2);
+                        __syncwarp();
+                        qHead = (qHead + 32) & (kRing - 1);
+                        qN -= 32;
+                    }
                 }
             }
-            // Reduce the stay-in-window sums of lanes sharing a window (up to three groups),
-            // then flush what remains lane by lane.
-            bool pending = accKey >= 0;
-#pragma unroll 1
-            for (int g = 0; g < 3; g++) {
-                const unsigned live = __ballot_sync(0xffffffffu, pending);
-                if (!live) break;
-                const int ref = __shfl_sync(0xffffffffu, accKey, __ffs(live) - 1);
-                const bool mine = pending && accKey == ref;
-                float s0v, s1v;
-                warpTransposeSum<NV>(acc, mine, lane, s0v, s1v);
-                const int b[3] = {(ref >> 16) - 4 + kG, ((ref >> 8) & 0xff) - 4 + kG, (ref & 0xff) - 4 + kG};
-                if (2 * lane < NV) jt.add(windowIdx<NWn>(TT, T1, T2, b, 2 * lane), s0v);
-                if (2 * lane + 1 < NV) jt.add(windowIdx<NWn>(TT, T1, T2, b, 2 * lane + 1), s1v);
-                if (mine) pending = false;
-            }
-            if (pending) {
-                const int b[3] = {(accKey >> 16) - 4 + kG, ((accKey >> 8) & 0xff) - 4 + kG, (accKey & 0xff) - 4 + kG};
+            // Deposit the segment's window sums: lane rows plus parked rows, by window.
 #pragma unroll
-                for (int j = 0; j < NV; j++)
-                    jt.add(windowIdx<NWn>(TT, T1, T2, b, j), acc[j]);
-            }
+            for (int j = 0; j < NV; j++) red[j * kRedRows + lane] = acc[j];
+            keys[lane] = accKey;
+            __syncwarp();
+            reduceRows<NWn, NV>(red, keys, nPark, jt, TT, T1, T2, lane);
+            __syncwarp();
         }
         __syncthreads();
         if (threadIdx.x == 0) sa.nleave[s] = s_nleave;
         __syncthreads();
     }
-    drainQueue<SHAPE>(myQ, nq, jt, TT, T1, T2);
+    if (qN > 0) drainRing<SHAPE>(ringS, qHead, qN, jts, TT, T1, T2);
     if (bad) atomicExch(a.flags, PICA_ERR_MIGRATION);
     __syncthreads();
-    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) {
+    for (int t = threadIdx.x; t < 3 * TT; t += THREADS) {
         const unsigned long long v = (unsigned long long)jt.node(t);
         if (v != 0ull) {
             const int c = t / TT, r = t - c * TT;

@@ -21,7 +21,9 @@ int launchOne(const PushArgs<CellPtrs>& a, cudaStream_t s) {
 template <int SHAPE, int SC, int K, int THREADS, int MINB>
 int launchEsirkepovV(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     const int TT = a.T[0] * a.T[1] * a.T[2];
-    const size_t smem = (size_t)6 * TT * sizeof(float) + (size_t)3 * TT * 2 * sizeof(uint32_t);
+    const int ETT = (a.S[0] + 3) * (a.S[1] + 3) * (a.S[2] + 3);
+    constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;
+    const size_t smem = (size_t)esirkepovSmemWords(TT, ETT, THREADS / 32, 3 * (NWn - 1) * NWn * NWn) * 4;
     auto k = k_push_cell_esirkepov<SHAPE, K, THREADS, MINB, SC>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -80,7 +82,7 @@ int launchMigrateCell(const MigrateArgs<CellPtrs>& a, int stage, cudaStream_t s)
         case kFill: k_migrate<CellPtrs, kFill><<<warpBlocks, 256, 0, s>>>(a); break;
         case kGatherOutbox: k_migrate<CellPtrs, kGatherOutbox><<<warpBlocks, 256, 0, s>>>(a); break;
         case kRebuild: k_migrate<CellPtrs, kRebuild><<<warpBlocks, 256, 0, s>>>(a); break;
-        case kResort: k_resort<CellPtrs><<<(int)((nscTot + 3) / 4), 128, 0, s>>>(a); break;
+        case kResort: k_resort<CellPtrs><<<(int)nscTot, kResortWarps * 32, 0, s>>>(a); break;
         default: return (int)cudaErrorInvalidValue;
     }
     return (int)cudaGetLastError();

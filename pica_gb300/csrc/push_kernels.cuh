@@ -820,15 +820,21 @@ __device__ __forceinline__ int localCell(const CellPtrs& p, int64_t i, const int
 }
 
 // Compact each supercell (drop dead slots) and sort it by cell, stably, into the new
-// layout of buffer dst.  One warp per supercell; 512 cell bins per warp in shared memory.
+// layout of buffer dst.  One CTA of kResortWarps warps per supercell: warp w owns
+// the w-th contiguous eighth of the slots; a first pass counts cells per warp, a
+// scan over (cell, warp) gives every warp its start in each cell, and a second
+// pass scatters each warp's particles in slot order (rank within a 32-slot step
+// from __match_any_sync).  The result is ordered by (cell, old slot).
+constexpr int kResortWarps = 8;
 template <class P>
-__global__ void __launch_bounds__(128) k_resort(const __grid_constant__ MigrateArgs<P> a) {
-    __shared__ int bins[4][512];
-    const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
+__global__ void __launch_bounds__(kResortWarps * 32) k_resort(const __grid_constant__ MigrateArgs<P> a) {
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr int kT = kResortWarps * 32;
+    constexpr int kBins = 512;  // largest supercell: 8 x 8 x 8 cells
+    __shared__ int cnt[kResortWarps][kBins];
+    __shared__ int wsum[kResortWarps];
+    const int d = blockIdx.x;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int d = blockIdx.x * 4 + warp;
-    if (d >= nscTot) return;
-    int* b = bins[warp];
     const int nb = a.S[0] * a.S[1] * a.S[2];
     const int dc[3] = {d / (a.nsc[1] * a.nsc[2]), (d / a.nsc[2]) % a.nsc[1], d % a.nsc[2]};
     const int m[3] = {dc[0] * a.S[0], dc[1] * a.S[1], dc[2] * a.S[2]};
@@ -836,43 +842,57 @@ __global__ void __launch_bounds__(128) k_resort(const __grid_constant__ MigrateA
     for (int spi = 0; spi < a.nspecies; spi++) {
         const MigrateSpecies<P>& sa = a.sp[spi];
         const int64_t start = sa.start[d], ns = sa.newStart[d];
-        const int cnt = sa.count[d];
-        for (int k = lane; k < nb; k += 32) b[k] = 0;
-        __syncwarp();
-        for (int i = lane; i < cnt; i += 32)
-            if (aliveAt(sa.a, start + i)) atomicAdd(&b[localCell(sa.a, start + i, m, a.S, a.invh)], 1);
-        __syncwarp();
-        // exclusive scan of the bins: 16 consecutive bins per lane
+        const int n = sa.count[d];
+        const int R = ((n + kT - 1) / kT) * 32;
+        const int lo = min(warp * R, n), hi = min(lo + R, n);
+        for (int k = threadIdx.x; k < kResortWarps * kBins; k += kT) (&cnt[0][0])[k] = 0;
+        __syncthreads();
+        for (int i0 = lo; i0 < hi; i0 += 32) {
+            const int i = i0 + lane;
+            const int key = (i < hi && aliveAt(sa.a, start + i)) ? localCell(sa.a, start + i, m, a.S, a.invh) : -1;
+            const unsigned grp = __match_any_sync(FULL, key);
+            if (key >= 0 && lane == __ffs(grp) - 1) cnt[warp][key] += __popc(grp);
+        }
+        __syncthreads();
+        // Exclusive scan over (cell, warp), cell-major: 16 consecutive entries per thread.
         {
+            const int E = nb * kResortWarps;
             int loc[16], sum = 0;
 #pragma unroll
-            for (int k = 0; k < 16; k++) { const int j = lane * 16 + k; loc[k] = j < nb ? b[j] : 0; sum += loc[k]; }
+            for (int q = 0; q < 16; q++) {
+                const int f = threadIdx.x * 16 + q;
+                loc[q] = f < E ? cnt[f % kResortWarps][f / kResortWarps] : 0;
+                sum += loc[q];
+            }
             int incl = sum;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                const int t = __shfl_up_sync(FULL, incl, o);
                 if (lane >= o) incl += t;
             }
+            if (lane == 31) wsum[warp] = incl;
+            __syncthreads();
             int run = incl - sum;
+            for (int w = 0; w < warp; w++) run += wsum[w];
 #pragma unroll
-            for (int k = 0; k < 16; k++) { const int j = lane * 16 + k; if (j < nb) b[j] = run; run += loc[k]; }
-        }
-        __syncwarp();
-        for (int i0 = 0; i0 < cnt; i0 += 32) {
-            const int i = i0 + lane;
-            const int key = (i < cnt && aliveAt(sa.a, start + i)) ? localCell(sa.a, start + i, m, a.S, a.invh) : -1;
-            const unsigned grp = __match_any_sync(0xffffffffu, key);
-            int base = 0;
-            if (key >= 0) base = b[key];
-            __syncwarp();
-            if (key >= 0) {
-                copyParticle(sa.a, start + i, sa.dst, ns + base + __popc(grp & lt));
-                if (lane == __ffs(grp) - 1) b[key] = base + __popc(grp);
+            for (int q = 0; q < 16; q++) {
+                const int f = threadIdx.x * 16 + q;
+                if (f < E) cnt[f % kResortWarps][f / kResortWarps] = run;
+                run += loc[q];
             }
+        }
+        __syncthreads();
+        for (int i0 = lo; i0 < hi; i0 += 32) {
+            const int i = i0 + lane;
+            const int key = (i < hi && aliveAt(sa.a, start + i)) ? localCell(sa.a, start + i, m, a.S, a.invh) : -1;
+            const unsigned grp = __match_any_sync(FULL, key);
+            if (key >= 0) copyParticle(sa.a, start + i, sa.dst, ns + cnt[warp][key] + __popc(grp & lt));
+            __syncwarp();
+            if (key >= 0 && lane == __ffs(grp) - 1) cnt[warp][key] += __popc(grp);
             __syncwarp();
         }
-        if (lane == 0) sa.count[d] = sa.alive[d];
-        __syncwarp();
+        __syncthreads();
+        if (threadIdx.x == 0) sa.count[d] = sa.alive[d];
     }
 }
 

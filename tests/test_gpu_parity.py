@@ -171,7 +171,10 @@ def test_migration_overflow_rebuild_keeps_order():
 def test_resort_cadence_matches_oracle_order(form):
     """With a resort every 2 steps (compact + sort each supercell by cell) the GPU
     keeps the oracle's exact ensemble order; without it the order differs but the
-    particles are the same (FP32: bit for bit, the deposit sums are exact)."""
+    particles are the same.  FP32: each lane pre-sums its particles' window
+    contributions in FP32 before the exact fixed-point deposit, so the in-supercell
+    order moves results by FP32 rounding (checked to 1e-6); for a given order the
+    results are bit-reproducible (test_fp32_deposit_is_deterministic)."""
     n, sc = (8, 8, 8), (2, 2, 2)
     d = thermal_inputs(n, 4, seed=12, u_sigma=0.2)
     tol = 1e-12 if form == pg.FORM_FP64_PLAIN else 1e-5
@@ -187,7 +190,7 @@ def test_resort_cadence_matches_oracle_order(form):
     ia, ib = key(a), key(b)
     for k in ("x", "ux", "w"):
         if form == pg.FORM_FP32_CELL:
-            assert np.array_equal(a[k][ia], b[k][ib]), k
+            assert rel_err(a[k][ia], b[k][ib]) < 1e-6, k
         else:
             assert rel_err(a[k][ia], b[k][ib]) < 1e-12, k
 
