@@ -36,6 +36,47 @@ BYTES_PER_PARTICLE_FP64 = 104  # x 24 + u 24, read and written, + weight read
 PUSH_GRID_BYTES_PER_CELL_FP32 = 36  # E/B gather 6 words + J write 3 words, FP32
 
 
+def batched_measure(args):
+    """The batching form on independent thermal plasmas of uneven size (members drawn
+    as in pica_gb300.workloads.batched_members; by default every edge halved).  Timed
+    with the host clock: every batch step ends with a stream synchronisation (the
+    host reads each member's migration flags)."""
+    import pica_gb300 as pg
+    from pica_gb300 import autotune, workloads
+    members = workloads.batched_members(count=args.batched, half=not args.batched_full)
+    b = pg.Batch([m["sim"] for m in members])
+    for sim, wl in zip(b.members, members):
+        parts = pg.generate_plasma(wl["specs"][0])
+        sim.upload_particles(*[parts[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w")], parts["species"])
+        sim.upload_fields([np.zeros(wl["sim"]["n"])] * 9)
+        del parts
+    npart = b.num_particles()
+    tune = autotune.tune_batch(b, steps=2)
+    best = min(tune, key=tune.get)
+    b.step(3)
+    K = args.batched_steps
+    s0 = b.stats()
+    t = time.perf_counter()
+    b.step(K)
+    el = time.perf_counter() - t
+    s1 = b.stats()
+    b.set_options(use_graph=False, variant=best)
+    b.step(1)
+    t = time.perf_counter()
+    b.step(K)
+    el_eager = time.perf_counter() - t
+    b.close()
+    edges = [m["sim"]["n"][0] for m in members]
+    return {"workload": f"{len(members)} thermal plasmas, edges {min(edges)}-{max(edges)} cells"
+                        f"{'' if args.batched_full else ' (member edges halved)'}, 16-128 ppc, CIC, Esirkepov, "
+                        "supercell 4^3, FP32 cell form",
+            "particles": npart, "steps": K, "value": npart * K / el, "unit": UNIT, "ms_per_step": 1e3 * el / K,
+            "timer": "host clock, each step synchronised", "graph_captures": s1["captures"] - s0["captures"],
+            "kernel_launches_per_step": (s1["kernel_launches"] - s0["kernel_launches"]) / K,
+            "eager_value": npart * K / el_eager, "push_variant": best,
+            "variant_s_per_step": {str(k): v for k, v in tune.items()}}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -47,8 +88,12 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--edge", type=int, default=128, help="grid edge (cells); 128 is the reference workload")
-    ap.add_argument("--resort-every", type=int, default=8, help="in-supercell cell sort cadence (steps)")
+    ap.add_argument("--resort-every", type=int, default=2, help="in-supercell cell sort cadence (steps)")
     ap.add_argument("--variant", type=int, default=-1, help="push-kernel launch variant (-1: autotune)")
+    ap.add_argument("--batched", type=int, default=64, help="members of the batching-form run (0: skip)")
+    ap.add_argument("--batched-full", action="store_true",
+                    help="batching form at the full member sizes (grids 32^3-96^3, ~1.5e9 particles)")
+    ap.add_argument("--batched-steps", type=int, default=10)
     ap.add_argument("--validate-steps", type=int, default=1000,
                     help="steps of the FP32-vs-FP64 error run on a 32^3 block (0: skip)")
     return ap.parse_args()
@@ -351,6 +396,11 @@ def main():
                 "steps": args.fp64_steps, "dtype": "fp64", "form": "FP64 plain (absolute positions)"}
         s64.close()
 
+    # ---------------- batching form: many plasmas, persistent push + CUDA graph ----------------
+    batched = None
+    if args.batched > 0 and rank == 0:
+        batched = batched_measure(args)
+
     # ---------------- FP32 form against the FP64 plain form (error metrics) ----------------
     errors = None
     if args.validate_steps > 0 and rank == 0:
@@ -379,6 +429,7 @@ def main():
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
         "fp64_form": fp64, "fp32_over_fp64": (value / world / fp64["value"]) if fp64 else None,
         "fp32_vs_fp64_errors": errors,
+        "batched": batched,
         "tuning": {"push_variant": sim_variant, "variant_s_per_step": {str(k): v for k, v in tune.items()},
                    "resort_every": args.resort_every},
     }

@@ -189,6 +189,32 @@ int     pica_field_energy_noalloc(const void* const* fields, int32_t fp64, const
 int64_t pica_state_slots(pica_ctx* ctx, int32_t species);
 int     pica_state_copy(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device);
 
+/* Batching form: many independent plasmas advanced together (FP32 cell form,
+ * Esirkepov deposition, one shape and one supercell size for all members; grids,
+ * particle counts and species may differ).  The push of every member is one
+ * persistent launch over all members' supercells; the device part of the step
+ * (flag reset, push, current conversion, B(dt/2) E(dt) B(dt/2), leaver sort,
+ * arrival count, fill) is captured once as a CUDA graph and replayed while its
+ * launch arguments stay the same (a resort or a capacity rebuild changes them
+ * and the graph is captured again).  After every step the host reads all
+ * members' flags and finishes their migrations (error, rebuild, resort).
+ * Results equal those of the members stepped one by one with pica_step.
+ * No counterpart in the reference (pica has no batched driver). */
+typedef struct pica_batch pica_batch;
+int       pica_batch_create(const pica_config* cfgs, int32_t count, pica_batch** out);
+int       pica_batch_destroy(pica_batch* batch);
+/* Member k: an ordinary context owned by the batch (upload, download, diagnostics;
+ * do not destroy it or change its stream).  Calling this marks the work order for
+ * recomputation from the members' particle counts at the next step. */
+pica_ctx* pica_batch_member(pica_batch* batch, int32_t k);
+/* use_graph: replay a captured CUDA graph (1) or enqueue every launch (0);
+ * variant: launch shape of the batched push, as pica_set_variant. */
+int       pica_batch_set_options(pica_batch* batch, int32_t use_graph, int32_t variant);
+int       pica_batch_step(pica_batch* batch, int32_t nsteps);
+/* out[0] graph captures, out[1] graph launches, out[2] kernel launches, out[3] steps. */
+int       pica_batch_stats(pica_batch* batch, int64_t* out4);
+const char* pica_batch_last_error(pica_batch* batch);
+
 /* Host-side plasma set-up (no device work). */
 int64_t pica_plasma_count(const pica_plasma_spec* spec);
 int     pica_plasma_generate(const pica_plasma_spec* spec, int32_t threads, double* x, double* y, double* z,

@@ -52,32 +52,39 @@ class Simulation:
     def __init__(self, n, h, dt, supercell=(2, 2, 2), form=FORM_FP64_PLAIN, shape=SHAPE_CIC,
                  deposit=DEPOSIT_DIRECT, species=(ELECTRON,), slack=0.15, resort_every=0, threads=0):
         self.lib = load()
-        cfg = PicaConfig()
-        for d in range(3):
-            cfg.n[d], cfg.sc[d], cfg.h[d] = int(n[d]), int(supercell[d]), float(h[d])
-        cfg.dt, cfg.form, cfg.shape, cfg.deposit = float(dt), int(form), int(shape), int(deposit)
-        cfg.nspecies = len(species)
-        for i, (m, q) in enumerate(species):
-            cfg.mass[i], cfg.charge[i] = float(m), float(q)
-        cfg.slack, cfg.resort_every, cfg.threads = float(slack), int(resort_every), int(threads)
-        self.cfg = cfg
-        self.n = tuple(int(v) for v in n)
-        self.h = tuple(float(v) for v in h)
-        self.dt = float(dt)
-        self.form = int(form)
-        self.nsc = tuple(self.n[d] // int(supercell[d]) for d in range(3))
-        self.nspecies = len(species)
-        self.species = tuple(species)
+        self._describe(make_config(n, h, dt, supercell, form, shape, deposit, species, slack, resort_every, threads))
         handle = C.c_void_p()
-        rc = self.lib.pica_ctx_create(C.byref(cfg), C.byref(handle))
+        rc = self.lib.pica_ctx_create(C.byref(self.cfg), C.byref(handle))
         if rc:
             raise PicaError(rc, self.lib.pica_status_string(rc).decode())
         self.ctx = handle
+        self._owned = True
+
+    def _describe(self, cfg):
+        self.cfg = cfg
+        self.n = tuple(int(cfg.n[d]) for d in range(3))
+        self.h = tuple(float(cfg.h[d]) for d in range(3))
+        self.dt = float(cfg.dt)
+        self.form = int(cfg.form)
+        self.nsc = tuple(self.n[d] // int(cfg.sc[d]) for d in range(3))
+        self.nspecies = int(cfg.nspecies)
+        self.species = tuple((cfg.mass[i], cfg.charge[i]) for i in range(self.nspecies))
+
+    @classmethod
+    def _member(cls, lib, handle, cfg):
+        """A context owned by a Batch (not destroyed by close())."""
+        self = cls.__new__(cls)
+        self.lib = lib
+        self._describe(cfg)
+        self.ctx = C.c_void_p(handle)
+        self._owned = False
+        return self
 
     # -- lifetime ------------------------------------------------------------
     def close(self):
         if getattr(self, "ctx", None):
-            self.lib.pica_ctx_destroy(self.ctx)
+            if getattr(self, "_owned", True):
+                self.lib.pica_ctx_destroy(self.ctx)
             self.ctx = None
 
     def __del__(self):
@@ -190,6 +197,83 @@ class Simulation:
     def state_copy(self, species, comp, host_ptr, to_device):
         self._check(self.lib.pica_state_copy(self.ctx, int(species), int(comp), C.c_void_p(int(host_ptr)),
                                              1 if to_device else 0))
+
+
+def make_config(n, h, dt, supercell=(2, 2, 2), form=FORM_FP64_PLAIN, shape=SHAPE_CIC, deposit=DEPOSIT_DIRECT,
+                species=(ELECTRON,), slack=0.15, resort_every=0, threads=0):
+    """pica_config for the given grid (cells n, step h), time step and supercell edges."""
+    cfg = PicaConfig()
+    for d in range(3):
+        cfg.n[d], cfg.sc[d], cfg.h[d] = int(n[d]), int(supercell[d]), float(h[d])
+    cfg.dt, cfg.form, cfg.shape, cfg.deposit = float(dt), int(form), int(shape), int(deposit)
+    cfg.nspecies = len(species)
+    for i, (m, q) in enumerate(species):
+        cfg.mass[i], cfg.charge[i] = float(m), float(q)
+    cfg.slack, cfg.resort_every, cfg.threads = float(slack), int(resort_every), int(threads)
+    return cfg
+
+
+class Batch:
+    """Many independent plasmas advanced together (the batching form, FP32 cell form
+    with Esirkepov deposition): one persistent push launch over every member's
+    supercells and the device part of the step replayed as a CUDA graph.
+    ``members`` is a list of Simulation keyword dicts (n, h, dt, supercell, shape,
+    species, resort_every, ...); ``batch.members[k]`` is a Simulation view of member k
+    for uploads, downloads and diagnostics."""
+
+    def __init__(self, members):
+        self.lib = load()
+        cfgs = (PicaConfig * len(members))()
+        for k, m in enumerate(members):
+            kw = dict(m)
+            kw.setdefault("form", FORM_FP32_CELL)
+            kw.setdefault("deposit", DEPOSIT_ESIRKEPOV)
+            cfgs[k] = make_config(**kw)
+        handle = C.c_void_p()
+        rc = self.lib.pica_batch_create(cfgs, len(members), C.byref(handle))
+        if rc:
+            raise PicaError(rc, self.lib.pica_status_string(rc).decode())
+        self.batch = handle
+        self.members = [Simulation._member(self.lib, self.lib.pica_batch_member(handle, k), cfgs[k])
+                        for k in range(len(members))]
+
+    def _check(self, rc):
+        if rc:
+            raise PicaError(rc, self.lib.pica_batch_last_error(self.batch).decode() or
+                            self.lib.pica_status_string(rc).decode())
+
+    def set_options(self, use_graph=True, variant=0):
+        self._check(self.lib.pica_batch_set_options(self.batch, 1 if use_graph else 0, int(variant)))
+
+    def step(self, nsteps=1):
+        self._check(self.lib.pica_batch_step(self.batch, int(nsteps)))
+
+    def stats(self):
+        out = (C.c_int64 * 4)()
+        self._check(self.lib.pica_batch_stats(self.batch, out))
+        return dict(captures=out[0], graph_launches=out[1], kernel_launches=out[2], steps=out[3])
+
+    def reorder(self):
+        """Recompute the work order from the members' particle counts at the next step
+        (after uploads through ``members``)."""
+        for k in range(len(self.members)):
+            self.lib.pica_batch_member(self.batch, k)
+
+    def num_particles(self):
+        return sum(m.num_particles() for m in self.members)
+
+    def close(self):
+        if getattr(self, "batch", None):
+            for m in self.members:
+                m.ctx = None
+            self.lib.pica_batch_destroy(self.batch)
+            self.batch = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def plasma_spec(n, h, ppc, sigma_u, weight, seed, species=0, density_mod=0.0, nbeams=1, drift_u=0.0, drift_axis=0):

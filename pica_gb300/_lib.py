@@ -62,6 +62,13 @@ SIGNATURES = {
     "pica_charge_density": (C.c_int, [_vp, _dp]),
     "pica_field_energy": (C.c_int, [_vp, _dp]),
     "pica_field_energy_noalloc": (C.c_int, [C.POINTER(_vp), _i32, _ip, _dp, _vp, _dp]),
+    "pica_batch_create": (C.c_int, [C.POINTER(PicaConfig), _i32, C.POINTER(_vp)]),
+    "pica_batch_destroy": (C.c_int, [_vp]),
+    "pica_batch_member": (_vp, [_vp, _i32]),
+    "pica_batch_set_options": (C.c_int, [_vp, _i32, _i32]),
+    "pica_batch_step": (C.c_int, [_vp, _i32]),
+    "pica_batch_stats": (C.c_int, [_vp, C.POINTER(C.c_int64)]),
+    "pica_batch_last_error": (C.c_char_p, [_vp]),
     "pica_state_slots": (_i64, [_vp, _i32]),
     "pica_state_copy": (C.c_int, [_vp, _i32, _i32, _vp, _i32]),
     "pica_plasma_count": (_i64, [C.POINTER(PicaPlasmaSpec)]),

@@ -48,6 +48,21 @@ def tune_variant(sim, steps=2):
     return times
 
 
+def tune_batch(batch, steps=2, variants=4):
+    """tune_variant for a Batch: time each launch variant of the batched push (graph
+    replay, after one capture step) and keep the fastest.  Returns {variant: s/step}."""
+    times = {}
+    for v in range(variants):
+        batch.set_options(use_graph=True, variant=v)
+        batch.step(1)
+        t = time.perf_counter()
+        batch.step(steps)
+        times[v] = (time.perf_counter() - t) / steps
+    best = min(times, key=times.get)
+    batch.set_options(use_graph=True, variant=best)
+    return times
+
+
 def config_key(n, ppc, form, shape, deposit):
     return f"{n[0]}x{n[1]}x{n[2]}|ppc={ppc}|form={form}|shape={shape}|deposit={deposit}"
 

@@ -141,6 +141,10 @@ void updateJFrac(pica_ctx* ctx) {
     ctx->jfrac = std::min(std::min(kJFracBitsMax, 62 - (int)std::ceil(std::log2(worst))), 29 + ctx->tileSplit - b);
 }
 
+// Slot arrays grow with 1/16 headroom, so that layouts that grow by a few slots
+// at a resort or rebuild do not reallocate (and synchronise the device) each time.
+int64_t withHeadroom(int64_t slots) { return std::max<int64_t>(slots, 1) + slots / 16 + 1024; }
+
 int ensureBuffer(pica_ctx* ctx, int spi, int b, int64_t slots) {
     SpeciesState& S = ctx->sp[spi];
     if (S.slots[b] >= slots) return PICA_OK;
@@ -149,8 +153,9 @@ int ensureBuffer(pica_ctx* ctx, int spi, int b, int64_t slots) {
         S.buf[b][k] = nullptr;
     }
     S.slots[b] = 0;
-    for (int k = 0; k < ctx->ncomp; k++) CK(cudaMalloc(&S.buf[b][k], std::max<int64_t>(slots, 1) * ctx->compBytes[k]));
-    S.slots[b] = slots;
+    const int64_t grown = withHeadroom(slots);
+    for (int k = 0; k < ctx->ncomp; k++) CK(cudaMalloc(&S.buf[b][k], grown * ctx->compBytes[k]));
+    S.slots[b] = grown;
     return PICA_OK;
 }
 
@@ -162,9 +167,10 @@ int ensureSlotArrays(pica_ctx* ctx, int spi, int64_t slots) {
     S.dir = nullptr;
     S.llist = nullptr;
     S.slotArrays = 0;
-    CK(cudaMalloc(&S.dir, std::max<int64_t>(slots, 1)));
-    CK(cudaMalloc(&S.llist, std::max<int64_t>(slots, 1) * 4));
-    S.slotArrays = slots;
+    const int64_t grown = withHeadroom(slots);
+    CK(cudaMalloc(&S.dir, grown));
+    CK(cudaMalloc(&S.llist, grown * 4));
+    S.slotArrays = grown;
     return PICA_OK;
 }
 
@@ -176,8 +182,9 @@ int ensureOutbox(pica_ctx* ctx, int spi, int64_t slots) {
         S.outbox[k] = nullptr;
     }
     S.outSlots = 0;
-    for (int k = 0; k < ctx->ncomp; k++) CK(cudaMalloc(&S.outbox[k], std::max<int64_t>(slots, 1) * ctx->compBytes[k]));
-    S.outSlots = slots;
+    const int64_t grown = withHeadroom(slots);
+    for (int k = 0; k < ctx->ncomp; k++) CK(cudaMalloc(&S.outbox[k], grown * ctx->compBytes[k]));
+    S.outSlots = grown;
     return PICA_OK;
 }
 
@@ -214,6 +221,37 @@ void parallelFor(int threads, int64_t n, const std::function<void(int64_t, int64
     for (auto& t : th) t.join();
 }
 }  // namespace
+
+// Kernel arguments of the push for the context's current layout (the buffers
+// themselves are set by the caller).
+template <class A>
+static void fillPushArgs(pica_ctx* ctx, A& a) {
+    const pica_config& c = ctx->cfg;
+    for (int d = 0; d < 3; d++) {
+        a.n[d] = c.n[d]; a.S[d] = c.sc[d]; a.nsc[d] = ctx->nsc[d]; a.T[d] = ctx->T[d];
+        a.h[d] = c.h[d]; a.invh[d] = 1.0 / c.h[d]; a.L[d] = (double)c.n[d] * c.h[d];
+        a.scInv[d] = 1.0 / ((double)c.sc[d] * ((a.L[d] - 0.0) / (double)c.n[d]));
+        a.cdth[d] = kC * c.dt / c.h[d];
+    }
+    a.dt = c.dt;
+    a.nspecies = c.nspecies;
+    for (int k = 0; k < 6; k++) a.eb[k] = ctx->f[k];
+    for (int k = 0; k < 3; k++) { a.jacc[k] = ctx->jacc[k]; a.j[k] = ctx->f[6 + k]; }
+    a.invUnit = std::ldexp(1.0, ctx->jfrac) / ctx->kmax;
+    a.tileSplit = ctx->tileSplit;
+    a.norm = 1.0 / (c.h[0] * c.h[1] * c.h[2]);   // CurrentDepositorYeeGrid.h:203
+    a.flags = ctx->d_flags;
+    for (int q = 0; q < c.nspecies; q++) {
+        SpeciesState& S = ctx->sp[q];
+        auto& sa = a.sp[q];
+        sa.start = S.d_start; sa.cap = S.d_cap; sa.count = S.d_count;
+        sa.nleave = S.d_nleave; sa.llist = S.llist; sa.dir = S.dir;
+        sa.ec = c.charge[q] * c.dt / (2.0 * c.mass[q] * kC);   // BorisPusher.h:29
+        sa.q = c.charge[q];
+        for (int d = 0; d < 3; d++) sa.kq[d] = -c.charge[q] * (c.h[d] / c.dt);
+        sa.qc = c.charge[q] * kC;
+    }
+}
 
 extern "C" {
 
@@ -599,40 +637,14 @@ int pica_push_deposit(pica_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->d_flags, 0, 4 * sizeof(int), ctx->stream));
     if (ctx->fp64)
         for (int k = 6; k < 9; k++) CK(cudaMemsetAsync(ctx->f[k], 0, nodes * 8, ctx->stream));
-    auto fill = [&](auto& a) {
-        for (int d = 0; d < 3; d++) {
-            a.n[d] = c.n[d]; a.S[d] = c.sc[d]; a.nsc[d] = ctx->nsc[d]; a.T[d] = ctx->T[d];
-            a.h[d] = c.h[d]; a.invh[d] = 1.0 / c.h[d]; a.L[d] = (double)c.n[d] * c.h[d];
-            a.scInv[d] = 1.0 / ((double)c.sc[d] * ((a.L[d] - 0.0) / (double)c.n[d]));
-            a.cdth[d] = kC * c.dt / c.h[d];
-        }
-        a.dt = c.dt;
-        a.nspecies = c.nspecies;
-        for (int k = 0; k < 6; k++) a.eb[k] = ctx->f[k];
-        for (int k = 0; k < 3; k++) { a.jacc[k] = ctx->jacc[k]; a.j[k] = ctx->f[6 + k]; }
-        a.invUnit = std::ldexp(1.0, ctx->jfrac) / ctx->kmax;
-        a.tileSplit = ctx->tileSplit;
-        a.norm = 1.0 / (c.h[0] * c.h[1] * c.h[2]);   // CurrentDepositorYeeGrid.h:203
-        a.flags = ctx->d_flags;
-        for (int q = 0; q < c.nspecies; q++) {
-            SpeciesState& S = ctx->sp[q];
-            auto& sa = a.sp[q];
-            sa.start = S.d_start; sa.cap = S.d_cap; sa.count = S.d_count;
-            sa.nleave = S.d_nleave; sa.llist = S.llist; sa.dir = S.dir;
-            sa.ec = c.charge[q] * c.dt / (2.0 * c.mass[q] * kC);   // BorisPusher.h:29
-            sa.q = c.charge[q];
-            for (int d = 0; d < 3; d++) sa.kq[d] = -c.charge[q] * (c.h[d] / c.dt);
-            sa.qc = c.charge[q] * kC;
-        }
-    };
     if (ctx->fp64) {
         PushArgs<PlainPtrs> a{};
-        fill(a);
+        fillPushArgs(ctx, a);
         for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = plainPtrs(ctx, q, ctx->cur); a.sp[q].out = plainPtrs(ctx, q, 1 - ctx->cur); }
         CKL(launchPushPlain(a, c.shape, c.deposit, ctx->stream));
     } else {
         PushArgs<CellPtrs> a{};
-        fill(a);
+        fillPushArgs(ctx, a);
         for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = cellPtrs(ctx, q, ctx->cur); a.sp[q].out = cellPtrs(ctx, q, 1 - ctx->cur); }
         CKL(launchPushCell(a, c.shape, c.deposit, ctx->variant, ctx->stream));
     }
@@ -685,49 +697,62 @@ static int stageLayout(pica_ctx* ctx, int q, const std::vector<int32_t>& counts,
 }
 
 template <class P>
-static int migrateImpl(pica_ctx* ctx) {
+static void migrateArgs(pica_ctx* ctx, MigrateArgs<P>& a) {
     const pica_config& c = ctx->cfg;
     const int A = ctx->cur, B = 1 - ctx->cur;
-    auto args = [&](MigrateArgs<P>& a) {
-        for (int d = 0; d < 3; d++) { a.nsc[d] = ctx->nsc[d]; a.S[d] = c.sc[d]; a.invh[d] = 1.0 / c.h[d]; }
-        a.nspecies = c.nspecies;
-        a.flags = ctx->d_flags;
-        int32_t maxCap = 0;
-        for (int q = 0; q < c.nspecies; q++) {
-            SpeciesState& S = ctx->sp[q];
-            for (int32_t v : S.h_cap) maxCap = std::max(maxCap, v);
-            auto& m = a.sp[q];
-            m.a = ptrsOf<P>(S.buf[A]); m.b = ptrsOf<P>(S.buf[B]); m.dst = ptrsOf<P>(S.buf[B]);
-            m.outbox = ptrsOf<P>(S.outbox);
-            m.start = S.d_start; m.cap = S.d_cap; m.count = S.d_count; m.alive = S.d_alive;
-            m.nleave = S.d_nleave; m.llist = S.llist; m.dir = S.dir;
-            m.needed = S.d_needed; m.neededAlive = S.d_neededAlive;
-            m.newStart = S.d_start2; m.outOff = S.d_outOff;
-        }
-        a.bitmapWords = (maxCap + 31) / 32;
-    };
+    for (int d = 0; d < 3; d++) { a.nsc[d] = ctx->nsc[d]; a.S[d] = c.sc[d]; a.invh[d] = 1.0 / c.h[d]; }
+    a.nspecies = c.nspecies;
+    a.flags = ctx->d_flags;
+    int32_t maxCap = 0;
+    for (int q = 0; q < c.nspecies; q++) {
+        SpeciesState& S = ctx->sp[q];
+        for (int32_t v : S.h_cap) maxCap = std::max(maxCap, v);
+        auto& m = a.sp[q];
+        m.a = ptrsOf<P>(S.buf[A]); m.b = ptrsOf<P>(S.buf[B]); m.dst = ptrsOf<P>(S.buf[B]);
+        m.outbox = ptrsOf<P>(S.outbox);
+        m.start = S.d_start; m.cap = S.d_cap; m.count = S.d_count; m.alive = S.d_alive;
+        m.nleave = S.d_nleave; m.llist = S.llist; m.dir = S.dir;
+        m.needed = S.d_needed; m.neededAlive = S.d_neededAlive;
+        m.newStart = S.d_start2; m.outOff = S.d_outOff;
+    }
+    a.bitmapWords = (maxCap + 31) / 32;
+}
+
+template <class P>
+static int launchMigrate(pica_ctx* ctx, MigrateArgs<P>& m, int stage) {
+    if constexpr (std::is_same<P, PlainPtrs>::value) return launchMigratePlain(m, stage, ctx->stream);
+    else return launchMigrateCell(m, stage, ctx->stream);
+}
+
+// Device part of the migration, enqueued without waiting: sort the leaver lists,
+// count arrivals (flags[1] set on a capacity overflow), fill the holes (the fill
+// returns at once when flags[0] or flags[1] is set).
+template <class P>
+static int migrateDevice(pica_ctx* ctx) {
     MigrateArgs<P> a{};
-    args(a);
+    migrateArgs(ctx, a);
     if ((size_t)a.bitmapWords * 4 > 200 * 1024) return fail(ctx, PICA_ERR_LIMIT, "supercell capacity too large for the leaver sort");
-    auto launch = [&](MigrateArgs<P>& m, int stage) -> int {
-        if constexpr (std::is_same<P, PlainPtrs>::value) return launchMigratePlain(m, stage, ctx->stream);
-        else return launchMigrateCell(m, stage, ctx->stream);
-    };
-    CKL(launch(a, kSortLeavers));
-    CKL(launch(a, kCountArrivals));
-    ctx->launches += 2;
-    CK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    CKL(launchMigrate(ctx, a, kSortLeavers));
+    CKL(launchMigrate(ctx, a, kCountArrivals));
+    CKL(launchMigrate(ctx, a, kFill));
+    ctx->launches += 3;
+    return PICA_OK;
+}
+
+// Host part, after the device part has finished and ctx->h_flags holds its flags:
+// report a migration error, or rebuild on a capacity overflow; then the periodic resort.
+template <class P>
+static int migrateFinish(pica_ctx* ctx) {
+    const pica_config& c = ctx->cfg;
+    const int A = ctx->cur, B = 1 - ctx->cur;
     if (ctx->h_flags[0]) return fail(ctx, ctx->h_flags[0], "a particle crossed more than one supercell in one step");
-    if (!ctx->h_flags[1]) {
-        CKL(launch(a, kFill));
-        ctx->launches++;
-    } else {
-        // Overflow: gather the leavers into the outbox (B is then free), rebuild A + arrivals
-        // into B with capacities for the new counts, and swap.
+    if (ctx->h_flags[1]) {
+        // Overflow (the fill did nothing): gather the leavers into the outbox (B is then
+        // free), rebuild A + arrivals into B with capacities for the new counts, and swap.
+        MigrateArgs<P> a{};
         for (int q = 0; q < c.nspecies; q++) {
             SpeciesState& S = ctx->sp[q];
-            std::vector<int32_t> nl(ctx->nscTot), needed(ctx->nscTot);
+            std::vector<int32_t> nl(ctx->nscTot);
             CK(cudaMemcpy(nl.data(), S.d_nleave, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
             std::vector<int64_t> off(ctx->nscTot);
             int64_t tot = 0;
@@ -736,8 +761,8 @@ static int migrateImpl(pica_ctx* ctx) {
             if ((rc = ensureOutbox(ctx, q, tot))) return rc;
             CK(cudaMemcpy(S.d_outOff, off.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice));
         }
-        args(a);
-        CKL(launch(a, kGatherOutbox));
+        migrateArgs(ctx, a);
+        CKL(launchMigrate(ctx, a, kGatherOutbox));
         ctx->launches++;
         CK(cudaStreamSynchronize(ctx->stream));
         for (int q = 0; q < c.nspecies; q++) {
@@ -748,8 +773,8 @@ static int migrateImpl(pica_ctx* ctx) {
             int rc;
             if ((rc = stageLayout(ctx, q, needed, total)) || (rc = ensureBuffer(ctx, q, B, total))) return rc;
         }
-        args(a);   // buffer B may have been reallocated
-        CKL(launch(a, kRebuild));
+        migrateArgs(ctx, a);   // buffer B may have been reallocated
+        CKL(launchMigrate(ctx, a, kRebuild));
         ctx->launches++;
         CK(cudaStreamSynchronize(ctx->stream));
         for (int q = 0; q < c.nspecies; q++) {
@@ -767,10 +792,10 @@ static int migrateImpl(pica_ctx* ctx) {
         // Compact every supercell and sort it by cell into the other buffer, with
         // capacities recomputed from the live counts.
         const int A2 = ctx->cur, B2 = 1 - ctx->cur;
+        CK(cudaStreamSynchronize(ctx->stream));
         for (int q = 0; q < c.nspecies; q++) {
             SpeciesState& S = ctx->sp[q];
             std::vector<int32_t> alive(ctx->nscTot);
-            CK(cudaStreamSynchronize(ctx->stream));
             CK(cudaMemcpy(alive.data(), S.d_alive, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
             int64_t total;
             int rc;
@@ -779,8 +804,8 @@ static int migrateImpl(pica_ctx* ctx) {
                 return rc;
         }
         MigrateArgs<P> r{};
-        args(r);   // a = current buffer A2, dst = B2
-        CKL(launch(r, kResort));
+        migrateArgs(ctx, r);   // a = current buffer A2, dst = B2
+        CKL(launchMigrate(ctx, r, kResort));
         ctx->launches++;
         CK(cudaStreamSynchronize(ctx->stream));
         for (int q = 0; q < c.nspecies; q++) {
@@ -794,6 +819,15 @@ static int migrateImpl(pica_ctx* ctx) {
         updateJFrac(ctx);
     }
     return PICA_OK;
+}
+
+template <class P>
+static int migrateImpl(pica_ctx* ctx) {
+    int rc = migrateDevice<P>(ctx);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return migrateFinish<P>(ctx);
 }
 
 extern "C" {
@@ -980,5 +1014,285 @@ int pica_plasma_generate(const pica_plasma_spec* s, int32_t threads, double* x, 
     for (auto& t : th) t.join();
     return PICA_OK;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batching form: many independent plasmas advanced together.  The push of every
+// member is one persistent launch over all members' supercells (arguments in a
+// device table); the rest of the step is enqueued per member.  The device part
+// of the step is captured once as a CUDA graph and replayed while the launch
+// arguments stay the same (they change at a resort or a capacity rebuild, when
+// the graph is captured again).  After each step the host reads every member's
+// flags and runs the host part of the migration (errors, rebuilds, resorts).
+// ---------------------------------------------------------------------------
+struct pica_batch {
+    std::vector<pica_ctx*> m;
+    cudaStream_t stream = nullptr;
+    int shape = PICA_SHAPE_CIC;
+    int S[3] = {};
+    int variant = 0;
+    bool useGraph = true;
+    PushArgs<CellPtrs>* d_table = nullptr;
+    PushArgs<CellPtrs>* h_table = nullptr;   // pinned staging of the table
+    int* d_base = nullptr;
+    int* d_counter = nullptr;
+    std::vector<int> order;                  // members in work order
+    int total = 0;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<unsigned char> sig;          // launch arguments the graph was captured with
+    int64_t captures = 0, graphLaunches = 0, steps = 0;
+    int64_t kernelLaunches = 0;              // launches of the device part of the steps
+    std::string err;
+};
+
+namespace {
+
+int batchFail(pica_batch* b, int code, const std::string& msg) {
+    b->err = msg;
+    return code;
+}
+
+#define BK(call)                                                                               \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return batchFail(b, e_ == cudaErrorMemoryAllocation ? PICA_ERR_OOM : PICA_ERR_CUDA, \
+                             std::string(#call) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+
+int memberFail(pica_batch* b, int k, int rc) {
+    return batchFail(b, rc, "member " + std::to_string(k) + ": " + (b->m[k]->err.empty() ? "error" : b->m[k]->err));
+}
+
+void memberPushArgs(pica_ctx* ctx, PushArgs<CellPtrs>& a) {
+    std::memset(&a, 0, sizeof a);
+    fillPushArgs(ctx, a);
+    for (int q = 0; q < ctx->cfg.nspecies; q++) {
+        a.sp[q].buf = cellPtrs(ctx, q, ctx->cur);
+        a.sp[q].out = cellPtrs(ctx, q, 1 - ctx->cur);
+    }
+}
+
+// Everything the captured step depends on: per member in work order, the push and
+// migration arguments and the current-conversion scale.
+void batchSignature(pica_batch* b, std::vector<unsigned char>& sig) {
+    sig.clear();
+    auto put = [&](const void* p, size_t n) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        sig.insert(sig.end(), c, c + n);
+    };
+    for (int k : b->order) {
+        pica_ctx* ctx = b->m[k];
+        PushArgs<CellPtrs> a;
+        memberPushArgs(ctx, a);
+        put(&a, sizeof a);
+        MigrateArgs<CellPtrs> ma;
+        std::memset(&ma, 0, sizeof ma);
+        migrateArgs(ctx, ma);
+        put(&ma, sizeof ma);
+        put(&ctx->jfrac, sizeof ctx->jfrac);
+        put(&ctx->kmax, sizeof ctx->kmax);
+        put(&ctx->cur, sizeof ctx->cur);
+    }
+    put(&b->variant, sizeof b->variant);
+}
+
+// The device part of one step of every member, enqueued on the batch stream.
+int batchEnqueue(pica_batch* b) {
+    for (int k : b->order) BK(cudaMemsetAsync(b->m[k]->d_flags, 0, 4 * sizeof(int), b->stream));
+    BK(cudaMemsetAsync(b->d_counter, 0, sizeof(int), b->stream));
+    BatchPushArgs ba{b->d_table, b->d_base, (int)b->order.size(), b->total, b->d_counter};
+    if (launchPushBatch(ba, b->shape, b->S, b->variant, b->stream)) return batchFail(b, PICA_ERR_CUDA, "batched push launch failed");
+    for (int k : b->order) {
+        pica_ctx* ctx = b->m[k];
+        const pica_config& c = ctx->cfg;
+        const int64_t nodes = (int64_t)c.n[0] * c.n[1] * c.n[2];
+        const double scale = (ctx->kmax * std::ldexp(1.0, -ctx->jfrac)) * (1.0 / (c.h[0] * c.h[1] * c.h[2]));
+        if (launchConvertJ(false, ctx->f + 6, ctx->jacc, nodes, scale, b->stream))
+            return batchFail(b, PICA_ERR_CUDA, "current conversion launch failed");
+        double cb[3], ce[3];
+        for (int d = 0; d < 3; d++) { cb[d] = (kC * (0.5 * c.dt)) / c.h[d]; ce[d] = (kC * c.dt) / c.h[d]; }
+        if (launchUpdateB(false, ctx->f, c.n, cb, b->stream) || launchUpdateE(false, ctx->f, c.n, -4.0 * kPiRef * c.dt, ce, b->stream) ||
+            launchUpdateB(false, ctx->f, c.n, cb, b->stream))
+            return batchFail(b, PICA_ERR_CUDA, "field update launch failed");
+    }
+    for (size_t i = 0; i < b->order.size(); i++) {
+        const int k = b->order[i];
+        pica_ctx* ctx = b->m[k];
+        const int64_t before = ctx->launches;   // counted per executed step by the caller
+        const int rc = migrateDevice<CellPtrs>(ctx);
+        ctx->launches = before;
+        if (rc) return memberFail(b, k, rc);
+    }
+    return PICA_OK;
+}
+
+// Kernel launches of the device part of one step: the batched push, then per member
+// the current conversion, three field updates and three migration stages.
+int64_t batchStepLaunches(const pica_batch* b) { return 1 + 7 * (int64_t)b->m.size(); }
+
+// Work order (most particles per supercell first, for a short tail) and the
+// prefix table of supercells.
+int batchOrder(pica_batch* b) {
+    const int n = (int)b->m.size();
+    std::vector<double> per(n);
+    for (int k = 0; k < n; k++) {
+        int64_t np = 0;
+        for (int q = 0; q < b->m[k]->cfg.nspecies; q++) np += b->m[k]->sp[q].layoutSlots;
+        per[k] = (double)np / b->m[k]->nscTot;
+    }
+    b->order.resize(n);
+    for (int k = 0; k < n; k++) b->order[k] = k;
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return per[x] > per[y]; });
+    std::vector<int> base(n + 1, 0);
+    for (int i = 0; i < n; i++) base[i + 1] = base[i] + b->m[b->order[i]]->nscTot;
+    b->total = base[n];
+    BK(cudaMemcpy(b->d_base, base.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    return PICA_OK;
+}
+
+int batchStepOnce(pica_batch* b) {
+    for (size_t k = 0; k < b->m.size(); k++) {
+        pica_ctx* ctx = b->m[k];
+        if (ctx->pending) return batchFail(b, PICA_ERR_STATE, "member " + std::to_string(k) + ": push pending");
+        ctx->stream = b->stream;
+    }
+    if (b->order.empty()) {
+        const int rc = batchOrder(b);
+        if (rc) return rc;
+    }
+    std::vector<unsigned char> sig;
+    batchSignature(b, sig);
+    if (sig != b->sig) {
+        for (size_t i = 0; i < b->order.size(); i++) memberPushArgs(b->m[b->order[i]], b->h_table[i]);
+        BK(cudaMemcpyAsync(b->d_table, b->h_table, b->order.size() * sizeof(PushArgs<CellPtrs>), cudaMemcpyHostToDevice,
+                           b->stream));
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
+        if (b->useGraph) {
+            cudaGraph_t g = nullptr;
+            BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
+            const int rc = batchEnqueue(b);
+            const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            BK(e);
+            const cudaError_t ei = cudaGraphInstantiate(&b->exec, g, 0);
+            cudaGraphDestroy(g);
+            BK(ei);
+            b->captures++;
+        }
+        b->sig.swap(sig);
+    }
+    if (b->useGraph) {
+        BK(cudaGraphLaunch(b->exec, b->stream));
+        b->graphLaunches++;
+    } else {
+        const int rc = batchEnqueue(b);
+        if (rc) return rc;
+    }
+    b->kernelLaunches += batchStepLaunches(b);
+    for (pica_ctx* ctx : b->m)
+        BK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    for (size_t k = 0; k < b->m.size(); k++) {
+        const int rc = migrateFinish<CellPtrs>(b->m[k]);
+        if (rc) return memberFail(b, (int)k, rc);
+    }
+    b->steps++;
+    return PICA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pica_batch_create(const pica_config* cfgs, int32_t count, pica_batch** out) {
+    if (!cfgs || !out || count < 1) return PICA_ERR_INVALID;
+    *out = nullptr;
+    for (int k = 0; k < count; k++) {
+        const pica_config& c = cfgs[k];
+        if (c.form != PICA_FORM_FP32_CELL || c.deposit != PICA_DEPOSIT_ESIRKEPOV || c.shape != cfgs[0].shape) return PICA_ERR_INVALID;
+        for (int d = 0; d < 3; d++)
+            if (c.sc[d] != cfgs[0].sc[d]) return PICA_ERR_INVALID;
+    }
+    pica_batch* b = new pica_batch();
+    b->shape = cfgs[0].shape;
+    for (int d = 0; d < 3; d++) b->S[d] = cfgs[0].sc[d];
+    auto bail = [&](int rc) {
+        pica_batch_destroy(b);
+        return rc;
+    };
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(PICA_ERR_CUDA);
+    for (int k = 0; k < count; k++) {
+        pica_ctx* ctx = nullptr;
+        const int rc = pica_ctx_create(&cfgs[k], &ctx);
+        if (rc) return bail(rc);
+        ctx->stream = b->stream;
+        b->m.push_back(ctx);
+    }
+    if (cudaMalloc(&b->d_table, count * sizeof(PushArgs<CellPtrs>)) != cudaSuccess ||
+        cudaMallocHost(&b->h_table, count * sizeof(PushArgs<CellPtrs>)) != cudaSuccess ||
+        cudaMalloc(&b->d_base, (count + 1) * sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_counter, sizeof(int)) != cudaSuccess)
+        return bail(PICA_ERR_OOM);
+    *out = b;
+    return PICA_OK;
+}
+
+int pica_batch_destroy(pica_batch* b) {
+    if (!b) return PICA_ERR_INVALID;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    for (pica_ctx* ctx : b->m) pica_ctx_destroy(ctx);
+    if (b->d_table) cudaFree(b->d_table);
+    if (b->h_table) cudaFreeHost(b->h_table);
+    if (b->d_base) cudaFree(b->d_base);
+    if (b->d_counter) cudaFree(b->d_counter);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return PICA_OK;
+}
+
+pica_ctx* pica_batch_member(pica_batch* b, int32_t k) {
+    if (!b || k < 0 || k >= (int)b->m.size()) return nullptr;
+    b->order.clear();   // particle counts may change: recompute the work order at the next step
+    b->sig.clear();
+    return b->m[k];
+}
+
+int pica_batch_set_options(pica_batch* b, int32_t use_graph, int32_t variant) {
+    if (!b || variant < 0 || variant >= kPushVariants) return PICA_ERR_INVALID;
+    b->useGraph = use_graph != 0;
+    b->variant = variant;
+    b->sig.clear();
+    return PICA_OK;
+}
+
+int pica_batch_step(pica_batch* b, int32_t nsteps) {
+    if (!b || nsteps < 0) return PICA_ERR_INVALID;
+    for (int s = 0; s < nsteps; s++) {
+        const int rc = batchStepOnce(b);
+        if (rc) return rc;
+    }
+    return PICA_OK;
+}
+
+int pica_batch_stats(pica_batch* b, int64_t* out4) {
+    if (!b || !out4) return PICA_ERR_INVALID;
+    int64_t launches = 0;
+    for (pica_ctx* ctx : b->m) launches += ctx->launches;
+    out4[0] = b->captures;
+    out4[1] = b->graphLaunches;
+    out4[2] = b->kernelLaunches + launches;   // device part of the steps + rebuilds and resorts
+    out4[3] = b->steps;
+    return PICA_OK;
+}
+
+const char* pica_batch_last_error(pica_batch* b) { return b ? b->err.c_str() : "null batch"; }
 
 }  // extern "C"

@@ -91,6 +91,16 @@ struct PushArgs {
     SpeciesArgs<P> sp[kMaxSpecies];
 };
 
+// Batching form: push arguments of every plasma in a device table; work item w
+// (one supercell) belongs to plasma k with base[k] <= w < base[k + 1].
+struct BatchPushArgs {
+    const PushArgs<CellPtrs>* members;
+    const int* base;   // count + 1 entries
+    int count;
+    int total;
+    int* counter;      // next work item; zero before the launch
+};
+
 template <class P>
 struct MigrateSpecies {
     P a;                    // A (current)
@@ -125,6 +135,9 @@ int launchPushPlain(const PushArgs<PlainPtrs>& a, int shape, int deposit, cudaSt
 // variant: launch shape of the FP32 Esirkepov kernel (0..kPushVariants-1), see push_fp32.cu.
 constexpr int kPushVariants = 4;
 int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int deposit, int variant, cudaStream_t s);
+// Persistent push over a batch (FP32 cell form, Esirkepov; S = supercell edges shared
+// by every plasma).  grid <= 0: one CTA per resident slot on every SM.
+int launchPushBatch(const BatchPushArgs& b, int shape, const int* S, int variant, cudaStream_t s);
 // Migration stages.
 enum MigrateStage { kSortLeavers = 0, kCountArrivals = 1, kFill = 2, kGatherOutbox = 3, kRebuild = 4, kResort = 5 };
 int launchMigratePlain(const MigrateArgs<PlainPtrs>& a, int stage, cudaStream_t s);

@@ -188,17 +188,18 @@ __host__ __device__ constexpr int64_t esirkepovSmemWords(int TT, int ETT, int wa
     return 6ll * TT + 6ll * ETT + (int64_t)warps * (kRing * kQWords + nv * kRedRows + kRedRows);
 }
 
-// SC > 0: cubic supercells of edge SC known at compile time (tile strides become
-// constants); SC == 0: edges read from the arguments.
-template <int SHAPE, int K, int THREADS, int MINB, int SC>
-__global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __grid_constant__ PushArgs<CellPtrs> a) {
+// One supercell s of the plasma described by a, on the whole CTA (smem_raw: the
+// dynamic shared memory, esirkepovSmemWords words).  SC > 0: cubic supercells of
+// edge SC known at compile time (tile strides become constants); SC == 0: edges
+// read from the arguments.
+template <int SHAPE, int K, int THREADS, int SC>
+__device__ __forceinline__ void pushSupercell(const PushArgs<CellPtrs>& a, const int s, unsigned char* smem_raw,
+                                              int& s_nleave) {
     constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;   // stay-in-window nodes per dimension
     constexpr int NV = 3 * (NWn - 1) * NWn * NWn;          // 54 (TSC) or 12 (CIC)
     constexpr int kWarps = THREADS / 32;
     constexpr int kPark = kRedRows - 32;
     constexpr unsigned FULL = 0xffffffffu;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int s_nleave;
 
     // Current tile: origin m - kG, edges S + 2kG + 1.  E/B tile: origin m - 1, edges S + 3.
     const int T1 = SC ? SC + 2 * kG + 1 : a.T[1], T2 = SC ? SC + 2 * kG + 1 : a.T[2];
@@ -223,7 +224,6 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
     jts.down = jt.down;
     const unsigned ringS = (unsigned)__cvta_generic_to_shared(ring);
 
-    const int s = blockIdx.x;
     int sc[3];
     sc[2] = s % a.nsc[2];
     sc[1] = (s / a.nsc[2]) % a.nsc[1];
@@ -516,6 +516,44 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
             const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
             atomicAdd(a.jacc[c] + ((int64_t)gx * a.n[1] + gy) * a.n[2] + gz, v);
         }
+    }
+}
+
+template <int SHAPE, int K, int THREADS, int MINB, int SC>
+__global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __grid_constant__ PushArgs<CellPtrs> a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_nleave;
+    pushSupercell<SHAPE, K, THREADS, SC>(a, blockIdx.x, smem_raw, s_nleave);
+}
+
+// Batching form: one persistent launch over the supercells of many independent
+// plasmas.  Each CTA takes the next work item from b.counter (zeroed before the
+// launch), finds its plasma by binary search over b.base and copies that
+// plasma's arguments into shared memory before pushing the supercell.
+template <int SHAPE, int K, int THREADS, int MINB, int SC>
+__global__ void __launch_bounds__(THREADS, MINB) k_push_batch(const __grid_constant__ BatchPushArgs b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_nleave;
+    __shared__ int s_work;
+    __shared__ __align__(16) PushArgs<CellPtrs> s_args;
+    constexpr int kArgWords = (int)(sizeof(PushArgs<CellPtrs>) / 4);
+    static_assert(sizeof(PushArgs<CellPtrs>) % 4 == 0, "argument table entries are copied as words");
+    for (;;) {
+        __syncthreads();   // the previous work item is done with the shared memory
+        if (threadIdx.x == 0) s_work = atomicAdd(b.counter, 1);
+        __syncthreads();
+        const int w = s_work;
+        if (w >= b.total) return;
+        int lo = 0, hi = b.count;   // largest k with base[k] <= w
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (b.base[mid] <= w) lo = mid; else hi = mid;
+        }
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(b.members + lo);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&s_args);
+        for (int t = threadIdx.x; t < kArgWords; t += THREADS) dst[t] = src[t];
+        __syncthreads();
+        pushSupercell<SHAPE, K, THREADS, SC>(s_args, w - b.base[lo], smem_raw, s_nleave);
     }
 }
 

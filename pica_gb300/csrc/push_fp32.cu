@@ -1,4 +1,6 @@
 // FP32 cell form: push and migration kernels (FMA contraction allowed).
+#include <algorithm>
+
 #include "push_fast.cuh"
 
 namespace pgb {
@@ -53,6 +55,42 @@ int launchEsirkepov(const PushArgs<CellPtrs>& a, int variant, cudaStream_t s) {
     const bool cubic = a.S[0] == a.S[1] && a.S[1] == a.S[2];
     if (cubic && a.S[0] == 4) return launchEsirkepovS<SHAPE, 4>(a, variant, s);
     return launchEsirkepovS<SHAPE, 0>(a, variant, s);
+}
+
+template <int SHAPE, int SC, int K, int THREADS, int MINB>
+int launchBatchV(const BatchPushArgs& b, const int* S, cudaStream_t s) {
+    const int TT = (S[0] + 2 * kG + 1) * (S[1] + 2 * kG + 1) * (S[2] + 2 * kG + 1);
+    const int ETT = (S[0] + 3) * (S[1] + 3) * (S[2] + 3);
+    constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;
+    const size_t smem = (size_t)esirkepovSmemWords(TT, ETT, THREADS / 32, 3 * (NWn - 1) * NWn * NWn) * 4;
+    auto k = k_push_batch<SHAPE, K, THREADS, MINB, SC>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return (int)e;
+    int dev = 0, sms = 0, per = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, THREADS, smem)) != cudaSuccess) return (int)e;
+    const int grid = std::max(1, std::min(b.total, sms * std::max(per, 1)));
+    k<<<grid, THREADS, smem, s>>>(b);
+    return (int)cudaGetLastError();
+}
+
+template <int SHAPE, int SC>
+int launchBatchS(const BatchPushArgs& b, const int* S, int variant, cudaStream_t s) {
+    switch (variant) {
+        case 1: return launchBatchV<SHAPE, SC, 8, 128, 2>(b, S, s);
+        case 2: return launchBatchV<SHAPE, SC, 8, 64, 6>(b, S, s);
+        case 3: return launchBatchV<SHAPE, SC, 8, 256, 1>(b, S, s);
+        default: return launchBatchV<SHAPE, SC, 8, 128, 3>(b, S, s);
+    }
+}
+
+int launchPushBatch(const BatchPushArgs& b, int shape, const int* S, int variant, cudaStream_t s) {
+    const bool sc4 = S[0] == 4 && S[1] == 4 && S[2] == 4;
+    if (shape == PICA_SHAPE_TSC) return sc4 ? launchBatchS<PICA_SHAPE_TSC, 4>(b, S, variant, s) : launchBatchS<PICA_SHAPE_TSC, 0>(b, S, variant, s);
+    if (shape == PICA_SHAPE_CIC) return sc4 ? launchBatchS<PICA_SHAPE_CIC, 4>(b, S, variant, s) : launchBatchS<PICA_SHAPE_CIC, 0>(b, S, variant, s);
+    return (int)cudaErrorInvalidValue;
 }
 
 int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int dep, int variant, cudaStream_t s) {

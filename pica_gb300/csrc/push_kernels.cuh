@@ -768,7 +768,7 @@ __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ Migrate
     const int d = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (d >= nscTot) return;
-    if (STAGE == kFill && a.flags[1] != 0) return;   // overflow: the rebuild path runs instead
+    if (STAGE == kFill && (a.flags[0] != 0 || a.flags[1] != 0)) return;   // error, or overflow: the rebuild runs instead
     for (int spi = 0; spi < a.nspecies; spi++) {
         const MigrateSpecies<P>& sa = a.sp[spi];
         const int64_t start = sa.start[d];

@@ -94,9 +94,11 @@ def config5():
     return weibel()
 
 
-def batched_members(count=64, seed_base=0):
+def batched_members(count=64, seed_base=0, half=False, resort_every=4):
     """64 independent thermal plasmas: plasma k seeded by k; edge in {32, 36, ..., 96}, ppc in
-    16..128, sigma in [0.02, 0.1].  Uses a SplitMix64 stream so the draws are reproducible."""
+    16..128, sigma in [0.02, 0.1].  Uses a SplitMix64 stream so the draws are reproducible.
+    half=True halves every edge (rounded to a multiple of 4): the same members at 1/8 of
+    the cells."""
     def mix(z):
         z = (z + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
         z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
@@ -107,8 +109,12 @@ def batched_members(count=64, seed_base=0):
     for k in range(count):
         r = [mix((seed_base + k) * 16 + i) for i in range(3)]
         edge = 32 + 4 * (r[0] % 17)
+        if half:
+            edge = 4 * round(edge / 8)
         ppc = 16 + r[1] % 113
         sigma = 0.02 + 0.08 * (r[2] >> 11) / float(1 << 53)
-        out.append(thermal(n=(edge, edge, edge), ppc=ppc, sigma=sigma, supercell=(4, 4, 4), form=FORM_FP32_CELL,
-                           shape=SHAPE_CIC, deposit=DEPOSIT_ESIRKEPOV, steps=200, seed=1000 + k))
+        wl = thermal(n=(edge, edge, edge), ppc=ppc, sigma=sigma, supercell=(4, 4, 4), form=FORM_FP32_CELL,
+                     shape=SHAPE_CIC, deposit=DEPOSIT_ESIRKEPOV, steps=200, seed=1000 + k)
+        wl["sim"]["resort_every"] = resort_every
+        out.append(wl)
     return out
