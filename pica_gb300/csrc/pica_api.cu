@@ -25,7 +25,9 @@ struct SpeciesState {
     void* buf[2][8] = {};        // A = buf[cur], B = buf[1 - cur]
     int64_t slots[2] = {0, 0};   // allocated slots of each buffer
     uint8_t* dir = nullptr;      // direction code per slot
-    int32_t* llist = nullptr;    // leaver slots per supercell (at [start, start + nleave))
+    int32_t* llist = nullptr;    // leaver slots per supercell (at [start, start + nleave)), by slot
+    int32_t* lbydir = nullptr;   // the same slots by (direction code, slot)
+    int32_t* d_dirOff = nullptr; // per supercell, 28 bucket offsets of lbydir
     int64_t slotArrays = 0;      // allocated entries of dir / llist
     void* outbox[8] = {};        // overflow rebuild: leavers gathered per source supercell
     int64_t outSlots = 0;
@@ -164,12 +166,15 @@ int ensureSlotArrays(pica_ctx* ctx, int spi, int64_t slots) {
     if (S.slotArrays >= slots) return PICA_OK;
     if (S.dir) CK(cudaFree(S.dir));
     if (S.llist) CK(cudaFree(S.llist));
+    if (S.lbydir) CK(cudaFree(S.lbydir));
     S.dir = nullptr;
     S.llist = nullptr;
+    S.lbydir = nullptr;
     S.slotArrays = 0;
     const int64_t grown = withHeadroom(slots);
     CK(cudaMalloc(&S.dir, grown));
     CK(cudaMalloc(&S.llist, grown * 4));
+    CK(cudaMalloc(&S.lbydir, grown * 4));
     S.slotArrays = grown;
     return PICA_OK;
 }
@@ -319,7 +324,7 @@ int pica_ctx_create(const pica_config* cfg, pica_ctx** out) {
         if (cudaMalloc(&S.d_start, n * 8) || cudaMalloc(&S.d_cap, n * 4) || cudaMalloc(&S.d_count, n * 4) ||
             cudaMalloc(&S.d_alive, n * 4) || cudaMalloc(&S.d_nleave, n * 4) || cudaMalloc(&S.d_needed, n * 4) ||
             cudaMalloc(&S.d_neededAlive, n * 4) || cudaMalloc(&S.d_start2, n * 8) || cudaMalloc(&S.d_cap2, n * 4) ||
-            cudaMalloc(&S.d_outOff, n * 8))
+            cudaMalloc(&S.d_outOff, n * 8) || cudaMalloc(&S.d_dirOff, n * kDirBuckets * 4))
             return bail(PICA_ERR_OOM);
         std::vector<int32_t> zero(n, 0);
         int64_t total;
@@ -353,7 +358,7 @@ int pica_ctx_destroy(pica_ctx* ctx) {
         for (auto p : S.outbox) if (p) cudaFree(p);
         for (void* p : {(void*)S.dir, (void*)S.llist, (void*)S.d_start, (void*)S.d_cap, (void*)S.d_count,
                         (void*)S.d_alive, (void*)S.d_nleave, (void*)S.d_needed, (void*)S.d_neededAlive,
-                        (void*)S.d_start2, (void*)S.d_cap2, (void*)S.d_outOff})
+                        (void*)S.d_start2, (void*)S.d_cap2, (void*)S.d_outOff, (void*)S.lbydir, (void*)S.d_dirOff})
             if (p) cudaFree(p);
     }
     if (ctx->d_flags) cudaFree(ctx->d_flags);
@@ -714,6 +719,7 @@ static void migrateArgs(pica_ctx* ctx, MigrateArgs<P>& a) {
         m.nleave = S.d_nleave; m.llist = S.llist; m.dir = S.dir;
         m.needed = S.d_needed; m.neededAlive = S.d_neededAlive;
         m.newStart = S.d_start2; m.outOff = S.d_outOff;
+        m.lbydir = S.lbydir; m.dirOff = S.d_dirOff;
     }
     a.bitmapWords = (maxCap + 31) / 32;
 }
@@ -1033,12 +1039,11 @@ struct pica_batch {
     int S[3] = {};
     int variant = 0;
     bool useGraph = true;
-    PushArgs<CellPtrs>* d_table = nullptr;
-    PushArgs<CellPtrs>* h_table = nullptr;   // pinned staging of the table
-    int* d_base = nullptr;
-    int* d_counter = nullptr;
+    int* d_counter = nullptr;                // one work counter per push launch
     std::vector<int> order;                  // members in work order
-    int total = 0;
+    int nsp = 1;                             // species slots of the push arguments (1 or 2)
+    std::vector<BatchPushArgs<1>> args1;     // one persistent push launch per batchMembers<NSP>() members
+    std::vector<BatchPushArgs<2>> args2;
     cudaGraphExec_t exec = nullptr;
     std::vector<unsigned char> sig;          // launch arguments the graph was captured with
     int64_t captures = 0, graphLaunches = 0, steps = 0;
@@ -1098,12 +1103,64 @@ void batchSignature(pica_batch* b, std::vector<unsigned char>& sig) {
     put(&b->variant, sizeof b->variant);
 }
 
+template <int NSP>
+void slimArgs(const PushArgs<CellPtrs>& a, PushArgsSlim<NSP>& o) {
+    std::memset(&o, 0, sizeof o);
+    for (int d = 0; d < 3; d++) {
+        o.n[d] = a.n[d]; o.S[d] = a.S[d]; o.nsc[d] = a.nsc[d]; o.T[d] = a.T[d];
+        o.cdth[d] = (float)a.cdth[d]; o.jacc[d] = a.jacc[d];
+    }
+    o.nspecies = a.nspecies;
+    o.tileSplit = a.tileSplit;
+    o.invUnit = (float)a.invUnit;
+    for (int k = 0; k < 6; k++) o.eb[k] = a.eb[k];
+    o.flags = a.flags;
+    for (int q = 0; q < a.nspecies && q < NSP; q++) {
+        const auto& x = a.sp[q];
+        auto& y = o.sp[q];
+        y.buf = x.buf; y.out = x.out; y.start = x.start; y.count = x.count;
+        y.nleave = x.nleave; y.llist = x.llist; y.dir = x.dir; y.ec = (float)x.ec;
+        for (int d = 0; d < 3; d++) y.kq[d] = (float)x.kq[d];
+    }
+}
+
+// Arguments of the persistent push launches for the current layouts (members in
+// work order, batchMembers<NSP>() per launch).
+template <int NSP>
+void batchLaunchArgs(pica_batch* b, std::vector<BatchPushArgs<NSP>>& out) {
+    constexpr int M = batchMembers<NSP>();
+    const int n = (int)b->order.size();
+    const int launches = (n + M - 1) / M;
+    out.resize(launches);
+    for (int c = 0; c < launches; c++) {
+        BatchPushArgs<NSP>& ba = out[c];
+        std::memset(&ba, 0, sizeof ba);
+        ba.count = std::min(M, n - c * M);
+        ba.counter = b->d_counter + c;
+        ba.base[0] = 0;
+        for (int i = 0; i < ba.count; i++) {
+            pica_ctx* ctx = b->m[b->order[c * M + i]];
+            PushArgs<CellPtrs> a;
+            memberPushArgs(ctx, a);
+            slimArgs(a, ba.members[i]);
+            ba.base[i + 1] = ba.base[i] + ctx->nscTot;
+        }
+        ba.total = ba.base[ba.count];
+    }
+}
+
+size_t batchPushLaunches(const pica_batch* b) { return b->nsp == 1 ? b->args1.size() : b->args2.size(); }
+
 // The device part of one step of every member, enqueued on the batch stream.
 int batchEnqueue(pica_batch* b) {
     for (int k : b->order) BK(cudaMemsetAsync(b->m[k]->d_flags, 0, 4 * sizeof(int), b->stream));
-    BK(cudaMemsetAsync(b->d_counter, 0, sizeof(int), b->stream));
-    BatchPushArgs ba{b->d_table, b->d_base, (int)b->order.size(), b->total, b->d_counter};
-    if (launchPushBatch(ba, b->shape, b->S, b->variant, b->stream)) return batchFail(b, PICA_ERR_CUDA, "batched push launch failed");
+    BK(cudaMemsetAsync(b->d_counter, 0, batchPushLaunches(b) * sizeof(int), b->stream));
+    for (const auto& ba : b->args1)
+        if (b->nsp == 1 && launchPushBatch(ba, b->shape, b->S, b->variant, b->stream))
+            return batchFail(b, PICA_ERR_CUDA, "batched push launch failed");
+    for (const auto& ba : b->args2)
+        if (b->nsp == 2 && launchPushBatch(ba, b->shape, b->S, b->variant, b->stream))
+            return batchFail(b, PICA_ERR_CUDA, "batched push launch failed");
     for (int k : b->order) {
         pica_ctx* ctx = b->m[k];
         const pica_config& c = ctx->cfg;
@@ -1128,12 +1185,11 @@ int batchEnqueue(pica_batch* b) {
     return PICA_OK;
 }
 
-// Kernel launches of the device part of one step: the batched push, then per member
-// the current conversion, three field updates and three migration stages.
-int64_t batchStepLaunches(const pica_batch* b) { return 1 + 7 * (int64_t)b->m.size(); }
+// Kernel launches of the device part of one step: the batched push launches, then per
+// member the current conversion, three field updates and three migration stages.
+int64_t batchStepLaunches(const pica_batch* b) { return (int64_t)batchPushLaunches(b) + 7 * (int64_t)b->m.size(); }
 
-// Work order (most particles per supercell first, for a short tail) and the
-// prefix table of supercells.
+// Work order: most particles per supercell first, for a short tail.
 int batchOrder(pica_batch* b) {
     const int n = (int)b->m.size();
     std::vector<double> per(n);
@@ -1145,10 +1201,6 @@ int batchOrder(pica_batch* b) {
     b->order.resize(n);
     for (int k = 0; k < n; k++) b->order[k] = k;
     std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return per[x] > per[y]; });
-    std::vector<int> base(n + 1, 0);
-    for (int i = 0; i < n; i++) base[i + 1] = base[i] + b->m[b->order[i]]->nscTot;
-    b->total = base[n];
-    BK(cudaMemcpy(b->d_base, base.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
     return PICA_OK;
 }
 
@@ -1165,9 +1217,8 @@ int batchStepOnce(pica_batch* b) {
     std::vector<unsigned char> sig;
     batchSignature(b, sig);
     if (sig != b->sig) {
-        for (size_t i = 0; i < b->order.size(); i++) memberPushArgs(b->m[b->order[i]], b->h_table[i]);
-        BK(cudaMemcpyAsync(b->d_table, b->h_table, b->order.size() * sizeof(PushArgs<CellPtrs>), cudaMemcpyHostToDevice,
-                           b->stream));
+        if (b->nsp == 1) batchLaunchArgs(b, b->args1);
+        else batchLaunchArgs(b, b->args2);
         if (b->exec) {
             cudaGraphExecDestroy(b->exec);
             b->exec = nullptr;
@@ -1217,12 +1268,15 @@ int pica_batch_create(const pica_config* cfgs, int32_t count, pica_batch** out) 
     *out = nullptr;
     for (int k = 0; k < count; k++) {
         const pica_config& c = cfgs[k];
-        if (c.form != PICA_FORM_FP32_CELL || c.deposit != PICA_DEPOSIT_ESIRKEPOV || c.shape != cfgs[0].shape) return PICA_ERR_INVALID;
+        if (c.form != PICA_FORM_FP32_CELL || c.deposit != PICA_DEPOSIT_ESIRKEPOV || c.shape != cfgs[0].shape ||
+            c.nspecies > kBatchSpecies)
+            return PICA_ERR_INVALID;
         for (int d = 0; d < 3; d++)
             if (c.sc[d] != cfgs[0].sc[d]) return PICA_ERR_INVALID;
     }
     pica_batch* b = new pica_batch();
     b->shape = cfgs[0].shape;
+    for (int k = 0; k < count; k++) b->nsp = std::max(b->nsp, (int)cfgs[k].nspecies);
     for (int d = 0; d < 3; d++) b->S[d] = cfgs[0].sc[d];
     auto bail = [&](int rc) {
         pica_batch_destroy(b);
@@ -1236,9 +1290,8 @@ int pica_batch_create(const pica_config* cfgs, int32_t count, pica_batch** out) 
         ctx->stream = b->stream;
         b->m.push_back(ctx);
     }
-    if (cudaMalloc(&b->d_table, count * sizeof(PushArgs<CellPtrs>)) != cudaSuccess ||
-        cudaMallocHost(&b->h_table, count * sizeof(PushArgs<CellPtrs>)) != cudaSuccess ||
-        cudaMalloc(&b->d_base, (count + 1) * sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_counter, sizeof(int)) != cudaSuccess)
+    if (cudaMalloc(&b->d_counter, ((count + batchMembers<kBatchSpecies>() - 1) / batchMembers<kBatchSpecies>()) * sizeof(int)) !=
+        cudaSuccess)
         return bail(PICA_ERR_OOM);
     *out = b;
     return PICA_OK;
@@ -1249,9 +1302,6 @@ int pica_batch_destroy(pica_batch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     for (pica_ctx* ctx : b->m) pica_ctx_destroy(ctx);
-    if (b->d_table) cudaFree(b->d_table);
-    if (b->h_table) cudaFreeHost(b->h_table);
-    if (b->d_base) cudaFree(b->d_base);
     if (b->d_counter) cudaFree(b->d_counter);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;

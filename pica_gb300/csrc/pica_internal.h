@@ -91,15 +91,50 @@ struct PushArgs {
     SpeciesArgs<P> sp[kMaxSpecies];
 };
 
-// Batching form: push arguments of every plasma in a device table; work item w
-// (one supercell) belongs to plasma k with base[k] <= w < base[k + 1].
+// Batching form: the push arguments of up to batchMembers<NSP>() plasmas of at most
+// NSP species travel in the kernel parameters (read-only, so the compiler uses them
+// as it uses the single-plasma kernel's); work item w (one supercell) belongs to
+// plasma k with base[k] <= w < base[k + 1].  Only the fields the FP32 Esirkepov push
+// reads; the FP32 values are the ones the kernel would round the FP64 values to.
+struct SpeciesArgsSlim {
+    CellPtrs buf;
+    CellPtrs out;
+    const int64_t* start;
+    const int32_t* count;
+    int32_t* nleave;
+    int32_t* llist;
+    uint8_t* dir;
+    float ec;
+    float kq[3];
+};
+template <int NSP>
+struct PushArgsSlim {
+    int n[3], S[3], nsc[3], T[3];
+    int nspecies;
+    int tileSplit;
+    float cdth[3];
+    float invUnit;
+    const void* eb[6];
+    unsigned long long* jacc[3];
+    int* flags;
+    SpeciesArgsSlim sp[NSP];
+};
+constexpr int kBatchParamBytes = 31 * 1024;
+template <int NSP>
+constexpr int batchMembers() { return (int)((kBatchParamBytes - 64) / (sizeof(PushArgsSlim<NSP>) + sizeof(int))); }
+template <int NSP>
 struct BatchPushArgs {
-    const PushArgs<CellPtrs>* members;
-    const int* base;   // count + 1 entries
     int count;
     int total;
     int* counter;      // next work item; zero before the launch
+    int base[batchMembers<NSP>() + 1];
+    PushArgsSlim<NSP> members[batchMembers<NSP>()];
 };
+static_assert(sizeof(BatchPushArgs<1>) <= 32000 && sizeof(BatchPushArgs<2>) <= 32000,
+              "batched push arguments exceed the kernel parameter space");
+constexpr int kBatchSpecies = 2;
+
+constexpr int kDirBuckets = 28;  // 27 direction codes + end
 
 template <class P>
 struct MigrateSpecies {
@@ -112,7 +147,9 @@ struct MigrateSpecies {
     int32_t* count;         // used slots (incl. dead)
     int32_t* alive;         // live particles
     const int32_t* nleave;
-    int32_t* llist;
+    int32_t* llist;         // leaver slots by slot (the holes, in fill order)
+    int32_t* lbydir;        // leaver slots by (direction code, slot)
+    int32_t* dirOff;        // per supercell: kDirBuckets offsets into lbydir (code c: [dirOff[c], dirOff[c+1]))
     const uint8_t* dir;
     int32_t* needed;        // count after migration
     int32_t* neededAlive;   // live particles after migration
@@ -137,7 +174,8 @@ constexpr int kPushVariants = 4;
 int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int deposit, int variant, cudaStream_t s);
 // Persistent push over a batch (FP32 cell form, Esirkepov; S = supercell edges shared
 // by every plasma).  grid <= 0: one CTA per resident slot on every SM.
-int launchPushBatch(const BatchPushArgs& b, int shape, const int* S, int variant, cudaStream_t s);
+template <int NSP>
+int launchPushBatch(const BatchPushArgs<NSP>& b, int shape, const int* S, int variant, cudaStream_t s);
 // Migration stages.
 enum MigrateStage { kSortLeavers = 0, kCountArrivals = 1, kFill = 2, kGatherOutbox = 3, kRebuild = 4, kResort = 5 };
 int launchMigratePlain(const MigrateArgs<PlainPtrs>& a, int stage, cudaStream_t s);

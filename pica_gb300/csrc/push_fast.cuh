@@ -7,9 +7,10 @@
 //    l handles the K consecutive particles lK .. lK+K-1 (the next one's data is
 //    loaded one iteration ahead), so a lane rarely changes cell and the warp's
 //    lanes mostly share one or two cells.
-//  * Particles that keep their rho-lattice window (the cell for TSC; about 96%
-//    per step for a thermal plasma at half the Courant step) deposit on a fixed
-//    small window of faces (54 values for TSC, 12 for CIC).  Each lane sums
+//  * Particles that stay in their cell (about 96% per step for a thermal plasma
+//    at half the Courant step) have old and new shapes on the rho-lattice nodes
+//    lc-1 .. lc+1 (TSC: all three; CIC: two of them, by the half of the cell),
+//    so they deposit on a fixed window of 54 face values.  Each lane sums
 //    its particles' window contributions in registers, keyed by the window.
 //    When a lane meets a particle of another window it parks its sums in a
 //    spare row of the warp's shared-memory reduction area.  At the end of the
@@ -18,7 +19,7 @@
 //    order they were taken): lane t sums values t and t+32 over the rows and
 //    issues one fixed-point shared-memory atomic per value.  The order depends
 //    only on the particle data, so the result is reproducible bit for bit.
-//  * Particles whose window changes are queued in a per-warp shared-memory
+//  * Particles that change cell are queued in a per-warp shared-memory
 //    ring and deposited on the general 4- (TSC) or 3-node (CIC) window, 32 at a
 //    time (one per lane), by one out-of-line routine.
 //  * Stayers are written back in place; leavers go to the side buffer at
@@ -66,6 +67,8 @@ __device__ __forceinline__ float borisFast(float ec, const float* eb, float* u) 
 }
 
 constexpr int kQWords = 11;  // queued window change: o[3], on[3], kq[3], packed lc, packed ln
+constexpr int kStayNodes = 3;    // stay-in-cell window: rho-lattice nodes lc-1 .. lc+1 per dimension
+constexpr int kStayValues = 54;  // its face values: 3 components x 2 faces x 3 x 3
 
 // Esirkepov deposit of a particle whose rho-lattice window changes (old shape on
 // nodes lo0.., new on lo1..): general NWn+1-node window with per-lane atomics.
@@ -192,11 +195,10 @@ __host__ __device__ constexpr int64_t esirkepovSmemWords(int TT, int ETT, int wa
 // dynamic shared memory, esirkepovSmemWords words).  SC > 0: cubic supercells of
 // edge SC known at compile time (tile strides become constants); SC == 0: edges
 // read from the arguments.
-template <int SHAPE, int K, int THREADS, int SC>
-__device__ __forceinline__ void pushSupercell(const PushArgs<CellPtrs>& a, const int s, unsigned char* smem_raw,
-                                              int& s_nleave) {
-    constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;   // stay-in-window nodes per dimension
-    constexpr int NV = 3 * (NWn - 1) * NWn * NWn;          // 54 (TSC) or 12 (CIC)
+template <int SHAPE, int K, int THREADS, int SC, class A>
+__device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned char* smem_raw, int& s_nleave) {
+    constexpr int NWn = kStayNodes;                        // stay-in-cell window: nodes lc-1 .. lc+1
+    constexpr int NV = kStayValues;                        // 54 face values
     constexpr int kWarps = THREADS / 32;
     constexpr int kPark = kRedRows - 32;
     constexpr unsigned FULL = 0xffffffffu;
@@ -244,7 +246,7 @@ __device__ __forceinline__ void pushSupercell(const PushArgs<CellPtrs>& a, const
     __syncthreads();
 
     for (int spi = 0; spi < a.nspecies; spi++) {
-        const SpeciesArgs<CellPtrs>& sa = a.sp[spi];
+        const auto& sa = a.sp[spi];
         const int64_t start = sa.start[s];
         const int count = sa.count[s];
         const float ec = (float)sa.ec;
@@ -294,7 +296,7 @@ __device__ __forceinline__ void pushSupercell(const PushArgs<CellPtrs>& a, const
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
                         lc[d] = c3[d] - m[d];
-                        lw[d] = SHAPE == PICA_SHAPE_TSC ? lc[d] - 1 : (o[d] >= 0.5f ? lc[d] : lc[d] - 1);
+                        lw[d] = lc[d] - 1;
                     }
                     key = ((lw[0] + 4) << 16) | ((lw[1] + 4) << 8) | (lw[2] + 4);
                 }
@@ -392,27 +394,23 @@ __device__ __forceinline__ void pushSupercell(const PushArgs<CellPtrs>& a, const
                         for (int d = 0; d < 3; d++) { ln[d] = lc[d]; on[d] = o[d]; }
                     }
                     const float kq[3] = {kqs[0] * wgt, kqs[1] * wgt, kqs[2] * wgt};
-                    // Old and new shapes on the rho lattice: TSC nodes lc-1..lc+1 (weights of o-1/2);
-                    // CIC nodes base, base+1 with base = lc or lc-1 by o >= 1/2.
-                    int lo0[3], lo1[3];
+                    // Old and new shapes on the rho-lattice nodes lc-1 .. lc+1 of the old cell (used
+                    // when the particle stays in its cell).  TSC: weights of o - 1/2 on all three.
+                    // CIC: nodes base, base+1 with base = lc or lc-1 by o >= 1/2, the third weight 0.
                     float w0[3][NWn], w1[3][NWn];
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
                         if constexpr (SHAPE == PICA_SHAPE_TSC) {
                             tscWeights(o[d] - 0.5f, w0[d]);
                             tscWeights(on[d] - 0.5f, w1[d]);
-                            lo0[d] = lc[d] - 1;
-                            lo1[d] = ln[d] - 1;
                         } else {
                             const bool h0 = o[d] >= 0.5f, h1 = on[d] >= 0.5f;
                             const float d0 = h0 ? o[d] - 0.5f : o[d] + 0.5f, d1 = h1 ? on[d] - 0.5f : on[d] + 0.5f;
-                            w0[d][0] = 1.0f - d0; w0[d][1] = d0;
-                            w1[d][0] = 1.0f - d1; w1[d][1] = d1;
-                            lo0[d] = h0 ? lc[d] : lc[d] - 1;
-                            lo1[d] = h1 ? ln[d] : ln[d] - 1;
+                            w0[d][0] = h0 ? 0.0f : 1.0f - d0; w0[d][1] = h0 ? 1.0f - d0 : d0; w0[d][2] = h0 ? d0 : 0.0f;
+                            w1[d][0] = h1 ? 0.0f : 1.0f - d1; w1[d][1] = h1 ? 1.0f - d1 : d1; w1[d][2] = h1 ? d1 : 0.0f;
                         }
                     }
-                    const bool sameWindow = inRange && lo0[0] == lo1[0] && lo0[1] == lo1[1] && lo0[2] == lo1[2];
+                    const bool sameWindow = inRange && ln[0] == lc[0] && ln[1] == lc[1] && ln[2] == lc[2];
                     if (sameWindow) {
                         // a = S0, dd = S1 - S0; p = a + d/2, q = a/2 + d/3; yz = a_y p_z + d_y q_z.
                         float aa[3][NWn], dd[3][NWn], pp[3][NWn], qq[3][NWn];
@@ -528,16 +526,13 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __g
 
 // Batching form: one persistent launch over the supercells of many independent
 // plasmas.  Each CTA takes the next work item from b.counter (zeroed before the
-// launch), finds its plasma by binary search over b.base and copies that
-// plasma's arguments into shared memory before pushing the supercell.
-template <int SHAPE, int K, int THREADS, int MINB, int SC>
-__global__ void __launch_bounds__(THREADS, MINB) k_push_batch(const __grid_constant__ BatchPushArgs b) {
+// launch) and finds its plasma by binary search over b.base; the plasma's
+// arguments are read from the kernel parameters.
+template <int SHAPE, int K, int THREADS, int MINB, int SC, int NSP>
+__global__ void __launch_bounds__(THREADS, MINB) k_push_batch(const __grid_constant__ BatchPushArgs<NSP> b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_nleave;
     __shared__ int s_work;
-    __shared__ __align__(16) PushArgs<CellPtrs> s_args;
-    constexpr int kArgWords = (int)(sizeof(PushArgs<CellPtrs>) / 4);
-    static_assert(sizeof(PushArgs<CellPtrs>) % 4 == 0, "argument table entries are copied as words");
     for (;;) {
         __syncthreads();   // the previous work item is done with the shared memory
         if (threadIdx.x == 0) s_work = atomicAdd(b.counter, 1);
@@ -549,11 +544,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_push_batch(const __grid_const
             const int mid = (lo + hi) >> 1;
             if (b.base[mid] <= w) lo = mid; else hi = mid;
         }
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(b.members + lo);
-        uint32_t* dst = reinterpret_cast<uint32_t*>(&s_args);
-        for (int t = threadIdx.x; t < kArgWords; t += THREADS) dst[t] = src[t];
-        __syncthreads();
-        pushSupercell<SHAPE, K, THREADS, SC>(s_args, w - b.base[lo], smem_raw, s_nleave);
+        pushSupercell<SHAPE, K, THREADS, SC>(b.members[lo], w - b.base[lo], smem_raw, s_nleave);
     }
 }
 

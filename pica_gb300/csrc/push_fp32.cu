@@ -24,8 +24,7 @@ template <int SHAPE, int SC, int K, int THREADS, int MINB>
 int launchEsirkepovV(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     const int TT = a.T[0] * a.T[1] * a.T[2];
     const int ETT = (a.S[0] + 3) * (a.S[1] + 3) * (a.S[2] + 3);
-    constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;
-    const size_t smem = (size_t)esirkepovSmemWords(TT, ETT, THREADS / 32, 3 * (NWn - 1) * NWn * NWn) * 4;
+    const size_t smem = (size_t)esirkepovSmemWords(TT, ETT, THREADS / 32, kStayValues) * 4;
     auto k = k_push_cell_esirkepov<SHAPE, K, THREADS, MINB, SC>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -57,13 +56,12 @@ int launchEsirkepov(const PushArgs<CellPtrs>& a, int variant, cudaStream_t s) {
     return launchEsirkepovS<SHAPE, 0>(a, variant, s);
 }
 
-template <int SHAPE, int SC, int K, int THREADS, int MINB>
-int launchBatchV(const BatchPushArgs& b, const int* S, cudaStream_t s) {
+template <int SHAPE, int SC, int K, int THREADS, int MINB, int NSP>
+int launchBatchV(const BatchPushArgs<NSP>& b, const int* S, cudaStream_t s) {
     const int TT = (S[0] + 2 * kG + 1) * (S[1] + 2 * kG + 1) * (S[2] + 2 * kG + 1);
     const int ETT = (S[0] + 3) * (S[1] + 3) * (S[2] + 3);
-    constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;
-    const size_t smem = (size_t)esirkepovSmemWords(TT, ETT, THREADS / 32, 3 * (NWn - 1) * NWn * NWn) * 4;
-    auto k = k_push_batch<SHAPE, K, THREADS, MINB, SC>;
+    const size_t smem = (size_t)esirkepovSmemWords(TT, ETT, THREADS / 32, kStayValues) * 4;
+    auto k = k_push_batch<SHAPE, K, THREADS, MINB, SC, NSP>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return (int)e;
@@ -76,8 +74,8 @@ int launchBatchV(const BatchPushArgs& b, const int* S, cudaStream_t s) {
     return (int)cudaGetLastError();
 }
 
-template <int SHAPE, int SC>
-int launchBatchS(const BatchPushArgs& b, const int* S, int variant, cudaStream_t s) {
+template <int SHAPE, int SC, int NSP>
+int launchBatchS(const BatchPushArgs<NSP>& b, const int* S, int variant, cudaStream_t s) {
     switch (variant) {
         case 1: return launchBatchV<SHAPE, SC, 8, 128, 2>(b, S, s);
         case 2: return launchBatchV<SHAPE, SC, 8, 64, 6>(b, S, s);
@@ -86,12 +84,15 @@ int launchBatchS(const BatchPushArgs& b, const int* S, int variant, cudaStream_t
     }
 }
 
-int launchPushBatch(const BatchPushArgs& b, int shape, const int* S, int variant, cudaStream_t s) {
+template <int NSP>
+int launchPushBatch(const BatchPushArgs<NSP>& b, int shape, const int* S, int variant, cudaStream_t s) {
     const bool sc4 = S[0] == 4 && S[1] == 4 && S[2] == 4;
     if (shape == PICA_SHAPE_TSC) return sc4 ? launchBatchS<PICA_SHAPE_TSC, 4>(b, S, variant, s) : launchBatchS<PICA_SHAPE_TSC, 0>(b, S, variant, s);
     if (shape == PICA_SHAPE_CIC) return sc4 ? launchBatchS<PICA_SHAPE_CIC, 4>(b, S, variant, s) : launchBatchS<PICA_SHAPE_CIC, 0>(b, S, variant, s);
     return (int)cudaErrorInvalidValue;
 }
+template int launchPushBatch<1>(const BatchPushArgs<1>&, int, const int*, int, cudaStream_t);
+template int launchPushBatch<2>(const BatchPushArgs<2>&, int, const int*, int, cudaStream_t);
 
 int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int dep, int variant, cudaStream_t s) {
     if (shape == PICA_SHAPE_TSC && dep == PICA_DEPOSIT_ESIRKEPOV) return launchEsirkepov<PICA_SHAPE_TSC>(a, variant, s);

@@ -691,73 +691,100 @@ __device__ __forceinline__ int neighbour(const int* nsc, const int* dc, int code
 template <class P>
 __global__ void __launch_bounds__(128) k_sortLeavers(const __grid_constant__ MigrateArgs<P> a) {
     extern __shared__ unsigned int bits[];
+    __shared__ int dcnt[kDirBuckets];
     const int s = blockIdx.x;
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     for (int spi = 0; spi < a.nspecies; spi++) {
         const MigrateSpecies<P>& sa = a.sp[spi];
         const int n = sa.nleave[s];
-        if (n <= 1) continue;   // uniform across the block
         const int64_t start = sa.start[s];
-        const int nw = (sa.count[s] + 31) / 32;
-        for (int w = threadIdx.x; w < nw; w += blockDim.x) bits[w] = 0u;
-        __syncthreads();
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            const int slot = sa.llist[start + k];
-            atomicOr(&bits[slot >> 5], 1u << (slot & 31));
-        }
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            int base = 0;
-            for (int w0 = 0; w0 < nw; w0 += 32) {
-                const int w = w0 + lane;
-                unsigned b = w < nw ? bits[w] : 0u;
-                const int c = __popc(b);
-                int incl = c;
+        if (n > 1) {   // uniform across the block
+            const int nw = (sa.count[s] + 31) / 32;
+            for (int w = threadIdx.x; w < nw; w += blockDim.x) bits[w] = 0u;
+            __syncthreads();
+            for (int k = threadIdx.x; k < n; k += blockDim.x) {
+                const int slot = sa.llist[start + k];
+                atomicOr(&bits[slot >> 5], 1u << (slot & 31));
+            }
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                int base = 0;
+                for (int w0 = 0; w0 < nw; w0 += 32) {
+                    const int w = w0 + lane;
+                    unsigned b = w < nw ? bits[w] : 0u;
+                    const int c = __popc(b);
+                    int incl = c;
 #pragma unroll
-                for (int d = 1; d < 32; d <<= 1) {
-                    const int t = __shfl_up_sync(0xffffffffu, incl, d);
-                    if (lane >= d) incl += t;
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const int t = __shfl_up_sync(0xffffffffu, incl, d);
+                        if (lane >= d) incl += t;
+                    }
+                    int pos = base + incl - c;
+                    while (b) {
+                        const int bit = __ffs(b) - 1;
+                        sa.llist[start + pos++] = w * 32 + bit;
+                        b &= b - 1u;
+                    }
+                    base += __shfl_sync(0xffffffffu, incl, 31);
                 }
-                int pos = base + incl - c;
-                while (b) {
-                    const int bit = __ffs(b) - 1;
-                    sa.llist[start + pos++] = w * 32 + bit;
-                    b &= b - 1u;
-                }
-                base += __shfl_sync(0xffffffffu, incl, 31);
+            }
+            __syncthreads();
+        }
+        // Buckets by direction code, each in slot order (one warp: counts, scan, scatter).
+        if (threadIdx.x < 32) {
+            if (lane < kDirBuckets) dcnt[lane] = 0;
+            __syncwarp();
+            for (int k0 = 0; k0 < n; k0 += 32) {
+                const int k = k0 + lane;
+                const int code = k < n ? sa.dir[start + sa.llist[start + k]] : -1;
+                const unsigned grp = __match_any_sync(0xffffffffu, code);
+                if (code >= 0 && lane == __ffs(grp) - 1) dcnt[code] += __popc(grp);
+                __syncwarp();
+            }
+            const int c = lane < 27 ? dcnt[lane] : 0;
+            int incl = c;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += t;
+            }
+            if (lane < kDirBuckets) sa.dirOff[(int64_t)s * kDirBuckets + lane] = incl - c;
+            __syncwarp();
+            if (lane < 27) dcnt[lane] = incl - c;
+            __syncwarp();
+            for (int k0 = 0; k0 < n; k0 += 32) {
+                const int k = k0 + lane;
+                const int slot = k < n ? sa.llist[start + k] : -1;
+                const int code = k < n ? sa.dir[start + slot] : -1;
+                const unsigned grp = __match_any_sync(0xffffffffu, code);
+                if (code >= 0) sa.lbydir[start + dcnt[code] + __popc(grp & lt)] = slot;
+                __syncwarp();
+                if (code >= 0 && lane == __ffs(grp) - 1) dcnt[code] += __popc(grp);
+                __syncwarp();
             }
         }
         __syncthreads();
     }
 }
 
-// Arrivals of destination d, walked in canonical order; fn(k, srcSupercell, srcSlot, r)
-// is called by the matching lane with k the arrival's rank at d and r its index in the
-// source's leaver list.  Returns the number of arrivals.
+// Arrivals at supercell d in canonical order: by direction code (the move from the
+// source, 0..26 without 13), then by source slot.  fn(k, src, slot, r): k-th arrival,
+// from slot `slot` of supercell src, entry r of src's lbydir list.
 template <class P, class F>
 __device__ __forceinline__ int forArrivals(const MigrateArgs<P>& a, const MigrateSpecies<P>& sa, int d, F&& fn) {
     const int lane = threadIdx.x & 31;
     const int dc[3] = {d / (a.nsc[1] * a.nsc[2]), (d / a.nsc[2]) % a.nsc[1], d % a.nsc[2]};
-    const unsigned lt = (1u << lane) - 1u;
     int pos = 0;
     for (int code = 0; code < 27; code++) {
         if (code == 13) continue;
         const int src = neighbour(a.nsc, dc, code);
-        const int L = sa.nleave[src];
-        if (L == 0) continue;
+        const int32_t* off = sa.dirOff + (int64_t)src * kDirBuckets;
+        const int b0 = off[code], b1 = off[code + 1];
+        if (b1 <= b0) continue;
         const int64_t sst = sa.start[src];
-        for (int r0 = 0; r0 < L; r0 += 32) {
-            const int r = r0 + lane;
-            int slot = -1;
-            bool match = false;
-            if (r < L) {
-                slot = sa.llist[sst + r];
-                match = sa.dir[sst + slot] == code;
-            }
-            const unsigned mk = __ballot_sync(0xffffffffu, match);
-            if (match) fn(pos + __popc(mk & lt), src, slot, r);
-            pos += __popc(mk);
-        }
+        for (int r = b0 + lane; r < b1; r += 32) fn(pos + (r - b0), src, sa.lbydir[sst + r], r);
+        pos += b1 - b0;
     }
     return pos;
 }
@@ -791,7 +818,7 @@ __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ Migrate
             if (lane == 0) { sa.count[d] = cnt + max(0, arrivals - nh); sa.alive[d] = sa.alive[d] - nh + arrivals; }
         } else if constexpr (STAGE == kGatherOutbox) {
             const int64_t off = sa.outOff[d];
-            for (int k = lane; k < nh; k += 32) copyParticle(sa.b, start + sa.llist[start + k], sa.outbox, off + k);
+            for (int k = lane; k < nh; k += 32) copyParticle(sa.b, start + sa.lbydir[start + k], sa.outbox, off + k);
         } else if constexpr (STAGE == kRebuild) {
             const int64_t ns = sa.newStart[d];
             for (int i = lane; i < cnt; i += 32) copyParticle(sa.a, start + i, sa.dst, ns + i);
@@ -805,18 +832,56 @@ __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ Migrate
     }
 }
 
-// Local cell (lx*Sy + ly)*Sz + lz of a live particle of supercell with origin cell m.
-__device__ __forceinline__ int localCell(const PlainPtrs& p, int64_t i, const int* m, const int* S, const double* invh) {
-    const double x[3] = {p.x[i], p.y[i], p.z[i]};
-    int l[3];
+// One particle's record, for copies that load several particles before storing any.
+template <class P>
+struct Rec;
+template <>
+struct Rec<CellPtrs> {
+    uint32_t c;
+    float f[7];
+    __device__ __forceinline__ void load(const CellPtrs& p, int64_t i) {
+        c = p.cell[i]; f[0] = p.ox[i]; f[1] = p.oy[i]; f[2] = p.oz[i];
+        f[3] = p.ux[i]; f[4] = p.uy[i]; f[5] = p.uz[i]; f[6] = p.w[i];
+    }
+    __device__ __forceinline__ void store(const CellPtrs& p, int64_t j) const {
+        p.cell[j] = c; p.ox[j] = f[0]; p.oy[j] = f[1]; p.oz[j] = f[2];
+        p.ux[j] = f[3]; p.uy[j] = f[4]; p.uz[j] = f[5]; p.w[j] = f[6];
+    }
+    __device__ __forceinline__ int key(const int* m, const int* S, const double*) const {
+        if (c == kDeadCell) return -1;
+        int x[3];
+        unpackCell(c, x[0], x[1], x[2]);
+        return ((x[0] - m[0]) * S[1] + (x[1] - m[1])) * S[2] + (x[2] - m[2]);
+    }
+};
+template <>
+struct Rec<PlainPtrs> {
+    double v[7];
+    __device__ __forceinline__ void load(const PlainPtrs& p, int64_t i) {
+        v[0] = p.x[i]; v[1] = p.y[i]; v[2] = p.z[i]; v[3] = p.ux[i]; v[4] = p.uy[i]; v[5] = p.uz[i]; v[6] = p.w[i];
+    }
+    __device__ __forceinline__ void store(const PlainPtrs& p, int64_t j) const {
+        p.x[j] = v[0]; p.y[j] = v[1]; p.z[j] = v[2]; p.ux[j] = v[3]; p.uy[j] = v[4]; p.uz[j] = v[5]; p.w[j] = v[6];
+    }
+    __device__ __forceinline__ int key(const int* m, const int* S, const double* invh) const {
+        if (!aliveX(v[0])) return -1;
+        int l[3];
 #pragma unroll
-    for (int d = 0; d < 3; d++) l[d] = min(max((int)floor(x[d] * invh[d]) - m[d], 0), S[d] - 1);
-    return (l[0] * S[1] + l[1]) * S[2] + l[2];
+        for (int d = 0; d < 3; d++) l[d] = min(max((int)floor(v[d] * invh[d]) - m[d], 0), S[d] - 1);
+        return (l[0] * S[1] + l[1]) * S[2] + l[2];
+    }
+};
+
+// Local cell of slot i, or -1 for a dead slot (loads only what the key needs).
+__device__ __forceinline__ int slotKey(const CellPtrs& p, int64_t i, const int* m, const int* S, const double* invh) {
+    Rec<CellPtrs> r;
+    r.c = p.cell[i];
+    return r.key(m, S, invh);
 }
-__device__ __forceinline__ int localCell(const CellPtrs& p, int64_t i, const int* m, const int* S, const double*) {
-    int c[3];
-    unpackCell(p.cell[i], c[0], c[1], c[2]);
-    return ((c[0] - m[0]) * S[1] + (c[1] - m[1])) * S[2] + (c[2] - m[2]);
+__device__ __forceinline__ int slotKey(const PlainPtrs& p, int64_t i, const int* m, const int* S, const double* invh) {
+    Rec<PlainPtrs> r;
+    r.v[0] = p.x[i]; r.v[1] = p.y[i]; r.v[2] = p.z[i];
+    return r.key(m, S, invh);
 }
 
 // Compact each supercell (drop dead slots) and sort it by cell, stably, into the new
@@ -824,12 +889,16 @@ __device__ __forceinline__ int localCell(const CellPtrs& p, int64_t i, const int
 // the w-th contiguous eighth of the slots; a first pass counts cells per warp, a
 // scan over (cell, warp) gives every warp its start in each cell, and a second
 // pass scatters each warp's particles in slot order (rank within a 32-slot step
-// from __match_any_sync).  The result is ordered by (cell, old slot).
+// from __match_any_sync).  Both passes load kResortUnroll steps of 32 slots before
+// using them, to keep several HBM requests in flight per warp.  The result is
+// ordered by (cell, old slot).
 constexpr int kResortWarps = 8;
+constexpr int kResortUnroll = 4;
 template <class P>
 __global__ void __launch_bounds__(kResortWarps * 32) k_resort(const __grid_constant__ MigrateArgs<P> a) {
     constexpr unsigned FULL = 0xffffffffu;
     constexpr int kT = kResortWarps * 32;
+    constexpr int U = kResortUnroll;
     constexpr int kBins = 512;  // largest supercell: 8 x 8 x 8 cells
     __shared__ int cnt[kResortWarps][kBins];
     __shared__ int wsum[kResortWarps];
@@ -845,13 +914,21 @@ __global__ void __launch_bounds__(kResortWarps * 32) k_resort(const __grid_const
         const int n = sa.count[d];
         const int R = ((n + kT - 1) / kT) * 32;
         const int lo = min(warp * R, n), hi = min(lo + R, n);
-        for (int k = threadIdx.x; k < kResortWarps * kBins; k += kT) (&cnt[0][0])[k] = 0;
+        for (int k = threadIdx.x; k < kResortWarps * nb; k += kT) cnt[k / nb][k % nb] = 0;
         __syncthreads();
-        for (int i0 = lo; i0 < hi; i0 += 32) {
-            const int i = i0 + lane;
-            const int key = (i < hi && aliveAt(sa.a, start + i)) ? localCell(sa.a, start + i, m, a.S, a.invh) : -1;
-            const unsigned grp = __match_any_sync(FULL, key);
-            if (key >= 0 && lane == __ffs(grp) - 1) cnt[warp][key] += __popc(grp);
+        for (int i0 = lo; i0 < hi; i0 += 32 * U) {
+            int key[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int i = i0 + u * 32 + lane;
+                key[u] = i < hi ? slotKey(sa.a, start + i, m, a.S, a.invh) : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const unsigned grp = __match_any_sync(FULL, key[u]);
+                if (key[u] >= 0 && lane == __ffs(grp) - 1) cnt[warp][key[u]] += __popc(grp);
+                __syncwarp();
+            }
         }
         __syncthreads();
         // Exclusive scan over (cell, warp), cell-major: 16 consecutive entries per thread.
@@ -882,14 +959,24 @@ __global__ void __launch_bounds__(kResortWarps * 32) k_resort(const __grid_const
             }
         }
         __syncthreads();
-        for (int i0 = lo; i0 < hi; i0 += 32) {
-            const int i = i0 + lane;
-            const int key = (i < hi && aliveAt(sa.a, start + i)) ? localCell(sa.a, start + i, m, a.S, a.invh) : -1;
-            const unsigned grp = __match_any_sync(FULL, key);
-            if (key >= 0) copyParticle(sa.a, start + i, sa.dst, ns + cnt[warp][key] + __popc(grp & lt));
-            __syncwarp();
-            if (key >= 0 && lane == __ffs(grp) - 1) cnt[warp][key] += __popc(grp);
-            __syncwarp();
+        for (int i0 = lo; i0 < hi; i0 += 32 * U) {
+            Rec<P> r[U];
+            int key[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int i = i0 + u * 32 + lane;
+                if (i < hi) r[u].load(sa.a, start + i);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) key[u] = i0 + u * 32 + lane < hi ? r[u].key(m, a.S, a.invh) : -1;
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const unsigned grp = __match_any_sync(FULL, key[u]);
+                if (key[u] >= 0) r[u].store(sa.dst, ns + cnt[warp][key[u]] + __popc(grp & lt));
+                __syncwarp();
+                if (key[u] >= 0 && lane == __ffs(grp) - 1) cnt[warp][key[u]] += __popc(grp);
+                __syncwarp();
+            }
         }
         __syncthreads();
         if (threadIdx.x == 0) sa.count[d] = sa.alive[d];
