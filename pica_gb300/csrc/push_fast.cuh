@@ -123,7 +123,7 @@ struct FixTileS {
     }
 };
 
-constexpr int kRing = 64;  // queued window changes per warp (ring)
+constexpr int kRing = 32;  // queued cell changes per warp (one drain = one per lane)
 
 // Deposit n <= 32 queued window changes of one warp starting at ring entry head,
 // one per lane.  Out of line: one copy of the general-window code serves every
@@ -145,18 +145,18 @@ __device__ __noinline__ void drainRing(unsigned ring, int head, int n, FixTileS 
 // Wrap a cell index that is at most one period out of range.
 __device__ __forceinline__ int wrapNear(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
-// Rows of a warp's reduction area: 32 lane rows and kPark rows for sums parked
-// when a lane changes window; odd, so that the column reads are conflict-free.
-constexpr int kRedRows = 41;
+// Rows of a warp's reduction area: 32 lane rows and 17 rows for sums parked when a
+// lane changes cell; odd, so that the column reads are conflict-free.
+constexpr int kRedRows = 49;
 
 // Add up, per window key, the rows of a warp's reduction area (value j of row r
 // at red[j * kRedRows + r]; keys[r] < 0: empty) and deposit the sums: lane t
-// sums values t and t + 32 over the member rows, lane rows first, then the np
-// park rows, in ascending order.
+// sums values t and t + 32 over the member rows, lane rows first (unless !lanes),
+// then the np park rows, in ascending order.
 template <int NWn, int NV>
-__device__ __forceinline__ void reduceRows(const float* red, const int* keys, int np, const FixTile& jt, int TT,
-                                           int T1, int T2, int lane) {
-    const int kl = keys[lane];
+__device__ __forceinline__ void reduceRows(const float* red, const int* keys, int np, bool lanes, const FixTile& jt,
+                                           int TT, int T1, int T2, int lane) {
+    const int kl = lanes ? keys[lane] : -1;
     const int kp = lane < np ? keys[32 + lane] : -1;
     unsigned pendL = __ballot_sync(0xffffffffu, kl >= 0);
     unsigned pendP = __ballot_sync(0xffffffffu, kp >= 0);
@@ -232,17 +232,25 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
     sc[0] = s / (a.nsc[1] * a.nsc[2]);
     const int m[3] = {sc[0] * Sx, sc[1] * Sy, sc[2] * Sz};
 
+    // Periodic grid index of tile node k along d (tile origin m - kG; k < 16 covers the
+    // largest tile), so that the staging and flush loops need no modulo.
+    __shared__ int s_wrap[3][16];
+    if (threadIdx.x < 48) {
+        const int d = threadIdx.x >> 4, k = threadIdx.x & 15;
+        s_wrap[d][k] = wrapi(m[d] - kG + k, a.n[d]);
+    }
+    __syncthreads();
     for (int t = threadIdx.x; t < 6 * ETT; t += THREADS) {
         const int c = t / ETT, r = t - c * ETT;
-        const int i = r / (E1 * E2), jj = (r / E2) % E1, k = r % E2;
-        const int gx = wrapi(m[0] - 1 + i, a.n[0]), gy = wrapi(m[1] - 1 + jj, a.n[1]), gz = wrapi(m[2] - 1 + k, a.n[2]);
-        eb[t] = static_cast<const float*>(a.eb[c])[((int64_t)gx * a.n[1] + gy) * a.n[2] + gz];
+        const int i = r / (E1 * E2), jj = (r / E2) % E1, k = r % E2;   // E/B tile origin m - 1
+        eb[t] = static_cast<const float*>(a.eb[c])[((int64_t)s_wrap[0][i + 1] * a.n[1] + s_wrap[1][jj + 1]) * a.n[2] +
+                                                   s_wrap[2][k + 1]];
     }
     for (int t = threadIdx.x; t < 3 * TT; t += THREADS) { jt.lo[t] = 0u; jt.hi[t] = 0; }
     const float invU = (float)a.invUnit;
     const float cdth[3] = {(float)a.cdth[0], (float)a.cdth[1], (float)a.cdth[2]};
     bool bad = false;
-    int qHead = 0, qN = 0;   // this warp's ring of queued window changes (warp-uniform)
+    int qN = 0;   // entries in this warp's queue of cell changes (warp-uniform)
     __syncthreads();
 
     for (int spi = 0; spi < a.nspecies; spi++) {
@@ -306,24 +314,34 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                 const bool park = sw && accKey >= 0;
                 const unsigned pm = __ballot_sync(FULL, park);
                 if (pm) {
-                    if (nPark + __popc(pm) > kPark) {
+                    const int np = __popc(pm);
+                    bool flushed = false;
+                    if (nPark + np > kPark) {
+                        if (np <= kPark) {
+                            // deposit the parked rows, then park
+                            reduceRows<NWn, NV>(red, keys, nPark, false, jt, TT, T1, T2, lane);
+                        } else {
+                            // more lanes switching than park rows: deposit every row now
 #pragma unroll
-                        for (int j = 0; j < NV; j++) red[j * kRedRows + lane] = acc[j];
-                        keys[lane] = accKey;
-                        __syncwarp();
-                        reduceRows<NWn, NV>(red, keys, nPark, jt, TT, T1, T2, lane);
-                        __syncwarp();
+                            for (int j = 0; j < NV; j++) red[j * kRedRows + lane] = acc[j];
+                            keys[lane] = accKey;
+                            __syncwarp();
+                            reduceRows<NWn, NV>(red, keys, nPark, true, jt, TT, T1, T2, lane);
 #pragma unroll
-                        for (int j = 0; j < NV; j++) acc[j] = 0.0f;
+                            for (int j = 0; j < NV; j++) acc[j] = 0.0f;
+                            flushed = true;
+                        }
+                        __syncwarp();
                         nPark = 0;
-                    } else {
+                    }
+                    if (!flushed) {
                         if (park) {
                             const int row = 32 + nPark + __popc(pm & lt);
 #pragma unroll
                             for (int j = 0; j < NV; j++) red[j * kRedRows + row] = acc[j];
                             keys[row] = accKey;
                         }
-                        nPark += __popc(pm);
+                        nPark += np;
                     }
                 }
                 if (sw) {
@@ -476,18 +494,22 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                 // Queue window changes in the ring; deposit 32 at a time (one per lane).
                 const unsigned qm = __ballot_sync(FULL, needQ);
                 if (qm) {
+                    if (qN + __popc(qm) > kRing) {   // no room: deposit what is queued
+                        drainRing<SHAPE>(ringS, 0, qN, jts, TT, T1, T2);
+                        __syncwarp();
+                        qN = 0;
+                    }
                     if (needQ) {
-                        float* e = ring + ((qHead + qN + __popc(qm & lt)) & (kRing - 1)) * kQWords;
+                        float* e = ring + (qN + __popc(qm & lt)) * kQWords;
 #pragma unroll
                         for (int k = 0; k < kQWords; k++) e[k] = qe[k];
                     }
                     qN += __popc(qm);
                     __syncwarp();
-                    if (qN >= 32) {
-                        drainRing<SHAPE>(ringS, qHead, 32, jts, TT, T1, T2);
+                    if (qN == kRing) {
+                        drainRing<SHAPE>(ringS, 0, kRing, jts, TT, T1, T2);
                         __syncwarp();
-                        qHead = (qHead + 32) & (kRing - 1);
-                        qN -= 32;
+                        qN = 0;
                     }
                 }
             }
@@ -496,14 +518,14 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
             for (int j = 0; j < NV; j++) red[j * kRedRows + lane] = acc[j];
             keys[lane] = accKey;
             __syncwarp();
-            reduceRows<NWn, NV>(red, keys, nPark, jt, TT, T1, T2, lane);
+            reduceRows<NWn, NV>(red, keys, nPark, true, jt, TT, T1, T2, lane);
             __syncwarp();
         }
         __syncthreads();
         if (threadIdx.x == 0) sa.nleave[s] = s_nleave;
         __syncthreads();
     }
-    if (qN > 0) drainRing<SHAPE>(ringS, qHead, qN, jts, TT, T1, T2);
+    if (qN > 0) drainRing<SHAPE>(ringS, 0, qN, jts, TT, T1, T2);
     if (bad) atomicExch(a.flags, PICA_ERR_MIGRATION);
     __syncthreads();
     for (int t = threadIdx.x; t < 3 * TT; t += THREADS) {
@@ -511,8 +533,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
         if (v != 0ull) {
             const int c = t / TT, r = t - c * TT;
             const int i = r / (T1 * T2), jj = (r / T2) % T1, k = r % T2;
-            const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
-            atomicAdd(a.jacc[c] + ((int64_t)gx * a.n[1] + gy) * a.n[2] + gz, v);
+            atomicAdd(a.jacc[c] + ((int64_t)s_wrap[0][i] * a.n[1] + s_wrap[1][jj]) * a.n[2] + s_wrap[2][k], v);
         }
     }
 }

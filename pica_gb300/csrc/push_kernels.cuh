@@ -768,25 +768,64 @@ __global__ void __launch_bounds__(128) k_sortLeavers(const __grid_constant__ Mig
     }
 }
 
-// Arrivals at supercell d in canonical order: by direction code (the move from the
-// source, 0..26 without 13), then by source slot.  fn(k, src, slot, r): k-th arrival,
-// from slot `slot` of supercell src, entry r of src's lbydir list.
-template <class P, class F>
-__device__ __forceinline__ int forArrivals(const MigrateArgs<P>& a, const MigrateSpecies<P>& sa, int d, F&& fn) {
+// The 26 arrival buckets of supercell d, one per lane (lanes 26..31 empty): the
+// source supercell, its lbydir start and entry b0 of the bucket, the bucket size,
+// and the exclusive prefix of the sizes in canonical order (direction code 0..26
+// without 13).  Returns the total.
+template <class P>
+__device__ __forceinline__ int arrivalBuckets(const MigrateArgs<P>& a, const MigrateSpecies<P>& sa, int d, int& src,
+                                              int64_t& sst, int& b0, int& pre) {
     const int lane = threadIdx.x & 31;
     const int dc[3] = {d / (a.nsc[1] * a.nsc[2]), (d / a.nsc[2]) % a.nsc[1], d % a.nsc[2]};
-    int pos = 0;
-    for (int code = 0; code < 27; code++) {
-        if (code == 13) continue;
-        const int src = neighbour(a.nsc, dc, code);
+    const int code = lane < 13 ? lane : lane + 1;
+    int cnt = 0;
+    src = 0; sst = 0; b0 = 0;
+    if (lane < 26) {
+        src = neighbour(a.nsc, dc, code);
         const int32_t* off = sa.dirOff + (int64_t)src * kDirBuckets;
-        const int b0 = off[code], b1 = off[code + 1];
-        if (b1 <= b0) continue;
-        const int64_t sst = sa.start[src];
-        for (int r = b0 + lane; r < b1; r += 32) fn(pos + (r - b0), src, sa.lbydir[sst + r], r);
-        pos += b1 - b0;
+        b0 = off[code];
+        cnt = off[code + 1] - b0;
+        sst = sa.start[src];
     }
-    return pos;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    pre = incl - cnt;
+    return __shfl_sync(0xffffffffu, incl, 31);
+}
+
+// Arrivals at supercell d in canonical order -- by direction code (the move from the
+// source), then by source slot -- 32 at a time across the buckets.  fn(k, src, slot, r):
+// the k-th arrival, from slot `slot` of supercell src, entry r of src's lbydir list.
+template <class P, class F>
+__device__ __forceinline__ int forArrivals(const MigrateArgs<P>& a, const MigrateSpecies<P>& sa, int d, F&& fn) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int src, b0, pre;
+    int64_t sst;
+    const int total = arrivalBuckets(a, sa, d, src, sst, b0, pre);
+    for (int k0 = 0; k0 < total; k0 += 32) {
+        const int k = k0 + lane;
+        int c = 0;   // last bucket with pre <= k (buckets 0..25)
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const int cand = c + step;
+            const int pc = __shfl_sync(FULL, pre, cand < 26 ? cand : 25);
+            if (cand < 26 && pc <= k) c = cand;
+        }
+        const int ks = __shfl_sync(FULL, src, c);
+        const int kb = __shfl_sync(FULL, b0, c);
+        const int kp = __shfl_sync(FULL, pre, c);
+        const int64_t kst = __shfl_sync(FULL, sst, c);
+        if (k < total) {
+            const int r = kb + (k - kp);
+            fn(k, ks, sa.lbydir[kst + r], r);
+        }
+    }
+    return total;
 }
 
 template <class P, int STAGE>
@@ -803,7 +842,9 @@ __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ Migrate
         const int cnt = sa.count[d];
         int arrivals;
         if constexpr (STAGE == kCountArrivals) {
-            arrivals = forArrivals(a, sa, d, [](int, int, int, int) {});
+            int src, b0, pre;
+            int64_t sst;
+            arrivals = arrivalBuckets(a, sa, d, src, sst, b0, pre);
             if (lane == 0) {
                 const int need = cnt + max(0, arrivals - nh);
                 sa.needed[d] = need;
