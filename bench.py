@@ -258,7 +258,8 @@ def main():
     # ---------------- FP32 form, device-resident ----------------
     wl = make_workload(args.edge, pg.FORM_FP32_CELL)
     spec = wl["specs"][0]
-    spec.seed = spec.seed + rank          # independent replica per rank (weak scaling)
+    from pica_gb300.replicas import job_throughput, replica_seed
+    spec.seed = replica_seed(spec.seed, rank)   # independent replica per rank (weak scaling)
     parts = pg.generate_plasma(spec)
     npart = len(parts["x"])
     ncells = int(np.prod(wl["sim"]["n"]))
@@ -305,11 +306,7 @@ def main():
     sim_variant = sim.variant()[0]
     elapsed = t_start.elapsed_time(t_end) / 1e3
     push_ms = [a.elapsed_time(b) for a, b in evs]
-    if dist is not None:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-    value = world * npart * K / elapsed
+    value, elapsed = job_throughput(npart, K, elapsed, dist, device="cuda")
     push_avg = float(np.mean(push_ms)) / 1e3
     peak, peak_kind = measured_hbm_peak()
     alg_bytes = BYTES_PER_PARTICLE_FP32 * npart + PUSH_GRID_BYTES_PER_CELL_FP32 * ncells

@@ -215,6 +215,19 @@ int       pica_batch_step(pica_batch* batch, int32_t nsteps);
 int       pica_batch_stats(pica_batch* batch, int64_t* out4);
 const char* pica_batch_last_error(pica_batch* batch);
 
+/* Checkpoint of the context between steps: configuration, fields, every
+ * species' slot layout and particle buffer, step counter and fixed-point scale.
+ * A context created with the same configuration and loaded from it continues like
+ * the original (the building block of a host loop's restart): bit for bit in the
+ * FP32 form; in the FP64 form to the rounding of its FP64 atomic current sums,
+ * whose order differs from run to run.
+ * Errors: PICA_ERR_INVALID for an unreadable file or a different configuration,
+ * PICA_ERR_STATE between push_deposit and migrate.  pica has no checkpoints. */
+int     pica_checkpoint_save(pica_ctx* ctx, const char* path);
+/* Steps completed since upload (restored by pica_checkpoint_load; drives the resort cadence). */
+int64_t pica_step_count(pica_ctx* ctx);
+int     pica_checkpoint_load(pica_ctx* ctx, const char* path);
+
 /* Host-side plasma set-up (no device work). */
 int64_t pica_plasma_count(const pica_plasma_spec* spec);
 int     pica_plasma_generate(const pica_plasma_spec* spec, int32_t threads, double* x, double* y, double* z,

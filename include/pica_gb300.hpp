@@ -22,7 +22,9 @@
 // the C ABI itself never throws.
 #pragma once
 
+#include <algorithm>
 #include <array>
+#include <functional>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -186,12 +188,46 @@ public:
         check(ctx_, pica_diagnostics(ctx_, bgDensity, &d));
         return d;
     }
+    int64_t stepCount() { return pica_step_count(ctx_); }
+    // Complete state between steps; a Simulation of the same Config loaded from it
+    // continues like this one (FP32 form: bit for bit).
+    void saveCheckpoint(const std::string& path) { check(ctx_, pica_checkpoint_save(ctx_, path.c_str())); }
+    void loadCheckpoint(const std::string& path) { check(ctx_, pica_checkpoint_load(ctx_, path.c_str())); }
 
 private:
     pica_ctx* ctx_ = nullptr;
     double dt_ = 0;
     YeeGrid grid_;
     EnsembleSupercells ens_;
+};
+
+// Host loop around a Simulation (the PICADOR driver's role; periodic boundaries):
+// run(n) steps in chunks, calls onDiagnostics every diagEvery steps and writes a
+// checkpoint every checkpointEvery steps to checkpointPath + "<step>".
+class Driver {
+public:
+    explicit Driver(Simulation& sim) : sim_(sim) {}
+    int diagEvery = 0;
+    int checkpointEvery = 0;
+    std::string checkpointPath;
+    double bgDensity = 0.0;
+    std::function<void(int64_t, const pica_diag&)> onDiagnostics;
+
+    void run(int64_t nsteps) {
+        const int64_t end = sim_.stepCount() + nsteps;
+        while (sim_.stepCount() < end) {
+            const int64_t now = sim_.stepCount();
+            int64_t target = end;
+            if (diagEvery > 0) target = std::min(target, (now / diagEvery + 1) * diagEvery);
+            if (checkpointEvery > 0) target = std::min(target, (now / checkpointEvery + 1) * checkpointEvery);
+            sim_.step((int)(target - now));
+            if (diagEvery > 0 && target % diagEvery == 0 && onDiagnostics) onDiagnostics(target, sim_.diagnostics(bgDensity));
+            if (checkpointEvery > 0 && target % checkpointEvery == 0) sim_.saveCheckpoint(checkpointPath + std::to_string(target));
+        }
+    }
+
+private:
+    Simulation& sim_;
 };
 
 void YeeGrid::upload() {

@@ -190,6 +190,19 @@ class Simulation:
         self._check(self.lib.pica_field_energy(self.ctx, C.byref(v)))
         return v.value
 
+    # -- checkpoints ---------------------------------------------------------------
+    def step_count(self):
+        return int(self.lib.pica_step_count(self.ctx))
+
+    def save_checkpoint(self, path):
+        """Complete state between steps; a Simulation of the same configuration loaded
+        from it continues like this one (FP32 form: bit for bit; FP64 form: to the
+        rounding of the FP64 atomic current sums)."""
+        self._check(self.lib.pica_checkpoint_save(self.ctx, str(path).encode()))
+
+    def load_checkpoint(self, path):
+        self._check(self.lib.pica_checkpoint_load(self.ctx, str(path).encode()))
+
     # -- raw device state (host loops that keep the state in host memory) ------
     def state_slots(self, species=0):
         return int(self.lib.pica_state_slots(self.ctx, int(species)))
@@ -197,6 +210,58 @@ class Simulation:
     def state_copy(self, species, comp, host_ptr, to_device):
         self._check(self.lib.pica_state_copy(self.ctx, int(species), int(comp), C.c_void_p(int(host_ptr)),
                                              1 if to_device else 0))
+
+
+class Driver:
+    """A host loop over a Simulation, in the role of the PICADOR driver around pica's
+    kernels: steps in chunks, takes the FP64 diagnostics every ``diag_every`` steps
+    and writes a checkpoint every ``checkpoint_every`` steps (``checkpoint_path`` may
+    hold ``{step}``).  Boundaries are periodic (the only kind the step supports).
+    ``run`` returns the diagnostics records [(step, dict), ...]; ``on_diag(step, d)``
+    is called for each as well."""
+
+    def __init__(self, sim, diag_every=0, checkpoint_every=0, checkpoint_path=None, bg_density=0.0, on_diag=None):
+        if checkpoint_every and not checkpoint_path:
+            raise ValueError("checkpoint_every needs checkpoint_path")
+        self.sim = sim
+        self.diag_every = int(diag_every)
+        self.checkpoint_every = int(checkpoint_every)
+        self.checkpoint_path = checkpoint_path
+        self.bg = float(bg_density)
+        self.on_diag = on_diag
+        self.checkpoints = []
+
+    @property
+    def step(self):
+        return self.sim.step_count()
+
+    def _next_event(self, step):
+        nxt = []
+        for every in (self.diag_every, self.checkpoint_every):
+            if every > 0:
+                nxt.append((step // every + 1) * every)
+        return min(nxt) if nxt else None
+
+    def run(self, nsteps):
+        records = []
+        end = self.step + int(nsteps)
+        if self.diag_every > 0 and self.step % self.diag_every == 0:
+            records.append((self.step, self.sim.diagnostics(self.bg)))
+        while self.step < end:
+            nxt = self._next_event(self.step)
+            target = end if nxt is None else min(nxt, end)
+            self.sim.step(target - self.step)
+            s = self.step
+            if self.diag_every > 0 and s % self.diag_every == 0:
+                d = self.sim.diagnostics(self.bg)
+                records.append((s, d))
+                if self.on_diag:
+                    self.on_diag(s, d)
+            if self.checkpoint_every > 0 and s % self.checkpoint_every == 0:
+                path = str(self.checkpoint_path).format(step=s)
+                self.sim.save_checkpoint(path)
+                self.checkpoints.append(path)
+        return records
 
 
 def make_config(n, h, dt, supercell=(2, 2, 2), form=FORM_FP64_PLAIN, shape=SHAPE_CIC, deposit=DEPOSIT_DIRECT,

@@ -62,6 +62,9 @@ SIGNATURES = {
     "pica_charge_density": (C.c_int, [_vp, _dp]),
     "pica_field_energy": (C.c_int, [_vp, _dp]),
     "pica_field_energy_noalloc": (C.c_int, [C.POINTER(_vp), _i32, _ip, _dp, _vp, _dp]),
+    "pica_checkpoint_save": (C.c_int, [_vp, C.c_char_p]),
+    "pica_step_count": (_i64, [_vp]),
+    "pica_checkpoint_load": (C.c_int, [_vp, C.c_char_p]),
     "pica_batch_create": (C.c_int, [C.POINTER(PicaConfig), _i32, C.POINTER(_vp)]),
     "pica_batch_destroy": (C.c_int, [_vp]),
     "pica_batch_member": (_vp, [_vp, _i32]),

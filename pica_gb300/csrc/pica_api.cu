@@ -1044,8 +1044,16 @@ struct pica_batch {
     int nsp = 1;                             // species slots of the push arguments (1 or 2)
     std::vector<BatchPushArgs<1>> args1;     // one persistent push launch per batchMembers<NSP>() members
     std::vector<BatchPushArgs<2>> args2;
-    cudaGraphExec_t exec = nullptr;
-    std::vector<unsigned char> sig;          // launch arguments the graph was captured with
+    // Instantiated graphs by the launch arguments they were captured with (a resort
+    // swaps the buffers, so the arguments alternate between a few states).
+    struct Graph {
+        std::vector<unsigned char> sig;
+        cudaGraphExec_t exec;
+        int64_t used;
+    };
+    std::vector<Graph> graphs;
+    cudaGraphExec_t exec = nullptr;          // the graph for the current arguments
+    std::vector<unsigned char> sig;          // the current launch arguments
     int64_t captures = 0, graphLaunches = 0, steps = 0;
     int64_t kernelLaunches = 0;              // launches of the device part of the steps
     std::string err;
@@ -1219,27 +1227,39 @@ int batchStepOnce(pica_batch* b) {
     if (sig != b->sig) {
         if (b->nsp == 1) batchLaunchArgs(b, b->args1);
         else batchLaunchArgs(b, b->args2);
-        if (b->exec) {
-            cudaGraphExecDestroy(b->exec);
-            b->exec = nullptr;
-        }
+        b->exec = nullptr;
         if (b->useGraph) {
-            cudaGraph_t g = nullptr;
-            BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
-            const int rc = batchEnqueue(b);
-            const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
-            if (rc) {
-                if (g) cudaGraphDestroy(g);
-                return rc;
+            for (auto& g : b->graphs)
+                if (g.sig == sig) b->exec = g.exec;
+            if (!b->exec) {
+                cudaGraph_t g = nullptr;
+                BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
+                const int rc = batchEnqueue(b);
+                const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+                if (rc) {
+                    if (g) cudaGraphDestroy(g);
+                    return rc;
+                }
+                BK(e);
+                cudaGraphExec_t x = nullptr;
+                const cudaError_t ei = cudaGraphInstantiate(&x, g, 0);
+                cudaGraphDestroy(g);
+                BK(ei);
+                b->captures++;
+                if (b->graphs.size() >= 4) {   // drop the least recently used
+                    auto lru = std::min_element(b->graphs.begin(), b->graphs.end(),
+                                                [](const pica_batch::Graph& u, const pica_batch::Graph& v) { return u.used < v.used; });
+                    cudaGraphExecDestroy(lru->exec);
+                    b->graphs.erase(lru);
+                }
+                b->graphs.push_back({sig, x, b->steps});
+                b->exec = x;
             }
-            BK(e);
-            const cudaError_t ei = cudaGraphInstantiate(&b->exec, g, 0);
-            cudaGraphDestroy(g);
-            BK(ei);
-            b->captures++;
         }
         b->sig.swap(sig);
     }
+    for (auto& g : b->graphs)
+        if (g.exec == b->exec) g.used = b->steps;
     if (b->useGraph) {
         BK(cudaGraphLaunch(b->exec, b->stream));
         b->graphLaunches++;
@@ -1300,7 +1320,7 @@ int pica_batch_create(const pica_config* cfgs, int32_t count, pica_batch** out) 
 int pica_batch_destroy(pica_batch* b) {
     if (!b) return PICA_ERR_INVALID;
     if (b->stream) cudaStreamSynchronize(b->stream);
-    if (b->exec) cudaGraphExecDestroy(b->exec);
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
     for (pica_ctx* ctx : b->m) pica_ctx_destroy(ctx);
     if (b->d_counter) cudaFree(b->d_counter);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -1318,7 +1338,7 @@ pica_ctx* pica_batch_member(pica_batch* b, int32_t k) {
 int pica_batch_set_options(pica_batch* b, int32_t use_graph, int32_t variant) {
     if (!b || variant < 0 || variant >= kPushVariants) return PICA_ERR_INVALID;
     b->useGraph = use_graph != 0;
-    b->variant = variant;
+    b->variant = variant;   // part of the signature: graphs of other variants stay cached
     b->sig.clear();
     return PICA_OK;
 }
@@ -1344,5 +1364,144 @@ int pica_batch_stats(pica_batch* b, int64_t* out4) {
 }
 
 const char* pica_batch_last_error(pica_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Checkpoints: the complete state of a context between steps, so that a context
+// loaded from one continues bit for bit like the original.  Layout (native byte
+// order): magic, version, the pica_config, the step counter and fixed-point
+// parameters, the nine field arrays as stored, then per species the slot layout
+// (start, capacity, used and live counts per supercell) and the current particle
+// buffer (every component, all slots of the layout).
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint64_t kCkptMagic = 0x31504B4341434950ull;   // "PICACKP1"
+constexpr uint32_t kCkptVersion = 1;
+
+struct CkptHeader {
+    uint64_t magic;
+    uint32_t version;
+    uint32_t fp64;
+    pica_config cfg;
+    int64_t steps;
+    double kmax;
+    int32_t jfrac, tileSplit;
+};
+
+struct FileCloser {
+    FILE* f;
+    ~FileCloser() { if (f) std::fclose(f); }
+};
+
+bool writeAll(FILE* f, const void* p, size_t n) { return n == 0 || std::fwrite(p, 1, n, f) == n; }
+bool readAll(FILE* f, void* p, size_t n) { return n == 0 || std::fread(p, 1, n, f) == n; }
+
+}  // namespace
+
+extern "C" {
+
+int64_t pica_step_count(pica_ctx* ctx) { return ctx ? ctx->steps : (int64_t)PICA_ERR_INVALID; }
+
+int pica_checkpoint_save(pica_ctx* ctx, const char* path) {
+    if (!ctx || !path) return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "checkpoint while a migration is pending");
+    CK(cudaStreamSynchronize(ctx->stream));
+    FileCloser fc{std::fopen(path, "wb")};
+    if (!fc.f) return fail(ctx, PICA_ERR_INVALID, std::string("cannot open ") + path);
+    CkptHeader h;
+    std::memset(&h, 0, sizeof h);
+    h.magic = kCkptMagic;
+    h.version = kCkptVersion;
+    h.fp64 = ctx->fp64 ? 1 : 0;
+    h.cfg = ctx->cfg;
+    h.steps = ctx->steps;
+    h.kmax = ctx->kmax;
+    h.jfrac = ctx->jfrac;
+    h.tileSplit = ctx->tileSplit;
+    if (!writeAll(fc.f, &h, sizeof h)) return fail(ctx, PICA_ERR_INVALID, "checkpoint write failed");
+    const pica_config& c = ctx->cfg;
+    const int64_t nodes = (int64_t)c.n[0] * c.n[1] * c.n[2];
+    const size_t rb = ctx->fp64 ? 8 : 4;
+    std::vector<unsigned char> buf(nodes * rb);
+    for (int k = 0; k < 9; k++) {
+        CK(cudaMemcpy(buf.data(), ctx->f[k], nodes * rb, cudaMemcpyDeviceToHost));
+        if (!writeAll(fc.f, buf.data(), buf.size())) return fail(ctx, PICA_ERR_INVALID, "checkpoint write failed");
+    }
+    const size_t n = ctx->nscTot;
+    for (int q = 0; q < c.nspecies; q++) {
+        SpeciesState& S = ctx->sp[q];
+        std::vector<int32_t> count(n), alive(n);
+        CK(cudaMemcpy(count.data(), S.d_count, n * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(alive.data(), S.d_alive, n * 4, cudaMemcpyDeviceToHost));
+        const int64_t slots = S.layoutSlots;
+        if (!writeAll(fc.f, &slots, 8) || !writeAll(fc.f, S.h_start.data(), n * 8) || !writeAll(fc.f, S.h_cap.data(), n * 4) ||
+            !writeAll(fc.f, count.data(), n * 4) || !writeAll(fc.f, alive.data(), n * 4))
+            return fail(ctx, PICA_ERR_INVALID, "checkpoint write failed");
+        for (int k = 0; k < ctx->ncomp; k++) {
+            std::vector<unsigned char> comp(slots * ctx->compBytes[k]);
+            CK(cudaMemcpy(comp.data(), S.buf[ctx->cur][k], comp.size(), cudaMemcpyDeviceToHost));
+            if (!writeAll(fc.f, comp.data(), comp.size())) return fail(ctx, PICA_ERR_INVALID, "checkpoint write failed");
+        }
+    }
+    return std::fflush(fc.f) == 0 ? PICA_OK : fail(ctx, PICA_ERR_INVALID, "checkpoint write failed");
+}
+
+int pica_checkpoint_load(pica_ctx* ctx, const char* path) {
+    if (!ctx || !path) return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "checkpoint load while a migration is pending");
+    CK(cudaStreamSynchronize(ctx->stream));
+    FileCloser fc{std::fopen(path, "rb")};
+    if (!fc.f) return fail(ctx, PICA_ERR_INVALID, std::string("cannot open ") + path);
+    CkptHeader h;
+    if (!readAll(fc.f, &h, sizeof h) || h.magic != kCkptMagic || h.version != kCkptVersion)
+        return fail(ctx, PICA_ERR_INVALID, "not a pica_gb300 checkpoint");
+    pica_config a = h.cfg, b = ctx->cfg;
+    a.threads = b.threads = 0;   // host threads do not change results
+    if (std::memcmp(&a, &b, sizeof(pica_config)) != 0 || h.fp64 != (ctx->fp64 ? 1u : 0u))
+        return fail(ctx, PICA_ERR_INVALID, "checkpoint of a different configuration");
+    const pica_config& c = ctx->cfg;
+    const int64_t nodes = (int64_t)c.n[0] * c.n[1] * c.n[2];
+    const size_t rb = ctx->fp64 ? 8 : 4;
+    std::vector<unsigned char> buf(nodes * rb);
+    for (int k = 0; k < 9; k++) {
+        if (!readAll(fc.f, buf.data(), buf.size())) return fail(ctx, PICA_ERR_INVALID, "truncated checkpoint");
+        CK(cudaMemcpy(ctx->f[k], buf.data(), buf.size(), cudaMemcpyHostToDevice));
+    }
+    const size_t n = ctx->nscTot;
+    for (int q = 0; q < c.nspecies; q++) {
+        SpeciesState& S = ctx->sp[q];
+        int64_t slots = 0;
+        std::vector<int64_t> start(n);
+        std::vector<int32_t> cap(n), count(n), alive(n);
+        if (!readAll(fc.f, &slots, 8) || !readAll(fc.f, start.data(), n * 8) || !readAll(fc.f, cap.data(), n * 4) ||
+            !readAll(fc.f, count.data(), n * 4) || !readAll(fc.f, alive.data(), n * 4))
+            return fail(ctx, PICA_ERR_INVALID, "truncated checkpoint");
+        if (slots < 0 || (n && (start[n - 1] + cap[n - 1] != slots))) return fail(ctx, PICA_ERR_INVALID, "corrupt checkpoint layout");
+        int rc;
+        if ((rc = ensureBuffer(ctx, q, 0, slots)) || (rc = ensureBuffer(ctx, q, 1, slots)) || (rc = ensureSlotArrays(ctx, q, slots)))
+            return rc;
+        for (int k = 0; k < ctx->ncomp; k++) {
+            std::vector<unsigned char> comp(slots * ctx->compBytes[k]);
+            if (!readAll(fc.f, comp.data(), comp.size())) return fail(ctx, PICA_ERR_INVALID, "truncated checkpoint");
+            CK(cudaMemcpy(S.buf[0][k], comp.data(), comp.size(), cudaMemcpyHostToDevice));
+        }
+        CK(cudaMemcpy(S.d_start, start.data(), n * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.d_cap, cap.data(), n * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.d_count, count.data(), n * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.d_alive, alive.data(), n * 4, cudaMemcpyHostToDevice));
+        S.h_start.swap(start);
+        S.h_cap.swap(cap);
+        S.layoutSlots = slots;
+    }
+    ctx->cur = 0;
+    ctx->steps = h.steps;
+    ctx->kmax = h.kmax;
+    ctx->jfrac = h.jfrac;
+    ctx->tileSplit = h.tileSplit;
+    for (auto p : ctx->jacc) CK(cudaMemset(p, 0, nodes * 8));
+    return PICA_OK;
+}
 
 }  // extern "C"

@@ -480,12 +480,16 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     const int code = dirCode(sc, nsc3, a.nsc, bad);
                     // Stayers in place (the weight does not change); a leaver goes to the side
                     // buffer at its own slot, its slot dies and joins the leaver list.
-                    const CellPtrs& o2 = code == 13 ? sa.buf : sa.out;
-                    o2.cell[slot] = packCell(gc[0], gc[1], gc[2]);
-                    o2.ox[slot] = on[0]; o2.oy[slot] = on[1]; o2.oz[slot] = on[2];
-                    o2.ux[slot] = u[0]; o2.uy[slot] = u[1]; o2.uz[slot] = u[2];
-                    if (code != 13) {
-                        o2.w[slot] = wgt;
+                    const uint32_t pc2 = packCell(gc[0], gc[1], gc[2]);
+                    if (code == 13) {
+                        sa.buf.cell[slot] = pc2;
+                        sa.buf.ox[slot] = on[0]; sa.buf.oy[slot] = on[1]; sa.buf.oz[slot] = on[2];
+                        sa.buf.ux[slot] = u[0]; sa.buf.uy[slot] = u[1]; sa.buf.uz[slot] = u[2];
+                    } else {
+                        sa.out.cell[slot] = pc2;
+                        sa.out.ox[slot] = on[0]; sa.out.oy[slot] = on[1]; sa.out.oz[slot] = on[2];
+                        sa.out.ux[slot] = u[0]; sa.out.uy[slot] = u[1]; sa.out.uz[slot] = u[2];
+                        sa.out.w[slot] = wgt;
                         sa.dir[slot] = (uint8_t)code;
                         sa.llist[start + atomicAdd(&s_nleave, 1)] = i;
                         sa.buf.cell[slot] = kDeadCell;

@@ -59,3 +59,15 @@ def test_cpp_host_loop_matches_python(tmp_path):
     for c, k in enumerate(("x", "y", "z", "ux", "uy", "uz")):
         assert np.max(np.abs(rows[:, c] - p[k])) <= 1e-13 * np.max(np.abs(p[k])), k
     np.testing.assert_allclose(last, [f[0][3, 4, 5], f[6][2, 2, 2], f[5][4, 4, 4]], rtol=1e-11, atol=0)
+
+
+def test_cpp_driver_and_checkpoint(tmp_path):
+    so = pg._lib.lib_path()
+    pg._lib.load()
+    exe = str(tmp_path / "driver_checkpoint")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "driver_checkpoint.cpp"), so, "-o", exe,
+                    "-Wl,-rpath," + os.path.dirname(so), "-lpthread"], check=True)
+    out = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True, check=True).stdout.split()
+    assert out == ["diag", "2", "1", "diag", "4", "1", "diag", "6", "1", "same"]
+    assert os.path.exists(tmp_path / "ckpt_3") and os.path.exists(tmp_path / "ckpt_6")
