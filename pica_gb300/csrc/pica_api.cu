@@ -1040,6 +1040,12 @@ struct pica_batch {
     int variant = 0;
     bool useGraph = true;
     int* d_counter = nullptr;                // one work counter per push launch
+    // The members' chains after the push (current conversion, field updates,
+    // migration) run on kBatchLanes streams forked from and joined back to `stream`.
+    static constexpr int kBatchLanes = 8;
+    cudaStream_t lanes[kBatchLanes] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kBatchLanes] = {};
     std::vector<int> order;                  // members in work order
     int nsp = 1;                             // species slots of the push arguments (1 or 2)
     std::vector<BatchPushArgs<1>> args1;     // one persistent push launch per batchMembers<NSP>() members
@@ -1169,26 +1175,34 @@ int batchEnqueue(pica_batch* b) {
     for (const auto& ba : b->args2)
         if (b->nsp == 2 && launchPushBatch(ba, b->shape, b->S, b->variant, b->stream))
             return batchFail(b, PICA_ERR_CUDA, "batched push launch failed");
-    for (int k : b->order) {
-        pica_ctx* ctx = b->m[k];
-        const pica_config& c = ctx->cfg;
-        const int64_t nodes = (int64_t)c.n[0] * c.n[1] * c.n[2];
-        const double scale = (ctx->kmax * std::ldexp(1.0, -ctx->jfrac)) * (1.0 / (c.h[0] * c.h[1] * c.h[2]));
-        if (launchConvertJ(false, ctx->f + 6, ctx->jacc, nodes, scale, b->stream))
-            return batchFail(b, PICA_ERR_CUDA, "current conversion launch failed");
-        double cb[3], ce[3];
-        for (int d = 0; d < 3; d++) { cb[d] = (kC * (0.5 * c.dt)) / c.h[d]; ce[d] = (kC * c.dt) / c.h[d]; }
-        if (launchUpdateB(false, ctx->f, c.n, cb, b->stream) || launchUpdateE(false, ctx->f, c.n, -4.0 * kPiRef * c.dt, ce, b->stream) ||
-            launchUpdateB(false, ctx->f, c.n, cb, b->stream))
-            return batchFail(b, PICA_ERR_CUDA, "field update launch failed");
-    }
+    // Fork: member i's chain goes to lane i % kBatchLanes, after the push.
+    BK(cudaEventRecord(b->fork, b->stream));
+    for (int l = 0; l < pica_batch::kBatchLanes; l++) BK(cudaStreamWaitEvent(b->lanes[l], b->fork, 0));
     for (size_t i = 0; i < b->order.size(); i++) {
         const int k = b->order[i];
         pica_ctx* ctx = b->m[k];
+        cudaStream_t ls = b->lanes[i % pica_batch::kBatchLanes];
+        const pica_config& c = ctx->cfg;
+        const int64_t nodes = (int64_t)c.n[0] * c.n[1] * c.n[2];
+        const double scale = (ctx->kmax * std::ldexp(1.0, -ctx->jfrac)) * (1.0 / (c.h[0] * c.h[1] * c.h[2]));
+        if (launchConvertJ(false, ctx->f + 6, ctx->jacc, nodes, scale, ls))
+            return batchFail(b, PICA_ERR_CUDA, "current conversion launch failed");
+        double cb[3], ce[3];
+        for (int d = 0; d < 3; d++) { cb[d] = (kC * (0.5 * c.dt)) / c.h[d]; ce[d] = (kC * c.dt) / c.h[d]; }
+        if (launchUpdateB(false, ctx->f, c.n, cb, ls) || launchUpdateE(false, ctx->f, c.n, -4.0 * kPiRef * c.dt, ce, ls) ||
+            launchUpdateB(false, ctx->f, c.n, cb, ls))
+            return batchFail(b, PICA_ERR_CUDA, "field update launch failed");
         const int64_t before = ctx->launches;   // counted per executed step by the caller
+        ctx->stream = ls;
         const int rc = migrateDevice<CellPtrs>(ctx);
+        ctx->stream = b->stream;
         ctx->launches = before;
         if (rc) return memberFail(b, k, rc);
+    }
+    // Join every lane back into the batch stream.
+    for (int l = 0; l < pica_batch::kBatchLanes; l++) {
+        BK(cudaEventRecord(b->join[l], b->lanes[l]));
+        BK(cudaStreamWaitEvent(b->stream, b->join[l], 0));
     }
     return PICA_OK;
 }
@@ -1303,6 +1317,11 @@ int pica_batch_create(const pica_config* cfgs, int32_t count, pica_batch** out) 
         return rc;
     };
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(PICA_ERR_CUDA);
+    if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) return bail(PICA_ERR_CUDA);
+    for (int l = 0; l < pica_batch::kBatchLanes; l++)
+        if (cudaStreamCreateWithFlags(&b->lanes[l], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->join[l], cudaEventDisableTiming) != cudaSuccess)
+            return bail(PICA_ERR_CUDA);
     for (int k = 0; k < count; k++) {
         pica_ctx* ctx = nullptr;
         const int rc = pica_ctx_create(&cfgs[k], &ctx);
@@ -1323,6 +1342,11 @@ int pica_batch_destroy(pica_batch* b) {
     for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
     for (pica_ctx* ctx : b->m) pica_ctx_destroy(ctx);
     if (b->d_counter) cudaFree(b->d_counter);
+    for (int l = 0; l < pica_batch::kBatchLanes; l++) {
+        if (b->lanes[l]) cudaStreamDestroy(b->lanes[l]);
+        if (b->join[l]) cudaEventDestroy(b->join[l]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return PICA_OK;

@@ -935,8 +935,13 @@ __device__ __forceinline__ int slotKey(const PlainPtrs& p, int64_t i, const int*
 // ordered by (cell, old slot).
 constexpr int kResortWarps = 8;
 constexpr int kResortUnroll = 4;
+// Resident CTAs per SM the register budget is set for: four with the FP32 records
+// (64 registers), two with the FP64 ones (no spills).
 template <class P>
-__global__ void __launch_bounds__(kResortWarps * 32) k_resort(const __grid_constant__ MigrateArgs<P> a) {
+constexpr int resortMinBlocks() { return std::is_same<P, CellPtrs>::value ? 4 : 2; }
+
+template <class P>
+__global__ void __launch_bounds__(kResortWarps * 32, resortMinBlocks<P>()) k_resort(const __grid_constant__ MigrateArgs<P> a) {
     constexpr unsigned FULL = 0xffffffffu;
     constexpr int kT = kResortWarps * 32;
     constexpr int U = kResortUnroll;
