@@ -44,6 +44,10 @@ struct SpeciesState {
     std::vector<int64_t> h_start;
     std::vector<int32_t> h_cap;
     int64_t layoutSlots = 0;     // sum of caps of the current layout
+    // Pinned staging of the resort's host round trip (live counts in, new layout out).
+    int32_t* h_pinAlive = nullptr;
+    int64_t* h_pinStart = nullptr;
+    int32_t* h_pinCap = nullptr;
 };
 
 }  // namespace
@@ -324,7 +328,8 @@ int pica_ctx_create(const pica_config* cfg, pica_ctx** out) {
         if (cudaMalloc(&S.d_start, n * 8) || cudaMalloc(&S.d_cap, n * 4) || cudaMalloc(&S.d_count, n * 4) ||
             cudaMalloc(&S.d_alive, n * 4) || cudaMalloc(&S.d_nleave, n * 4) || cudaMalloc(&S.d_needed, n * 4) ||
             cudaMalloc(&S.d_neededAlive, n * 4) || cudaMalloc(&S.d_start2, n * 8) || cudaMalloc(&S.d_cap2, n * 4) ||
-            cudaMalloc(&S.d_outOff, n * 8) || cudaMalloc(&S.d_dirOff, n * kDirBuckets * 4))
+            cudaMalloc(&S.d_outOff, n * 8) || cudaMalloc(&S.d_dirOff, n * kDirBuckets * 4) ||
+            cudaMallocHost(&S.h_pinAlive, n * 4) || cudaMallocHost(&S.h_pinStart, n * 8) || cudaMallocHost(&S.h_pinCap, n * 4))
             return bail(PICA_ERR_OOM);
         std::vector<int32_t> zero(n, 0);
         int64_t total;
@@ -360,6 +365,8 @@ int pica_ctx_destroy(pica_ctx* ctx) {
                         (void*)S.d_alive, (void*)S.d_nleave, (void*)S.d_needed, (void*)S.d_neededAlive,
                         (void*)S.d_start2, (void*)S.d_cap2, (void*)S.d_outOff, (void*)S.lbydir, (void*)S.d_dirOff})
             if (p) cudaFree(p);
+        for (void* p : {(void*)S.h_pinAlive, (void*)S.h_pinStart, (void*)S.h_pinCap})
+            if (p) cudaFreeHost(p);
     }
     if (ctx->d_flags) cudaFree(ctx->d_flags);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
@@ -746,7 +753,7 @@ static int migrateDevice(pica_ctx* ctx) {
 }
 
 // Host part, after the device part has finished and ctx->h_flags holds its flags:
-// report a migration error, or rebuild on a capacity overflow; then the periodic resort.
+// report a migration error, or rebuild on a capacity overflow; count the step.
 template <class P>
 static int migrateFinish(pica_ctx* ctx) {
     const pica_config& c = ctx->cfg;
@@ -794,37 +801,75 @@ static int migrateFinish(pica_ctx* ctx) {
         updateJFrac(ctx);
     }
     ctx->steps++;
-    if (c.resort_every > 0 && ctx->steps % c.resort_every == 0) {
-        // Compact every supercell and sort it by cell into the other buffer, with
-        // capacities recomputed from the live counts.
-        const int A2 = ctx->cur, B2 = 1 - ctx->cur;
-        CK(cudaStreamSynchronize(ctx->stream));
-        for (int q = 0; q < c.nspecies; q++) {
-            SpeciesState& S = ctx->sp[q];
-            std::vector<int32_t> alive(ctx->nscTot);
-            CK(cudaMemcpy(alive.data(), S.d_alive, ctx->nscTot * 4, cudaMemcpyDeviceToHost));
-            int64_t total;
-            int rc;
-            if ((rc = stageLayout(ctx, q, alive, total)) || (rc = ensureBuffer(ctx, q, B2, total)) ||
-                (rc = ensureSlotArrays(ctx, q, total)))
-                return rc;
-        }
-        MigrateArgs<P> r{};
-        migrateArgs(ctx, r);   // a = current buffer A2, dst = B2
-        CKL(launchMigrate(ctx, r, kResort));
-        ctx->launches++;
-        CK(cudaStreamSynchronize(ctx->stream));
-        for (int q = 0; q < c.nspecies; q++) {
-            SpeciesState& S = ctx->sp[q];
-            std::swap(S.d_start, S.d_start2);
-            std::swap(S.d_cap, S.d_cap2);
-            int rc;
-            if ((rc = ensureBuffer(ctx, q, A2, S.layoutSlots))) return rc;
-        }
-        ctx->cur = B2;
-        updateJFrac(ctx);
-    }
     return PICA_OK;
+}
+
+// The periodic resort, in three parts so that a batch can do each part for all its
+// members before waiting: enqueue the copy of the live counts; once they have
+// arrived, lay out the new capacities, upload them and launch the resort into the
+// other buffer; once that has finished, swap layouts and buffers.
+static bool resortDue(const pica_ctx* ctx) {
+    return ctx->cfg.resort_every > 0 && ctx->steps > 0 && ctx->steps % ctx->cfg.resort_every == 0;
+}
+
+static int resortFetchCounts(pica_ctx* ctx) {
+    for (int q = 0; q < ctx->cfg.nspecies; q++)
+        CK(cudaMemcpyAsync(ctx->sp[q].h_pinAlive, ctx->sp[q].d_alive, ctx->nscTot * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    return PICA_OK;
+}
+
+template <class P>
+static int resortLaunch(pica_ctx* ctx) {
+    const int B2 = 1 - ctx->cur;
+    const size_t n = ctx->nscTot;
+    for (int q = 0; q < ctx->cfg.nspecies; q++) {
+        SpeciesState& S = ctx->sp[q];
+        std::vector<int32_t> alive(S.h_pinAlive, S.h_pinAlive + n);
+        std::vector<int64_t> nstart;
+        std::vector<int32_t> ncap;
+        int64_t total;
+        layoutFrom(ctx, alive, nstart, ncap, total);
+        std::copy(nstart.begin(), nstart.end(), S.h_pinStart);
+        std::copy(ncap.begin(), ncap.end(), S.h_pinCap);
+        int rc;
+        if ((rc = ensureBuffer(ctx, q, B2, total)) || (rc = ensureSlotArrays(ctx, q, total))) return rc;
+        CK(cudaMemcpyAsync(S.d_start2, S.h_pinStart, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(S.d_cap2, S.h_pinCap, n * 4, cudaMemcpyHostToDevice, ctx->stream));
+        S.h_start.swap(nstart);
+        S.h_cap.swap(ncap);
+        S.layoutSlots = total;
+    }
+    MigrateArgs<P> r{};
+    migrateArgs(ctx, r);   // a = current buffer, dst = the other one, newStart = the uploaded layout
+    CKL(launchMigrate(ctx, r, kResort));
+    ctx->launches++;
+    return PICA_OK;
+}
+
+static int resortFinish(pica_ctx* ctx) {
+    const int A2 = ctx->cur;
+    for (int q = 0; q < ctx->cfg.nspecies; q++) {
+        SpeciesState& S = ctx->sp[q];
+        std::swap(S.d_start, S.d_start2);
+        std::swap(S.d_cap, S.d_cap2);
+        int rc;
+        if ((rc = ensureBuffer(ctx, q, A2, S.layoutSlots))) return rc;
+    }
+    ctx->cur = 1 - A2;
+    updateJFrac(ctx);
+    return PICA_OK;
+}
+
+// Compact every supercell and sort it by cell into the other buffer, with
+// capacities recomputed from the live counts.
+template <class P>
+static int resortNow(pica_ctx* ctx) {
+    int rc = resortFetchCounts(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if ((rc = resortLaunch<P>(ctx))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return resortFinish(ctx);
 }
 
 template <class P>
@@ -833,7 +878,8 @@ static int migrateImpl(pica_ctx* ctx) {
     if (rc) return rc;
     CK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    return migrateFinish<P>(ctx);
+    if ((rc = migrateFinish<P>(ctx))) return rc;
+    return resortDue(ctx) ? resortNow<P>(ctx) : PICA_OK;
 }
 
 extern "C" {
@@ -1285,9 +1331,32 @@ int batchStepOnce(pica_batch* b) {
     for (pica_ctx* ctx : b->m)
         BK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
     BK(cudaStreamSynchronize(b->stream));
+    std::vector<int> due;
     for (size_t k = 0; k < b->m.size(); k++) {
         const int rc = migrateFinish<CellPtrs>(b->m[k]);
         if (rc) return memberFail(b, (int)k, rc);
+        if (resortDue(b->m[k])) due.push_back((int)k);
+    }
+    if (!due.empty()) {
+        // Resorts of every member due: counts of all, one wait; layouts and launches on
+        // the lanes; one wait; swaps.
+        for (int k : due) {
+            const int rc = resortFetchCounts(b->m[k]);
+            if (rc) return memberFail(b, k, rc);
+        }
+        BK(cudaStreamSynchronize(b->stream));
+        for (size_t i = 0; i < due.size(); i++) {
+            pica_ctx* ctx = b->m[due[i]];
+            ctx->stream = b->lanes[i % pica_batch::kBatchLanes];
+            const int rc = resortLaunch<CellPtrs>(ctx);
+            ctx->stream = b->stream;
+            if (rc) return memberFail(b, due[i], rc);
+        }
+        for (int l = 0; l < pica_batch::kBatchLanes; l++) BK(cudaStreamSynchronize(b->lanes[l]));
+        for (int k : due) {
+            const int rc = resortFinish(b->m[k]);
+            if (rc) return memberFail(b, k, rc);
+        }
     }
     b->steps++;
     return PICA_OK;

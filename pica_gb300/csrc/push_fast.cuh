@@ -145,12 +145,23 @@ __device__ __noinline__ void drainRing(unsigned ring, int head, int n, FixTileS 
 // Wrap a cell index that is at most one period out of range.
 __device__ __forceinline__ int wrapNear(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
-// Rows of a warp's reduction area: 32 lane rows and 17 rows for sums parked when a
-// lane changes cell; odd, so that the column reads are conflict-free.
-constexpr int kRedRows = 49;
+// A warp's reduction area: 32 lane rows and 15 rows for sums parked when a lane
+// changes cell, row r at red[r * kRowStride] (odd stride: a lane writing its row
+// and lanes reading one value of a row are both free of bank conflicts).  While
+// the segment runs the lane-row block is free and stages the segment's particle
+// outputs (kStageWords), which are then written back with coalesced stores.
+constexpr int kRedRows = 47;
+constexpr int kRowStride = 57;
+constexpr int kStageWords = 7 * 256;   // cell, ox, oy, oz, ux, uy, uz of 32 * K = 256 particles
+static_assert(32 * kRowStride >= kStageWords, "the lane-row block holds a segment's outputs");
+
+// Staging slot of component w of segment particle p (lane p / 8, iteration p % 8):
+// the XOR swizzle makes both the per-iteration writes (p = 8 lane + it) and the
+// coalesced read-back (p = lane + 32 q) free of bank conflicts.
+__device__ __forceinline__ int stageIdx(int w, int p) { return w * 256 + (p ^ ((p >> 5) & 7)); }
 
 // Add up, per window key, the rows of a warp's reduction area (value j of row r
-// at red[j * kRedRows + r]; keys[r] < 0: empty) and deposit the sums: lane t
+// at red[r * kRowStride + j]; keys[r] < 0: empty) and deposit the sums: lane t
 // sums values t and t + 32 over the member rows, lane rows first (unless !lanes),
 // then the np park rows, in ascending order.
 template <int NWn, int NV>
@@ -160,8 +171,8 @@ __device__ __forceinline__ void reduceRows(const float* red, const int* keys, in
     const int kp = lane < np ? keys[32 + lane] : -1;
     unsigned pendL = __ballot_sync(0xffffffffu, kl >= 0);
     unsigned pendP = __ballot_sync(0xffffffffu, kp >= 0);
-    const float* c0 = red + lane * kRedRows;
-    const float* c1 = red + (lane + 32) * kRedRows;
+    const float* c0 = red + lane;
+    const float* c1 = red + lane + 32;
     while (pendL | pendP) {
         const int ref = pendL ? __shfl_sync(0xffffffffu, kl, __ffs(pendL) - 1)
                               : __shfl_sync(0xffffffffu, kp, __ffs(pendP) - 1);
@@ -171,12 +182,12 @@ __device__ __forceinline__ void reduceRows(const float* red, const int* keys, in
         pendP &= ~mP;
         float s0 = 0.0f, s1 = 0.0f;
         for (unsigned m = mL; m; m &= m - 1) {
-            const int r = __ffs(m) - 1;
+            const int r = (__ffs(m) - 1) * kRowStride;
             if (lane < NV) s0 += c0[r];
             if (lane + 32 < NV) s1 += c1[r];
         }
         for (unsigned m = mP; m; m &= m - 1) {
-            const int r = 32 + __ffs(m) - 1;
+            const int r = (32 + __ffs(m) - 1) * kRowStride;
             if (lane < NV) s0 += c0[r];
             if (lane + 32 < NV) s1 += c1[r];
         }
@@ -187,8 +198,8 @@ __device__ __forceinline__ void reduceRows(const float* red, const int* keys, in
 }
 
 // Dynamic shared memory of k_push_cell_esirkepov, in 4-byte words.
-__host__ __device__ constexpr int64_t esirkepovSmemWords(int TT, int ETT, int warps, int nv) {
-    return 6ll * TT + 6ll * ETT + (int64_t)warps * (kRing * kQWords + nv * kRedRows + kRedRows);
+__host__ __device__ constexpr int64_t esirkepovSmemWords(int TT, int ETT, int warps) {
+    return 6ll * TT + 6ll * ETT + (int64_t)warps * (kRing * kQWords + kRedRows * kRowStride + kRedRows);
 }
 
 // One supercell s of the plasma described by a, on the whole CTA (smem_raw: the
@@ -201,6 +212,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
     constexpr int NV = kStayValues;                        // 54 face values
     constexpr int kWarps = THREADS / 32;
     constexpr int kPark = kRedRows - 32;
+    static_assert(K == 8, "a segment of 32 x 8 particles is staged in the lane-row block");
     constexpr unsigned FULL = 0xffffffffu;
 
     // Current tile: origin m - kG, edges S + 2kG + 1.  E/B tile: origin m - 1, edges S + 3.
@@ -217,8 +229,9 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
     jt.setSplit(a.tileSplit);
     float* eb = reinterpret_cast<float*>(jt.hi + 3 * TT);
     float* ring = eb + 6 * ETT + warp * (kRing * kQWords);
-    float* red = eb + 6 * ETT + kWarps * (kRing * kQWords) + warp * (NV * kRedRows);
-    int* keys = reinterpret_cast<int*>(eb + 6 * ETT + kWarps * (kRing * kQWords + NV * kRedRows)) + warp * kRedRows;
+    float* red = eb + 6 * ETT + kWarps * (kRing * kQWords) + warp * (kRedRows * kRowStride);
+    int* keys = reinterpret_cast<int*>(eb + 6 * ETT + kWarps * (kRing * kQWords + kRedRows * kRowStride)) + warp * kRedRows;
+    uint32_t* stage = reinterpret_cast<uint32_t*>(red);   // the lane-row block, while a segment runs
     FixTileS jts;
     jts.lo = (unsigned)__cvta_generic_to_shared(jt.lo);
     jts.hi = (unsigned)__cvta_generic_to_shared(jt.hi);
@@ -295,6 +308,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     pw = sa.buf.w[sl];
                 }
                 const bool act = i < count && cellv != kDeadCell;
+                if (!act && i < count) stage[stageIdx(0, lane * K + it)] = kDeadCell;   // stays dead
                 int lc[3] = {0, 0, 0};
                 int key = -1;
                 if (act) {
@@ -308,41 +322,29 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     }
                     key = ((lw[0] + 4) << 16) | ((lw[1] + 4) << 8) | (lw[2] + 4);
                 }
-                // A lane meeting another window parks its sums (or, when the park rows
-                // are used up, the warp deposits every row now and starts afresh).
+                // A lane meeting another window parks its sums in a park row; when the park
+                // rows run out the warp deposits them and goes on parking.
                 const bool sw = act && key != accKey;
                 const bool park = sw && accKey >= 0;
-                const unsigned pm = __ballot_sync(FULL, park);
-                if (pm) {
-                    const int np = __popc(pm);
-                    bool flushed = false;
-                    if (nPark + np > kPark) {
-                        if (np <= kPark) {
-                            // deposit the parked rows, then park
-                            reduceRows<NWn, NV>(red, keys, nPark, false, jt, TT, T1, T2, lane);
-                        } else {
-                            // more lanes switching than park rows: deposit every row now
-#pragma unroll
-                            for (int j = 0; j < NV; j++) red[j * kRedRows + lane] = acc[j];
-                            keys[lane] = accKey;
-                            __syncwarp();
-                            reduceRows<NWn, NV>(red, keys, nPark, true, jt, TT, T1, T2, lane);
-#pragma unroll
-                            for (int j = 0; j < NV; j++) acc[j] = 0.0f;
-                            flushed = true;
-                        }
+                unsigned rem = __ballot_sync(FULL, park);
+                while (rem) {
+                    if (nPark == kPark) {
+                        reduceRows<NWn, NV>(red, keys, nPark, false, jt, TT, T1, T2, lane);
                         __syncwarp();
                         nPark = 0;
                     }
-                    if (!flushed) {
-                        if (park) {
-                            const int row = 32 + nPark + __popc(pm & lt);
+                    const int rank = __popc(rem & lt);
+                    const bool mine = ((rem >> lane) & 1u) && rank < kPark - nPark;
+                    const unsigned now = __ballot_sync(FULL, mine);
+                    if (mine) {
+                        const int row = 32 + nPark + rank;
 #pragma unroll
-                            for (int j = 0; j < NV; j++) red[j * kRedRows + row] = acc[j];
-                            keys[row] = accKey;
-                        }
-                        nPark += np;
+                        for (int j = 0; j < NV; j++) red[row * kRowStride + j] = acc[j];
+                        keys[row] = accKey;
                     }
+                    nPark += __popc(now);
+                    rem &= ~now;
+                    __syncwarp();
                 }
                 if (sw) {
 #pragma unroll
@@ -481,18 +483,21 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     // Stayers in place (the weight does not change); a leaver goes to the side
                     // buffer at its own slot, its slot dies and joins the leaver list.
                     const uint32_t pc2 = packCell(gc[0], gc[1], gc[2]);
-                    if (code == 13) {
-                        sa.buf.cell[slot] = pc2;
-                        sa.buf.ox[slot] = on[0]; sa.buf.oy[slot] = on[1]; sa.buf.oz[slot] = on[2];
-                        sa.buf.ux[slot] = u[0]; sa.buf.uy[slot] = u[1]; sa.buf.uz[slot] = u[2];
-                    } else {
+                    const int sp = lane * K + it;   // staged; written back at the end of the segment
+                    stage[stageIdx(0, sp)] = code == 13 ? pc2 : kDeadCell;
+                    stage[stageIdx(1, sp)] = __float_as_uint(on[0]);
+                    stage[stageIdx(2, sp)] = __float_as_uint(on[1]);
+                    stage[stageIdx(3, sp)] = __float_as_uint(on[2]);
+                    stage[stageIdx(4, sp)] = __float_as_uint(u[0]);
+                    stage[stageIdx(5, sp)] = __float_as_uint(u[1]);
+                    stage[stageIdx(6, sp)] = __float_as_uint(u[2]);
+                    if (code != 13) {
                         sa.out.cell[slot] = pc2;
                         sa.out.ox[slot] = on[0]; sa.out.oy[slot] = on[1]; sa.out.oz[slot] = on[2];
                         sa.out.ux[slot] = u[0]; sa.out.uy[slot] = u[1]; sa.out.uz[slot] = u[2];
                         sa.out.w[slot] = wgt;
                         sa.dir[slot] = (uint8_t)code;
                         sa.llist[start + atomicAdd(&s_nleave, 1)] = i;
-                        sa.buf.cell[slot] = kDeadCell;
                     }
                 }
                 // Queue window changes in the ring; deposit 32 at a time (one per lane).
@@ -517,9 +522,26 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     }
                 }
             }
+            // Write the segment's particles back, coalesced: cell, offsets, momenta (the
+            // weight does not change; leavers went to the side buffer).
+            __syncwarp();
+            {
+                const int nValid = min(32 * K, count - seg * 32 * K);
+                const int64_t base = start + (int64_t)seg * 32 * K;
+                for (int p = lane; p < nValid; p += 32) {
+                    sa.buf.cell[base + p] = stage[stageIdx(0, p)];
+                    sa.buf.ox[base + p] = __uint_as_float(stage[stageIdx(1, p)]);
+                    sa.buf.oy[base + p] = __uint_as_float(stage[stageIdx(2, p)]);
+                    sa.buf.oz[base + p] = __uint_as_float(stage[stageIdx(3, p)]);
+                    sa.buf.ux[base + p] = __uint_as_float(stage[stageIdx(4, p)]);
+                    sa.buf.uy[base + p] = __uint_as_float(stage[stageIdx(5, p)]);
+                    sa.buf.uz[base + p] = __uint_as_float(stage[stageIdx(6, p)]);
+                }
+            }
+            __syncwarp();
             // Deposit the segment's window sums: lane rows plus parked rows, by window.
 #pragma unroll
-            for (int j = 0; j < NV; j++) red[j * kRedRows + lane] = acc[j];
+            for (int j = 0; j < NV; j++) red[lane * kRowStride + j] = acc[j];
             keys[lane] = accKey;
             __syncwarp();
             reduceRows<NWn, NV>(red, keys, nPark, true, jt, TT, T1, T2, lane);

@@ -24,7 +24,7 @@ template <int SHAPE, int SC, int K, int THREADS, int MINB>
 int launchEsirkepovV(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     const int TT = a.T[0] * a.T[1] * a.T[2];
     const int ETT = (a.S[0] + 3) * (a.S[1] + 3) * (a.S[2] + 3);
-    const size_t smem = (size_t)esirkepovSmemWords(TT, ETT, THREADS / 32, kStayValues) * 4;
+    const size_t smem = (size_t)esirkepovSmemWords(TT, ETT, THREADS / 32) * 4;
     auto k = k_push_cell_esirkepov<SHAPE, K, THREADS, MINB, SC>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -60,7 +60,7 @@ template <int SHAPE, int SC, int K, int THREADS, int MINB, int NSP>
 int launchBatchV(const BatchPushArgs<NSP>& b, const int* S, cudaStream_t s) {
     const int TT = (S[0] + 2 * kG + 1) * (S[1] + 2 * kG + 1) * (S[2] + 2 * kG + 1);
     const int ETT = (S[0] + 3) * (S[1] + 3) * (S[2] + 3);
-    const size_t smem = (size_t)esirkepovSmemWords(TT, ETT, THREADS / 32, kStayValues) * 4;
+    const size_t smem = (size_t)esirkepovSmemWords(TT, ETT, THREADS / 32) * 4;
     auto k = k_push_batch<SHAPE, K, THREADS, MINB, SC, NSP>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
