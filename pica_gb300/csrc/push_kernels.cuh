@@ -81,9 +81,35 @@ struct FixTile {
     }
     __device__ __forceinline__ long long node(int idx) const { return ((long long)hi[idx] << L) + (long long)lo[idx]; }
 };
+// FP64 tile.  A shared-memory FP64 atomicAdd retries while lanes of the warp hold
+// the same node (sorted particles: most of a warp sits in one cell), and every
+// retry costs an FP64 add on a part whose FP64 rate is low.  So when the whole
+// warp is active, each run of consecutive lanes on the same node is first summed
+// with a segmented scan over shuffles, and the run's last lane adds the sum.
 struct DblTile {
     double* p;
-    __device__ __forceinline__ void add(int idx, double v) const { atomicAdd(p + idx, v); }
+    __device__ __forceinline__ void add(int idx, double v) const {
+        const unsigned mask = __activemask();
+        if (mask != 0xffffffffu) {
+            atomicAdd(p + idx, v);
+            return;
+        }
+        const int lane = threadIdx.x & 31;
+        const int prev = __shfl_up_sync(mask, idx, 1);
+        int head = (lane == 0 || prev != idx) ? lane : 0;   // first lane of this lane's run
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int h = __shfl_up_sync(mask, head, o);
+            if (lane >= o) head = max(head, h);
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double t = __shfl_up_sync(mask, v, o);
+            if (lane - o >= head) v += t;
+        }
+        const int next = __shfl_down_sync(mask, idx, 1);
+        if (lane == 31 || next != idx) atomicAdd(p + idx, v);
+    }
 };
 
 // Separable W^3-point gather: sum_i wx_i sum_j wy_j (sum_k wz_k F), left to right.
