@@ -66,6 +66,34 @@ __device__ __forceinline__ float borisFast(float ec, const float* eb, float* u) 
     return rsqrtf(1.0f + (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
 }
 
+// Two field components gathered together with packed FP32x2 arithmetic (each half
+// rounds exactly as the scalar gatherSep does): component A from tile tA with base
+// ta and weights wxa, wya, wza; component B likewise.
+template <int W>
+__device__ __forceinline__ float2 gatherPair(const float* tA, const float* tB, int E1, int E2, const int* ta,
+                                             const int* tb, const float* wxa, const float* wya, const float* wza,
+                                             const float* wxb, const float* wyb, const float* wzb) {
+    float2 wz[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) wz[k] = make_float2(wza[k], wzb[k]);
+    float2 r = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+        float2 ry = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int j = 0; j < W; j++) {
+            const float* ra = tA + ((ta[0] + i) * E1 + (ta[1] + j)) * E2 + ta[2];
+            const float* rb = tB + ((tb[0] + i) * E1 + (tb[1] + j)) * E2 + tb[2];
+            float2 rz = __fmul2_rn(make_float2(ra[0], rb[0]), wz[0]);
+#pragma unroll
+            for (int k = 1; k < W; k++) rz = __ffma2_rn(make_float2(ra[k], rb[k]), wz[k], rz);
+            ry = __ffma2_rn(make_float2(wya[j], wyb[j]), rz, ry);
+        }
+        r = __ffma2_rn(make_float2(wxa[i], wxb[i]), ry, r);
+    }
+    return r;
+}
+
 constexpr int kQWords = 11;  // queued window change: o[3], on[3], kq[3], packed lc, packed ln
 constexpr int kStayNodes = 3;    // stay-in-cell window: rho-lattice nodes lc-1 .. lc+1 per dimension
 constexpr int kStayValues = 54;  // its face values: 3 components x 2 faces x 3 x 3
@@ -383,12 +411,19 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                             bs[d] = lc[d]; tscWeights(o[d] - 0.5f, ws[d]);
                         }
 #pragma unroll
-                        for (int comp = 0; comp < 6; comp++) {
-                            int t0[3];
+                        for (int cp = 0; cp < 6; cp += 2) {   // (Ex, Ey), (Ez, Bx), (By, Bz)
+                            int ta[3], tb[3];
 #pragma unroll
-                            for (int d = 0; d < 3; d++) t0[d] = stag(comp, d) ? bs[d] : bc[d];
-                            eb6[comp] = gatherSep<float, 3>(eb + comp * ETT, E1, E2, t0, stag(comp, 0) ? ws[0] : wc[0],
-                                                            stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2]);
+                            for (int d = 0; d < 3; d++) {
+                                ta[d] = stag(cp, d) ? bs[d] : bc[d];
+                                tb[d] = stag(cp + 1, d) ? bs[d] : bc[d];
+                            }
+                            const float2 g = gatherPair<3>(
+                                eb + cp * ETT, eb + (cp + 1) * ETT, E1, E2, ta, tb, stag(cp, 0) ? ws[0] : wc[0],
+                                stag(cp, 1) ? ws[1] : wc[1], stag(cp, 2) ? ws[2] : wc[2], stag(cp + 1, 0) ? ws[0] : wc[0],
+                                stag(cp + 1, 1) ? ws[1] : wc[1], stag(cp + 1, 2) ? ws[2] : wc[2]);
+                            eb6[cp] = g.x;
+                            eb6[cp + 1] = g.y;
                         }
                     }
                     const float ig = borisFast(ec, eb6, u);
