@@ -394,12 +394,19 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                             bs[d] = hi ? lc[d] + 1 : lc[d]; ws[d][0] = 1.0f - dd; ws[d][1] = dd;
                         }
 #pragma unroll
-                        for (int comp = 0; comp < 6; comp++) {
-                            int t0[3];
+                        for (int cp = 0; cp < 6; cp += 2) {   // (Ex, Ey), (Ez, Bx), (By, Bz)
+                            int ta[3], tb[3];
 #pragma unroll
-                            for (int d = 0; d < 3; d++) t0[d] = stag(comp, d) ? bs[d] : bc[d];
-                            eb6[comp] = gatherSep<float, 2>(eb + comp * ETT, E1, E2, t0, stag(comp, 0) ? ws[0] : wc[0],
-                                                            stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2]);
+                            for (int d = 0; d < 3; d++) {
+                                ta[d] = stag(cp, d) ? bs[d] : bc[d];
+                                tb[d] = stag(cp + 1, d) ? bs[d] : bc[d];
+                            }
+                            const float2 g = gatherPair<2>(
+                                eb + cp * ETT, eb + (cp + 1) * ETT, E1, E2, ta, tb, stag(cp, 0) ? ws[0] : wc[0],
+                                stag(cp, 1) ? ws[1] : wc[1], stag(cp, 2) ? ws[2] : wc[2], stag(cp + 1, 0) ? ws[0] : wc[0],
+                                stag(cp + 1, 1) ? ws[1] : wc[1], stag(cp + 1, 2) ? ws[2] : wc[2]);
+                            eb6[cp] = g.x;
+                            eb6[cp + 1] = g.y;
                         }
                     } else {
                         int bc[3], bs[3];
@@ -486,17 +493,39 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
 #pragma unroll
                             for (int f = 0; f < NWn - 1; f++) { run += dd[d][f]; e[d][f] = kq[d] * run; }
                         }
+                        // Jx and Jy share the z factors (pp2, qq2): their terms and sums go in
+                        // packed FP32x2 pairs (each half rounds as the scalar form); Jz alone.
                         constexpr int P = (NWn - 1) * NWn * NWn;
+                        float2 ad[NWn], dd01[NWn], ef[NWn - 1];
+#pragma unroll
+                        for (int y = 0; y < NWn; y++) {
+                            ad[y] = make_float2(aa[1][y], aa[0][y]);
+                            dd01[y] = make_float2(dd[1][y], dd[0][y]);
+                        }
+#pragma unroll
+                        for (int f = 0; f < NWn - 1; f++) ef[f] = make_float2(e[0][f], e[1][f]);
+#pragma unroll
+                        for (int z = 0; z < NWn; z++) {
+                            const float2 p2 = make_float2(pp[2][z], pp[2][z]), q2 = make_float2(qq[2][z], qq[2][z]);
+#pragma unroll
+                            for (int y = 0; y < NWn; y++) {
+                                const float2 t = __ffma2_rn(dd01[y], q2, __fmul2_rn(ad[y], p2));
+#pragma unroll
+                                for (int f = 0; f < NWn - 1; f++) {
+                                    float2 s2 = make_float2(acc[f * NWn * NWn + y * NWn + z], acc[P + y * (NWn - 1) * NWn + f * NWn + z]);
+                                    s2 = __ffma2_rn(ef[f], t, s2);
+                                    acc[f * NWn * NWn + y * NWn + z] = s2.x;
+                                    acc[P + y * (NWn - 1) * NWn + f * NWn + z] = s2.y;
+                                }
+                            }
+                        }
 #pragma unroll
                         for (int f = 0; f < NWn - 1; f++)
 #pragma unroll
                             for (int y = 0; y < NWn; y++)
 #pragma unroll
-                                for (int z = 0; z < NWn; z++) {
-                                    acc[f * NWn * NWn + y * NWn + z] += e[0][f] * (aa[1][y] * pp[2][z] + dd[1][y] * qq[2][z]);
-                                    acc[P + y * (NWn - 1) * NWn + f * NWn + z] += e[1][f] * (aa[0][y] * pp[2][z] + dd[0][y] * qq[2][z]);
+                                for (int z = 0; z < NWn; z++)
                                     acc[2 * P + y * NWn * (NWn - 1) + z * (NWn - 1) + f] += e[2][f] * (aa[0][y] * pp[1][z] + dd[0][y] * qq[1][z]);
-                                }
                     } else if (inRange) {
                         needQ = true;
 #pragma unroll
