@@ -118,7 +118,7 @@ int launchMigrateCell(const MigrateArgs<CellPtrs>& a, int stage, cudaStream_t s)
             break;
         }
         case kCountArrivals: k_migrate<CellPtrs, kCountArrivals><<<warpBlocks, 256, 0, s>>>(a); break;
-        case kFill: k_migrate<CellPtrs, kFill><<<warpBlocks, 256, 0, s>>>(a); break;
+        case kFill: k_fill<CellPtrs><<<(int)nscTot, kFillWarps * 32, 0, s>>>(a); break;
         case kGatherOutbox: k_migrate<CellPtrs, kGatherOutbox><<<warpBlocks, 256, 0, s>>>(a); break;
         case kRebuild: k_migrate<CellPtrs, kRebuild><<<warpBlocks, 256, 0, s>>>(a); break;
         case kResort: k_resort<CellPtrs><<<(int)nscTot, kResortWarps * 32, 0, s>>>(a); break;

@@ -41,7 +41,7 @@ int launchMigratePlain(const MigrateArgs<PlainPtrs>& a, int stage, cudaStream_t 
             break;
         }
         case kCountArrivals: k_migrate<PlainPtrs, kCountArrivals><<<warpBlocks, 256, 0, s>>>(a); break;
-        case kFill: k_migrate<PlainPtrs, kFill><<<warpBlocks, 256, 0, s>>>(a); break;
+        case kFill: k_fill<PlainPtrs><<<(int)nscTot, kFillWarps * 32, 0, s>>>(a); break;
         case kGatherOutbox: k_migrate<PlainPtrs, kGatherOutbox><<<warpBlocks, 256, 0, s>>>(a); break;
         case kRebuild: k_migrate<PlainPtrs, kRebuild><<<warpBlocks, 256, 0, s>>>(a); break;
         case kResort: k_resort<PlainPtrs><<<(int)nscTot, kResortWarps * 32, 0, s>>>(a); break;

@@ -827,13 +827,14 @@ __device__ __forceinline__ int arrivalBuckets(const MigrateArgs<P>& a, const Mig
 // source), then by source slot -- 32 at a time across the buckets.  fn(k, src, slot, r):
 // the k-th arrival, from slot `slot` of supercell src, entry r of src's lbydir list.
 template <class P, class F>
-__device__ __forceinline__ int forArrivals(const MigrateArgs<P>& a, const MigrateSpecies<P>& sa, int d, F&& fn) {
+__device__ __forceinline__ int forArrivals(const MigrateArgs<P>& a, const MigrateSpecies<P>& sa, int d, F&& fn, int sub = 0,
+                                          int nsub = 1) {
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     int src, b0, pre;
     int64_t sst;
     const int total = arrivalBuckets(a, sa, d, src, sst, b0, pre);
-    for (int k0 = 0; k0 < total; k0 += 32) {
+    for (int k0 = 32 * sub; k0 < total; k0 += 32 * nsub) {   // warp `sub` of nsub takes every nsub-th step
         const int k = k0 + lane;
         int c = 0;   // last bucket with pre <= k (buckets 0..25)
 #pragma unroll
@@ -860,7 +861,6 @@ __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ Migrate
     const int d = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (d >= nscTot) return;
-    if (STAGE == kFill && (a.flags[0] != 0 || a.flags[1] != 0)) return;   // error, or overflow: the rebuild runs instead
     for (int spi = 0; spi < a.nspecies; spi++) {
         const MigrateSpecies<P>& sa = a.sp[spi];
         const int64_t start = sa.start[d];
@@ -877,12 +877,6 @@ __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ Migrate
                 sa.neededAlive[d] = sa.alive[d] - nh + arrivals;
                 if (need > sa.cap[d]) atomicExch(a.flags + 1, 1);
             }
-        } else if constexpr (STAGE == kFill) {
-            arrivals = forArrivals(a, sa, d, [&](int k, int src, int slot, int) {
-                const int target = k < nh ? sa.llist[start + k] : cnt + (k - nh);
-                copyParticle(sa.b, sa.start[src] + slot, sa.a, start + target);
-            });
-            if (lane == 0) { sa.count[d] = cnt + max(0, arrivals - nh); sa.alive[d] = sa.alive[d] - nh + arrivals; }
         } else if constexpr (STAGE == kGatherOutbox) {
             const int64_t off = sa.outOff[d];
             for (int k = lane; k < nh; k += 32) copyParticle(sa.b, start + sa.lbydir[start + k], sa.outbox, off + k);
@@ -895,6 +889,35 @@ __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ Migrate
                 copyParticle(sa.outbox, sa.outOff[src] + r, sa.dst, ns + target);
             });
             if (lane == 0) { sa.count[d] = cnt + max(0, arrivals - nh); sa.alive[d] = sa.alive[d] - nh + arrivals; }
+        }
+    }
+}
+
+// The fill stage with kFillWarps warps per supercell (one CTA), which share its
+// arrivals 32 at a time; the used and live counts are updated once all have copied.
+constexpr int kFillWarps = 4;
+template <class P>
+__global__ void __launch_bounds__(kFillWarps * 32) k_fill(const __grid_constant__ MigrateArgs<P> a) {
+    if (a.flags[0] != 0 || a.flags[1] != 0) return;   // error, or overflow: the rebuild runs instead
+    const int d = blockIdx.x;
+    const int warp = threadIdx.x >> 5;
+    for (int spi = 0; spi < a.nspecies; spi++) {
+        const MigrateSpecies<P>& sa = a.sp[spi];
+        const int64_t start = sa.start[d];
+        const int nh = sa.nleave[d];
+        const int cnt = sa.count[d];
+        const int alive = sa.alive[d];
+        const int arrivals = forArrivals(
+            a, sa, d,
+            [&](int k, int src, int slot, int) {
+                const int target = k < nh ? sa.llist[start + k] : cnt + (k - nh);
+                copyParticle(sa.b, sa.start[src] + slot, sa.a, start + target);
+            },
+            warp, kFillWarps);
+        __syncthreads();   // every warp has read count and alive
+        if (threadIdx.x == 0) {
+            sa.count[d] = cnt + max(0, arrivals - nh);
+            sa.alive[d] = alive - nh + arrivals;
         }
     }
 }
