@@ -5,9 +5,10 @@
 //
 // One CTA owns one supercell.  It stages the E/B tile of nodes [m-2, m+S+3)
 // per dimension (periodic) into shared memory, accumulates the supercell's
-// current in a shared-memory tile of the same extent (64-bit fixed point,
-// native integer shared-memory atomics), and adds the tile to the global
-// accumulator once (periodic) at the end -- the GPU form of pica's
+// current in a shared-memory tile of the same extent (FP32 form: exact fixed
+// point in split 32-bit words, native integer shared-memory atomics; FP64 form:
+// FP64, warp lanes on one node summed before the atomic), and adds the tile to the
+// global field once (periodic) at the end -- the GPU form of pica's
 // FieldInterpolatorCICSupercell / CurrentDepositorCICSupercell pair
 // (fieldInterpolation/FieldInterpolatorYeeGrid.h:188-283,
 //  currentDeposition/CurrentDepositorYeeGrid.h:168-264).
