@@ -13,6 +13,11 @@ to pinned host memory every step (`e2e`), the push kernel against the HBM
 roofline, the FP64 plain form of the same workload, and the oracle
 restatement timed on this machine's host cores (`cpu_baseline`).
 
+`--workload two_stream` / `--workload weibel` time the same step on the
+two-stream (256x256x128, 8.4e8 electrons, CIC) and Weibel (256^3, 2.1e9
+electrons and ions, TSC) plasmas instead, generated on the device; their
+lines carry `value`, the push roofline and the clocks only.
+
 `--impl reference` times the CPU implementation of the same step instead
 (the oracle restatement built from this tree, all host cores).
 """
@@ -88,7 +93,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--edge", type=int, default=128, help="grid edge (cells); 128 is the reference workload")
-    ap.add_argument("--resort-every", type=int, default=2, help="in-supercell cell sort cadence (steps)")
+    ap.add_argument("--workload", default="thermal", choices=["thermal", "two_stream", "weibel"],
+                    help="thermal: 128^3 x 100 ppc (the headline); two_stream: 256x256x128, 10-190 ppc, CIC; "
+                         "weibel: 256^3, electrons and ions, 2.1e9 particles (both generated on the device)")
+    ap.add_argument("--resort-every", type=int, default=None,
+                    help="in-supercell cell sort cadence (steps; default 2, two_stream 4)")
     ap.add_argument("--variant", type=int, default=-1, help="push-kernel launch variant (-1: autotune)")
     ap.add_argument("--batched", type=int, default=64, help="members of the batching-form run (0: skip)")
     ap.add_argument("--batched-full", action="store_true",
@@ -180,6 +189,18 @@ def make_workload(edge, form):
     return wl
 
 
+def named_workload(name):
+    """The two-stream (256x256x128, CIC) and Weibel (256^3, TSC, two species) plasmas."""
+    from pica_gb300 import workloads
+
+    wl = workloads.config3() if name == "two_stream" else workloads.config5()
+    desc = {"two_stream": "two-stream 256x256x128 cells, two electron beams +-0.2c along x, density "
+                          "1 + 0.9 cos(2 pi x / Lx) (10-190 ppc), FP32 cell+offset form, CIC, Esirkepov, supercell 4^3",
+            "weibel": "Weibel 256^3 cells, electrons and ions (m_i = 100 m_e), beams +-0.3c along z, 32 ppc per "
+                      "species per beam, FP32 cell+offset form, TSC, Esirkepov, supercell 4^3"}[name]
+    return wl, desc
+
+
 def cpu_sample(args, steps=None, seconds=None):
     """Oracle restatement of the same step on a 32^3-cell block of the workload (same ppc,
     supercell, form factor and deposition), all host cores.  Returns (value, cores, sample)."""
@@ -256,17 +277,30 @@ def main():
         torch.cuda.synchronize()
 
     # ---------------- FP32 form, device-resident ----------------
-    wl = make_workload(args.edge, pg.FORM_FP32_CELL)
-    spec = wl["specs"][0]
+    headline = args.workload == "thermal"
     from pica_gb300.replicas import job_throughput, replica_seed
-    spec.seed = replica_seed(spec.seed, rank)   # independent replica per rank (weak scaling)
-    parts = pg.generate_plasma(spec)
-    npart = len(parts["x"])
-    ncells = int(np.prod(wl["sim"]["n"]))
-    sim = pg.Simulation(**wl["sim"], resort_every=args.resort_every)
     stream = torch.cuda.current_stream()
+    if headline:
+        wl = make_workload(args.edge, pg.FORM_FP32_CELL)
+        desc = (f"thermal electron plasma {args.edge}^3 cells x 100 ppc, FP32 cell+offset form, TSC, Esirkepov, "
+                "supercell 4^3, Boris, periodic")
+        resort = 2 if args.resort_every is None else args.resort_every
+    else:
+        wl, desc = named_workload(args.workload)
+        resort = wl["sim"].get("resort_every", 2) if args.resort_every is None else args.resort_every
+    for spec in wl["specs"]:
+        spec.seed = replica_seed(spec.seed, rank)   # independent replica per rank (weak scaling)
+    ncells = int(np.prod(wl["sim"]["n"]))
+    sim = pg.Simulation(**dict(wl["sim"], resort_every=resort))
     sim.set_stream(stream.cuda_stream)
-    sim.upload_particles(*[parts[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w")], parts["species"])
+    if headline:
+        parts = pg.generate_plasma(wl["specs"][0])
+        sim.upload_particles(*[parts[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w")], parts["species"])
+        npart = len(parts["x"])
+    else:
+        sim.generate_plasma(wl["specs"])   # on the device: no host copy of 1e9 particles
+        parts = None
+        npart = sim.num_particles()
     sim.upload_fields([np.zeros(wl["sim"]["n"])] * 9)
     dt = wl["sim"]["dt"]
 
@@ -311,8 +345,9 @@ def main():
     peak, peak_kind = measured_hbm_peak()
     alg_bytes = BYTES_PER_PARTICLE_FP32 * npart + PUSH_GRID_BYTES_PER_CELL_FP32 * ncells
     achieved = alg_bytes / push_avg / 1e9
-    tpp = profiled_traffic_per_particle()
-    roofline = {"bound": "hbm", "kernel": "k_push<fp32, TSC, Esirkepov>", "achieved": achieved, "peak": peak,
+    tpp = profiled_traffic_per_particle() if headline else None
+    kname = "CIC" if wl["sim"]["shape"] == pg.SHAPE_CIC else "TSC"
+    roofline = {"bound": "hbm", "kernel": f"k_push_cell_esirkepov<{kname}>", "achieved": achieved, "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": None if tpp is None else tpp * npart,
                 "algorithmic_bytes_per_launch": alg_bytes, "push_ms": 1e3 * push_avg,
@@ -322,7 +357,7 @@ def main():
 
     # ---------------- e2e through the C ABI with host buffers ----------------
     e2e = None
-    if True:
+    if headline and args.e2e_steps > 0:
         comps = 8
         alloc = 0
         host = []
@@ -375,7 +410,7 @@ def main():
 
     # ---------------- FP64 plain form of the same workload ----------------
     fp64 = None
-    if args.fp64_steps > 0:
+    if headline and args.fp64_steps > 0:
         wl64 = make_workload(args.edge, pg.FORM_FP64_PLAIN)
         s64 = pg.Simulation(**wl64["sim"])
         s64.set_stream(stream.cuda_stream)
@@ -395,12 +430,12 @@ def main():
 
     # ---------------- batching form: many plasmas, persistent push + CUDA graph ----------------
     batched = None
-    if args.batched > 0 and rank == 0:
+    if headline and args.batched > 0 and rank == 0:
         batched = batched_measure(args)
 
     # ---------------- FP32 form against the FP64 plain form (error metrics) ----------------
     errors = None
-    if args.validate_steps > 0 and rank == 0:
+    if headline and args.validate_steps > 0 and rank == 0:
         from pica_gb300 import validate
         errors = validate.compare_forms(n=(32, 32, 32), ppc=100, steps=args.validate_steps, every=20)
 
@@ -410,15 +445,14 @@ def main():
             dist.destroy_process_group()
         return
     cpu = None
-    if not args.no_cpu_baseline:
+    if headline and not args.no_cpu_baseline:
         v, cores, sample, _ = cpu_sample(args, seconds=args.cpu_seconds)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": 1e3 * elapsed / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": f"thermal electron plasma {args.edge}^3 cells x 100 ppc ({npart} electrons per GPU), "
-                               "FP32 cell+offset form, TSC, Esirkepov, supercell 4^3, Boris, periodic",
+        "config": {"workload": f"{desc} ({npart} particles per GPU)",
                    "particles_per_gpu": npart, "cells": ncells, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (particle state %.1f GB)" % (npart * 32 / 1e9)},
         "roofline": roofline,
@@ -428,7 +462,7 @@ def main():
         "fp32_vs_fp64_errors": errors,
         "batched": batched,
         "tuning": {"push_variant": sim_variant, "variant_s_per_step": {str(k): v for k, v in tune.items()},
-                   "resort_every": args.resort_every},
+                   "resort_every": resort},
     }
     print(json.dumps(line), flush=True)
     if dist is not None:

@@ -228,6 +228,18 @@ int     pica_checkpoint_save(pica_ctx* ctx, const char* path);
 int64_t pica_step_count(pica_ctx* ctx);
 int     pica_checkpoint_load(pica_ctx* ctx, const char* path);
 
+/* Synthetic plasma generated on the device, in place of pica_upload_particles
+ * (FP32 cell form): the populations `specs[0..nspecs)` (grid and cell size equal
+ * to the context's; at most 8 per species) replace the particle state.  The
+ * particles are those pica_plasma_generate draws for the same specifications,
+ * each in the cell it was drawn in, with the in-cell offset the FP32 rounding
+ * of the uniform draw; they are stored in the order pica_upload_particles gives
+ * that output (supercell, cell, population, particle).  No host memory holds the
+ * ensemble.  pica has no generator; this replaces a host loop of
+ * EnsembleSupercells::add (particles/EnsembleSupercells.h:41-45) over generated
+ * particles.  PICA_ERR_INVALID for the FP64 form or a bad specification. */
+int     pica_generate_plasma(pica_ctx* ctx, const pica_plasma_spec* specs, int32_t nspecs);
+
 /* Host-side plasma set-up (no device work). */
 int64_t pica_plasma_count(const pica_plasma_spec* spec);
 int     pica_plasma_generate(const pica_plasma_spec* spec, int32_t threads, double* x, double* y, double* z,

@@ -189,6 +189,11 @@ public:
         return d;
     }
     int64_t stepCount() { return pica_step_count(ctx_); }
+    // Synthetic plasma generated on the device in place of ensemble().upload()
+    // (FP32 cell form; see pica_generate_plasma).
+    void generatePlasma(const std::vector<pica_plasma_spec>& specs) {
+        check(ctx_, pica_generate_plasma(ctx_, specs.data(), (int32_t)specs.size()));
+    }
     // Complete state between steps; a Simulation of the same Config loaded from it
     // continues like this one (FP32 form: bit for bit).
     void saveCheckpoint(const std::string& path) { check(ctx_, pica_checkpoint_save(ctx_, path.c_str())); }

@@ -123,6 +123,14 @@ class Simulation:
         self._check(self.lib.pica_upload_particles(self.ctx, len(arrs[0]), *[_dp(a) for a in arrs],
                                                    None if sp is None else _ip(sp)))
 
+    def generate_plasma(self, specs):
+        """Synthetic plasma drawn on the device (FP32 cell form) in place of an upload:
+        ``specs`` are ``plasma_spec`` populations on this grid (see pica_generate_plasma)."""
+        if isinstance(specs, PicaPlasmaSpec):
+            specs = [specs]
+        arr = (PicaPlasmaSpec * len(specs))(*specs)
+        self._check(self.lib.pica_generate_plasma(self.ctx, arr, len(specs)))
+
     def num_particles(self):
         n = int(self.lib.pica_num_particles(self.ctx))
         if n < 0:

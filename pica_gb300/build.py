@@ -18,11 +18,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "-I", os.path.join(HERE, "..", "include")]
 UNITS = [
-    ("pica_api.cu", []),
+    ("pica_api.cu", ["-Xcompiler", "-ffp-contract=off"]),
     ("push_fp64.cu", ["--fmad=false"]),
     ("push_fp32.cu", []),
     ("grid_kernels.cu", ["--fmad=false"]),
     ("noalloc.cu", ["--fmad=false"]),
+    ("plasma_gen.cu", ["--fmad=false"]),
 ]
 
 

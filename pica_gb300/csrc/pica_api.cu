@@ -125,6 +125,25 @@ void layoutFrom(const pica_ctx* c, const std::vector<int32_t>& counts, std::vect
     }
 }
 
+// Largest particle count of one supercell and species: its capacity (count plus
+// slack) stays an int32.
+constexpr int64_t kMaxSupercellCount = 1ll << 30;
+
+// Particles per cell of x-plane i of a synthetic population (host generator and
+// device generator alike): round(ppc (1 + a cos(2 pi (i + 1/2) / nx))).
+int cellCount(const pica_plasma_spec* s, int i) {
+    const double f = 1.0 + s->density_mod * std::cos(2.0 * 3.14159265358979323846 * (i + 0.5) / s->n[0]);
+    return (int)std::lround(s->ppc * f);
+}
+
+// Fixed-point unit of the J accumulators: kmax = 2^ceil(log2 max |q w| max(c, h/dt)).
+void setCurrentUnit(pica_ctx* ctx, double maxQW) {
+    const pica_config& c = ctx->cfg;
+    const double hmax = std::max(std::max(c.h[0], c.h[1]), c.h[2]);
+    const double bound = maxQW * std::max(kC, hmax / c.dt);
+    ctx->kmax = bound > 0 ? std::ldexp(1.0, (int)std::ceil(std::log2(bound))) : 1.0;
+}
+
 // Fraction bits of the J fixed point for the current layout: a node can receive one
 // contribution per particle of every supercell whose tile covers it.
 void updateJFrac(pica_ctx* ctx) {
@@ -194,6 +213,28 @@ int ensureOutbox(pica_ctx* ctx, int spi, int64_t slots) {
     const int64_t grown = withHeadroom(slots);
     for (int k = 0; k < ctx->ncomp; k++) CK(cudaMalloc(&S.outbox[k], grown * ctx->compBytes[k]));
     S.outSlots = grown;
+    return PICA_OK;
+}
+
+// Fresh layout of species q for the given per-supercell counts (slots
+// [start, start + count) used, none dead), in host and device copies.
+int installLayout(pica_ctx* ctx, int q, const std::vector<int32_t>& counts) {
+    SpeciesState& S = ctx->sp[q];
+    int64_t total;
+    layoutFrom(ctx, counts, S.h_start, S.h_cap, total);
+    S.layoutSlots = total;
+    int rc;
+    if ((rc = ensureBuffer(ctx, q, 0, total)) || (rc = ensureBuffer(ctx, q, 1, total)) ||
+        (rc = ensureSlotArrays(ctx, q, total)))
+        return rc;
+    // Ordered on the context's stream (which may be a non-blocking stream), and
+    // complete before return.
+    CK(cudaMemcpyAsync(S.d_start, S.h_start.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.d_cap, S.h_cap.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.d_count, counts.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.d_alive, counts.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(S.d_nleave, 0, ctx->nscTot * 4, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return PICA_OK;
 }
 
@@ -464,38 +505,27 @@ int pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const doubl
     });
     if (bad == 1) return fail(ctx, PICA_ERR_INVALID, "species index out of range");
     if (bad == 2) return fail(ctx, PICA_ERR_INVALID, "non-finite value or position outside [0, n h)");
-    // Fixed-point unit of the J accumulators: kmax = 2^ceil(log2 max |q w| max(c, h/dt)).
     {
-        double hmax = std::max(std::max(c.h[0], c.h[1]), c.h[2]);
-        double vmax = std::max(kC, hmax / c.dt), bound = 0.0;
-        for (int64_t i = 0; i < n; i++) {
-            const int q = species ? species[i] : 0;
-            bound = std::max(bound, std::fabs(c.charge[q] * w[i]) * vmax);
-        }
-        ctx->kmax = bound > 0 ? std::ldexp(1.0, (int)std::ceil(std::log2(bound))) : 1.0;
+        double maxQW = 0.0;
+        for (int64_t i = 0; i < n; i++) maxQW = std::max(maxQW, std::fabs(c.charge[species ? species[i] : 0] * w[i]));
+        setCurrentUnit(ctx, maxQW);
     }
     const int64_t nkeys = (int64_t)nsp * ctx->nscTot;
     std::vector<int64_t> cnt(nkeys + 1, 0);
     for (int64_t i = 0; i < n; i++) cnt[key[i] + 1]++;
     // Per species layout.
     for (int q = 0; q < nsp; q++) {
-        SpeciesState& S = ctx->sp[q];
         std::vector<int32_t> counts(ctx->nscTot);
-        for (int s = 0; s < ctx->nscTot; s++) counts[s] = (int32_t)cnt[(int64_t)q * ctx->nscTot + s + 1];
-        int64_t total;
-        layoutFrom(ctx, counts, S.h_start, S.h_cap, total);
-        S.layoutSlots = total;
+        for (int s = 0; s < ctx->nscTot; s++) {
+            const int64_t v = cnt[(int64_t)q * ctx->nscTot + s + 1];
+            if (v > kMaxSupercellCount) return fail(ctx, PICA_ERR_LIMIT, "too many particles in one supercell");
+            counts[s] = (int32_t)v;
+        }
         int rc;
-        if ((rc = ensureBuffer(ctx, q, 0, total)) || (rc = ensureBuffer(ctx, q, 1, total)) ||
-            (rc = ensureSlotArrays(ctx, q, total)))
-            return rc;
-        CK(cudaMemcpy(S.d_start, S.h_start.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(S.d_cap, S.h_cap.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(S.d_count, counts.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(S.d_alive, counts.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
-        CK(cudaMemset(S.d_nleave, 0, ctx->nscTot * 4));
+        if ((rc = installLayout(ctx, q, counts))) return rc;
     }
     updateJFrac(ctx);
+    ctx->steps = 0;
     // Slot of each particle: start of its supercell + its rank by (local cell, input order).
     std::vector<int64_t> base2((size_t)nkeys * S3 + 1, 0);
     for (int64_t i = 0; i < n; i++) base2[(size_t)key[i] * S3 + lcell[i] + 1]++;
@@ -534,9 +564,109 @@ int pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const doubl
                     }
                 }
             });
-            CK(cudaMemcpy(S.buf[0][k], host.data(), total * ctx->compBytes[k], cudaMemcpyHostToDevice));
+            // From pageable memory: staged before the call returns, ordered on the stream.
+            CK(cudaMemcpyAsync(S.buf[0][k], host.data(), total * ctx->compBytes[k], cudaMemcpyHostToDevice,
+                               ctx->stream));
         }
     }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PICA_OK;
+}
+
+int pica_generate_plasma(pica_ctx* ctx, const pica_plasma_spec* specs, int32_t nspecs) {
+    if (!ctx) return PICA_ERR_INVALID;
+    if (!specs || nspecs < 1) return fail(ctx, PICA_ERR_INVALID, "no plasma specification");
+    if (ctx->fp64) return fail(ctx, PICA_ERR_INVALID, "the device generator writes the FP32 cell form only");
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "generate while a migration is pending");
+    const pica_config& c = ctx->cfg;
+    const int nx = c.n[0];
+    std::vector<int> perSpecies(c.nspecies, 0);
+    double maxQW = 0.0;
+    for (int k = 0; k < nspecs; k++) {
+        const pica_plasma_spec& g = specs[k];
+        if (pica_plasma_count(&g) < 0) return fail(ctx, PICA_ERR_INVALID, "invalid plasma specification");
+        for (int d = 0; d < 3; d++)
+            if (g.n[d] != c.n[d] || g.h[d] != c.h[d])
+                return fail(ctx, PICA_ERR_INVALID, "plasma specification on another grid than the context's");
+        if (g.species < 0 || g.species >= c.nspecies) return fail(ctx, PICA_ERR_INVALID, "species index out of range");
+        if ((g.nbeams != 1 && g.nbeams != 2) || g.drift_axis < 0 || g.drift_axis > 2)
+            return fail(ctx, PICA_ERR_INVALID, "beams must be 1 or 2 and the drift axis 0, 1 or 2");
+        if (!std::isfinite(g.sigma_u) || !std::isfinite(g.drift_u) || !std::isfinite(g.weight) ||
+            !std::isfinite(g.ppc) || !std::isfinite(g.density_mod))
+            return fail(ctx, PICA_ERR_INVALID, "non-finite plasma parameter");
+        if (++perSpecies[g.species] > kGenMaxSpecs)
+            return fail(ctx, PICA_ERR_LIMIT, "more than 8 plasma specifications for one species");
+        maxQW = std::max(maxQW, std::fabs(c.charge[g.species] * g.weight));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    // Particles per cell of every x-plane, from the host's count rule (the layout
+    // below and the device kernel both read this table).
+    std::vector<int32_t> per((size_t)nspecs * nx);
+    for (int k = 0; k < nspecs; k++)
+        for (int i = 0; i < nx; i++) {
+            const int v = cellCount(&specs[k], i);
+            if (v < 0) return fail(ctx, PICA_ERR_INVALID, "negative particle count");
+            per[(size_t)k * nx + i] = v;
+        }
+    const int64_t cellsYZ = (int64_t)c.sc[1] * c.sc[2];
+    for (int q = 0; q < c.nspecies; q++) {
+        std::vector<int32_t> counts(ctx->nscTot);
+        for (int s = 0; s < ctx->nscTot; s++) {
+            const int sx = s / (ctx->nsc[1] * ctx->nsc[2]);
+            int64_t v = 0;
+            for (int k = 0; k < nspecs; k++)
+                if (specs[k].species == q)
+                    for (int lx = 0; lx < c.sc[0]; lx++) v += (int64_t)per[(size_t)k * nx + sx * c.sc[0] + lx] * cellsYZ;
+            if (v > kMaxSupercellCount) return fail(ctx, PICA_ERR_LIMIT, "too many particles in one supercell");
+            counts[s] = (int32_t)v;
+        }
+        int rc;
+        if ((rc = installLayout(ctx, q, counts))) return rc;
+    }
+    setCurrentUnit(ctx, maxQW);
+    updateJFrac(ctx);
+    ctx->cur = 0;
+    ctx->steps = 0;
+    int32_t* d_per = nullptr;
+    CK(cudaMalloc(&d_per, per.size() * 4));
+    int err = 0;
+    for (int q = 0; q < c.nspecies && !err; q++) {
+        SpeciesState& S = ctx->sp[q];
+        for (int k = 0; k < ctx->ncomp && !err; k++)   // unused slots read as zero, as after an upload
+            err = cudaMemsetAsync(S.buf[0][k], 0, S.layoutSlots * ctx->compBytes[k], ctx->stream);
+        if (err || perSpecies[q] == 0) continue;
+        GenArgs a{};
+        for (int d = 0; d < 3; d++) {
+            a.n[d] = c.n[d];
+            a.S[d] = c.sc[d];
+            a.nsc[d] = ctx->nsc[d];
+        }
+        std::vector<int32_t> mine;
+        for (int k = 0; k < nspecs; k++) {
+            if (specs[k].species != q) continue;
+            const pica_plasma_spec& g = specs[k];
+            a.sp[a.nspecs] = GenSpec{g.sigma_u, g.drift_u, g.weight, g.seed, g.nbeams, g.drift_axis};
+            mine.insert(mine.end(), per.begin() + (size_t)k * nx, per.begin() + (size_t)(k + 1) * nx);
+            a.nspecs++;
+        }
+        // This species' rows of the table, in the order of its populations (a copy from
+        // pageable memory: staged before the call returns).
+        err = cudaMemcpyAsync(d_per, mine.data(), mine.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+        if (err) break;
+        a.per = d_per;
+        a.start = S.d_start;
+        CellPtrs& b = a.buf;
+        b.cell = (uint32_t*)S.buf[0][0];
+        b.ox = (float*)S.buf[0][1]; b.oy = (float*)S.buf[0][2]; b.oz = (float*)S.buf[0][3];
+        b.ux = (float*)S.buf[0][4]; b.uy = (float*)S.buf[0][5]; b.uz = (float*)S.buf[0][6];
+        b.w = (float*)S.buf[0][7];
+        err = launchGenerate(a, (int)ctx->nscTot, ctx->stream);
+        ctx->launches++;
+        if (!err) err = cudaStreamSynchronize(ctx->stream);   // d_per is rewritten for the next species
+    }
+    if (!err) err = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_per);
+    if (err) return fail(ctx, PICA_ERR_CUDA, std::string("device generation: ") + cudaGetErrorString((cudaError_t)err));
     return PICA_OK;
 }
 
@@ -1001,25 +1131,6 @@ int pica_state_copy(pica_ctx* ctx, int32_t species, int32_t comp, void* host, in
 // thread count.  Positions uniform in the cell; u = drift + N(0, sigma) per
 // component (Box-Muller).
 // ---------------------------------------------------------------------------
-static inline uint64_t mix64(uint64_t z) {
-    z += 0x9E3779B97F4A7C15ull;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-static inline double uni(uint64_t seed, int64_t cell, int64_t p, int draw) {
-    const uint64_t key = ((uint64_t)cell << 24) ^ ((uint64_t)p << 4) ^ (uint64_t)draw;
-    return (double)(mix64(mix64(seed) ^ key) >> 11) * 0x1.0p-53;
-}
-static inline double normal(uint64_t seed, int64_t cell, int64_t p, int draw) {
-    const double u1 = 1.0 - uni(seed, cell, p, draw), u2 = uni(seed, cell, p, draw + 1);
-    return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2);
-}
-static inline int cellCount(const pica_plasma_spec* s, int i) {
-    const double f = 1.0 + s->density_mod * std::cos(2.0 * 3.14159265358979323846 * (i + 0.5) / s->n[0]);
-    return (int)std::lround(s->ppc * f);
-}
-
 int64_t pica_plasma_count(const pica_plasma_spec* s) {
     if (!s || s->n[0] <= 0 || s->n[1] <= 0 || s->n[2] <= 0 || s->ppc < 0) return PICA_ERR_INVALID;
     int64_t total = 0;
@@ -1042,11 +1153,11 @@ int pica_plasma_generate(const pica_plasma_spec* s, int32_t threads, double* x, 
                 for (int k = 0; k < nz; k++) {
                     const int64_t cell = ((int64_t)i * ny + j) * nz + k;
                     for (int p = 0; p < per; p++, o++) {
-                        x[o] = ((double)i + uni(s->seed, cell, p, 0)) * s->h[0];
-                        y[o] = ((double)j + uni(s->seed, cell, p, 1)) * s->h[1];
-                        z[o] = ((double)k + uni(s->seed, cell, p, 2)) * s->h[2];
-                        double u3[3] = {s->sigma_u * normal(s->seed, cell, p, 3), s->sigma_u * normal(s->seed, cell, p, 5),
-                                        s->sigma_u * normal(s->seed, cell, p, 7)};
+                        x[o] = ((double)i + uniDraw(s->seed, cell, p, 0)) * s->h[0];
+                        y[o] = ((double)j + uniDraw(s->seed, cell, p, 1)) * s->h[1];
+                        z[o] = ((double)k + uniDraw(s->seed, cell, p, 2)) * s->h[2];
+                        double u3[3] = {s->sigma_u * normalDraw(s->seed, cell, p, 3), s->sigma_u * normalDraw(s->seed, cell, p, 5),
+                                        s->sigma_u * normalDraw(s->seed, cell, p, 7)};
                         if (s->nbeams == 2) u3[s->drift_axis] += (p % 2 == 0) ? s->drift_u : -s->drift_u;
                         else u3[s->drift_axis] += s->drift_u;
                         ux[o] = u3[0]; uy[o] = u3[1]; uz[o] = u3[2];

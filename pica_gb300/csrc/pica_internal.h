@@ -18,6 +18,7 @@
 //   sorted by cell into B, and A and B swap.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -44,6 +45,27 @@ __host__ __device__ inline uint32_t packCell(int x, int y, int z) {
 }
 __host__ __device__ inline void unpackCell(uint32_t c, int& x, int& y, int& z) {
     x = (int)(c >> 21); y = (int)((c >> 10) & 0x7FFu); z = (int)(c & 0x3FFu);
+}
+
+// Counter-based draws of the synthetic plasma generator, shared by the host
+// generator and the device generator: draw `draw` of particle p of cell `cell`
+// is the splitmix64 finaliser (S. Vigna) of the seed's hash xor a key made
+// from (cell, p, draw), so any particle can be drawn alone, in any order.
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+// Uniform in [0, 1) with 53 random bits.
+__host__ __device__ inline double uniDraw(uint64_t seed, int64_t cell, int64_t p, int draw) {
+    const uint64_t key = ((uint64_t)cell << 24) ^ ((uint64_t)p << 4) ^ (uint64_t)draw;
+    return (double)(mix64(mix64(seed) ^ key) >> 11) * 0x1.0p-53;
+}
+// Standard normal by Box-Muller from draws `draw` and `draw + 1`.
+__host__ __device__ inline double normalDraw(uint64_t seed, int64_t cell, int64_t p, int draw) {
+    const double u1 = 1.0 - uniDraw(seed, cell, p, draw), u2 = uniDraw(seed, cell, p, draw + 1);
+    return sqrt(-2.0 * log(u1)) * cos(2.0 * 3.14159265358979323846 * u2);
 }
 
 struct PlainPtrs {  // FP64 plain form particle SoA
@@ -221,6 +243,23 @@ struct RhoArgs {
     double q[kMaxSpecies];
 };
 int launchRho(const RhoArgs& a, double* rho, cudaStream_t s);
+// Device generator of a synthetic plasma (pica_generate_plasma): the populations
+// of one species, written in the FP32 cell form's layout (one CTA per supercell).
+constexpr int kGenMaxSpecs = 8;
+struct GenSpec {
+    double sigma, drift, weight;
+    uint64_t seed;
+    int nbeams, axis;
+};
+struct GenArgs {
+    int n[3], S[3], nsc[3];
+    int nspecs;                 // populations of this species, in the caller's order
+    GenSpec sp[kGenMaxSpecs];
+    const int32_t* per;         // particles per cell of x-plane i of population k at [k * n[0] + i]
+    const int64_t* start;       // first slot of each supercell
+    CellPtrs buf;
+};
+int launchGenerate(const GenArgs& a, int nscTot, cudaStream_t s);
 // Gauss residual: max |div E - 4 pi (rho + bg)| and max |rho|; partial: 2*kReduceBlocks doubles.
 int launchGauss(bool fp64, void* const* f, const double* rho, const int* n, const double* h, double bg,
                 double* partial, double* out2, cudaStream_t s);
