@@ -92,7 +92,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--edge", type=int, default=128, help="grid edge (cells); 128 is the reference workload")
+    ap.add_argument("--edge", type=int, default=None,
+                    help="grid edge in cells (thermal: 128; two_stream: 256, grid edge x edge x edge/2; weibel: 256)")
     ap.add_argument("--workload", default="thermal", choices=["thermal", "two_stream", "weibel"],
                     help="thermal: 128^3 x 100 ppc (the headline); two_stream: 256x256x128, 10-190 ppc, CIC; "
                          "weibel: 256^3, electrons and ions, 2.1e9 particles (both generated on the device)")
@@ -189,15 +190,20 @@ def make_workload(edge, form):
     return wl
 
 
-def named_workload(name):
-    """The two-stream (256x256x128, CIC) and Weibel (256^3, TSC, two species) plasmas."""
+def named_workload(name, edge=None):
+    """The two-stream (256x256x128, CIC) and Weibel (256^3, TSC, two species) plasmas;
+    `edge` scales the grid (a smaller case of the same plasma for profiling)."""
     from pica_gb300 import workloads
 
-    wl = workloads.config3() if name == "two_stream" else workloads.config5()
-    desc = {"two_stream": "two-stream 256x256x128 cells, two electron beams +-0.2c along x, density "
-                          "1 + 0.9 cos(2 pi x / Lx) (10-190 ppc), FP32 cell+offset form, CIC, Esirkepov, supercell 4^3",
-            "weibel": "Weibel 256^3 cells, electrons and ions (m_i = 100 m_e), beams +-0.3c along z, 32 ppc per "
-                      "species per beam, FP32 cell+offset form, TSC, Esirkepov, supercell 4^3"}[name]
+    e = edge or 256
+    if name == "two_stream":
+        wl = workloads.two_stream(n=(e, e, e // 2))
+        desc = (f"two-stream {e}x{e}x{e // 2} cells, two electron beams +-0.2c along x, density "
+                "1 + 0.9 cos(2 pi x / Lx) (10-190 ppc), FP32 cell+offset form, CIC, Esirkepov, supercell 4^3")
+    else:
+        wl = workloads.weibel(n=(e, e, e))
+        desc = (f"Weibel {e}^3 cells, electrons and ions (m_i = 100 m_e), beams +-0.3c along z, 32 ppc per "
+                "species per beam, FP32 cell+offset form, TSC, Esirkepov, supercell 4^3")
     return wl, desc
 
 
@@ -244,7 +250,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / (args.steps + args.warmup),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": f"thermal electron plasma {args.edge}^3 x 100 ppc, TSC, Esirkepov, supercell 4^3 "
+        "config": {"workload": f"thermal electron plasma {args.edge or 128}^3 x 100 ppc, TSC, Esirkepov, supercell 4^3 "
                                f"(CPU step on a 32^3 block of it)", "parallelism": "OpenMP over supercells"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -281,12 +287,13 @@ def main():
     from pica_gb300.replicas import job_throughput, replica_seed
     stream = torch.cuda.current_stream()
     if headline:
+        args.edge = args.edge or 128
         wl = make_workload(args.edge, pg.FORM_FP32_CELL)
         desc = (f"thermal electron plasma {args.edge}^3 cells x 100 ppc, FP32 cell+offset form, TSC, Esirkepov, "
                 "supercell 4^3, Boris, periodic")
         resort = 2 if args.resort_every is None else args.resort_every
     else:
-        wl, desc = named_workload(args.workload)
+        wl, desc = named_workload(args.workload, args.edge)
         resort = wl["sim"].get("resort_every", 2) if args.resort_every is None else args.resort_every
     for spec in wl["specs"]:
         spec.seed = replica_seed(spec.seed, rank)   # independent replica per rank (weak scaling)

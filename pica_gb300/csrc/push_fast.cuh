@@ -98,6 +98,71 @@ constexpr int kQWords = 11;  // queued window change: o[3], on[3], kq[3], packed
 constexpr int kStayNodes = 3;    // stay-in-cell window: rho-lattice nodes lc-1 .. lc+1 per dimension
 constexpr int kStayValues = 54;  // its face values: 3 components x 2 faces x 3 x 3
 
+// Entry i (a runtime index) of an N-entry register array, by selects, so that
+// the array stays in registers.
+template <int N>
+__device__ __forceinline__ float pickN(const float* a, int i) {
+    float v = a[0];
+#pragma unroll
+    for (int k = 1; k < N; k++) v = (i == k) ? a[k] : v;
+    return v;
+}
+
+// esirkepov() (push_kernels.cuh) in FP32 with the loop over the transverse node
+// pair rolled: the same values from the same expressions, in about a tenth of
+// the code.  The general window runs once per queue drain, straight through, so
+// its unrolled form is fetched from the instruction cache hierarchy at every
+// call; the selects of the rolled loop cost less than those fetch stalls.  A node
+// pair outside both shapes (zero transverse factor) adds nothing and is skipped.
+template <int NW, typename Tile>
+__device__ __forceinline__ void esirkepovRolled(const Tile& jt, int TT, int T1, int T2, const int* b,
+                                                const float (*s0)[NW], const float (*s1)[NW], const float* k) {
+    float ds[3][NW];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int i = 0; i < NW; i++) ds[d][i] = s1[d][i] - s0[d][i];
+    const float hf = 0.5f, th = (float)kThird;
+#pragma unroll 1
+    for (int q = 0; q < NW * NW; q++) {
+        const int u = q / NW, v = q - u * NW;
+        const float a0u = pickN<NW>(s0[0], u), d0u = pickN<NW>(ds[0], u);
+        const float a1u = pickN<NW>(s0[1], u), d1u = pickN<NW>(ds[1], u);
+        const float a1v = pickN<NW>(s0[1], v), d1v = pickN<NW>(ds[1], v);
+        const float a2v = pickN<NW>(s0[2], v), d2v = pickN<NW>(ds[2], v);
+        // Jx on transverse nodes (j, l) = (u, v).
+        const float yz = a1u * a2v + hf * (d1u * a2v + a1u * d2v) + th * (d1u * d2v);
+        if (yz != 0.f) {
+            float acc = 0.f;
+#pragma unroll
+            for (int i = 0; i < NW - 1; i++) {
+                acc = acc + ds[0][i] * yz;
+                jt.add(((b[0] + i + 1) * T1 + (b[1] + u)) * T2 + (b[2] + v), acc * k[0]);
+            }
+        }
+        // Jy on (i, l) = (u, v).
+        const float xz = a0u * a2v + hf * (d0u * a2v + a0u * d2v) + th * (d0u * d2v);
+        if (xz != 0.f) {
+            float acc = 0.f;
+#pragma unroll
+            for (int j = 0; j < NW - 1; j++) {
+                acc = acc + ds[1][j] * xz;
+                jt.add(TT + ((b[0] + u) * T1 + (b[1] + j + 1)) * T2 + (b[2] + v), acc * k[1]);
+            }
+        }
+        // Jz on (i, j) = (u, v).
+        const float xy = a0u * a1v + hf * (d0u * a1v + a0u * d1v) + th * (d0u * d1v);
+        if (xy != 0.f) {
+            float acc = 0.f;
+#pragma unroll
+            for (int l = 0; l < NW - 1; l++) {
+                acc = acc + ds[2][l] * xy;
+                jt.add(2 * TT + ((b[0] + u) * T1 + (b[1] + v)) * T2 + (b[2] + l + 1), acc * k[2]);
+            }
+        }
+    }
+}
+
 // Esirkepov deposit of a particle whose rho-lattice window changes (old shape on
 // nodes lo0.., new on lo1..): general NWn+1-node window with per-lane atomics.
 template <int SHAPE, typename Tile>
@@ -129,7 +194,7 @@ __device__ __forceinline__ void generalWindow(const Tile& jt, int TT, int T1, in
         placeShape<float, NW4, NWn>(s1[d], lo1, base, w1);
         b[d] = base + kG;
     }
-    esirkepov<float, NW4>(jt, TT, T1, T2, b, s0, s1, kq);
+    esirkepovRolled<NW4>(jt, TT, T1, T2, b, s0, s1, kq);
 }
 
 // Fixed-point tile addressed by shared-window byte addresses, for code that is
