@@ -1274,27 +1274,6 @@ void batchSignature(pica_batch* b, std::vector<unsigned char>& sig) {
     put(&b->variant, sizeof b->variant);
 }
 
-template <int NSP>
-void slimArgs(const PushArgs<CellPtrs>& a, PushArgsSlim<NSP>& o) {
-    std::memset(&o, 0, sizeof o);
-    for (int d = 0; d < 3; d++) {
-        o.n[d] = a.n[d]; o.S[d] = a.S[d]; o.nsc[d] = a.nsc[d]; o.T[d] = a.T[d];
-        o.cdth[d] = (float)a.cdth[d]; o.jacc[d] = a.jacc[d];
-    }
-    o.nspecies = a.nspecies;
-    o.tileSplit = a.tileSplit;
-    o.invUnit = (float)a.invUnit;
-    for (int k = 0; k < 6; k++) o.eb[k] = a.eb[k];
-    o.flags = a.flags;
-    for (int q = 0; q < a.nspecies && q < NSP; q++) {
-        const auto& x = a.sp[q];
-        auto& y = o.sp[q];
-        y.buf = x.buf; y.out = x.out; y.start = x.start; y.count = x.count;
-        y.nleave = x.nleave; y.llist = x.llist; y.dir = x.dir; y.ec = (float)x.ec;
-        for (int d = 0; d < 3; d++) y.kq[d] = (float)x.kq[d];
-    }
-}
-
 // Arguments of the persistent push launches for the current layouts (members in
 // work order, batchMembers<NSP>() per launch).
 template <int NSP>

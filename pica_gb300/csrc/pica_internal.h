@@ -20,6 +20,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #include "../../include/pica_gb300.h"
@@ -113,11 +114,11 @@ struct PushArgs {
     SpeciesArgs<P> sp[kMaxSpecies];
 };
 
-// Batching form: the push arguments of up to batchMembers<NSP>() plasmas of at most
-// NSP species travel in the kernel parameters (read-only, so the compiler uses them
-// as it uses the single-plasma kernel's); work item w (one supercell) belongs to
-// plasma k with base[k] <= w < base[k + 1].  Only the fields the FP32 Esirkepov push
-// reads; the FP32 values are the ones the kernel would round the FP64 values to.
+// Arguments of the FP32 Esirkepov push: only the fields it reads, FP64 factors
+// rounded to FP32.  The single-plasma kernel takes one; the batching form takes
+// those of up to batchMembers<NSP>() plasmas of at most NSP species in its kernel
+// parameters, work item w (one supercell) belonging to plasma k with
+// base[k] <= w < base[k + 1].
 struct SpeciesArgsSlim {
     CellPtrs buf;
     CellPtrs out;
@@ -141,6 +142,30 @@ struct PushArgsSlim {
     int* flags;
     SpeciesArgsSlim sp[NSP];
 };
+// The FP32 push arguments of one plasma, FP64 factors rounded to FP32 on the
+// host (the FP32 kernels read only these; a conversion from FP64 in the kernel
+// would run on the narrow FP64 pipe).
+template <int NSP>
+inline void slimArgs(const PushArgs<CellPtrs>& a, PushArgsSlim<NSP>& o) {
+    std::memset(&o, 0, sizeof o);
+    for (int d = 0; d < 3; d++) {
+        o.n[d] = a.n[d]; o.S[d] = a.S[d]; o.nsc[d] = a.nsc[d]; o.T[d] = a.T[d];
+        o.cdth[d] = (float)a.cdth[d]; o.jacc[d] = a.jacc[d];
+    }
+    o.nspecies = a.nspecies;
+    o.tileSplit = a.tileSplit;
+    o.invUnit = (float)a.invUnit;
+    for (int k = 0; k < 6; k++) o.eb[k] = a.eb[k];
+    o.flags = a.flags;
+    for (int q = 0; q < a.nspecies && q < NSP; q++) {
+        const auto& x = a.sp[q];
+        auto& y = o.sp[q];
+        y.buf = x.buf; y.out = x.out; y.start = x.start; y.count = x.count;
+        y.nleave = x.nleave; y.llist = x.llist; y.dir = x.dir; y.ec = (float)x.ec;
+        for (int d = 0; d < 3; d++) y.kq[d] = (float)x.kq[d];
+    }
+}
+
 constexpr int kBatchParamBytes = 31 * 1024;
 template <int NSP>
 constexpr int batchMembers() { return (int)((kBatchParamBytes - 64) / (sizeof(PushArgsSlim<NSP>) + sizeof(int))); }
