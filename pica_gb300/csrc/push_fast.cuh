@@ -3,10 +3,11 @@
 // order (they are generated that way and kept so by the periodic in-supercell
 // sort):
 //
-//  * A warp owns a contiguous segment of 32*K particles of its supercell; lane
+//  * A warp owns contiguous segments of 32*K particles of its supercell; lane
 //    l handles the K consecutive particles lK .. lK+K-1 (the next one's data is
 //    loaded one iteration ahead), so a lane rarely changes cell and the warp's
-//    lanes mostly share one or two cells.
+//    lanes mostly share one or two cells.  The supercell's last segments are cut
+//    into 8 shorter ones so that every warp of the CTA gets the same work.
 //  * Particles that stay in their cell (about 96% per step for a thermal plasma
 //    at half the Courant step) have old and new shapes on the rho-lattice nodes
 //    lc-1 .. lc+1 (TSC: all three; CIC: two of them, by the half of the cell),
@@ -367,18 +368,31 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
         const float kqs[3] = {(float)sa.kq[0] * invU, (float)sa.kq[1] * invU, (float)sa.kq[2] * invU};
         if (threadIdx.x == 0) s_nleave = 0;
         __syncthreads();
-        const int nseg = (count + 32 * K - 1) / (32 * K);
-        for (int seg = warp; seg < nseg; seg += kWarps) {
+        // Work units: full segments of 32 K particles (lane l takes K consecutive
+        // ones), except that the last (full segments mod 8) of them and the remainder
+        // are re-cut into 8 equal sub-segments of 32 subK.  The cut depends only on
+        // the count, so the particles summed together (and every rounding) are the
+        // same for every CTA size, and the warps of a CTA of 2, 4 or 8 warps get the
+        // same number of particle iterations.
+        const int nmain = (count / (32 * K)) & ~7;
+        const int rest = count - nmain * 32 * K;
+        const int subK = (rest + 8 * 32 - 1) / (8 * 32);
+        const int nunits = nmain + (rest > 0 ? 8 : 0);
+        for (int unit = warp; unit < nunits; unit += kWarps) {
+            const int kk = unit < nmain ? K : subK;
+            const int segStart = unit < nmain ? unit * 32 * K : nmain * 32 * K + (unit - nmain) * 32 * subK;
+            const int segEnd = min(count, segStart + 32 * kk);
+            if (segStart >= segEnd) continue;
             float acc[NV];
 #pragma unroll
             for (int k = 0; k < NV; k++) acc[k] = 0.0f;
             int accKey = -1;
             int nPark = 0;   // warp-uniform
-            const int i0 = seg * 32 * K + lane * K;
+            const int i0 = segStart + lane * kk;
             // Particle data one iteration ahead.
             uint32_t pc = kDeadCell;
             float po[3] = {0.f, 0.f, 0.f}, pu[3] = {0.f, 0.f, 0.f}, pw = 0.f;
-            if (i0 < count) {
+            if (i0 < segEnd) {
                 const int64_t sl = start + i0;
                 pc = sa.buf.cell[sl];
                 po[0] = sa.buf.ox[sl]; po[1] = sa.buf.oy[sl]; po[2] = sa.buf.oz[sl];
@@ -386,22 +400,22 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                 pw = sa.buf.w[sl];
             }
 #pragma unroll 1
-            for (int it = 0; it < K; it++) {
+            for (int it = 0; it < kk; it++) {
                 const int i = i0 + it;
                 const int64_t slot = start + i;
                 const uint32_t cellv = pc;
                 const float o[3] = {po[0], po[1], po[2]};
                 float u[3] = {pu[0], pu[1], pu[2]};
                 const float wgt = pw;
-                if (it + 1 < K && i + 1 < count) {
+                if (it + 1 < kk && i + 1 < segEnd) {
                     const int64_t sl = slot + 1;
                     pc = sa.buf.cell[sl];
                     po[0] = sa.buf.ox[sl]; po[1] = sa.buf.oy[sl]; po[2] = sa.buf.oz[sl];
                     pu[0] = sa.buf.ux[sl]; pu[1] = sa.buf.uy[sl]; pu[2] = sa.buf.uz[sl];
                     pw = sa.buf.w[sl];
                 }
-                const bool act = i < count && cellv != kDeadCell;
-                if (!act && i < count) stage[stageIdx(0, lane * K + it)] = kDeadCell;   // stays dead
+                const bool act = i < segEnd && cellv != kDeadCell;
+                if (!act && i < segEnd) stage[stageIdx(0, lane * kk + it)] = kDeadCell;   // stays dead
                 int lc[3] = {0, 0, 0};
                 int key = -1;
                 if (act) {
@@ -612,7 +626,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     // Stayers in place (the weight does not change); a leaver goes to the side
                     // buffer at its own slot, its slot dies and joins the leaver list.
                     const uint32_t pc2 = packCell(gc[0], gc[1], gc[2]);
-                    const int sp = lane * K + it;   // staged; written back at the end of the segment
+                    const int sp = lane * kk + it;   // staged; written back at the end of the segment
                     stage[stageIdx(0, sp)] = code == 13 ? pc2 : kDeadCell;
                     stage[stageIdx(1, sp)] = __float_as_uint(on[0]);
                     stage[stageIdx(2, sp)] = __float_as_uint(on[1]);
@@ -655,8 +669,8 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
             // weight does not change; leavers went to the side buffer).
             __syncwarp();
             {
-                const int nValid = min(32 * K, count - seg * 32 * K);
-                const int64_t base = start + (int64_t)seg * 32 * K;
+                const int nValid = segEnd - segStart;
+                const int64_t base = start + segStart;
                 for (int p = lane; p < nValid; p += 32) {
                     sa.buf.cell[base + p] = stage[stageIdx(0, p)];
                     sa.buf.ox[base + p] = __uint_as_float(stage[stageIdx(1, p)]);
