@@ -830,8 +830,9 @@ static int stageLayout(pica_ctx* ctx, int q, const std::vector<int32_t>& counts,
     std::vector<int64_t> nstart;
     std::vector<int32_t> ncap;
     layoutFrom(ctx, counts, nstart, ncap, total);
-    CK(cudaMemcpy(S.d_start2, nstart.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(S.d_cap2, ncap.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice));
+    // From pageable memory: staged before the calls return, ordered on the stream.
+    CK(cudaMemcpyAsync(S.d_start2, nstart.data(), ctx->nscTot * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.d_cap2, ncap.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice, ctx->stream));
     S.h_start.swap(nstart);
     S.h_cap.swap(ncap);
     S.layoutSlots = total;
@@ -952,6 +953,9 @@ template <class P>
 static int resortLaunch(pica_ctx* ctx) {
     const int B2 = 1 - ctx->cur;
     const size_t n = ctx->nscTot;
+    int32_t srcMaxCap = 0;   // of the layout being resorted
+    for (int q = 0; q < ctx->cfg.nspecies; q++)
+        for (int32_t v : ctx->sp[q].h_cap) srcMaxCap = std::max(srcMaxCap, v);
     for (int q = 0; q < ctx->cfg.nspecies; q++) {
         SpeciesState& S = ctx->sp[q];
         std::vector<int32_t> alive(S.h_pinAlive, S.h_pinAlive + n);
@@ -971,6 +975,7 @@ static int resortLaunch(pica_ctx* ctx) {
     }
     MigrateArgs<P> r{};
     migrateArgs(ctx, r);   // a = current buffer, dst = the other one, newStart = the uploaded layout
+    r.srcMaxCap = srcMaxCap;
     CKL(launchMigrate(ctx, r, kResort));
     ctx->launches++;
     return PICA_OK;

@@ -210,6 +210,7 @@ struct MigrateArgs {
     int nspecies;
     double invh[3];         // FP64 resort: local cell from x
     int bitmapWords;        // leaver sort: 32-bit words covering the largest count
+    int srcMaxCap;          // resort: largest capacity of the source layout (any species)
     int* flags;             // flags[0] error code, flags[1] overflow
     MigrateSpecies<P> sp[kMaxSpecies];
 };

@@ -123,7 +123,20 @@ int launchMigrateCell(const MigrateArgs<CellPtrs>& a, int stage, cudaStream_t s)
         case kFill: k_fill<CellPtrs><<<(int)nscTot, kFillWarps * 32, 0, s>>>(a); break;
         case kGatherOutbox: k_migrate<CellPtrs, kGatherOutbox><<<warpBlocks, 256, 0, s>>>(a); break;
         case kRebuild: k_migrate<CellPtrs, kRebuild><<<warpBlocks, 256, 0, s>>>(a); break;
-        case kResort: k_resort<CellPtrs><<<(int)nscTot, kResortWarps * 32, 0, s>>>(a); break;
+        case kResort: {
+            // Staged through shared memory while at least two CTAs fit on an SM (16-bit
+            // destinations need supercells below 65535 slots); else the two-pass kernel.
+            const int nb = a.S[0] * a.S[1] * a.S[2];
+            const size_t smem = stagedResortSmem(a.srcMaxCap, nb);
+            if (a.srcMaxCap > 0 && a.srcMaxCap < 65535 && smem <= 110 * 1024) {
+                const cudaError_t e = cudaFuncSetAttribute(k_resortStaged<CellPtrs>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) return (int)e;
+                k_resortStaged<CellPtrs><<<(int)nscTot, kStagedWarps * 32, smem, s>>>(a);
+            } else {
+                k_resort<CellPtrs><<<(int)nscTot, kResortWarps * 32, 0, s>>>(a);
+            }
+            break;
+        }
         default: return (int)cudaErrorInvalidValue;
     }
     return (int)cudaGetLastError();

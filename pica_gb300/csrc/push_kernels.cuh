@@ -1079,4 +1079,140 @@ __global__ void __launch_bounds__(kResortWarps * 32, resortMinBlocks<P>()) k_res
     }
 }
 
+
+// FP32 cell form resort with each supercell staged through shared memory.  The
+// cell array comes in first (cp.async, 16-byte pieces); the ranks of k_resort
+// -- (cell, old slot) order, per-warp contiguous slot ranges, __match_any_sync
+// groups -- are computed from it once and kept as 16-bit destinations; then
+// each array in turn is copied in and scattered from shared memory to its
+// sorted position.  Every array is read from HBM once, in large asynchronous
+// pieces, where k_resort reads the cells twice and keeps only a few loads in
+// flight per warp.  Shared memory: 6 B per slot of the largest source supercell
+// plus the per-warp cell counts (stagedResortSmem).
+constexpr int kStagedWarps = 8;
+
+__host__ __device__ constexpr int stagedResortWords(int maxCap) { return (maxCap + 3) & ~3; }
+__host__ __device__ constexpr size_t stagedResortSmem(int maxCap, int nb) {
+    return (size_t)stagedResortWords(maxCap) * 6 + (size_t)kStagedWarps * nb * 4 + 16;
+}
+
+__device__ __forceinline__ void cpAsync16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ uint32_t* cellArray(const CellPtrs& p, int k) {
+    switch (k) {
+        case 0: return p.cell;
+        case 1: return reinterpret_cast<uint32_t*>(p.ox);
+        case 2: return reinterpret_cast<uint32_t*>(p.oy);
+        case 3: return reinterpret_cast<uint32_t*>(p.oz);
+        case 4: return reinterpret_cast<uint32_t*>(p.ux);
+        case 5: return reinterpret_cast<uint32_t*>(p.uy);
+        case 6: return reinterpret_cast<uint32_t*>(p.uz);
+        default: return reinterpret_cast<uint32_t*>(p.w);
+    }
+}
+
+template <class P>
+__global__ void __launch_bounds__(kStagedWarps * 32, 4) k_resortStaged(const __grid_constant__ MigrateArgs<P> a) {
+    static_assert(std::is_same<P, CellPtrs>::value, "the staged resort moves 4-byte components");
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr int kT = kStagedWarps * 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int W = stagedResortWords(a.srcMaxCap);
+    uint32_t* buf = reinterpret_cast<uint32_t*>(smem);                  // W words
+    uint16_t* pos = reinterpret_cast<uint16_t*>(smem + (size_t)W * 4);  // W entries; 0xFFFF: dead
+    const int nb = a.S[0] * a.S[1] * a.S[2];
+    int* cnt = reinterpret_cast<int*>(smem + (size_t)W * 6);            // [warp][cell]
+    __shared__ int wsum[kStagedWarps];
+    const int d = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int dc[3] = {d / (a.nsc[1] * a.nsc[2]), (d / a.nsc[2]) % a.nsc[1], d % a.nsc[2]};
+    const int m[3] = {dc[0] * a.S[0], dc[1] * a.S[1], dc[2] * a.S[2]};
+    const unsigned lt = (1u << lane) - 1u;
+    for (int spi = 0; spi < a.nspecies; spi++) {
+        const MigrateSpecies<P>& sa = a.sp[spi];
+        const int64_t start = sa.start[d], ns = sa.newStart[d];
+        const int n = sa.count[d];
+        const int nw = (n + 3) & ~3;   // <= the supercell's capacity (a multiple of 32), so in bounds
+        // Cells in; per-warp counts zeroed meanwhile.
+        for (int c = threadIdx.x; c < nw / 4; c += kT) cpAsync16(buf + 4 * c, sa.a.cell + start + 4 * c);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        for (int k = threadIdx.x; k < kStagedWarps * nb; k += kT) cnt[k] = 0;
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();
+        const int R = ((n + kT - 1) / kT) * 32;
+        const int lo = min(warp * R, n), hi = min(lo + R, n);
+        for (int i0 = lo; i0 < hi; i0 += 32) {
+            const int i = i0 + lane;
+            Rec<CellPtrs> r;
+            r.c = i < hi ? buf[i] : kDeadCell;
+            const int key = r.key(m, a.S, nullptr);
+            const unsigned grp = __match_any_sync(FULL, key);
+            if (key >= 0 && lane == __ffs(grp) - 1) cnt[warp * nb + key] += __popc(grp);
+            __syncwarp();
+        }
+        __syncthreads();
+        // Exclusive scan over (cell, warp), cell-major, as in k_resort.
+        {
+            const int E = nb * kStagedWarps;
+            const int per = (E + kT - 1) / kT;   // <= 16 for nb <= 512
+            int loc[16], sum = 0;
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                const int f = threadIdx.x * per + q;
+                loc[q] = (q < per && f < E) ? cnt[(f % kStagedWarps) * nb + f / kStagedWarps] : 0;
+                sum += loc[q];
+            }
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (lane == 31) wsum[warp] = incl;
+            __syncthreads();
+            int run = incl - sum;
+            for (int w = 0; w < warp; w++) run += wsum[w];
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                const int f = threadIdx.x * per + q;
+                if (q < per && f < E) cnt[(f % kStagedWarps) * nb + f / kStagedWarps] = run;
+                run += loc[q];
+            }
+        }
+        __syncthreads();
+        for (int i0 = lo; i0 < hi; i0 += 32) {
+            const int i = i0 + lane;
+            Rec<CellPtrs> r;
+            r.c = i < hi ? buf[i] : kDeadCell;
+            const int key = r.key(m, a.S, nullptr);
+            const unsigned grp = __match_any_sync(FULL, key);
+            if (i < hi) pos[i] = key >= 0 ? (uint16_t)(cnt[warp * nb + key] + __popc(grp & lt)) : (uint16_t)0xFFFFu;
+            __syncwarp();
+            if (key >= 0 && lane == __ffs(grp) - 1) cnt[warp * nb + key] += __popc(grp);
+            __syncwarp();
+        }
+        __syncthreads();
+        // Each array: scatter from shared memory (the cells are already in), then bring in the next.
+        for (int k = 0; k < 8; k++) {
+            uint32_t* dst = cellArray(sa.dst, k) + ns;
+            for (int i = threadIdx.x; i < n; i += kT) {
+                const unsigned p = pos[i];
+                if (p != 0xFFFFu) dst[p] = buf[i];
+            }
+            __syncthreads();
+            if (k == 7) break;
+            const uint32_t* src = cellArray(sa.a, k + 1) + start;
+            for (int c = threadIdx.x; c < nw / 4; c += kT) cpAsync16(buf + 4 * c, src + 4 * c);
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) sa.count[d] = sa.alive[d];
+        __syncthreads();
+    }
+}
+
 }  // namespace pgb
