@@ -24,7 +24,7 @@ inline int wrapHost(int a, int n) { a %= n; return a < 0 ? a + n : a; }
 struct SpeciesState {
     void* buf[2][8] = {};        // A = buf[cur], B = buf[1 - cur]
     int64_t slots[2] = {0, 0};   // allocated slots of each buffer
-    uint8_t* dir = nullptr;      // direction code per slot
+    uint32_t* dir = nullptr;     // per slot: direction code | (packed leaver record index << 5)
     int32_t* llist = nullptr;    // leaver slots per supercell (at [start, start + nleave)), by slot
     int32_t* lbydir = nullptr;   // the same slots by (direction code, slot)
     int32_t* d_dirOff = nullptr; // per supercell, 28 bucket offsets of lbydir
@@ -195,7 +195,7 @@ int ensureSlotArrays(pica_ctx* ctx, int spi, int64_t slots) {
     S.lbydir = nullptr;
     S.slotArrays = 0;
     const int64_t grown = withHeadroom(slots);
-    CK(cudaMalloc(&S.dir, grown));
+    CK(cudaMalloc(&S.dir, grown * 4));
     CK(cudaMalloc(&S.llist, grown * 4));
     CK(cudaMalloc(&S.lbydir, grown * 4));
     S.slotArrays = grown;

@@ -11,8 +11,10 @@
 //             FP32 cell form  : cell(uint32 packed) ox oy oz ux uy uz w (4 B each, 32 B;
 //                               dead: cell = 0xFFFFFFFF)
 //   A step: the push kernel updates A in place; a particle that leaves its
-//   supercell is copied to B at its own slot index, its slot in A becomes
-//   dead and the slot joins the supercell's leaver list.  Migration fills
+//   supercell is the supercell's k-th leaver (k from a shared-memory counter):
+//   its record goes to B at start + k, so a supercell's leaver records are
+//   packed; its slot in A becomes dead and joins the leaver list, and the slot's
+//   direction word holds the move's direction code and k.  Migration fills
 //   each destination's fresh holes with its arrivals (canonical order), then
 //   appends.  Every resort_every steps each supercell is compacted and
 //   sorted by cell into B, and A and B swap.
@@ -85,13 +87,13 @@ __host__ __device__ inline bool aliveX(double x) { return x > -1.0e299; }
 template <class P>
 struct SpeciesArgs {
     P buf;             // A: updated in place
-    P out;             // B: leaver copies at their own slot index
+    P out;             // B: leaver records, packed at start + k
     const int64_t* start;
     const int32_t* cap;
     const int32_t* count;
     int32_t* nleave;   // leavers per supercell (this step)
     int32_t* llist;    // leaver slots, list of supercell s at [start[s], start[s] + nleave[s])
-    uint8_t* dir;      // direction code per slot (valid for leavers)
+    uint32_t* dir;     // per slot, valid for leavers: direction code | (packed record index << 5)
     double ec;         // q dt / (2 m c)   (BorisPusher.h:29)
     double q;          // charge
     double kq[3];      // -q h_d / dt      (Esirkepov current factor per unit weight)
@@ -126,7 +128,7 @@ struct SpeciesArgsSlim {
     const int32_t* count;
     int32_t* nleave;
     int32_t* llist;
-    uint8_t* dir;
+    uint32_t* dir;
     float ec;
     float kq[3];
 };
@@ -186,7 +188,7 @@ constexpr int kDirBuckets = 28;  // 27 direction codes + end
 template <class P>
 struct MigrateSpecies {
     P a;                    // A (current)
-    P b;                    // B (leaver copies at their slot index)
+    P b;                    // B (leaver records, packed at start + k)
     P dst;                  // rebuild / resort destination (new layout)
     P outbox;               // rebuild: leaver copies gathered per source supercell
     const int64_t* start;
@@ -195,9 +197,9 @@ struct MigrateSpecies {
     int32_t* alive;         // live particles
     const int32_t* nleave;
     int32_t* llist;         // leaver slots by slot (the holes, in fill order)
-    int32_t* lbydir;        // leaver slots by (direction code, slot)
+    int32_t* lbydir;        // leaver record indices k, by (direction code, slot)
     int32_t* dirOff;        // per supercell: kDirBuckets offsets into lbydir (code c: [dirOff[c], dirOff[c+1]))
-    const uint8_t* dir;
+    const uint32_t* dir;
     int32_t* needed;        // count after migration
     int32_t* neededAlive;   // live particles after migration
     const int64_t* newStart;// rebuild / resort: new layout

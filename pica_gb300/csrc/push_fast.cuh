@@ -23,8 +23,8 @@
 //  * Particles that change cell are queued in a per-warp shared-memory
 //    ring and deposited on the general 4- (TSC) or 3-node (CIC) window, 32 at a
 //    time (one per lane), by one out-of-line routine.
-//  * Stayers are written back in place; leavers go to the side buffer at
-//    their own slot (see pica_internal.h), so the kernel needs no block-wide
+//  * Stayers are written back in place; leavers go to the side buffer, packed
+//    per supercell (see pica_internal.h), so the kernel needs no block-wide
 //    synchronisation between the tile staging and the final tile flush.
 //  * The E/B tile holds only the nodes that the gather reads, m-1 .. m+S+1
 //    per dimension; the current tile spans m-2 .. m+S+2 (general windows).
@@ -633,7 +633,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     }
                     const int code = dirCode(sc, nsc3, a.nsc, bad);
                     // Stayers in place (the weight does not change); a leaver goes to the side
-                    // buffer at its own slot, its slot dies and joins the leaver list.
+                    // buffer, its slot dies and joins the leaver list.
                     const uint32_t pc2 = packCell(gc[0], gc[1], gc[2]);
                     const int sp = lane * kk + it;   // staged; written back at the end of the segment
                     stage[stageIdx(0, sp)] = code == 13 ? pc2 : kDeadCell;
@@ -644,12 +644,14 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     stage[stageIdx(5, sp)] = __float_as_uint(u[1]);
                     stage[stageIdx(6, sp)] = __float_as_uint(u[2]);
                     if (code != 13) {
-                        sa.out.cell[slot] = pc2;
-                        sa.out.ox[slot] = on[0]; sa.out.oy[slot] = on[1]; sa.out.oz[slot] = on[2];
-                        sa.out.ux[slot] = u[0]; sa.out.uy[slot] = u[1]; sa.out.uz[slot] = u[2];
-                        sa.out.w[slot] = wgt;
-                        sa.dir[slot] = (uint8_t)code;
-                        sa.llist[start + atomicAdd(&s_nleave, 1)] = i;
+                        const int k = atomicAdd(&s_nleave, 1);
+                        const int64_t o = start + k;   // leaver records are packed (see pica_internal.h)
+                        sa.out.cell[o] = pc2;
+                        sa.out.ox[o] = on[0]; sa.out.oy[o] = on[1]; sa.out.oz[o] = on[2];
+                        sa.out.ux[o] = u[0]; sa.out.uy[o] = u[1]; sa.out.uz[o] = u[2];
+                        sa.out.w[o] = wgt;
+                        sa.dir[slot] = (uint32_t)code | ((uint32_t)k << 5);
+                        sa.llist[o] = i;
                     }
                 }
                 // Queue window changes in the ring; deposit 32 at a time (one per lane).

@@ -661,19 +661,22 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                 }
                 nu[0] = u[0]; nu[1] = u[1]; nu[2] = u[2];
             }
-            // Stayers are updated in place (the weight does not change); a leaver is copied to
-            // the side buffer at its own slot, its slot dies and joins the leaver list.
+            // Stayers are updated in place (the weight does not change); a leaver's record
+            // goes to the side buffer, packed at start + k (k: its rank of arrival in the
+            // leaver list), its slot dies and joins the leaver list.
+            const int k = code == 13 ? 0 : atomicAdd(&s_nleave, 1);
+            const int64_t w = code == 13 ? slot : start + k;
             const P& o = code == 13 ? sa.buf : sa.out;
             if constexpr (PLAIN) {
-                o.x[slot] = npos[0]; o.y[slot] = npos[1]; o.z[slot] = npos[2];
+                o.x[w] = npos[0]; o.y[w] = npos[1]; o.z[w] = npos[2];
             } else {
-                o.cell[slot] = ncell; o.ox[slot] = no3[0]; o.oy[slot] = no3[1]; o.oz[slot] = no3[2];
+                o.cell[w] = ncell; o.ox[w] = no3[0]; o.oy[w] = no3[1]; o.oz[w] = no3[2];
             }
-            o.ux[slot] = nu[0]; o.uy[slot] = nu[1]; o.uz[slot] = nu[2];
+            o.ux[w] = nu[0]; o.uy[w] = nu[1]; o.uz[w] = nu[2];
             if (code != 13) {
-                o.w[slot] = sa.buf.w[slot];
-                sa.dir[slot] = (uint8_t)code;
-                sa.llist[start + atomicAdd(&s_nleave, 1)] = i;
+                o.w[w] = sa.buf.w[slot];
+                sa.dir[slot] = (uint32_t)code | ((uint32_t)k << 5);
+                sa.llist[w] = i;
                 killAt(sa.buf, slot);
             }
         }
@@ -764,7 +767,7 @@ __global__ void __launch_bounds__(128) k_sortLeavers(const __grid_constant__ Mig
             __syncwarp();
             for (int k0 = 0; k0 < n; k0 += 32) {
                 const int k = k0 + lane;
-                const int code = k < n ? sa.dir[start + sa.llist[start + k]] : -1;
+                const int code = k < n ? (int)(sa.dir[start + sa.llist[start + k]] & 31u) : -1;
                 const unsigned grp = __match_any_sync(0xffffffffu, code);
                 if (code >= 0 && lane == __ffs(grp) - 1) dcnt[code] += __popc(grp);
                 __syncwarp();
@@ -783,9 +786,10 @@ __global__ void __launch_bounds__(128) k_sortLeavers(const __grid_constant__ Mig
             for (int k0 = 0; k0 < n; k0 += 32) {
                 const int k = k0 + lane;
                 const int slot = k < n ? sa.llist[start + k] : -1;
-                const int code = k < n ? sa.dir[start + slot] : -1;
+                const uint32_t dk = k < n ? sa.dir[start + slot] : 0u;
+                const int code = k < n ? (int)(dk & 31u) : -1;
                 const unsigned grp = __match_any_sync(0xffffffffu, code);
-                if (code >= 0) sa.lbydir[start + dcnt[code] + __popc(grp & lt)] = slot;
+                if (code >= 0) sa.lbydir[start + dcnt[code] + __popc(grp & lt)] = (int32_t)(dk >> 5);
                 __syncwarp();
                 if (code >= 0 && lane == __ffs(grp) - 1) dcnt[code] += __popc(grp);
                 __syncwarp();
