@@ -82,7 +82,7 @@ def weibel(n=(256, 256, 256), ppc_per_beam=32, beta=0.3, sigma=0.01, mass_ratio=
     hh = (h, h, h)
     ion = (ELECTRON_MASS * mass_ratio, -ELECTRON_CHARGE)
     sim = dict(n=n, h=hh, dt=time_step(h), supercell=supercell, form=form, shape=SHAPE_TSC,
-               deposit=DEPOSIT_ESIRKEPOV, species=((ELECTRON_MASS, ELECTRON_CHARGE), ion), resort_every=2)
+               deposit=DEPOSIT_ESIRKEPOV, species=((ELECTRON_MASS, ELECTRON_CHARGE), ion), resort_every=1)
     w = N0 * h ** 3 / (2 * ppc_per_beam)
     u = _u_of_beta(beta)
     specs = [plasma_spec(n, hh, 2 * ppc_per_beam, sigma, w, seed, species=0, nbeams=2, drift_u=u, drift_axis=2),
