@@ -51,10 +51,9 @@ def batched_measure(args):
     members = workloads.batched_members(count=args.batched, half=not args.batched_full)
     b = pg.Batch([m["sim"] for m in members])
     for sim, wl in zip(b.members, members):
-        parts = pg.generate_plasma(wl["specs"][0])
-        sim.upload_particles(*[parts[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w")], parts["species"])
+        sim.generate_plasma(wl["specs"])   # drawn on the device
         sim.upload_fields([np.zeros(wl["sim"]["n"])] * 9)
-        del parts
+    b.reorder()
     npart = b.num_particles()
     tune = autotune.tune_batch(b, steps=2)
     best = min(tune, key=tune.get)

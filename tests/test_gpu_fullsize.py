@@ -1,8 +1,9 @@
-"""The three single-plasma workloads at full size, generated on the device:
-thermal 128^3 x 100 ppc (2.1e8 electrons, TSC), two-stream 256x256x128 with
-10-190 ppc (8.4e8 electrons, CIC) and Weibel 256^3 with electrons and ions
-(2.1e9 particles, TSC; about 200 GB of device memory).  Too large for the
-oracle, so they are checked through properties that hold at any size:
+"""The workloads at full size, generated on the device: thermal 128^3 x 100 ppc
+(2.1e8 electrons, TSC), two-stream 256x256x128 with 10-190 ppc (8.4e8
+electrons, CIC), Weibel 256^3 with electrons and ions (2.1e9 particles, TSC;
+about 200 GB of device memory), and the 64-plasma batch (grids 32^3-96^3,
+16-128 ppc, 1.9e9 particles in all, batching form).  Too large for the oracle,
+so they are checked through properties that hold at any size:
 
 * particle number per species, exactly, after every checked step;
 * charge conservation over one step: max |(rho^{n+1} - rho^n)/dt + div J| at most
@@ -73,3 +74,35 @@ def test_full_size_workload_properties(name):
     assert np.array_equal(c1, c2)
     for c in range(9):
         assert np.array_equal(f1[c], f2[c]), c
+
+
+def run_batch(members, steps):
+    b = pg.Batch([m["sim"] for m in members])
+    for sim, wl in zip(b.members, members):
+        sim.generate_plasma(wl["specs"])
+        sim.upload_fields([np.zeros(wl["sim"]["n"])] * 9)
+    b.reorder()
+    expect = [expected_counts(sim, wl) for sim, wl in zip(b.members, members)]
+    b.step(steps)
+    counts = [sim.counts() for sim in b.members]
+    for c, e in zip(counts, expect):
+        assert c.sum(axis=1).tolist() == e
+    # Field energy and the J components of every member (a checksum per member).
+    sums = [(sim.field_energy(), [float(np.sum(f)) for f in sim.fields()[6:]]) for sim in b.members]
+    stats = b.stats()
+    b.close()
+    return counts, sums, stats
+
+
+def test_full_size_batch_properties():
+    """The 64-plasma batch at full member sizes: particle numbers conserved per member,
+    and a second run equal to the first (counts, field energy and current sums of every
+    member, bit for bit)."""
+    members = workloads.batched_members(count=64)
+    steps = 5
+    c1, s1, st = run_batch(members, steps)
+    assert st["steps"] == steps
+    c2, s2, _ = run_batch(members, steps)
+    for a, b in zip(c1, c2):
+        assert np.array_equal(a, b)
+    assert s1 == s2
