@@ -87,7 +87,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=6)
+    ap.add_argument("--e2e-steps", type=int, default=12)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -363,7 +363,8 @@ def main():
 
     # ---------------- e2e through the C ABI with host buffers ----------------
     # Every step uploads the particle state from pinned host memory, steps, and
-    # downloads it again (pica_state_copy, one call per component).  Uploads run on
+    # downloads it again (the packed image of the used slots, pica_state_copy_packed,
+    # one call per component).  Uploads run on
     # one copy stream and downloads on another: component c of step n+1 goes up as
     # soon as component c of step n is down, so the two link directions overlap;
     # the step itself waits for all of its uploads.
@@ -375,10 +376,11 @@ def main():
         # Pinned host buffers are set up once, outside the timed region, with room
         # for the layout to grow at a resort or capacity rebuild.
         torch.cuda.synchronize()
-        alloc = int(sim.state_slots(0) * 1.25) + 1024
+        slots = sim.state_packed_slots(0)
+        alloc = int(slots * 1.25) + 1024
         host = [torch.empty(alloc * 4, dtype=torch.uint8, pin_memory=True) for _ in range(comps)]
         for c in range(comps):
-            sim.state_copy(0, c, host[c].data_ptr(), False)
+            sim.state_copy_packed(0, c, host[c].data_ptr(), False)
         torch.cuda.synchronize()
         downed = [None] * comps
         te0, te1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -387,13 +389,12 @@ def main():
         te0.record(stream)
         up.wait_event(te0)
         for _ in range(args.e2e_steps):
-            slots = sim.state_slots(0)
             upped = []
             sim.set_stream(up.cuda_stream)
             for c in range(comps):
                 if downed[c] is not None:
                     up.wait_event(downed[c])
-                sim.state_copy(0, c, host[c].data_ptr(), True)
+                sim.state_copy_packed(0, c, host[c].data_ptr(), True)
                 ev = torch.cuda.Event()
                 ev.record(up)
                 upped.append(ev)
@@ -402,7 +403,7 @@ def main():
                 stream.wait_event(ev)
             sim.set_stream(stream.cuda_stream)
             one_step()   # returns once the step's device work is done (the migration reads flags)
-            slots = sim.state_slots(0)   # the layout can change at a resort
+            slots = sim.state_packed_slots(0)   # the image of the new layout and counts
             if slots > alloc:            # no copy is in flight here
                 torch.cuda.synchronize()
                 host = [torch.empty(slots * 4, dtype=torch.uint8, pin_memory=True) for _ in range(comps)]
@@ -412,7 +413,7 @@ def main():
             down.wait_event(stepped)
             sim.set_stream(down.cuda_stream)
             for c in range(comps):
-                sim.state_copy(0, c, host[c].data_ptr(), False)
+                sim.state_copy_packed(0, c, host[c].data_ptr(), False)
                 downed[c] = torch.cuda.Event()
                 downed[c].record(down)
             sim.set_stream(stream.cuda_stream)
@@ -426,9 +427,10 @@ def main():
         e_el = te0.elapsed_time(te1) / 1e3
         e2e = {"value": world * npart * done / max(e_el, wall), "unit": UNIT,
                "h2d_bytes_per_step": h2d // max(1, done), "d2h_bytes_per_step": d2h // max(1, done),
-               "steps": done, "path": "pica_state_copy (pinned host) -> pica_push_deposit/update_b/update_e/"
-                                      "update_b/migrate -> pica_state_copy; uploads and downloads on two "
-                                      "copy streams, overlapped across steps"}
+               "steps": done, "path": "pica_state_copy_packed (pinned host) -> pica_push_deposit/update_b/"
+                                      "update_e/update_b/migrate -> pica_state_packed_slots, "
+                                      "pica_state_copy_packed; uploads and downloads on two copy streams, "
+                                      "overlapped across steps"}
         del host
     sim.close()
     del sim

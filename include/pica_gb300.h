@@ -188,6 +188,17 @@ int     pica_field_energy_noalloc(const void* const* fields, int32_t fp64, const
  * 1..7 = ox oy oz ux uy uz w (float). */
 int64_t pica_state_slots(pica_ctx* ctx, int32_t species);
 int     pica_state_copy(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device);
+/* Packed particle state: the used slots of every supercell (dead ones
+ * included), back to back in supercell order -- the slot state without the
+ * layout's slack.  pica_state_packed_slots() reads the current counts
+ * (synchronising the context stream), lays the image out and returns its size in
+ * slots; pica_state_copy_packed() then moves one component of the image between
+ * the device and host memory on the context stream (a gather or scatter kernel
+ * and one copy; the device keeps a staging copy of the image).  The image is
+ * valid until the next step or change of layout: pica_state_copy_packed returns
+ * PICA_ERR_STATE once it is out of date.  Components as for pica_state_copy. */
+int64_t pica_state_packed_slots(pica_ctx* ctx, int32_t species);
+int     pica_state_copy_packed(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device);
 
 /* Batching form: many independent plasmas advanced together (FP32 cell form,
  * Esirkepov deposition, one shape and one supercell size for all members; grids,

@@ -219,6 +219,17 @@ class Simulation:
         self._check(self.lib.pica_state_copy(self.ctx, int(species), int(comp), C.c_void_p(int(host_ptr)),
                                              1 if to_device else 0))
 
+    def state_packed_slots(self, species=0):
+        """Lay out the packed state image (used slots only) and return its size in slots."""
+        n = int(self.lib.pica_state_packed_slots(self.ctx, int(species)))
+        if n < 0:
+            self._check(n)
+        return n
+
+    def state_copy_packed(self, species, comp, host_ptr, to_device):
+        self._check(self.lib.pica_state_copy_packed(self.ctx, int(species), int(comp), C.c_void_p(int(host_ptr)),
+                                                    1 if to_device else 0))
+
 
 class Driver:
     """A host loop over a Simulation, in the role of the PICADOR driver around pica's

@@ -311,4 +311,27 @@ int launchGauss(bool fp64, void* const* f, const double* rho, const int* n, cons
     return (int)cudaGetLastError();
 }
 
+namespace {
+__global__ void __launch_bounds__(256) k_packCopy(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
+                                                  const int64_t* start, const int32_t* count, const int64_t* off,
+                                                  int words, bool gather) {
+    const int s = blockIdx.x;
+    const int64_t a = start[s] * words, b = off[s] * words;
+    const int n = count[s] * words;
+    if (gather) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) dst[b + i] = src[a + i];
+    } else {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) dst[a + i] = src[b + i];
+    }
+}
+}  // namespace
+
+int launchPackCopy(const void* src, void* dst, const int64_t* start, const int32_t* count, const int64_t* off,
+                   int nscTot, int words, bool gather, cudaStream_t s) {
+    if (nscTot <= 0) return 0;
+    k_packCopy<<<nscTot, 256, 0, s>>>(static_cast<const uint32_t*>(src), static_cast<uint32_t*>(dst), start, count,
+                                      off, words, gather);
+    return (int)cudaGetLastError();
+}
+
 }  // namespace pgb

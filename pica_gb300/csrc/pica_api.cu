@@ -45,6 +45,14 @@ struct SpeciesState {
     std::vector<int32_t> h_cap;
     int64_t layoutSlots = 0;     // sum of caps of the current layout
     // Pinned staging of the resort's host round trip (live counts in, new layout out).
+    // Packed state image (pica_state_packed_slots / pica_state_copy_packed): supercell
+    // offsets of the image, its size, the epoch it was laid out for, and one device
+    // staging buffer per component.
+    int64_t* d_packOff = nullptr;
+    int64_t packSlots = -1;
+    int64_t packEpoch = -1;
+    int64_t packCap = 0;
+    void* d_pack[8] = {};
     int32_t* h_pinAlive = nullptr;
     int64_t* h_pinStart = nullptr;
     int32_t* h_pinCap = nullptr;
@@ -78,6 +86,7 @@ struct pica_ctx {
     std::string err;
     int64_t launches = 0;
     int64_t steps = 0;
+    int64_t epoch = 0;      // bumped by every step and every change of layout (packed-image validity)
     int threads = 1;
 };
 
@@ -235,6 +244,7 @@ int installLayout(pica_ctx* ctx, int q, const std::vector<int32_t>& counts) {
     CK(cudaMemcpyAsync(S.d_alive, counts.data(), ctx->nscTot * 4, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemsetAsync(S.d_nleave, 0, ctx->nscTot * 4, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    ctx->epoch++;
     return PICA_OK;
 }
 
@@ -408,6 +418,8 @@ int pica_ctx_destroy(pica_ctx* ctx) {
             if (p) cudaFree(p);
         for (void* p : {(void*)S.h_pinAlive, (void*)S.h_pinStart, (void*)S.h_pinCap})
             if (p) cudaFreeHost(p);
+        if (S.d_packOff) cudaFree(S.d_packOff);
+        for (auto p : S.d_pack) if (p) cudaFree(p);
     }
     if (ctx->d_flags) cudaFree(ctx->d_flags);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
@@ -932,6 +944,7 @@ static int migrateFinish(pica_ctx* ctx) {
         updateJFrac(ctx);
     }
     ctx->steps++;
+    ctx->epoch++;
     return PICA_OK;
 }
 
@@ -992,6 +1005,7 @@ static int resortFinish(pica_ctx* ctx) {
     }
     ctx->cur = 1 - A2;
     updateJFrac(ctx);
+    ctx->epoch++;
     return PICA_OK;
 }
 
@@ -1127,6 +1141,59 @@ int pica_state_copy(pica_ctx* ctx, int32_t species, int32_t comp, void* host, in
     const size_t bytes = S.layoutSlots * ctx->compBytes[comp];
     if (to_device) CK(cudaMemcpyAsync(S.buf[ctx->cur][comp], host, bytes, cudaMemcpyHostToDevice, ctx->stream));
     else CK(cudaMemcpyAsync(host, S.buf[ctx->cur][comp], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return PICA_OK;
+}
+
+int64_t pica_state_packed_slots(pica_ctx* ctx, int32_t species) {
+    if (!ctx || species < 0 || species >= ctx->cfg.nspecies) return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "packed state while a migration is pending");
+    SpeciesState& S = ctx->sp[species];
+    const int n = ctx->nscTot;
+    std::vector<int32_t> count(n);
+    std::vector<int64_t> off(n);
+    CK(cudaMemcpyAsync(count.data(), S.d_count, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    int64_t total = 0;
+    for (int s = 0; s < n; s++) { off[s] = total; total += count[s]; }
+    if (!S.d_packOff) CK(cudaMalloc(&S.d_packOff, (size_t)n * 8));
+    CK(cudaMemcpyAsync(S.d_packOff, off.data(), (size_t)n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    if (total > S.packCap) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (auto& p : S.d_pack) {
+            if (p) CK(cudaFree(p));
+            p = nullptr;
+        }
+        S.packCap = 0;
+        const int64_t cap = withHeadroom(total);
+        for (int k = 0; k < ctx->ncomp; k++) CK(cudaMalloc(&S.d_pack[k], cap * ctx->compBytes[k]));
+        S.packCap = cap;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));   // the offsets are in place before the host vector goes
+    S.packSlots = total;
+    S.packEpoch = ctx->epoch;
+    return total;
+}
+
+int pica_state_copy_packed(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device) {
+    if (!ctx || !host || species < 0 || species >= ctx->cfg.nspecies || comp < 0 || comp >= ctx->ncomp)
+        return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "state copy while a migration is pending");
+    SpeciesState& S = ctx->sp[species];
+    if (S.packEpoch != ctx->epoch)
+        return fail(ctx, PICA_ERR_STATE, "packed layout out of date: call pica_state_packed_slots after each step");
+    const size_t bytes = (size_t)S.packSlots * ctx->compBytes[comp];
+    const int words = (int)(ctx->compBytes[comp] / 4);
+    if (S.packSlots == 0) return PICA_OK;
+    if (to_device) {
+        CK(cudaMemcpyAsync(S.d_pack[comp], host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        CKL(launchPackCopy(S.d_pack[comp], S.buf[ctx->cur][comp], S.d_start, S.d_count, S.d_packOff, ctx->nscTot,
+                           words, false, ctx->stream));
+    } else {
+        CKL(launchPackCopy(S.buf[ctx->cur][comp], S.d_pack[comp], S.d_start, S.d_count, S.d_packOff, ctx->nscTot,
+                           words, true, ctx->stream));
+        CK(cudaMemcpyAsync(host, S.d_pack[comp], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    ctx->launches++;
     return PICA_OK;
 }
 
@@ -1685,6 +1752,7 @@ int pica_checkpoint_load(pica_ctx* ctx, const char* path) {
     }
     ctx->cur = 0;
     ctx->steps = h.steps;
+    ctx->epoch++;
     ctx->kmax = h.kmax;
     ctx->jfrac = h.jfrac;
     ctx->tileSplit = h.tileSplit;

@@ -288,6 +288,12 @@ struct GenArgs {
     CellPtrs buf;
 };
 int launchGenerate(const GenArgs& a, int nscTot, cudaStream_t s);
+// Packed state image: supercell s's used slots [start[s], start[s] + count[s]) of a
+// component (words 4-byte words per slot) to or from image offset off[s] (slots).
+// gather: slots -> image (src = slot array, dst = image); else image -> slots
+// (src = image, dst = slot array).
+int launchPackCopy(const void* src, void* dst, const int64_t* start, const int32_t* count, const int64_t* off,
+                   int nscTot, int words, bool gather, cudaStream_t s);
 // Gauss residual: max |div E - 4 pi (rho + bg)| and max |rho|; partial: 2*kReduceBlocks doubles.
 int launchGauss(bool fp64, void* const* f, const double* rho, const int* n, const double* h, double bg,
                 double* partial, double* out2, cudaStream_t s);

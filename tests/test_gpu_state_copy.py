@@ -77,3 +77,83 @@ def test_state_round_trip_on_copy_streams_equals_plain_steps():
         assert np.array_equal(fa[c], fr[c]), c
     a.close()
     ref.close()
+
+
+def test_packed_round_trip_on_copy_streams_equals_plain_steps():
+    """The same host loop with the packed image (used slots only)."""
+    n = (16, 8, 8)
+    d = thermal_inputs(n, 6, seed=74, u_sigma=0.2)
+    steps, comps = 5, 8
+    ref = make(d, n)
+    ref.step(steps)
+    a = make(d, n)
+    main = torch.cuda.current_stream()
+    a.set_stream(main.cuda_stream)
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
+    packed = a.state_packed_slots(0)
+    assert 0 < packed <= a.state_slots(0)
+    alloc = 2 * packed + 1024
+    host = [torch.empty(alloc * 4, dtype=torch.uint8, pin_memory=True) for _ in range(comps)]
+    for c in range(comps):
+        a.state_copy_packed(0, c, host[c].data_ptr(), False)
+    torch.cuda.synchronize()
+    downed = [None] * comps
+    for _ in range(steps):
+        a.set_stream(up.cuda_stream)
+        upped = []
+        for c in range(comps):
+            if downed[c] is not None:
+                up.wait_event(downed[c])
+            a.state_copy_packed(0, c, host[c].data_ptr(), True)
+            ev = torch.cuda.Event()
+            ev.record(up)
+            upped.append(ev)
+        for ev in upped:
+            main.wait_event(ev)
+        a.set_stream(main.cuda_stream)
+        a.step(1)
+        packed = a.state_packed_slots(0)
+        assert packed <= alloc
+        stepped = torch.cuda.Event()
+        stepped.record(main)
+        down.wait_event(stepped)
+        a.set_stream(down.cuda_stream)
+        for c in range(comps):
+            a.state_copy_packed(0, c, host[c].data_ptr(), False)
+            downed[c] = torch.cuda.Event()
+            downed[c].record(down)
+        a.set_stream(main.cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(a.counts(), ref.counts())
+    pa, pr = a.particles(), ref.particles()
+    for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species", "supercell"):
+        assert np.array_equal(pa[k], pr[k]), k
+    fa, fr = a.fields(), ref.fields()
+    for c in range(9):
+        assert np.array_equal(fa[c], fr[c]), c
+    a.close()
+    ref.close()
+
+
+def test_packed_image_holds_the_ensemble_and_goes_stale_after_a_step():
+    n = (8, 8, 8)
+    d = thermal_inputs(n, 4, seed=75, u_sigma=0.2)
+    s = make(d, n)
+    s.step(3)
+    m = s.state_packed_slots(0)
+    cell = np.empty(m, np.uint32)
+    s.state_copy_packed(0, 0, cell.ctypes.data, False)
+    comp = {}
+    for c, k in ((4, "ux"), (5, "uy"), (6, "uz"), (7, "w")):
+        comp[k] = np.empty(m, np.float32)
+        s.state_copy_packed(0, c, comp[k].ctypes.data, False)
+    s.synchronize()
+    p = s.particles()
+    live = cell != 0xFFFFFFFF   # dead slots of the used range carry the dead-cell marker
+    assert live.sum() == len(p["ux"]) == s.counts().sum()
+    for k, v in comp.items():
+        assert np.array_equal(v[live].astype(np.float64), p[k]), k
+    s.step(1)
+    with pytest.raises(pg.PicaError):
+        s.state_copy_packed(0, 4, comp["ux"].ctypes.data, False)
+    s.close()
