@@ -194,6 +194,17 @@ public:
     void generatePlasma(const std::vector<pica_plasma_spec>& specs) {
         check(ctx_, pica_generate_plasma(ctx_, specs.data(), (int32_t)specs.size()));
     }
+    // Packed particle state of one species (used slots only; see pica_state_packed_slots):
+    // statePackedSlots() lays the image out, copyStatePacked() moves one component of
+    // it (host: pinned memory of statePackedSlots() x 4 or 8 bytes).
+    int64_t statePackedSlots(int species = 0) {
+        const int64_t n = pica_state_packed_slots(ctx_, species);
+        if (n < 0) check(ctx_, (int)n);
+        return n;
+    }
+    void copyStatePacked(int species, int comp, void* host, bool toDevice) {
+        check(ctx_, pica_state_copy_packed(ctx_, species, comp, host, toDevice ? 1 : 0));
+    }
     // Complete state between steps; a Simulation of the same Config loaded from it
     // continues like this one (FP32 form: bit for bit).
     void saveCheckpoint(const std::string& path) { check(ctx_, pica_checkpoint_save(ctx_, path.c_str())); }
