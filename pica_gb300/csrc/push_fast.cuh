@@ -625,13 +625,21 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     // supercell coordinates (with one or two supercells along a dimension
                     // the periodic +1 and -1 neighbours coincide; dirCode resolves that
                     // the same way the oracle does).
-                    int gc[3], nsc3[3];
+                    // A particle still inside the supercell stays (code 13) and needs no wrap.
+                    int gc[3];
+                    int code = 13;
+                    if (ln[0] >= 0 && ln[0] < Sv[0] && ln[1] >= 0 && ln[1] < Sv[1] && ln[2] >= 0 && ln[2] < Sv[2]) {
 #pragma unroll
-                    for (int d = 0; d < 3; d++) {
-                        gc[d] = wrapNear(m[d] + ln[d], a.n[d]);
-                        nsc3[d] = gc[d] / Sv[d];
+                        for (int d = 0; d < 3; d++) gc[d] = m[d] + ln[d];
+                    } else {
+                        int nsc3[3];
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            gc[d] = wrapNear(m[d] + ln[d], a.n[d]);
+                            nsc3[d] = gc[d] / Sv[d];
+                        }
+                        code = dirCode(sc, nsc3, a.nsc, bad);
                     }
-                    const int code = dirCode(sc, nsc3, a.nsc, bad);
                     // Stayers in place (the weight does not change); a leaver goes to the side
                     // buffer, its slot dies and joins the leaver list.
                     const uint32_t pc2 = packCell(gc[0], gc[1], gc[2]);
