@@ -95,3 +95,17 @@ def test_species_without_particles_and_empty_supercells(form, shape, dep):
     s, o = run_both(n, sc, d, 8, form, shape, dep, species=((ME, E), ion))
     assert s.counts()[1].sum() == 0
     check(s, o, n, d["h"], form)
+
+
+@pytest.mark.parametrize("form,shape,dep", FORMS)
+@pytest.mark.parametrize("n,sc", [((16, 8, 1), (4, 4, 1)), ((32, 1, 1), (4, 1, 1))])
+def test_two_and_one_dimensional_grids(n, sc, form, shape, dep):
+    """A grid one cell thick along z (2D) or along y and z (1D), periodic: the 3D step
+    reduces to the 2D / 1D one (the derivatives along a one-cell periodic axis are exact
+    zeros, and the gather and deposit along it sum their weights on the single node).
+    Against the oracle on the same grid."""
+    d = thermal_inputs(n, 6, seed=66, u_sigma=0.15)
+    rng = np.random.default_rng(67)
+    f9 = [1e3 * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3
+    s, o = run_both(n, sc, d, 5, form, shape, dep, fields=f9, resort_every=2)
+    check(s, o, n, d["h"], form)
