@@ -88,6 +88,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=12)
+    ap.add_argument("--e2e-chunks", type=int, default=8, help="supercell ranges of the e2e upload / push pipeline")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -363,16 +364,19 @@ def main():
 
     # ---------------- e2e through the C ABI with host buffers ----------------
     # Every step uploads the particle state from pinned host memory, steps, and
-    # downloads it again (the packed image of the used slots, pica_state_copy_packed,
-    # one call per component).  Uploads run on
-    # one copy stream and downloads on another: component c of step n+1 goes up as
-    # soon as component c of step n is down, so the two link directions overlap;
-    # the step itself waits for all of its uploads.
+    # downloads it again: the packed image of the used slots, moved in supercell
+    # ranges (pica_state_copy_packed_range).  Uploads run on one copy stream and
+    # downloads on another; range r of step n+1 goes up as soon as range r of step
+    # n is down, so the two link directions overlap, and the push of range r starts
+    # as soon as its upload is in (pica_push_deposit_chunked), overlapping the rest
+    # of the upload.
     e2e = None
     if headline and args.e2e_steps > 0:
         comps = 8
         done = h2d = d2h = 0
-        up, down = torch.cuda.Stream(), torch.cuda.Stream()
+        # High priority: the copy streams' pack and unpack kernels get SMs ahead of the push.
+        up, down = torch.cuda.Stream(priority=-1), torch.cuda.Stream(priority=-1)
+        ranges = sim.chunk_ranges(args.e2e_chunks)
         # Pinned host buffers are set up once, outside the timed region, with room
         # for the layout to grow at a resort or capacity rebuild.
         torch.cuda.synchronize()
@@ -382,7 +386,7 @@ def main():
         for c in range(comps):
             sim.state_copy_packed(0, c, host[c].data_ptr(), False)
         torch.cuda.synchronize()
-        downed = [None] * comps
+        downed = [None] * len(ranges)
         te0, te1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier()
         w0 = time.perf_counter()
@@ -391,18 +395,21 @@ def main():
         for _ in range(args.e2e_steps):
             upped = []
             sim.set_stream(up.cuda_stream)
-            for c in range(comps):
-                if downed[c] is not None:
-                    up.wait_event(downed[c])
-                sim.state_copy_packed(0, c, host[c].data_ptr(), True)
+            for r, rg in enumerate(ranges):
+                if downed[r] is not None:
+                    up.wait_event(downed[r])
+                for c in range(comps):
+                    sim.state_copy_packed(0, c, host[c].data_ptr(), True, sc_range=rg)
                 ev = torch.cuda.Event()
                 ev.record(up)
                 upped.append(ev)
             h2d += slots * 4 * comps
-            for ev in upped:
-                stream.wait_event(ev)
             sim.set_stream(stream.cuda_stream)
-            one_step()   # returns once the step's device work is done (the migration reads flags)
+            sim.push_deposit_chunked([ev.cuda_event for ev in upped])
+            sim.update_b(0.5 * dt)
+            sim.update_e(dt)
+            sim.update_b(0.5 * dt)
+            sim.migrate()   # returns once the step's device work is done (it reads the flags)
             slots = sim.state_packed_slots(0)   # the image of the new layout and counts
             if slots > alloc:            # no copy is in flight here
                 torch.cuda.synchronize()
@@ -412,10 +419,11 @@ def main():
             stepped.record(stream)
             down.wait_event(stepped)
             sim.set_stream(down.cuda_stream)
-            for c in range(comps):
-                sim.state_copy_packed(0, c, host[c].data_ptr(), False)
-                downed[c] = torch.cuda.Event()
-                downed[c].record(down)
+            for r, rg in enumerate(ranges):
+                for c in range(comps):
+                    sim.state_copy_packed(0, c, host[c].data_ptr(), False, sc_range=rg)
+                downed[r] = torch.cuda.Event()
+                downed[r].record(down)
             sim.set_stream(stream.cuda_stream)
             d2h += slots * 4 * comps
             done += 1
@@ -427,10 +435,11 @@ def main():
         e_el = te0.elapsed_time(te1) / 1e3
         e2e = {"value": world * npart * done / max(e_el, wall), "unit": UNIT,
                "h2d_bytes_per_step": h2d // max(1, done), "d2h_bytes_per_step": d2h // max(1, done),
-               "steps": done, "path": "pica_state_copy_packed (pinned host) -> pica_push_deposit/update_b/"
-                                      "update_e/update_b/migrate -> pica_state_packed_slots, "
-                                      "pica_state_copy_packed; uploads and downloads on two copy streams, "
-                                      "overlapped across steps"}
+               "steps": done, "ranges": len(ranges),
+               "path": "pica_state_copy_packed_range (pinned host, per supercell range) -> "
+                       "pica_push_deposit_chunked (each range after its upload) -> pica_update_b/update_e/update_b/"
+                       "migrate -> pica_state_packed_slots, pica_state_copy_packed_range; uploads and downloads "
+                       "on two copy streams, overlapped across steps"}
         del host
     sim.close()
     del sim

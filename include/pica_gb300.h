@@ -151,6 +151,16 @@ int     pica_download_fields(pica_ctx* ctx, double* const* f9);
  *   then arrivals by direction code, each in source-slot order).
  * pica_step: push_deposit; update_b(dt/2); update_e(dt); update_b(dt/2); migrate. */
 int     pica_push_deposit(pica_ctx* ctx);
+/* pica_push_deposit as nchunks launches over consecutive ranges of supercells
+ * (range r: linear supercells [nscTot r / nchunks, nscTot (r+1) / nchunks)), the
+ * launch of range r enqueued on the context stream after a wait for
+ * wait_events[r] (a cudaEvent_t; NULL entries and a NULL array wait for nothing).
+ * A host loop that uploads the packed state range by range
+ * (pica_state_copy_packed_range) records one event per range, and the push of
+ * each range starts as soon as its particles are in.  Results equal those of
+ * pica_push_deposit bit for bit (FP32 form).  Forms other than the FP32
+ * Esirkepov one push in one launch after all the waits. */
+int     pica_push_deposit_chunked(pica_ctx* ctx, int32_t nchunks, void* const* wait_events);
 int     pica_update_b(pica_ctx* ctx, double dt);
 int     pica_update_e(pica_ctx* ctx, double dt);
 int     pica_migrate(pica_ctx* ctx);
@@ -199,6 +209,10 @@ int     pica_state_copy(pica_ctx* ctx, int32_t species, int32_t comp, void* host
  * PICA_ERR_STATE once it is out of date.  Components as for pica_state_copy. */
 int64_t pica_state_packed_slots(pica_ctx* ctx, int32_t species);
 int     pica_state_copy_packed(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device);
+/* The part of the image that belongs to supercells [sc_begin, sc_end) (linear
+ * supercell index, z fastest); host is still the start of the whole image. */
+int     pica_state_copy_packed_range(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device,
+                                     int32_t sc_begin, int32_t sc_end);
 
 /* Batching form: many independent plasmas advanced together (FP32 cell form,
  * Esirkepov deposition, one shape and one supercell size for all members; grids,

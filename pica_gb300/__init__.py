@@ -226,9 +226,27 @@ class Simulation:
             self._check(n)
         return n
 
-    def state_copy_packed(self, species, comp, host_ptr, to_device):
-        self._check(self.lib.pica_state_copy_packed(self.ctx, int(species), int(comp), C.c_void_p(int(host_ptr)),
-                                                    1 if to_device else 0))
+    def state_copy_packed(self, species, comp, host_ptr, to_device, sc_range=None):
+        """One component of the packed image; ``sc_range=(begin, end)``: only the part of
+        those supercells (host_ptr is still the start of the whole image)."""
+        if sc_range is None:
+            self._check(self.lib.pica_state_copy_packed(self.ctx, int(species), int(comp), C.c_void_p(int(host_ptr)),
+                                                        1 if to_device else 0))
+        else:
+            self._check(self.lib.pica_state_copy_packed_range(self.ctx, int(species), int(comp),
+                                                              C.c_void_p(int(host_ptr)), 1 if to_device else 0,
+                                                              int(sc_range[0]), int(sc_range[1])))
+
+    def chunk_ranges(self, nchunks):
+        """Supercell ranges of pica_push_deposit_chunked: [n r / nchunks, n (r+1) / nchunks)."""
+        tot = int(np.prod(self.nsc))
+        return [(tot * r // nchunks, tot * (r + 1) // nchunks) for r in range(nchunks)]
+
+    def push_deposit_chunked(self, wait_events):
+        """pica_push_deposit in len(wait_events) supercell ranges, range r launched after
+        a wait for wait_events[r] (cudaEvent_t handles as ints, or None)."""
+        arr = (C.c_void_p * len(wait_events))(*[C.c_void_p(int(e)) if e else None for e in wait_events])
+        self._check(self.lib.pica_push_deposit_chunked(self.ctx, len(wait_events), arr))
 
 
 class Driver:

@@ -314,8 +314,8 @@ int launchGauss(bool fp64, void* const* f, const double* rho, const int* n, cons
 namespace {
 __global__ void __launch_bounds__(256) k_packCopy(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
                                                   const int64_t* start, const int32_t* count, const int64_t* off,
-                                                  int words, bool gather) {
-    const int s = blockIdx.x;
+                                                  int scBegin, int words, bool gather) {
+    const int s = scBegin + blockIdx.x;
     const int64_t a = start[s] * words, b = off[s] * words;
     const int n = count[s] * words;
     if (gather) {
@@ -327,10 +327,10 @@ __global__ void __launch_bounds__(256) k_packCopy(const uint32_t* __restrict__ s
 }  // namespace
 
 int launchPackCopy(const void* src, void* dst, const int64_t* start, const int32_t* count, const int64_t* off,
-                   int nscTot, int words, bool gather, cudaStream_t s) {
-    if (nscTot <= 0) return 0;
-    k_packCopy<<<nscTot, 256, 0, s>>>(static_cast<const uint32_t*>(src), static_cast<uint32_t*>(dst), start, count,
-                                      off, words, gather);
+                   int scBegin, int scEnd, int words, bool gather, cudaStream_t s) {
+    if (scEnd <= scBegin) return 0;
+    k_packCopy<<<scEnd - scBegin, 256, 0, s>>>(static_cast<const uint32_t*>(src), static_cast<uint32_t*>(dst), start,
+                                               count, off, scBegin, words, gather);
     return (int)cudaGetLastError();
 }
 

@@ -49,6 +49,7 @@ struct SpeciesState {
     // offsets of the image, its size, the epoch it was laid out for, and one device
     // staging buffer per component.
     int64_t* d_packOff = nullptr;
+    std::vector<int64_t> h_packOff;   // host copy, nscTot + 1 entries
     int64_t packSlots = -1;
     int64_t packEpoch = -1;
     int64_t packCap = 0;
@@ -783,7 +784,12 @@ int pica_download_fields(pica_ctx* ctx, double* const* f9) {
     return PICA_OK;
 }
 
-int pica_push_deposit(pica_ctx* ctx) {
+}  // extern "C"
+
+// The push over all supercells, as nchunks launches over consecutive supercell
+// ranges (FP32 Esirkepov kernel; the other kernels take one launch after all
+// waits), the launch of range r enqueued after a wait for events[r] when given.
+static int pushImpl(pica_ctx* ctx, int nchunks, void* const* events) {
     if (!ctx) return PICA_ERR_INVALID;
     if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "push_deposit called twice without migrate");
     const pica_config& c = ctx->cfg;
@@ -791,18 +797,34 @@ int pica_push_deposit(pica_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->d_flags, 0, 4 * sizeof(int), ctx->stream));
     if (ctx->fp64)
         for (int k = 6; k < 9; k++) CK(cudaMemsetAsync(ctx->f[k], 0, nodes * 8, ctx->stream));
+    const bool ranges = !ctx->fp64 && c.deposit == PICA_DEPOSIT_ESIRKEPOV && nchunks > 1;
+    if (!ranges)
+        for (int r = 0; r < nchunks; r++)
+            if (events && events[r]) CK(cudaStreamWaitEvent(ctx->stream, static_cast<cudaEvent_t>(events[r]), 0));
     if (ctx->fp64) {
         PushArgs<PlainPtrs> a{};
         fillPushArgs(ctx, a);
         for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = plainPtrs(ctx, q, ctx->cur); a.sp[q].out = plainPtrs(ctx, q, 1 - ctx->cur); }
         CKL(launchPushPlain(a, c.shape, c.deposit, ctx->stream));
+        ctx->launches++;
     } else {
         PushArgs<CellPtrs> a{};
         fillPushArgs(ctx, a);
         for (int q = 0; q < c.nspecies; q++) { a.sp[q].buf = cellPtrs(ctx, q, ctx->cur); a.sp[q].out = cellPtrs(ctx, q, 1 - ctx->cur); }
-        CKL(launchPushCell(a, c.shape, c.deposit, ctx->variant, ctx->stream));
+        if (!ranges) {
+            CKL(launchPushCell(a, c.shape, c.deposit, ctx->variant, ctx->stream));
+            ctx->launches++;
+        } else {
+            for (int r = 0; r < nchunks; r++) {
+                if (events && events[r]) CK(cudaStreamWaitEvent(ctx->stream, static_cast<cudaEvent_t>(events[r]), 0));
+                a.scBegin = (int)((int64_t)ctx->nscTot * r / nchunks);
+                a.scEnd = (int)((int64_t)ctx->nscTot * (r + 1) / nchunks);
+                if (a.scEnd <= a.scBegin) continue;
+                CKL(launchPushCell(a, c.shape, c.deposit, ctx->variant, ctx->stream));
+                ctx->launches++;
+            }
+        }
     }
-    ctx->launches++;
     if (!ctx->fp64) {
         // J = sum / h^3 (CurrentDepositorYeeGrid.h:203), from the exact fixed-point sums.
         const double scale = (ctx->kmax * std::ldexp(1.0, -ctx->jfrac)) * (1.0 / (c.h[0] * c.h[1] * c.h[2]));
@@ -811,6 +833,16 @@ int pica_push_deposit(pica_ctx* ctx) {
     }
     ctx->pending = true;
     return PICA_OK;
+}
+
+extern "C" {
+
+int pica_push_deposit(pica_ctx* ctx) { return pushImpl(ctx, 1, nullptr); }
+
+int pica_push_deposit_chunked(pica_ctx* ctx, int32_t nchunks, void* const* wait_events) {
+    if (!ctx) return PICA_ERR_INVALID;
+    if (nchunks < 1 || nchunks > 4096) return fail(ctx, PICA_ERR_INVALID, "chunk count out of range (1..4096)");
+    return pushImpl(ctx, nchunks, wait_events);
 }
 
 int pica_update_b(pica_ctx* ctx, double dt) {
@@ -1155,6 +1187,8 @@ int64_t pica_state_packed_slots(pica_ctx* ctx, int32_t species) {
     CK(cudaStreamSynchronize(ctx->stream));
     int64_t total = 0;
     for (int s = 0; s < n; s++) { off[s] = total; total += count[s]; }
+    S.h_packOff.assign(off.begin(), off.end());
+    S.h_packOff.push_back(total);
     if (!S.d_packOff) CK(cudaMalloc(&S.d_packOff, (size_t)n * 8));
     CK(cudaMemcpyAsync(S.d_packOff, off.data(), (size_t)n * 8, cudaMemcpyHostToDevice, ctx->stream));
     if (total > S.packCap) {
@@ -1175,23 +1209,35 @@ int64_t pica_state_packed_slots(pica_ctx* ctx, int32_t species) {
 }
 
 int pica_state_copy_packed(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device) {
-    if (!ctx || !host || species < 0 || species >= ctx->cfg.nspecies || comp < 0 || comp >= ctx->ncomp)
+    if (!ctx) return PICA_ERR_INVALID;
+    return pica_state_copy_packed_range(ctx, species, comp, host, to_device, 0, ctx->nscTot);
+}
+
+int pica_state_copy_packed_range(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device,
+                                 int32_t sc_begin, int32_t sc_end) {
+    if (!ctx || !host || species < 0 || species >= ctx->cfg.nspecies || comp < 0 || comp >= ctx->ncomp ||
+        sc_begin < 0 || sc_end < sc_begin || sc_end > ctx->nscTot)
         return PICA_ERR_INVALID;
     if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "state copy while a migration is pending");
     SpeciesState& S = ctx->sp[species];
     if (S.packEpoch != ctx->epoch)
         return fail(ctx, PICA_ERR_STATE, "packed layout out of date: call pica_state_packed_slots after each step");
-    const size_t bytes = (size_t)S.packSlots * ctx->compBytes[comp];
-    const int words = (int)(ctx->compBytes[comp] / 4);
-    if (S.packSlots == 0) return PICA_OK;
+    // Image slots [off[sc_begin], off[sc_end]) of the host image and of the staging copy.
+    const size_t cb = ctx->compBytes[comp];
+    const int64_t o0 = S.h_packOff[sc_begin], o1 = S.h_packOff[sc_end];
+    const size_t bytes = (size_t)(o1 - o0) * cb;
+    const int words = (int)(cb / 4);
+    if (bytes == 0) return PICA_OK;
+    char* hp = static_cast<char*>(host) + (size_t)o0 * cb;
+    char* dp = static_cast<char*>(S.d_pack[comp]) + (size_t)o0 * cb;
     if (to_device) {
-        CK(cudaMemcpyAsync(S.d_pack[comp], host, bytes, cudaMemcpyHostToDevice, ctx->stream));
-        CKL(launchPackCopy(S.d_pack[comp], S.buf[ctx->cur][comp], S.d_start, S.d_count, S.d_packOff, ctx->nscTot,
+        CK(cudaMemcpyAsync(dp, hp, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        CKL(launchPackCopy(S.d_pack[comp], S.buf[ctx->cur][comp], S.d_start, S.d_count, S.d_packOff, sc_begin, sc_end,
                            words, false, ctx->stream));
     } else {
-        CKL(launchPackCopy(S.buf[ctx->cur][comp], S.d_pack[comp], S.d_start, S.d_count, S.d_packOff, ctx->nscTot,
+        CKL(launchPackCopy(S.buf[ctx->cur][comp], S.d_pack[comp], S.d_start, S.d_count, S.d_packOff, sc_begin, sc_end,
                            words, true, ctx->stream));
-        CK(cudaMemcpyAsync(host, S.d_pack[comp], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(hp, dp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     }
     ctx->launches++;
     return PICA_OK;

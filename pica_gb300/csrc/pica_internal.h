@@ -113,6 +113,7 @@ struct PushArgs {
     void* j[3];         // FP64 form: jx jy jz (double), summed with FP64 atomics
     double norm;        // FP64 form: 1 / (hx hy hz)
     int* flags;         // flags[0]: error code (0 = ok)
+    int scBegin, scEnd; // FP32 Esirkepov push: supercells [scBegin, scEnd) (scEnd 0: all)
     SpeciesArgs<P> sp[kMaxSpecies];
 };
 
@@ -137,6 +138,7 @@ struct PushArgsSlim {
     int n[3], S[3], nsc[3], T[3];
     int nspecies;
     int tileSplit;
+    int scOffset;       // first supercell of the launch (block b works on supercell scOffset + b)
     float cdth[3];
     float invUnit;
     const void* eb[6];
@@ -156,6 +158,7 @@ inline void slimArgs(const PushArgs<CellPtrs>& a, PushArgsSlim<NSP>& o) {
     }
     o.nspecies = a.nspecies;
     o.tileSplit = a.tileSplit;
+    o.scOffset = a.scBegin;
     o.invUnit = (float)a.invUnit;
     for (int k = 0; k < 6; k++) o.eb[k] = a.eb[k];
     o.flags = a.flags;
@@ -293,7 +296,7 @@ int launchGenerate(const GenArgs& a, int nscTot, cudaStream_t s);
 // gather: slots -> image (src = slot array, dst = image); else image -> slots
 // (src = image, dst = slot array).
 int launchPackCopy(const void* src, void* dst, const int64_t* start, const int32_t* count, const int64_t* off,
-                   int nscTot, int words, bool gather, cudaStream_t s);
+                   int scBegin, int scEnd, int words, bool gather, cudaStream_t s);
 // Gauss residual: max |div E - 4 pi (rho + bg)| and max |rho|; partial: 2*kReduceBlocks doubles.
 int launchGauss(bool fp64, void* const* f, const double* rho, const int* n, const double* h, double bg,
                 double* partial, double* out2, cudaStream_t s);

@@ -730,7 +730,7 @@ template <int SHAPE, int K, int THREADS, int MINB, int SC>
 __global__ void __launch_bounds__(THREADS, MINB) k_push_cell_esirkepov(const __grid_constant__ PushArgsSlim<kMaxSpecies> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_nleave;
-    pushSupercell<SHAPE, K, THREADS, SC>(a, blockIdx.x, smem_raw, s_nleave);
+    pushSupercell<SHAPE, K, THREADS, SC>(a, a.scOffset + (int)blockIdx.x, smem_raw, s_nleave);
 }
 
 // Batching form: one persistent launch over the supercells of many independent

@@ -30,9 +30,10 @@ int launchEsirkepovV(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return (int)e;
     const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
+    const int n = a.scEnd > a.scBegin ? a.scEnd - a.scBegin : nscTot;
     PushArgsSlim<kMaxSpecies> sl;
     slimArgs(a, sl);
-    k<<<nscTot, THREADS, smem, s>>>(sl);
+    k<<<n, THREADS, smem, s>>>(sl);
     return (int)cudaGetLastError();
 }
 

@@ -157,3 +157,66 @@ def test_packed_image_holds_the_ensemble_and_goes_stale_after_a_step():
     with pytest.raises(pg.PicaError):
         s.state_copy_packed(0, 4, comp["ux"].ctypes.data, False)
     s.close()
+
+
+@pytest.mark.parametrize("nchunks", [3, 8])
+def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks):
+    """The packed image uploaded supercell range by supercell range, each range's push
+    launched once its upload is in (pica_push_deposit_chunked), downloaded range by
+    range: equal to plain steps bit for bit."""
+    n = (16, 8, 8)
+    d = thermal_inputs(n, 6, seed=76, u_sigma=0.2)
+    steps, comps = 5, 8
+    ref = make(d, n)
+    ref.step(steps)
+    a = make(d, n)
+    main = torch.cuda.current_stream()
+    a.set_stream(main.cuda_stream)
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
+    ranges = a.chunk_ranges(nchunks)
+    assert ranges[0][0] == 0 and ranges[-1][1] == int(np.prod(a.nsc))
+    packed = a.state_packed_slots(0)
+    alloc = 2 * packed + 1024
+    host = [torch.empty(alloc * 4, dtype=torch.uint8, pin_memory=True) for _ in range(comps)]
+    for c in range(comps):
+        a.state_copy_packed(0, c, host[c].data_ptr(), False)
+    torch.cuda.synchronize()
+    downed = [None] * nchunks
+    for _ in range(steps):
+        a.set_stream(up.cuda_stream)
+        upped = []
+        for r, rg in enumerate(ranges):
+            if downed[r] is not None:
+                up.wait_event(downed[r])
+            for c in range(comps):
+                a.state_copy_packed(0, c, host[c].data_ptr(), True, sc_range=rg)
+            ev = torch.cuda.Event()
+            ev.record(up)
+            upped.append(ev)
+        a.set_stream(main.cuda_stream)
+        a.push_deposit_chunked([ev.cuda_event for ev in upped])
+        a.update_b(0.5 * a.dt)
+        a.update_e(a.dt)
+        a.update_b(0.5 * a.dt)
+        a.migrate()
+        assert a.state_packed_slots(0) <= alloc
+        stepped = torch.cuda.Event()
+        stepped.record(main)
+        down.wait_event(stepped)
+        a.set_stream(down.cuda_stream)
+        for r, rg in enumerate(ranges):
+            for c in range(comps):
+                a.state_copy_packed(0, c, host[c].data_ptr(), False, sc_range=rg)
+            downed[r] = torch.cuda.Event()
+            downed[r].record(down)
+        a.set_stream(main.cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(a.counts(), ref.counts())
+    pa, pr = a.particles(), ref.particles()
+    for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species", "supercell"):
+        assert np.array_equal(pa[k], pr[k]), k
+    fa, fr = a.fields(), ref.fields()
+    for c in range(9):
+        assert np.array_equal(fa[c], fr[c]), c
+    a.close()
+    ref.close()
