@@ -205,6 +205,16 @@ public:
     void copyStatePacked(int species, int comp, void* host, bool toDevice) {
         check(ctx_, pica_state_copy_packed(ctx_, species, comp, host, toDevice ? 1 : 0));
     }
+    // The image part of supercells [scBegin, scEnd) (host: start of the whole image).
+    void copyStatePackedRange(int species, int comp, void* host, bool toDevice, int scBegin, int scEnd) {
+        check(ctx_, pica_state_copy_packed_range(ctx_, species, comp, host, toDevice ? 1 : 0, scBegin, scEnd));
+    }
+    // The push in waitEvents.size() supercell ranges, range r after a wait for
+    // waitEvents[r] (cudaEvent_t or nullptr); the rest of the step follows as in a
+    // pica host loop: YeeSolver updateB(dt/2), updateE(dt), updateB(dt/2), ensemble().migrate().
+    void pushDepositChunked(const std::vector<void*>& waitEvents) {
+        check(ctx_, pica_push_deposit_chunked(ctx_, (int32_t)waitEvents.size(), waitEvents.data()));
+    }
     // Complete state between steps; a Simulation of the same Config loaded from it
     // continues like this one (FP32 form: bit for bit).
     void saveCheckpoint(const std::string& path) { check(ctx_, pica_checkpoint_save(ctx_, path.c_str())); }
