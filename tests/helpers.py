@@ -57,3 +57,24 @@ def thermal_inputs(n, ppc, seed, u_sigma=0.05, hscale=(1.0, 1.0, 1.0), nspecies=
 
 def particle_args(d):
     return [d[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w")] + [d["species"]]
+
+
+def run_1d_golden(make_sim, g, sc=(4, 1, 1)):
+    """Run the pica_1d_cic_direct fixture (pica's YeeGrid<One> path) on a grid one cell
+    thick along y and z; make_sim(n3, sc, h3, dt) returns an object with load-style
+    (upload, set_fields, step, fields, particles) callables.  Returns (fields, particles
+    sorted by x, the fixture's outputs sorted by x)."""
+    n, h = int(g["n"]), float(g["h"])
+    np_ = len(g["in_x"])
+    yz = np.full(np_, 0.5 * h)
+    load, set_fields, step, fields, particles = make_sim((n, 1, 1), sc, (h, h, h), float(g["dt"]))
+    load(g["in_x"], yz, yz, g["in_ux"], g["in_uy"], g["in_uz"], g["in_w"], np.zeros(np_, np.int32))
+    set_fields([a.reshape(n, 1, 1) for a in g["in_fields"][:6]] + [np.zeros((n, 1, 1))] * 3)
+    step(int(g["steps"]))
+    f = [a.reshape(-1) for a in fields()]
+    p = particles()
+    order = np.argsort(p["x"])
+    ref_order = np.argsort(g["out_x"])
+    got = {k: p[k][order] for k in ("x", "ux", "uy", "uz")}
+    ref = {k: g["out_" + k][ref_order] for k in ("x", "ux", "uy", "uz")}
+    return f, got, ref

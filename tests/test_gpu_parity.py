@@ -11,7 +11,7 @@ import pytest
 
 import pica_gb300 as pg
 from oracle import pic_oracle as po
-from tests.helpers import load_golden, particle_args, periodic_err, rel_err, species_of, thermal_inputs
+from tests.helpers import load_golden, particle_args, periodic_err, rel_err, run_1d_golden, species_of, thermal_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -295,3 +295,23 @@ def test_autotune_picks_a_variant():
     assert len(times) == s.variant()[1]
     assert s.variant()[0] == min(times, key=times.get)
     assert s.num_particles() == len(d["x"])
+
+
+def test_fp64_one_cell_thick_grid_matches_pica_1d_classes():
+    """The FP64 plain form on a grid one cell thick along y and z against pica's own 1D
+    path (golden fixture from oracle/ref_harness_1d.cpp): fields and particles within
+    FP64_TOL."""
+    g = load_golden("pica_1d_cic_direct")
+    sims = []
+
+    def make(n3, sc, h3, dt):
+        s = gpu_sim(n3, sc, h3, dt)
+        sims.append(s)
+        return s.upload_particles, s.upload_fields, s.step, s.fields, s.particles
+
+    f, got, ref = run_1d_golden(make, g)
+    for c in range(9):
+        assert rel_err(f[c], g["out_fields"][c]) <= FP64_TOL, c
+    for k in ("x", "ux", "uy", "uz"):
+        assert rel_err(got[k], ref[k]) <= FP64_TOL, k
+    sims[0].close()

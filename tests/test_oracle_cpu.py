@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from oracle import pic_oracle as po
-from tests.helpers import C, E, ME, load_golden, rel_err, species_of, thermal_inputs
+from tests.helpers import C, E, ME, load_golden, rel_err, run_1d_golden, species_of, thermal_inputs
 
 REFERENCE_AVAILABLE = os.path.isdir("/root/reference/include/pica") or os.path.exists(po.REF_SO)
 
@@ -169,3 +169,20 @@ def test_diagnostics_conservation():
     assert abs(e1 - e0) / e0 < 2e-2
     # Esirkepov keeps div E - 4 pi rho at its initial value.
     assert abs(d1["gauss_max"] - d0["gauss_max"]) / d0["gauss_max"] < 0.5
+
+
+def test_oracle_one_cell_thick_grid_matches_pica_1d_classes():
+    """A grid one cell thick along y and z against pica's own 1D path (YeeGrid<One>,
+    FieldInterpolatorCIC / CurrentDepositorCIC<YeeGrid<One>>, the 1D YeeSolver; golden
+    fixture from oracle/ref_harness_1d.cpp): fields and particles within 1e-12."""
+    g = load_golden("pica_1d_cic_direct")
+
+    def make(n3, sc, h3, dt):
+        o = po.Oracle(n3, sc, h3, dt, form=po.FORM_FP64_PLAIN, shape=po.SHAPE_CIC, deposit=po.DEPOSIT_DIRECT)
+        return o.load, o.set_fields, o.step, o.get_fields, o.particles
+
+    f, got, ref = run_1d_golden(make, g)
+    for c in range(9):
+        assert rel_err(f[c], g["out_fields"][c]) <= 1e-12, c
+    for k in ("x", "ux", "uy", "uz"):
+        assert rel_err(got[k], ref[k]) <= 1e-12, k
