@@ -68,6 +68,86 @@ __global__ void __launch_bounds__(256) k_updateE(R* __restrict__ ex, R* __restri
     }
 }
 
+// FP32 forms of the two stencils with float4 accesses along z (nz a multiple of 4):
+// one thread updates four consecutive cells of a row.  The x and y neighbours are
+// whole float4 rows of the neighbouring planes; the z neighbour of the first (B) or
+// last (E) cell comes from one more scalar load, wrapped within the row.  Each
+// element is the scalar kernel's expression, so results are the same.
+struct Row4 {
+    int64_t o, xm, ym, xp, yp, zm1, zp4;   // row starts of the neighbours; the z neighbours' scalars
+};
+__device__ __forceinline__ Row4 row4(int64_t g, int nx, int ny, int nz) {
+    const int nz4 = nz >> 2;
+    const int k0 = (int)(g % nz4) * 4;
+    const int j = (int)((g / nz4) % ny);
+    const int i = (int)(g / ((int64_t)nz4 * ny));
+    const int64_t sx = (int64_t)ny * nz, sy = nz;
+    Row4 r;
+    r.o = ((int64_t)i * ny + j) * nz + k0;
+    r.xm = r.o + (i == 0 ? (int64_t)(nx - 1) * sx : -sx);
+    r.xp = r.o + (i == nx - 1 ? -(int64_t)(nx - 1) * sx : sx);
+    r.ym = r.o + (j == 0 ? (int64_t)(ny - 1) * sy : -sy);
+    r.yp = r.o + (j == ny - 1 ? -(int64_t)(ny - 1) * sy : sy);
+    r.zm1 = k0 == 0 ? r.o + nz - 1 : r.o - 1;
+    r.zp4 = k0 + 4 == nz ? r.o - (nz - 4) : r.o + 4;
+    return r;
+}
+__device__ __forceinline__ float4 ld4(const float* p, int64_t i) { return *reinterpret_cast<const float4*>(p + i); }
+__device__ __forceinline__ float el(const float4& v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
+__device__ __forceinline__ void setEl(float4& v, int e, float x) {
+    if (e == 0) v.x = x; else if (e == 1) v.y = x; else if (e == 2) v.z = x; else v.w = x;
+}
+
+__global__ void __launch_bounds__(256) k_updateB4(float* __restrict__ bx, float* __restrict__ by, float* __restrict__ bz,
+                                                  const float* __restrict__ ex, const float* __restrict__ ey,
+                                                  const float* __restrict__ ez, int nx, int ny, int nz, float cx,
+                                                  float cy, float cz) {
+    const int64_t total = (int64_t)nx * ny * (nz >> 2);
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const Row4 r = row4(g, nx, ny, nz);
+        const float4 exo = ld4(ex, r.o), eyo = ld4(ey, r.o), ezo = ld4(ez, r.o);
+        const float4 exym = ld4(ex, r.ym), eyxm = ld4(ey, r.xm), ezxm = ld4(ez, r.xm), ezym = ld4(ez, r.ym);
+        const float exzm0 = ex[r.zm1], eyzm0 = ey[r.zm1];
+        float4 b0 = ld4(bx, r.o), b1 = ld4(by, r.o), b2 = ld4(bz, r.o);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const float eyzm = e == 0 ? eyzm0 : el(eyo, e - 1), exzm = e == 0 ? exzm0 : el(exo, e - 1);
+            setEl(b0, e, el(b0, e) + (cz * (el(eyo, e) - eyzm) - cy * (el(ezo, e) - el(ezym, e))));
+            setEl(b1, e, el(b1, e) + (cx * (el(ezo, e) - el(ezxm, e)) - cz * (el(exo, e) - exzm)));
+            setEl(b2, e, el(b2, e) + (cy * (el(exo, e) - el(exym, e)) - cx * (el(eyo, e) - el(eyxm, e))));
+        }
+        *reinterpret_cast<float4*>(bx + r.o) = b0;
+        *reinterpret_cast<float4*>(by + r.o) = b1;
+        *reinterpret_cast<float4*>(bz + r.o) = b2;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_updateE4(float* __restrict__ ex, float* __restrict__ ey, float* __restrict__ ez,
+                                                  const float* __restrict__ bx, const float* __restrict__ by,
+                                                  const float* __restrict__ bz, const float* __restrict__ jx,
+                                                  const float* __restrict__ jy, const float* __restrict__ jz, int nx,
+                                                  int ny, int nz, float cc, float cx, float cy, float cz) {
+    const int64_t total = (int64_t)nx * ny * (nz >> 2);
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const Row4 r = row4(g, nx, ny, nz);
+        const float4 bxo = ld4(bx, r.o), byo = ld4(by, r.o), bzo = ld4(bz, r.o);
+        const float4 bzyp = ld4(bz, r.yp), bzxp = ld4(bz, r.xp), byxp = ld4(by, r.xp), bxyp = ld4(bx, r.yp);
+        const float byzp3 = by[r.zp4], bxzp3 = bx[r.zp4];
+        const float4 j0 = ld4(jx, r.o), j1 = ld4(jy, r.o), j2 = ld4(jz, r.o);
+        float4 e0 = ld4(ex, r.o), e1 = ld4(ey, r.o), e2 = ld4(ez, r.o);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const float byzp = e == 3 ? byzp3 : el(byo, e + 1), bxzp = e == 3 ? bxzp3 : el(bxo, e + 1);
+            setEl(e0, e, el(e0, e) + (cc * el(j0, e) + cy * (el(bzyp, e) - el(bzo, e)) - cz * (byzp - el(byo, e))));
+            setEl(e1, e, el(e1, e) + (cc * el(j1, e) + cz * (bxzp - el(bxo, e)) - cx * (el(bzxp, e) - el(bzo, e))));
+            setEl(e2, e, el(e2, e) + (cc * el(j2, e) + cx * (el(byxp, e) - el(byo, e)) - cy * (el(bxyp, e) - el(bxo, e))));
+        }
+        *reinterpret_cast<float4*>(ex + r.o) = e0;
+        *reinterpret_cast<float4*>(ey + r.o) = e1;
+        *reinterpret_cast<float4*>(ez + r.o) = e2;
+    }
+}
+
 // J = Jacc * scale (one rounding from the exact integer sum), and clear Jacc for the next deposit.
 template <typename R>
 __global__ void __launch_bounds__(256) k_convertJ(R* __restrict__ jx, R* __restrict__ jy, R* __restrict__ jz,
@@ -255,6 +335,10 @@ int launchUpdateB(bool fp64, void* const* f, const int* n, const double* c, cuda
     if (fp64)
         k_updateB<double><<<gridFor(total), 256, 0, s>>>((double*)f[3], (double*)f[4], (double*)f[5], (const double*)f[0],
                                                          (const double*)f[1], (const double*)f[2], n[0], n[1], n[2], c[0], c[1], c[2]);
+    else if (n[2] % 4 == 0)
+        k_updateB4<<<gridFor(total / 4), 256, 0, s>>>((float*)f[3], (float*)f[4], (float*)f[5], (const float*)f[0],
+                                                       (const float*)f[1], (const float*)f[2], n[0], n[1], n[2],
+                                                       (float)c[0], (float)c[1], (float)c[2]);
     else
         k_updateB<float><<<gridFor(total), 256, 0, s>>>((float*)f[3], (float*)f[4], (float*)f[5], (const float*)f[0],
                                                         (const float*)f[1], (const float*)f[2], n[0], n[1], n[2], (float)c[0],
@@ -269,6 +353,11 @@ int launchUpdateE(bool fp64, void* const* f, const int* n, double cc, const doub
                                                          (const double*)f[4], (const double*)f[5], (const double*)f[6],
                                                          (const double*)f[7], (const double*)f[8], n[0], n[1], n[2], cc,
                                                          c[0], c[1], c[2]);
+    else if (n[2] % 4 == 0)
+        k_updateE4<<<gridFor(total / 4), 256, 0, s>>>((float*)f[0], (float*)f[1], (float*)f[2], (const float*)f[3],
+                                                       (const float*)f[4], (const float*)f[5], (const float*)f[6],
+                                                       (const float*)f[7], (const float*)f[8], n[0], n[1], n[2],
+                                                       (float)cc, (float)c[0], (float)c[1], (float)c[2]);
     else
         k_updateE<float><<<gridFor(total), 256, 0, s>>>((float*)f[0], (float*)f[1], (float*)f[2], (const float*)f[3],
                                                         (const float*)f[4], (const float*)f[5], (const float*)f[6],
