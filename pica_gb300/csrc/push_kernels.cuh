@@ -829,8 +829,9 @@ __device__ __forceinline__ int arrivalBuckets(const MigrateArgs<P>& a, const Mig
 }
 
 // Arrivals at supercell d in canonical order -- by direction code (the move from the
-// source), then by source slot -- 32 at a time across the buckets.  fn(k, src, slot, r):
-// the k-th arrival, from slot `slot` of supercell src, entry r of src's lbydir list.
+// source), then by source slot -- 32 at a time across the buckets.  fn(k, src, rec, r,
+// srcStart): the k-th arrival, whose record is at srcStart + rec in the side buffer
+// (srcStart: the first slot of supercell src), entry r of src's lbydir list.
 template <class P, class F>
 __device__ __forceinline__ int forArrivals(const MigrateArgs<P>& a, const MigrateSpecies<P>& sa, int d, F&& fn, int sub = 0,
                                           int nsub = 1) {
@@ -854,7 +855,7 @@ __device__ __forceinline__ int forArrivals(const MigrateArgs<P>& a, const Migrat
         const int64_t kst = __shfl_sync(FULL, sst, c);
         if (k < total) {
             const int r = kb + (k - kp);
-            fn(k, ks, sa.lbydir[kst + r], r);
+            fn(k, ks, sa.lbydir[kst + r], r, kst);
         }
     }
     return total;
@@ -889,7 +890,7 @@ __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ Migrate
             const int64_t ns = sa.newStart[d];
             for (int i = lane; i < cnt; i += 32) copyParticle(sa.a, start + i, sa.dst, ns + i);
             __syncwarp();
-            arrivals = forArrivals(a, sa, d, [&](int k, int src, int, int r) {
+            arrivals = forArrivals(a, sa, d, [&](int k, int src, int, int r, int64_t) {
                 const int target = k < nh ? sa.llist[start + k] : cnt + (k - nh);
                 copyParticle(sa.outbox, sa.outOff[src] + r, sa.dst, ns + target);
             });
@@ -914,9 +915,9 @@ __global__ void __launch_bounds__(kFillWarps * 32) k_fill(const __grid_constant_
         const int alive = sa.alive[d];
         const int arrivals = forArrivals(
             a, sa, d,
-            [&](int k, int src, int slot, int) {
+            [&](int k, int, int slot, int, int64_t srcStart) {
                 const int target = k < nh ? sa.llist[start + k] : cnt + (k - nh);
-                copyParticle(sa.b, sa.start[src] + slot, sa.a, start + target);
+                copyParticle(sa.b, srcStart + slot, sa.a, start + target);
             },
             warp, kFillWarps);
         __syncthreads();   // every warp has read count and alive
