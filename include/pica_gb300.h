@@ -151,6 +151,12 @@ int     pica_download_fields(pica_ctx* ctx, double* const* f9);
  *   then arrivals by direction code, each in source-slot order).
  * pica_step: push_deposit; update_b(dt/2); update_e(dt); update_b(dt/2); migrate. */
 int     pica_push_deposit(pica_ctx* ctx);
+/* Sort every supercell by cell now, dropping its dead slots (what the periodic
+ * resort does every resort_every steps): the GPU counterpart of
+ * EnsembleOrdered::reorder (particles/EnsembleOrdered.h:61-71), which sorts a flat
+ * array by position; here the order is (species, supercell, cell, slot).
+ * PICA_ERR_STATE between push_deposit and migrate. */
+int     pica_reorder(pica_ctx* ctx);
 /* pica_push_deposit as nchunks launches over consecutive ranges of supercells
  * (range r: linear supercells [nscTot r / nchunks, nscTot (r+1) / nchunks)), the
  * launch of range r enqueued on the context stream after a wait for

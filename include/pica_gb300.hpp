@@ -136,6 +136,8 @@ public:
     Int3 getNumSupercells() const { return nsc_; }
     Int3 getNumCellsPerSupercell() const { return S_; }
     inline void migrate();
+    // Sort every supercell by cell now (EnsembleOrdered::reorder, EnsembleOrdered.h:61-71).
+    inline void reorder();
 
 private:
     friend class Simulation;
@@ -295,6 +297,7 @@ std::vector<int32_t> EnsembleSupercells::counts() const {
     return c;
 }
 void EnsembleSupercells::migrate() { check(ctx_, pica_migrate(ctx_)); }
+void EnsembleSupercells::reorder() { check(ctx_, pica_reorder(ctx_)); }
 
 // pica YeeSolver (fieldSolver/YeeSolver.h:11-38) on the periodic device grid.
 class YeeSolver {

@@ -237,6 +237,10 @@ class Simulation:
                                                               C.c_void_p(int(host_ptr)), 1 if to_device else 0,
                                                               int(sc_range[0]), int(sc_range[1])))
 
+    def reorder(self):
+        """Sort every supercell by cell now (EnsembleOrdered::reorder's role)."""
+        self._check(self.lib.pica_reorder(self.ctx))
+
     def chunk_ranges(self, nchunks):
         """Supercell ranges of pica_push_deposit_chunked: [n r / nchunks, n (r+1) / nchunks)."""
         tot = int(np.prod(self.nsc))

@@ -1072,6 +1072,12 @@ int pica_migrate(pica_ctx* ctx) {
     return ctx->fp64 ? migrateImpl<PlainPtrs>(ctx) : migrateImpl<CellPtrs>(ctx);
 }
 
+int pica_reorder(pica_ctx* ctx) {
+    if (!ctx) return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "reorder between push_deposit and migrate");
+    return ctx->fp64 ? resortNow<PlainPtrs>(ctx) : resortNow<CellPtrs>(ctx);
+}
+
 int pica_step(pica_ctx* ctx, int32_t nsteps) {
     if (!ctx || nsteps < 0) return PICA_ERR_INVALID;
     const double dt = ctx->cfg.dt;

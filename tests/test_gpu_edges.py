@@ -109,3 +109,32 @@ def test_two_and_one_dimensional_grids(n, sc, form, shape, dep):
     f9 = [1e3 * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3
     s, o = run_both(n, sc, d, 5, form, shape, dep, fields=f9, resort_every=2)
     check(s, o, n, d["h"], form)
+
+
+@pytest.mark.parametrize("form,shape,dep", FORMS)
+def test_reorder_sorts_each_supercell_like_the_oracle_load(form, shape, dep):
+    """pica_reorder (EnsembleOrdered::reorder's role): after steps without a resort the
+    particles are out of cell order; reordering gives each supercell its live particles
+    by (cell, slot), the order the oracle's stable load of the same particles gives."""
+    n, sc = (8, 8, 8), (4, 4, 4)
+    d = thermal_inputs(n, 6, seed=68, u_sigma=0.3)
+    s = pg.Simulation(n, d["h"], d["dt"], supercell=sc, form=form, shape=shape, deposit=dep)
+    s.upload_particles(*particle_args(d))
+    s.upload_fields([np.zeros(n)] * 9)
+    s.step(4)
+    before = s.particles()
+    s.reorder()
+    after = s.particles()
+    o = po.Oracle(n, sc, d["h"], d["dt"], form=form, shape=shape, deposit=dep)
+    o.load(*[before[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species")])
+    ref = o.particles()
+    assert np.array_equal(s.counts(), o.counts())
+    for k in ("species", "supercell", "ux", "uy", "uz", "w"):
+        assert np.array_equal(after[k], ref[k]), k
+    # Positions pass through the oracle's load (FP32 form: back to cell + offset), so to
+    # the rounding of that conversion; an order difference would show as O(h).
+    for k in ("x", "y", "z"):
+        assert np.max(np.abs(after[k] - ref[k])) <= 1e-9 * d["h"][0], k
+    s.step(1)   # the context steps on from the new order
+    assert s.num_particles() == len(before["x"])
+    s.close()
