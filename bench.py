@@ -207,21 +207,25 @@ def named_workload(name, edge=None):
     return wl, desc
 
 
-def cpu_sample(args, steps=None, seconds=None):
+def cpu_sample(args, steps=None, seconds=None, pica_path=False):
     """Oracle restatement of the same step on a 32^3-cell block of the workload (same ppc,
-    supercell, form factor and deposition), all host cores.  Returns (value, cores, sample)."""
+    supercell, form factor and deposition), all host cores.  With `pica_path`, the same block
+    through pica's own arithmetic instead: FP64 positions, CIC, Boris, direct deposition (the
+    oracle form equal bit for bit to a harness over pica's headers).  Returns (value, cores,
+    sample, seconds)."""
     import pica_gb300 as pg
     from oracle import pic_oracle as po
 
-    from pica_gb300 import workloads
-
     edge = 32
-    wl = make_workload(edge, pg.FORM_FP32_CELL)
+    wl = make_workload(edge, pg.FORM_FP64_PLAIN if pica_path else pg.FORM_FP32_CELL)
     p = pg.generate_plasma(wl["specs"][0])
     sim = wl["sim"]
     cores = os.cpu_count() or 1
-    o = po.Oracle(sim["n"], sim["supercell"], sim["h"], sim["dt"], form=po.FORM_FP32_CELL, shape=po.SHAPE_TSC,
-                  deposit=po.DEPOSIT_ESIRKEPOV, threads=cores)
+    if pica_path:
+        kw = dict(form=po.FORM_FP64_PLAIN, shape=po.SHAPE_CIC, deposit=po.DEPOSIT_DIRECT)
+    else:
+        kw = dict(form=po.FORM_FP32_CELL, shape=po.SHAPE_TSC, deposit=po.DEPOSIT_ESIRKEPOV)
+    o = po.Oracle(sim["n"], sim["supercell"], sim["h"], sim["dt"], threads=cores, **kw)
     o.load(p["x"], p["y"], p["z"], p["ux"], p["uy"], p["uz"], p["w"], p["species"])
     o.set_fields([np.zeros(sim["n"])] * 9)
     npart = len(p["x"])
@@ -233,9 +237,13 @@ def cpu_sample(args, steps=None, seconds=None):
     t = time.perf_counter()
     o.step(steps)
     el = time.perf_counter() - t
-    del workloads
-    sample = (f"{edge}^3 cells x 100 ppc ({npart} electrons), TSC, Esirkepov, supercell 4^3, FP32 cell form, "
-              f"{steps} steps, oracle restatement (pica has no TSC/Esirkepov), OpenMP {cores} threads")
+    if pica_path:
+        sample = (f"{edge}^3 cells x 100 ppc ({npart} electrons), pica's path: FP64 positions, CIC, Boris, direct "
+                  f"deposition, supercell 4^3, {steps} steps, oracle form equal bit for bit to pica's headers, "
+                  f"OpenMP {cores} threads")
+    else:
+        sample = (f"{edge}^3 cells x 100 ppc ({npart} electrons), TSC, Esirkepov, supercell 4^3, FP32 cell form, "
+                  f"{steps} steps, oracle restatement (pica has no TSC/Esirkepov), OpenMP {cores} threads")
     return npart * steps / el, cores, sample, el
 
 
@@ -485,6 +493,8 @@ def main():
     if headline and not args.no_cpu_baseline:
         v, cores, sample, _ = cpu_sample(args, seconds=args.cpu_seconds)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        v, cores, sample, _ = cpu_sample(args, seconds=0.5 * args.cpu_seconds, pica_path=True)
+        cpu["pica_path"] = {"value": v, "unit": UNIT, "cores": cores, "sample": sample}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": 1e3 * elapsed / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
