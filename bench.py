@@ -88,7 +88,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=12)
-    ap.add_argument("--e2e-chunks", type=int, default=8, help="supercell ranges of the e2e upload / push pipeline")
+    ap.add_argument("--e2e-chunks", type=int, default=16, help="supercell ranges of the e2e upload / push pipeline")
+    ap.add_argument("--e2e-split", type=int, default=1,
+                    help="1: e2e host copies on copy streams of their own, gather / scatter kernels on two more")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -377,13 +379,19 @@ def main():
     # downloads on another; range r of step n+1 goes up as soon as range r of step
     # n is down, so the two link directions overlap, and the push of range r starts
     # as soon as its upload is in (pica_push_deposit_chunked), overlapping the rest
-    # of the upload.
+    # of the upload.  With --e2e-split the host copies run on two copy streams and
+    # the gather / scatter kernels on two others (pica_state_copy_packed_range_on),
+    # so that each direction's copies follow one another without waiting for the
+    # kernels in between.
     e2e = None
     if headline and args.e2e_steps > 0:
         comps = 8
         done = h2d = d2h = 0
         # High priority: the copy streams' pack and unpack kernels get SMs ahead of the push.
         up, down = torch.cuda.Stream(priority=-1), torch.cuda.Stream(priority=-1)
+        upc, downc = (torch.cuda.Stream(priority=-1), torch.cuda.Stream(priority=-1)) if args.e2e_split else (up, down)
+        cs_up = upc.cuda_stream if args.e2e_split else None
+        cs_down = downc.cuda_stream if args.e2e_split else None
         ranges = sim.chunk_ranges(args.e2e_chunks)
         # Pinned host buffers are set up once, outside the timed region, with room
         # for the layout to grow at a resort or capacity rebuild.
@@ -400,14 +408,15 @@ def main():
         w0 = time.perf_counter()
         te0.record(stream)
         up.wait_event(te0)
+        upc.wait_event(te0)
         for _ in range(args.e2e_steps):
             upped = []
             sim.set_stream(up.cuda_stream)
             for r, rg in enumerate(ranges):
                 if downed[r] is not None:
-                    up.wait_event(downed[r])
+                    upc.wait_event(downed[r])
                 for c in range(comps):
-                    sim.state_copy_packed(0, c, host[c].data_ptr(), True, sc_range=rg)
+                    sim.state_copy_packed(0, c, host[c].data_ptr(), True, sc_range=rg, copy_stream=cs_up)
                 ev = torch.cuda.Event()
                 ev.record(up)
                 upped.append(ev)
@@ -429,9 +438,9 @@ def main():
             sim.set_stream(down.cuda_stream)
             for r, rg in enumerate(ranges):
                 for c in range(comps):
-                    sim.state_copy_packed(0, c, host[c].data_ptr(), False, sc_range=rg)
+                    sim.state_copy_packed(0, c, host[c].data_ptr(), False, sc_range=rg, copy_stream=cs_down)
                 downed[r] = torch.cuda.Event()
-                downed[r].record(down)
+                downed[r].record(downc)
             sim.set_stream(stream.cuda_stream)
             d2h += slots * 4 * comps
             done += 1
@@ -443,8 +452,13 @@ def main():
         e_el = te0.elapsed_time(te1) / 1e3
         e2e = {"value": world * npart * done / max(e_el, wall), "unit": UNIT,
                "h2d_bytes_per_step": h2d // max(1, done), "d2h_bytes_per_step": d2h // max(1, done),
-               "steps": done, "ranges": len(ranges),
-               "path": "pica_state_copy_packed_range (pinned host, per supercell range) -> "
+               "steps": done, "ranges": len(ranges), "split_copy_streams": bool(args.e2e_split),
+               "path": "pica_state_copy_packed_range_on (pinned host, per supercell range) -> "
+                       "pica_push_deposit_chunked (each range after its upload) -> pica_update_b/update_e/update_b/"
+                       "migrate -> pica_state_packed_slots, pica_state_copy_packed_range_on; uploads and downloads "
+                       "overlapped across steps, host copies on copy streams apart from the gather / scatter "
+                       "kernels" if args.e2e_split else
+                       "pica_state_copy_packed_range (pinned host, per supercell range) -> "
                        "pica_push_deposit_chunked (each range after its upload) -> pica_update_b/update_e/update_b/"
                        "migrate -> pica_state_packed_slots, pica_state_copy_packed_range; uploads and downloads "
                        "on two copy streams, overlapped across steps"}

@@ -219,6 +219,15 @@ int     pica_state_copy_packed(pica_ctx* ctx, int32_t species, int32_t comp, voi
  * supercell index, z fastest); host is still the start of the whole image. */
 int     pica_state_copy_packed_range(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device,
                                      int32_t sc_begin, int32_t sc_end);
+/* pica_state_copy_packed_range with the host copy enqueued on copy_stream (a
+ * cudaStream_t; NULL: the context stream) and the gather / scatter kernel on the
+ * context stream, ordered by an event: an upload's scatter waits for its copy,
+ * a download's copy for its gather.  A host loop that keeps its copies on streams
+ * of their own runs them back to back instead of behind each range's kernels.
+ * The caller orders later work against the copy stream (a download is complete
+ * once the copy stream has passed it). */
+int     pica_state_copy_packed_range_on(pica_ctx* ctx, int32_t species, int32_t comp, void* host,
+                                        int32_t to_device, int32_t sc_begin, int32_t sc_end, void* copy_stream);
 
 /* Batching form: many independent plasmas advanced together (FP32 cell form,
  * Esirkepov deposition, one shape and one supercell size for all members; grids,

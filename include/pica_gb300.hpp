@@ -207,9 +207,13 @@ public:
     void copyStatePacked(int species, int comp, void* host, bool toDevice) {
         check(ctx_, pica_state_copy_packed(ctx_, species, comp, host, toDevice ? 1 : 0));
     }
-    // The image part of supercells [scBegin, scEnd) (host: start of the whole image).
-    void copyStatePackedRange(int species, int comp, void* host, bool toDevice, int scBegin, int scEnd) {
-        check(ctx_, pica_state_copy_packed_range(ctx_, species, comp, host, toDevice ? 1 : 0, scBegin, scEnd));
+    // The image part of supercells [scBegin, scEnd) (host: start of the whole image);
+    // copyStream: the host copy on that cudaStream_t, the gather / scatter kernel on
+    // the context stream (pica_state_copy_packed_range_on).
+    void copyStatePackedRange(int species, int comp, void* host, bool toDevice, int scBegin, int scEnd,
+                              void* copyStream = nullptr) {
+        check(ctx_, pica_state_copy_packed_range_on(ctx_, species, comp, host, toDevice ? 1 : 0, scBegin, scEnd,
+                                                    copyStream));
     }
     // The push in waitEvents.size() supercell ranges, range r after a wait for
     // waitEvents[r] (cudaEvent_t or nullptr); the rest of the step follows as in a

@@ -226,10 +226,17 @@ class Simulation:
             self._check(n)
         return n
 
-    def state_copy_packed(self, species, comp, host_ptr, to_device, sc_range=None):
+    def state_copy_packed(self, species, comp, host_ptr, to_device, sc_range=None, copy_stream=None):
         """One component of the packed image; ``sc_range=(begin, end)``: only the part of
-        those supercells (host_ptr is still the start of the whole image)."""
-        if sc_range is None:
+        those supercells (host_ptr is still the start of the whole image).  ``copy_stream``
+        (a cudaStream_t as an int): the host copy goes on that stream, the gather / scatter
+        kernel stays on the context stream (pica_state_copy_packed_range_on)."""
+        if copy_stream is not None:
+            b, e = sc_range if sc_range is not None else (0, int(np.prod(self.nsc)))
+            self._check(self.lib.pica_state_copy_packed_range_on(self.ctx, int(species), int(comp),
+                                                                 C.c_void_p(int(host_ptr)), 1 if to_device else 0,
+                                                                 int(b), int(e), C.c_void_p(int(copy_stream))))
+        elif sc_range is None:
             self._check(self.lib.pica_state_copy_packed(self.ctx, int(species), int(comp), C.c_void_p(int(host_ptr)),
                                                         1 if to_device else 0))
         else:

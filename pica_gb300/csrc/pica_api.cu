@@ -89,6 +89,7 @@ struct pica_ctx {
     int64_t steps = 0;
     int64_t epoch = 0;      // bumped by every step and every change of layout (packed-image validity)
     int threads = 1;
+    cudaEvent_t copyOrder = nullptr;   // orders a host copy on a caller's copy stream against the context stream
 };
 
 namespace {
@@ -428,6 +429,7 @@ int pica_ctx_destroy(pica_ctx* ctx) {
     if (ctx->d_out) cudaFree(ctx->d_out);
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
     if (ctx->d_rho) cudaFree(ctx->d_rho);
+    if (ctx->copyOrder) cudaEventDestroy(ctx->copyOrder);
     delete ctx;
     return PICA_OK;
 }
@@ -1221,6 +1223,11 @@ int pica_state_copy_packed(pica_ctx* ctx, int32_t species, int32_t comp, void* h
 
 int pica_state_copy_packed_range(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device,
                                  int32_t sc_begin, int32_t sc_end) {
+    return pica_state_copy_packed_range_on(ctx, species, comp, host, to_device, sc_begin, sc_end, nullptr);
+}
+
+int pica_state_copy_packed_range_on(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device,
+                                    int32_t sc_begin, int32_t sc_end, void* copy_stream) {
     if (!ctx || !host || species < 0 || species >= ctx->cfg.nspecies || comp < 0 || comp >= ctx->ncomp ||
         sc_begin < 0 || sc_end < sc_begin || sc_end > ctx->nscTot)
         return PICA_ERR_INVALID;
@@ -1236,14 +1243,27 @@ int pica_state_copy_packed_range(pica_ctx* ctx, int32_t species, int32_t comp, v
     if (bytes == 0) return PICA_OK;
     char* hp = static_cast<char*>(host) + (size_t)o0 * cb;
     char* dp = static_cast<char*>(S.d_pack[comp]) + (size_t)o0 * cb;
+    // With a copy stream the host copy goes there, and one event orders it against
+    // the gather / scatter kernel on the context stream (a wait takes the event's
+    // latest record when it is enqueued, so the one event serves every call).
+    cudaStream_t cs = copy_stream ? static_cast<cudaStream_t>(copy_stream) : ctx->stream;
+    if (cs != ctx->stream && !ctx->copyOrder) CK(cudaEventCreateWithFlags(&ctx->copyOrder, cudaEventDisableTiming));
     if (to_device) {
-        CK(cudaMemcpyAsync(dp, hp, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(dp, hp, bytes, cudaMemcpyHostToDevice, cs));
+        if (cs != ctx->stream) {
+            CK(cudaEventRecord(ctx->copyOrder, cs));
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->copyOrder, 0));
+        }
         CKL(launchPackCopy(S.d_pack[comp], S.buf[ctx->cur][comp], S.d_start, S.d_count, S.d_packOff, sc_begin, sc_end,
                            words, false, ctx->stream));
     } else {
         CKL(launchPackCopy(S.buf[ctx->cur][comp], S.d_pack[comp], S.d_start, S.d_count, S.d_packOff, sc_begin, sc_end,
                            words, true, ctx->stream));
-        CK(cudaMemcpyAsync(hp, dp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (cs != ctx->stream) {
+            CK(cudaEventRecord(ctx->copyOrder, ctx->stream));
+            CK(cudaStreamWaitEvent(cs, ctx->copyOrder, 0));
+        }
+        CK(cudaMemcpyAsync(hp, dp, bytes, cudaMemcpyDeviceToHost, cs));
     }
     ctx->launches++;
     return PICA_OK;

@@ -159,11 +159,12 @@ def test_packed_image_holds_the_ensemble_and_goes_stale_after_a_step():
     s.close()
 
 
-@pytest.mark.parametrize("nchunks", [3, 8])
-def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks):
+@pytest.mark.parametrize("nchunks,split", [(3, False), (8, False), (8, True), (16, True)])
+def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks, split):
     """The packed image uploaded supercell range by supercell range, each range's push
     launched once its upload is in (pica_push_deposit_chunked), downloaded range by
-    range: equal to plain steps bit for bit."""
+    range: equal to plain steps bit for bit.  split: the host copies on copy streams
+    of their own, apart from the gather / scatter kernels (pica_state_copy_packed_range_on)."""
     n = (16, 8, 8)
     d = thermal_inputs(n, 6, seed=76, u_sigma=0.2)
     steps, comps = 5, 8
@@ -173,6 +174,9 @@ def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks):
     main = torch.cuda.current_stream()
     a.set_stream(main.cuda_stream)
     up, down = torch.cuda.Stream(), torch.cuda.Stream()
+    upc, downc = (torch.cuda.Stream(), torch.cuda.Stream()) if split else (up, down)
+    cs_up = upc.cuda_stream if split else None
+    cs_down = downc.cuda_stream if split else None
     ranges = a.chunk_ranges(nchunks)
     assert ranges[0][0] == 0 and ranges[-1][1] == int(np.prod(a.nsc))
     packed = a.state_packed_slots(0)
@@ -187,9 +191,9 @@ def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks):
         upped = []
         for r, rg in enumerate(ranges):
             if downed[r] is not None:
-                up.wait_event(downed[r])
+                upc.wait_event(downed[r])
             for c in range(comps):
-                a.state_copy_packed(0, c, host[c].data_ptr(), True, sc_range=rg)
+                a.state_copy_packed(0, c, host[c].data_ptr(), True, sc_range=rg, copy_stream=cs_up)
             ev = torch.cuda.Event()
             ev.record(up)
             upped.append(ev)
@@ -206,9 +210,9 @@ def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks):
         a.set_stream(down.cuda_stream)
         for r, rg in enumerate(ranges):
             for c in range(comps):
-                a.state_copy_packed(0, c, host[c].data_ptr(), False, sc_range=rg)
+                a.state_copy_packed(0, c, host[c].data_ptr(), False, sc_range=rg, copy_stream=cs_down)
             downed[r] = torch.cuda.Event()
-            downed[r].record(down)
+            downed[r].record(downc)
         a.set_stream(main.cuda_stream)
     torch.cuda.synchronize()
     assert np.array_equal(a.counts(), ref.counts())
