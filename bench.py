@@ -89,6 +89,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=12)
     ap.add_argument("--e2e-chunks", type=int, default=16, help="supercell ranges of the e2e upload / push pipeline")
+    ap.add_argument("--e2e-edge-split", type=int, default=1,
+                    help="the first and last e2e ranges are cut into this many pieces (pica_push_deposit_ranges)")
+    ap.add_argument("--e2e-copy-split", type=int, default=1,
+                    help="each e2e push range's host copies in this many pieces (upload piece after download piece)")
     ap.add_argument("--e2e-split", type=int, default=1,
                     help="1: e2e host copies on copy streams of their own, gather / scatter kernels on two more")
     ap.add_argument("--fp64-steps", type=int, default=2)
@@ -392,7 +396,10 @@ def main():
         upc, downc = (torch.cuda.Stream(priority=-1), torch.cuda.Stream(priority=-1)) if args.e2e_split else (up, down)
         cs_up = upc.cuda_stream if args.e2e_split else None
         cs_down = downc.cuda_stream if args.e2e_split else None
-        ranges = sim.chunk_ranges(args.e2e_chunks)
+        ranges = sim.edge_split_ranges(args.e2e_chunks, args.e2e_edge_split)
+        k = max(1, args.e2e_copy_split)
+        pieces = [[(b + (e - b) * i // k, b + (e - b) * (i + 1) // k) for i in range(k)] for b, e in ranges]
+        flat = [p for ps in pieces for p in ps]
         # Pinned host buffers are set up once, outside the timed region, with room
         # for the layout to grow at a resort or capacity rebuild.
         torch.cuda.synchronize()
@@ -402,7 +409,7 @@ def main():
         for c in range(comps):
             sim.state_copy_packed(0, c, host[c].data_ptr(), False)
         torch.cuda.synchronize()
-        downed = [None] * len(ranges)
+        downed = [None] * len(flat)
         te0, te1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier()
         w0 = time.perf_counter()
@@ -412,17 +419,18 @@ def main():
         for _ in range(args.e2e_steps):
             upped = []
             sim.set_stream(up.cuda_stream)
-            for r, rg in enumerate(ranges):
-                if downed[r] is not None:
-                    upc.wait_event(downed[r])
-                for c in range(comps):
-                    sim.state_copy_packed(0, c, host[c].data_ptr(), True, sc_range=rg, copy_stream=cs_up)
+            for r in range(len(ranges)):
+                for q in range(r * k, (r + 1) * k):
+                    if downed[q] is not None:
+                        upc.wait_event(downed[q])
+                    for c in range(comps):
+                        sim.state_copy_packed(0, c, host[c].data_ptr(), True, sc_range=flat[q], copy_stream=cs_up)
                 ev = torch.cuda.Event()
                 ev.record(up)
                 upped.append(ev)
             h2d += slots * 4 * comps
             sim.set_stream(stream.cuda_stream)
-            sim.push_deposit_chunked([ev.cuda_event for ev in upped])
+            sim.push_deposit_ranges(ranges, [ev.cuda_event for ev in upped])
             sim.update_b(0.5 * dt)
             sim.update_e(dt)
             sim.update_b(0.5 * dt)
@@ -436,11 +444,11 @@ def main():
             stepped.record(stream)
             down.wait_event(stepped)
             sim.set_stream(down.cuda_stream)
-            for r, rg in enumerate(ranges):
+            for q, rg in enumerate(flat):
                 for c in range(comps):
                     sim.state_copy_packed(0, c, host[c].data_ptr(), False, sc_range=rg, copy_stream=cs_down)
-                downed[r] = torch.cuda.Event()
-                downed[r].record(downc)
+                downed[q] = torch.cuda.Event()
+                downed[q].record(downc)
             sim.set_stream(stream.cuda_stream)
             d2h += slots * 4 * comps
             done += 1
@@ -452,14 +460,15 @@ def main():
         e_el = te0.elapsed_time(te1) / 1e3
         e2e = {"value": world * npart * done / max(e_el, wall), "unit": UNIT,
                "h2d_bytes_per_step": h2d // max(1, done), "d2h_bytes_per_step": d2h // max(1, done),
-               "steps": done, "ranges": len(ranges), "split_copy_streams": bool(args.e2e_split),
+               "steps": done, "ranges": len(ranges), "edge_split": args.e2e_edge_split, "copy_pieces": k,
+               "split_copy_streams": bool(args.e2e_split),
                "path": "pica_state_copy_packed_range_on (pinned host, per supercell range) -> "
-                       "pica_push_deposit_chunked (each range after its upload) -> pica_update_b/update_e/update_b/"
+                       "pica_push_deposit_ranges (each range after its upload) -> pica_update_b/update_e/update_b/"
                        "migrate -> pica_state_packed_slots, pica_state_copy_packed_range_on; uploads and downloads "
                        "overlapped across steps, host copies on copy streams apart from the gather / scatter "
                        "kernels" if args.e2e_split else
                        "pica_state_copy_packed_range (pinned host, per supercell range) -> "
-                       "pica_push_deposit_chunked (each range after its upload) -> pica_update_b/update_e/update_b/"
+                       "pica_push_deposit_ranges (each range after its upload) -> pica_update_b/update_e/update_b/"
                        "migrate -> pica_state_packed_slots, pica_state_copy_packed_range; uploads and downloads "
                        "on two copy streams, overlapped across steps"}
         del host

@@ -167,6 +167,12 @@ int     pica_reorder(pica_ctx* ctx);
  * pica_push_deposit bit for bit (FP32 form).  Forms other than the FP32
  * Esirkepov one push in one launch after all the waits. */
 int     pica_push_deposit_chunked(pica_ctx* ctx, int32_t nchunks, void* const* wait_events);
+/* pica_push_deposit_chunked over ranges of the caller's choice: range r is
+ * supercells [bounds[r], bounds[r+1]) (nranges + 1 bounds, not decreasing, from 0
+ * to the supercell count; empty ranges launch nothing but still wait).  A host
+ * loop that moves small ranges first and last keeps the link busy at the ends of
+ * a step.  PICA_ERR_INVALID for bounds that do not cover the supercells. */
+int     pica_push_deposit_ranges(pica_ctx* ctx, int32_t nranges, const int32_t* bounds, void* const* wait_events);
 int     pica_update_b(pica_ctx* ctx, double dt);
 int     pica_update_e(pica_ctx* ctx, double dt);
 int     pica_migrate(pica_ctx* ctx);

@@ -221,6 +221,12 @@ public:
     void pushDepositChunked(const std::vector<void*>& waitEvents) {
         check(ctx_, pica_push_deposit_chunked(ctx_, (int32_t)waitEvents.size(), waitEvents.data()));
     }
+    // The same over supercell ranges [bounds[r], bounds[r+1]) of the caller's choice
+    // (bounds.size() == waitEvents.size() + 1, from 0 to the supercell count).
+    void pushDepositRanges(const std::vector<int32_t>& bounds, const std::vector<void*>& waitEvents) {
+        if (bounds.size() != waitEvents.size() + 1) throw Error(PICA_ERR_INVALID, "one more bound than wait events");
+        check(ctx_, pica_push_deposit_ranges(ctx_, (int32_t)waitEvents.size(), bounds.data(), waitEvents.data()));
+    }
     // Complete state between steps; a Simulation of the same Config loaded from it
     // continues like this one (FP32 form: bit for bit).
     void saveCheckpoint(const std::string& path) { check(ctx_, pica_checkpoint_save(ctx_, path.c_str())); }

@@ -259,6 +259,29 @@ class Simulation:
         arr = (C.c_void_p * len(wait_events))(*[C.c_void_p(int(e)) if e else None for e in wait_events])
         self._check(self.lib.pica_push_deposit_chunked(self.ctx, len(wait_events), arr))
 
+    def edge_split_ranges(self, nchunks, split):
+        """chunk_ranges(nchunks) with the first and the last range each cut into `split`
+        equal pieces: the ranges of a host loop that keeps the link busy at the ends of
+        a step (the first download and the last upload and push are short)."""
+        out = []
+        for r, (b, e) in enumerate(self.chunk_ranges(nchunks)):
+            k = split if (r == 0 or r == nchunks - 1) and split > 1 else 1
+            out += [(b + (e - b) * i // k, b + (e - b) * (i + 1) // k) for i in range(k)]
+        return out
+
+    def push_deposit_ranges(self, ranges, wait_events):
+        """pica_push_deposit over the consecutive supercell ranges ``[(begin, end), ...]``
+        (covering every supercell once, in order), range r launched after a wait for
+        wait_events[r] (pica_push_deposit_ranges)."""
+        if len(ranges) != len(wait_events):
+            raise ValueError("one wait event (or None) per range")
+        bounds = (C.c_int32 * (len(ranges) + 1))(*([int(r[0]) for r in ranges] + [int(ranges[-1][1])]))
+        for (b0, e0), (b1, _) in zip(ranges, ranges[1:]):
+            if e0 != b1:
+                raise ValueError("ranges must be consecutive")
+        arr = (C.c_void_p * len(wait_events))(*[C.c_void_p(int(e)) if e else None for e in wait_events])
+        self._check(self.lib.pica_push_deposit_ranges(self.ctx, len(ranges), bounds, arr))
+
 
 class Driver:
     """A host loop over a Simulation, in the role of the PICADOR driver around pica's

@@ -789,9 +789,10 @@ int pica_download_fields(pica_ctx* ctx, double* const* f9) {
 }  // extern "C"
 
 // The push over all supercells, as nchunks launches over consecutive supercell
-// ranges (FP32 Esirkepov kernel; the other kernels take one launch after all
-// waits), the launch of range r enqueued after a wait for events[r] when given.
-static int pushImpl(pica_ctx* ctx, int nchunks, void* const* events) {
+// ranges [bounds[r], bounds[r+1]) (FP32 Esirkepov kernel; the other kernels take
+// one launch after all waits), the launch of range r enqueued after a wait for
+// events[r] when given.  bounds == nullptr: one launch over all supercells.
+static int pushImpl(pica_ctx* ctx, int nchunks, const int32_t* bounds, void* const* events) {
     if (!ctx) return PICA_ERR_INVALID;
     if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "push_deposit called twice without migrate");
     const pica_config& c = ctx->cfg;
@@ -799,7 +800,7 @@ static int pushImpl(pica_ctx* ctx, int nchunks, void* const* events) {
     CK(cudaMemsetAsync(ctx->d_flags, 0, 4 * sizeof(int), ctx->stream));
     if (ctx->fp64)
         for (int k = 6; k < 9; k++) CK(cudaMemsetAsync(ctx->f[k], 0, nodes * 8, ctx->stream));
-    const bool ranges = !ctx->fp64 && c.deposit == PICA_DEPOSIT_ESIRKEPOV && nchunks > 1;
+    const bool ranges = !ctx->fp64 && c.deposit == PICA_DEPOSIT_ESIRKEPOV && nchunks > 1 && bounds;
     if (!ranges)
         for (int r = 0; r < nchunks; r++)
             if (events && events[r]) CK(cudaStreamWaitEvent(ctx->stream, static_cast<cudaEvent_t>(events[r]), 0));
@@ -819,8 +820,8 @@ static int pushImpl(pica_ctx* ctx, int nchunks, void* const* events) {
         } else {
             for (int r = 0; r < nchunks; r++) {
                 if (events && events[r]) CK(cudaStreamWaitEvent(ctx->stream, static_cast<cudaEvent_t>(events[r]), 0));
-                a.scBegin = (int)((int64_t)ctx->nscTot * r / nchunks);
-                a.scEnd = (int)((int64_t)ctx->nscTot * (r + 1) / nchunks);
+                a.scBegin = bounds[r];
+                a.scEnd = bounds[r + 1];
                 if (a.scEnd <= a.scBegin) continue;
                 CKL(launchPushCell(a, c.shape, c.deposit, ctx->variant, ctx->stream));
                 ctx->launches++;
@@ -839,12 +840,25 @@ static int pushImpl(pica_ctx* ctx, int nchunks, void* const* events) {
 
 extern "C" {
 
-int pica_push_deposit(pica_ctx* ctx) { return pushImpl(ctx, 1, nullptr); }
+int pica_push_deposit(pica_ctx* ctx) { return pushImpl(ctx, 1, nullptr, nullptr); }
 
 int pica_push_deposit_chunked(pica_ctx* ctx, int32_t nchunks, void* const* wait_events) {
     if (!ctx) return PICA_ERR_INVALID;
     if (nchunks < 1 || nchunks > 4096) return fail(ctx, PICA_ERR_INVALID, "chunk count out of range (1..4096)");
-    return pushImpl(ctx, nchunks, wait_events);
+    std::vector<int32_t> bounds(nchunks + 1);
+    for (int r = 0; r <= nchunks; r++) bounds[r] = (int32_t)((int64_t)ctx->nscTot * r / nchunks);
+    return pushImpl(ctx, nchunks, bounds.data(), wait_events);
+}
+
+int pica_push_deposit_ranges(pica_ctx* ctx, int32_t nranges, const int32_t* bounds, void* const* wait_events) {
+    if (!ctx) return PICA_ERR_INVALID;
+    if (nranges < 1 || nranges > 4096 || !bounds)
+        return fail(ctx, PICA_ERR_INVALID, "range count out of range (1..4096) or no bounds");
+    if (bounds[0] != 0 || bounds[nranges] != ctx->nscTot)
+        return fail(ctx, PICA_ERR_INVALID, "ranges must start at supercell 0 and end at the supercell count");
+    for (int r = 0; r < nranges; r++)
+        if (bounds[r + 1] < bounds[r]) return fail(ctx, PICA_ERR_INVALID, "range bounds must not decrease");
+    return pushImpl(ctx, nranges, bounds, wait_events);
 }
 
 int pica_update_b(pica_ctx* ctx, double dt) {

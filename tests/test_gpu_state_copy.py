@@ -159,12 +159,15 @@ def test_packed_image_holds_the_ensemble_and_goes_stale_after_a_step():
     s.close()
 
 
-@pytest.mark.parametrize("nchunks,split", [(3, False), (8, False), (8, True), (16, True)])
-def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks, split):
+@pytest.mark.parametrize("nchunks,split,edge", [(3, False, 1), (8, False, 1), (8, True, 1), (16, True, 1),
+                                               (6, True, 4)])
+def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks, split, edge):
     """The packed image uploaded supercell range by supercell range, each range's push
     launched once its upload is in (pica_push_deposit_chunked), downloaded range by
     range: equal to plain steps bit for bit.  split: the host copies on copy streams
-    of their own, apart from the gather / scatter kernels (pica_state_copy_packed_range_on)."""
+    of their own, apart from the gather / scatter kernels (pica_state_copy_packed_range_on).
+    edge > 1: the first and last ranges cut into that many pieces, the push over those
+    ranges (pica_push_deposit_ranges)."""
     n = (16, 8, 8)
     d = thermal_inputs(n, 6, seed=76, u_sigma=0.2)
     steps, comps = 5, 8
@@ -177,15 +180,16 @@ def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks, split):
     upc, downc = (torch.cuda.Stream(), torch.cuda.Stream()) if split else (up, down)
     cs_up = upc.cuda_stream if split else None
     cs_down = downc.cuda_stream if split else None
-    ranges = a.chunk_ranges(nchunks)
+    ranges = a.edge_split_ranges(nchunks, edge) if edge > 1 else a.chunk_ranges(nchunks)
     assert ranges[0][0] == 0 and ranges[-1][1] == int(np.prod(a.nsc))
+    assert all(r0[1] == r1[0] for r0, r1 in zip(ranges, ranges[1:]))
     packed = a.state_packed_slots(0)
     alloc = 2 * packed + 1024
     host = [torch.empty(alloc * 4, dtype=torch.uint8, pin_memory=True) for _ in range(comps)]
     for c in range(comps):
         a.state_copy_packed(0, c, host[c].data_ptr(), False)
     torch.cuda.synchronize()
-    downed = [None] * nchunks
+    downed = [None] * len(ranges)
     for _ in range(steps):
         a.set_stream(up.cuda_stream)
         upped = []
@@ -198,7 +202,10 @@ def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks, split):
             ev.record(up)
             upped.append(ev)
         a.set_stream(main.cuda_stream)
-        a.push_deposit_chunked([ev.cuda_event for ev in upped])
+        if edge > 1:
+            a.push_deposit_ranges(ranges, [ev.cuda_event for ev in upped])
+        else:
+            a.push_deposit_chunked([ev.cuda_event for ev in upped])
         a.update_b(0.5 * a.dt)
         a.update_e(a.dt)
         a.update_b(0.5 * a.dt)
@@ -224,3 +231,18 @@ def test_chunked_push_from_host_ranges_equals_plain_steps(nchunks, split):
         assert np.array_equal(fa[c], fr[c]), c
     a.close()
     ref.close()
+
+
+def test_push_ranges_reject_bounds_that_do_not_cover_the_supercells():
+    n = (8, 8, 8)
+    d = thermal_inputs(n, 2, seed=77, u_sigma=0.1)
+    s = make(d, n)
+    tot = int(np.prod(s.nsc))
+    for bad in ([(0, tot - 1)], [(1, tot)], [(0, 5), (5, 3), (3, tot)]):
+        with pytest.raises(pg.PicaError):
+            s.push_deposit_ranges(bad, [None] * len(bad))
+    with pytest.raises(ValueError):
+        s.push_deposit_ranges([(0, 3), (4, tot)], [None, None])
+    s.step(1)   # nothing was left pending
+    assert s.step_count() == 1
+    s.close()
