@@ -250,8 +250,7 @@ class Simulation:
 
     def chunk_ranges(self, nchunks):
         """Supercell ranges of pica_push_deposit_chunked: [n r / nchunks, n (r+1) / nchunks)."""
-        tot = int(np.prod(self.nsc))
-        return [(tot * r // nchunks, tot * (r + 1) // nchunks) for r in range(nchunks)]
+        return supercell_ranges(int(np.prod(self.nsc)), nchunks)
 
     def push_deposit_chunked(self, wait_events):
         """pica_push_deposit in len(wait_events) supercell ranges, range r launched after
@@ -263,11 +262,7 @@ class Simulation:
         """chunk_ranges(nchunks) with the first and the last range each cut into `split`
         equal pieces: the ranges of a host loop that keeps the link busy at the ends of
         a step (the first download and the last upload and push are short)."""
-        out = []
-        for r, (b, e) in enumerate(self.chunk_ranges(nchunks)):
-            k = split if (r == 0 or r == nchunks - 1) and split > 1 else 1
-            out += [(b + (e - b) * i // k, b + (e - b) * (i + 1) // k) for i in range(k)]
-        return out
+        return supercell_ranges(int(np.prod(self.nsc)), nchunks, split)
 
     def push_deposit_ranges(self, ranges, wait_events):
         """pica_push_deposit over the consecutive supercell ranges ``[(begin, end), ...]``
@@ -420,6 +415,20 @@ def plasma_spec(n, h, ppc, sigma_u, weight, seed, species=0, density_mod=0.0, nb
     s.drift_u, s.sigma_u, s.weight, s.seed = float(drift_u), float(sigma_u), float(weight), int(seed)
     s.nbeams, s.drift_axis = int(nbeams), int(drift_axis)
     return s
+
+
+def supercell_ranges(total, nchunks, edge_split=1):
+    """Consecutive supercell ranges [(begin, end), ...] covering 0..total: the nchunks
+    ranges [total r / nchunks, total (r+1) / nchunks) of pica_push_deposit_chunked, with
+    the first and the last cut into edge_split equal pieces when edge_split > 1."""
+    if nchunks < 1 or total < 0:
+        raise ValueError("nchunks >= 1 and total >= 0")
+    out = []
+    for r in range(nchunks):
+        b, e = total * r // nchunks, total * (r + 1) // nchunks
+        k = edge_split if (r == 0 or r == nchunks - 1) and edge_split > 1 else 1
+        out += [(b + (e - b) * i // k, b + (e - b) * (i + 1) // k) for i in range(k)]
+    return out
 
 
 def generate_plasma(spec, threads=0):

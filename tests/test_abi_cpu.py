@@ -71,3 +71,27 @@ def test_workload_sizes():
     assert len(members) == 64
     edges = [m["sim"]["n"][0] for m in members]
     assert min(edges) >= 32 and max(edges) <= 96 and all(e % 4 == 0 for e in edges)
+
+
+def test_supercell_ranges_cover_every_supercell_once():
+    for total, n, k in ((32768, 16, 1), (32768, 16, 8), (1000, 7, 3), (5, 8, 1), (5, 1, 4)):
+        r = pica_gb300.supercell_ranges(total, n, k)
+        assert r[0][0] == 0 and r[-1][1] == total
+        assert all(a[1] == b[0] and a[0] <= a[1] for a, b in zip(r, r[1:]))
+        assert len(r) == (n + (2 * (k - 1) if n > 1 else k - 1) if k > 1 else n)
+    # uniform ranges are those of pica_push_deposit_chunked: [total r / n, total (r+1) / n)
+    assert pica_gb300.supercell_ranges(10, 3) == [(0, 3), (3, 6), (6, 10)]
+
+
+def test_cpp_mirror_compiles_and_links_against_the_library(tmp_path):
+    """The C++ header mirror and the host loops of the GPU tests compile and link
+    against the library (running them needs a GPU)."""
+    import subprocess
+    so = _lib.lib_path()
+    _lib.load()
+    for src in ("host_loop.cpp", "driver_checkpoint.cpp"):
+        exe = str(tmp_path / src.replace(".cpp", ""))
+        subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", src), so, "-o", exe,
+                        "-Wl,-rpath," + os.path.dirname(so), "-lpthread"], check=True)
+        assert os.path.exists(exe)
