@@ -41,14 +41,33 @@ BYTES_PER_PARTICLE_FP64 = 104  # x 24 + u 24, read and written, + weight read
 PUSH_GRID_BYTES_PER_CELL_FP32 = 36  # E/B gather 6 words + J write 3 words, FP32
 
 
-def batched_measure(args):
+def batched_measure(args, rank=0, world=1, dist=None):
     """The batching form on independent thermal plasmas of uneven size (members drawn
     as in pica_gb300.workloads.batched_members; by default every edge halved).  Timed
     with the host clock: every batch step ends with a stream synchronisation (the
-    host reads each member's migration flags)."""
+    host reads each member's migration flags).  On N ranks the plasmas are binned
+    over the ranks by particle count (no communication on the data path); the job's
+    throughput is every rank's particles over the slowest rank's time.  Every rank
+    calls this; rank 0 gets the result."""
+    import torch
+
     import pica_gb300 as pg
     from pica_gb300 import autotune, workloads
+    from pica_gb300.replicas import bin_members, job_throughput_binned
     members = workloads.batched_members(count=args.batched, half=not args.batched_full)
+    edges = [m["sim"]["n"][0] for m in members]
+    nall = len(members)
+    if world > 1:
+        counts = [sum(pg.plasma_count(s) for s in m["specs"]) for m in members]
+        mine = bin_members(counts, world)[rank]
+        members = [members[i] for i in mine]
+    K = args.batched_steps
+    if not members:   # more ranks than plasmas: this rank only takes part in the timing
+        for _ in range(2):   # the graph run and the eager run, as below
+            if dist is not None:
+                dist.barrier()
+            job_throughput_binned(0, K, 0.0, dist, device="cuda")
+        return None
     b = pg.Batch([m["sim"] for m in members])
     for sim, wl in zip(b.members, members):
         sim.generate_plasma(wl["specs"])   # drawn on the device
@@ -58,26 +77,37 @@ def batched_measure(args):
     tune = autotune.tune_batch(b, steps=2)
     best = min(tune, key=tune.get)
     b.step(3)
-    K = args.batched_steps
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
     s0 = b.stats()
     t = time.perf_counter()
     b.step(K)
     el = time.perf_counter() - t
     s1 = b.stats()
+    value, el = job_throughput_binned(npart, K, el, dist, device="cuda")
     b.set_options(use_graph=False, variant=best)
     b.step(1)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
     t = time.perf_counter()
     b.step(K)
     el_eager = time.perf_counter() - t
+    eager_value, _ = job_throughput_binned(npart, K, el_eager, dist, device="cuda")
     b.close()
-    edges = [m["sim"]["n"][0] for m in members]
-    return {"workload": f"{len(members)} thermal plasmas, edges {min(edges)}-{max(edges)} cells"
+    if rank != 0:
+        return None
+    return {"workload": f"{nall} thermal plasmas, edges {min(edges)}-{max(edges)} cells"
                         f"{'' if args.batched_full else ' (member edges halved)'}, 16-128 ppc, CIC, Esirkepov, "
                         "supercell 4^3, FP32 cell form",
-            "particles": npart, "steps": K, "value": npart * K / el, "unit": UNIT, "ms_per_step": 1e3 * el / K,
+            "ranks": world, "members_on_rank0": len(members),
+            "sharding": "plasmas binned over the ranks by particle count, no communication" if world > 1 else None,
+            "particles": int(round(value * el / K)), "steps": K, "value": value, "unit": UNIT,
+            "ms_per_step": 1e3 * el / K,
             "timer": "host clock, each step synchronised", "graph_captures": s1["captures"] - s0["captures"],
             "kernel_launches_per_step": (s1["kernel_launches"] - s0["kernel_launches"]) / K,
-            "eager_value": npart * K / el_eager, "push_variant": best,
+            "eager_value": eager_value, "push_variant": best,
             "variant_s_per_step": {str(k): v for k, v in tune.items()}}
 
 
@@ -498,8 +528,8 @@ def main():
 
     # ---------------- batching form: many plasmas, persistent push + CUDA graph ----------------
     batched = None
-    if headline and args.batched > 0 and rank == 0:
-        batched = batched_measure(args)
+    if headline and args.batched > 0:
+        batched = batched_measure(args, rank, world, dist)
 
     # ---------------- FP32 form against the FP64 plain form (error metrics) ----------------
     errors = None

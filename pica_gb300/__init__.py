@@ -431,6 +431,14 @@ def supercell_ranges(total, nchunks, edge_split=1):
     return out
 
 
+def plasma_count(spec):
+    """Particles that `spec` (a plasma_spec) draws, computed on the host."""
+    n = int(load().pica_plasma_count(C.byref(spec)))
+    if n < 0:
+        raise PicaError(n, "bad plasma spec")
+    return n
+
+
 def generate_plasma(spec, threads=0):
     """Synthetic plasma on the host (counter-based RNG; independent of thread count)."""
     lib = load()
