@@ -145,6 +145,52 @@ def parse():
     return ap.parse_args()
 
 
+def host_link_probe(nbytes=1 << 30, reps=3):
+    """Pinned host memory <-> device bandwidth of this machine by the copy engines: one
+    direction alone, and both at once on two streams (GB/s, CUDA events).  The
+    ceiling of the end-to-end loop, which moves the particle state both ways."""
+    import torch
+
+    h_up = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    h_down = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d_up = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d_down = torch.ones(nbytes, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    cur = torch.cuda.current_stream()
+
+    def timed(fn, moved):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(cur)
+        for _ in range(reps):
+            s1.wait_stream(cur)
+            s2.wait_stream(cur)
+            fn()
+            cur.wait_stream(s1)
+            cur.wait_stream(s2)
+        b.record(cur)
+        torch.cuda.synchronize()
+        return moved * reps / (a.elapsed_time(b) * 1e-3) / 1e9
+
+    def up():
+        with torch.cuda.stream(s1):
+            d_up.copy_(h_up, non_blocking=True)
+
+    def down():
+        with torch.cuda.stream(s2):
+            h_down.copy_(d_down, non_blocking=True)
+
+    def both():
+        up()
+        down()
+
+    out = {"h2d_gbs": timed(up, nbytes), "d2h_gbs": timed(down, nbytes), "both_gbs": timed(both, 2 * nbytes),
+           "bytes_per_copy": nbytes, "source": "pinned host memory, copy engines, CUDA events"}
+    del h_up, h_down, d_up, d_down
+    return out
+
+
 def measured_hbm_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -488,8 +534,11 @@ def main():
         barrier()
         wall = time.perf_counter() - w0
         e_el = te0.elapsed_time(te1) / 1e3
+        link = host_link_probe()   # outside the timed region
+        moved = (h2d + d2h) / max(e_el, wall) / 1e9
         e2e = {"value": world * npart * done / max(e_el, wall), "unit": UNIT,
                "h2d_bytes_per_step": h2d // max(1, done), "d2h_bytes_per_step": d2h // max(1, done),
+               "link_gbs": moved, "host_link": link, "link_frac": moved / link["both_gbs"],
                "steps": done, "ranges": len(ranges), "edge_split": args.e2e_edge_split, "copy_pieces": k,
                "split_copy_streams": bool(args.e2e_split),
                "path": "pica_state_copy_packed_range_on (pinned host, per supercell range) -> "
