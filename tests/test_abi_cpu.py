@@ -87,11 +87,15 @@ def test_cpp_mirror_compiles_and_links_against_the_library(tmp_path):
     """The C++ header mirror and the host loops of the GPU tests compile and link
     against the library (running them needs a GPU)."""
     import subprocess
+    from pica_gb300.build import NVCC
     so = _lib.lib_path()
     _lib.load()
-    for src in ("host_loop.cpp", "driver_checkpoint.cpp"):
+    cuda = os.path.dirname(os.path.dirname(NVCC))
+    runtime = ["-I", os.path.join(cuda, "include"), "-L", os.path.join(cuda, "lib64"), "-lcudart"]
+    for src in ("host_loop.cpp", "driver_checkpoint.cpp", "host_resident_loop.cpp"):
         exe = str(tmp_path / src.replace(".cpp", ""))
+        extra = runtime if src == "host_resident_loop.cpp" else []
         subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
-                        os.path.join(ROOT, "tests", "cpp", src), so, "-o", exe,
+                        os.path.join(ROOT, "tests", "cpp", src), so] + extra + ["-o", exe,
                         "-Wl,-rpath," + os.path.dirname(so), "-lpthread"], check=True)
         assert os.path.exists(exe)

@@ -71,3 +71,20 @@ def test_cpp_driver_and_checkpoint(tmp_path):
     out = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True, check=True).stdout.split()
     assert out == ["diag", "2", "1", "diag", "4", "1", "diag", "6", "1", "same"]
     assert os.path.exists(tmp_path / "ckpt_3") and os.path.exists(tmp_path / "ckpt_6")
+
+
+@pytest.mark.parametrize("nranges", [3, 4])
+def test_cpp_host_resident_loop_equals_plain_steps(tmp_path, nranges):
+    """tests/cpp/host_resident_loop.cpp: the state kept in pinned host memory, moved
+    range by range on copy streams every step, equals plain steps bit for bit."""
+    from pica_gb300.build import NVCC
+    so = pg._lib.lib_path()
+    pg._lib.load()
+    cuda = os.path.dirname(os.path.dirname(NVCC))
+    exe = str(tmp_path / "host_resident_loop")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(cuda, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "host_resident_loop.cpp"), so, "-L", os.path.join(cuda, "lib64"),
+                    "-lcudart", "-o", exe, "-Wl,-rpath," + os.path.dirname(so), "-lpthread"], check=True)
+    r = subprocess.run([exe, "5", str(nranges)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.strip().endswith(f"{nranges} ranges, same"), r.stdout
