@@ -289,43 +289,53 @@ def named_workload(name, edge=None):
     return wl, desc
 
 
-def cpu_sample(args, steps=None, seconds=None, pica_path=False):
-    """Oracle restatement of the same step on a 32^3-cell block of the workload (same ppc,
-    supercell, form factor and deposition), all host cores.  With `pica_path`, the same block
-    through pica's own arithmetic instead: FP64 positions, CIC, Boris, direct deposition (the
-    oracle form equal bit for bit to a harness over pica's headers).  Returns (value, cores,
-    sample, seconds)."""
+def cpu_sample(args, steps=None, seconds=None, pica_path=False, workload="thermal", warmup=1):
+    """Oracle restatement of the workload's step on a small block of it (32^3 cells; the
+    two-stream plasma 32x32x16; same ppc, species, supercell, form factor and
+    deposition), all host cores.  With `pica_path`, the same block through pica's own
+    arithmetic instead: FP64 positions, CIC, Boris, direct deposition (the oracle form
+    equal bit for bit to a harness over pica's headers).  `warmup` untimed steps, then
+    `steps` timed ones (or as many as fill `seconds`).  Returns (value, cores, sample,
+    seconds)."""
     import pica_gb300 as pg
     from oracle import pic_oracle as po
 
     edge = 32
-    wl = make_workload(edge, pg.FORM_FP64_PLAIN if pica_path else pg.FORM_FP32_CELL)
-    p = pg.generate_plasma(wl["specs"][0])
+    if workload == "thermal":
+        wl = make_workload(edge, pg.FORM_FP32_CELL)
+        what = f"{edge}^3 cells x 100 ppc"
+    else:
+        wl, what = named_workload(workload, edge)
+        what = what.split(",")[0]
     sim = wl["sim"]
+    parts = [pg.generate_plasma(spec) for spec in wl["specs"]]
+    p = {k: np.concatenate([q[k] for q in parts]) for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species")}
     cores = os.cpu_count() or 1
     if pica_path:
         kw = dict(form=po.FORM_FP64_PLAIN, shape=po.SHAPE_CIC, deposit=po.DEPOSIT_DIRECT)
     else:
-        kw = dict(form=po.FORM_FP32_CELL, shape=po.SHAPE_TSC, deposit=po.DEPOSIT_ESIRKEPOV)
-    o = po.Oracle(sim["n"], sim["supercell"], sim["h"], sim["dt"], threads=cores, **kw)
+        kw = dict(form=po.FORM_FP32_CELL, shape=sim["shape"], deposit=sim["deposit"])
+    species = sim.get("species", ((pg.ELECTRON_MASS, pg.ELECTRON_CHARGE),))
+    o = po.Oracle(sim["n"], sim["supercell"], sim["h"], sim["dt"], threads=cores, species=species, **kw)
     o.load(p["x"], p["y"], p["z"], p["ux"], p["uy"], p["uz"], p["w"], p["species"])
     o.set_fields([np.zeros(sim["n"])] * 9)
     npart = len(p["x"])
     t = time.perf_counter()
-    o.step(1)
-    t1 = time.perf_counter() - t
+    o.step(max(1, int(warmup)))
+    t1 = (time.perf_counter() - t) / max(1, int(warmup))
     if steps is None:
         steps = int(max(1, min(50, math.ceil((seconds or 12.0) / max(t1, 1e-3)))))
     t = time.perf_counter()
     o.step(steps)
     el = time.perf_counter() - t
+    shape = "TSC" if sim["shape"] == pg.SHAPE_TSC else "CIC"
     if pica_path:
-        sample = (f"{edge}^3 cells x 100 ppc ({npart} electrons), pica's path: FP64 positions, CIC, Boris, direct "
-                  f"deposition, supercell 4^3, {steps} steps, oracle form equal bit for bit to pica's headers, "
-                  f"OpenMP {cores} threads")
+        sample = (f"{what} ({npart} particles), pica's path: FP64 positions, CIC, Boris, direct deposition, "
+                  f"supercell 4^3, {steps} steps, oracle form equal bit for bit to pica's headers, OpenMP {cores} threads")
     else:
-        sample = (f"{edge}^3 cells x 100 ppc ({npart} electrons), TSC, Esirkepov, supercell 4^3, FP32 cell form, "
-                  f"{steps} steps, oracle restatement (pica has no TSC/Esirkepov), OpenMP {cores} threads")
+        sample = (f"{what} ({npart} particles), {shape}, Esirkepov, supercell 4^3, FP32 cell form, {steps} steps, "
+                  f"oracle restatement (pica has no Esirkepov{'' if shape == 'CIC' else ' or TSC'}), "
+                  f"OpenMP {cores} threads")
     return npart * steps / el, cores, sample, el
 
 
@@ -333,15 +343,19 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    # warm-up steps then exactly K timed steps of the CPU step on the bounded sample
+    # W untimed warm-up steps, then exactly K timed steps of the CPU step on the bounded sample
     import pica_gb300 as pg  # noqa: F401  (host-side plasma generator only)
-    value, cores, sample, el = cpu_sample(args, steps=args.steps + args.warmup)
+    value, cores, sample, el = cpu_sample(args, steps=args.steps, warmup=args.warmup, workload=args.workload)
+    if args.workload == "thermal":
+        what = (f"thermal electron plasma {args.edge or 128}^3 x 100 ppc, TSC, Esirkepov, supercell 4^3 "
+                f"(CPU step on a 32^3 block of it)")
+    else:
+        what = named_workload(args.workload, args.edge)[1] + " (CPU step on a small block of it)"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / (args.steps + args.warmup),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / max(1, args.steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": f"thermal electron plasma {args.edge or 128}^3 x 100 ppc, TSC, Esirkepov, supercell 4^3 "
-                               f"(CPU step on a 32^3 block of it)", "parallelism": "OpenMP over supercells"},
+        "config": {"workload": what, "parallelism": "OpenMP over supercells"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -592,10 +606,10 @@ def main():
             dist.destroy_process_group()
         return
     cpu = None
-    if headline and not args.no_cpu_baseline:
-        v, cores, sample, _ = cpu_sample(args, seconds=args.cpu_seconds)
+    if not args.no_cpu_baseline:
+        v, cores, sample, _ = cpu_sample(args, seconds=args.cpu_seconds, workload=args.workload)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
-        v, cores, sample, _ = cpu_sample(args, seconds=0.5 * args.cpu_seconds, pica_path=True)
+        v, cores, sample, _ = cpu_sample(args, seconds=0.5 * args.cpu_seconds, pica_path=True, workload=args.workload)
         cpu["pica_path"] = {"value": v, "unit": UNIT, "cores": cores, "sample": sample}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
