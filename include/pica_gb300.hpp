@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <array>
+#include <cmath>
 #include <functional>
 #include <cstdint>
 #include <stdexcept>
@@ -38,31 +39,100 @@ struct FP3 {
     double x = 0, y = 0, z = 0;
     FP3() = default;
     FP3(double a, double b, double c) : x(a), y(b), z(c) {}
+    double norm2() const { return x * x + y * y + z * z; }
+    double norm() const { return std::sqrt(norm2()); }
 };
+inline FP3 operator+(const FP3& a, const FP3& b) { return FP3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline FP3 operator-(const FP3& a, const FP3& b) { return FP3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline FP3 operator*(const FP3& a, double s) { return FP3(a.x * s, a.y * s, a.z * s); }
+inline FP3 operator*(double s, const FP3& a) { return a * s; }
+inline FP3 operator/(const FP3& a, double s) { return FP3(a.x / s, a.y / s, a.z / s); }
 struct Int3 {
     int x = 0, y = 0, z = 0;
     Int3() = default;
     Int3(int a, int b, int c) : x(a), y(b), z(c) {}
 };
 
-// Constants of pica math/Constants.h:10-14 (CGS, pi truncated as in pica).
+// Constants of pica math/Constants.h:9-18 (CGS, pi truncated as in pica), and the
+// Constants<Real> accessors of Constants.h:23-34: each the namespace value cast to Real.
 namespace constants {
 const double pi = 3.14159265358;
 const double c = 29979245800.0;
+const double lightVelocity = c;
 const double electronCharge = -4.80320427e-10;
 const double electronMass = 9.10938215e-28;
+const double protonMass = 1.672622964e-24;
+const double planck = 1.0545716818e-27;
+const double eV = 1.60217656535e-12;
+const double meV = 1e6 * eV;
 }  // namespace constants
+
+template <typename Real>
+struct Constants {
+    static Real pi() { return static_cast<Real>(constants::pi); }
+    static Real c() { return static_cast<Real>(constants::c); }
+    static Real lightVelocity() { return static_cast<Real>(constants::lightVelocity); }
+    static Real electronCharge() { return static_cast<Real>(constants::electronCharge); }
+    static Real electronMass() { return static_cast<Real>(constants::electronMass); }
+    static Real protonMass() { return static_cast<Real>(constants::protonMass); }
+    static Real planck() { return static_cast<Real>(constants::planck); }
+    static Real eV() { return static_cast<Real>(constants::eV); }
+    static Real meV() { return static_cast<Real>(constants::meV); }
+};
 
 // One entry of pica's ParticleTypes table (particles/Particle.h:21-31).
 struct ParticleType {
     double mass, charge;
 };
 
-// Particle<Three> with normalised momentum p = u/(m c) (particles/Particle.h:34-112).
+// pica's global particle type table (particles/Particle.h:26-31).  Simulation fills
+// it from Config::types; a host loop may set it itself before creating particles,
+// as a pica host loop does.
+namespace ParticleTypes {
+inline std::vector<ParticleType> typesVector{{constants::electronMass, constants::electronCharge}};
+inline const ParticleType* types = nullptr;   // nullptr: typesVector
+inline int numTypes = 1;
+inline const ParticleType& at(int i) { return types ? types[i] : typesVector[(size_t)i]; }
+}  // namespace ParticleTypes
+
+// Particle<Three> (particles/Particle.h:34-112): position, momentum stored
+// normalised as p = P / (m c), weight factor and type index.  The fields are
+// public; the accessors follow pica's: gamma = 1 / invGamma with invGamma =
+// 1 / sqrt(1 + |p|^2), velocity p c invGamma, setVelocity p = v / sqrt(c^2 - |v|^2),
+// mass and charge from the type table.
 struct Particle3d {
+    typedef FP3 PositionType;
+    typedef FP3 MomentumType;
+    typedef double GammaType, MassType, ChargeType, FactorType;
+    typedef short TypeIndexType;
+
     FP3 position, p;
     double factor = 1.0;
     short typeIndex = 0;
+
+    Particle3d() = default;
+    Particle3d(const FP3& pos, const FP3& momentum, double f = 1, short type = 0)
+        : position(pos), factor(f), typeIndex(type) {
+        setMomentum(momentum);
+    }
+    FP3 getPosition() const { return position; }
+    void setPosition(const FP3& v) { position = v; }
+    FP3 getMomentum() const { return p * Constants<double>::c() * getMass(); }
+    void setMomentum(const FP3& m) { p = m / (Constants<double>::c() * getMass()); }
+    FP3 getP() const { return p; }
+    void setP(const FP3& v) { p = v; }
+    FP3 getVelocity() const { return p * (Constants<double>::c() * invGamma()); }
+    void setVelocity(const FP3& v) { p = v / std::sqrt(constants::c * constants::c - v.norm2()); }
+    double getGamma() const { return 1.0 / invGamma(); }
+    double getMass() const { return ParticleTypes::at(typeIndex).mass; }
+    double getCharge() const { return ParticleTypes::at(typeIndex).charge; }
+    double getFactor() const { return factor; }
+    void setFactor(double f) { factor = f; }
+    short getType() const { return typeIndex; }
+    void setType(short t) { typeIndex = t; }
+
+private:
+    double invGamma() const { return 1.0 / std::sqrt(1.0 + p.norm2()); }
 };
 
 class Error : public std::runtime_error {
@@ -166,6 +236,10 @@ public:
         cfg.slack = c.slack;
         cfg.resort_every = c.resortEvery;
         check(nullptr, pica_ctx_create(&cfg, &ctx_));
+        // The configured species become pica's global type table (Particle3d::getMass / getCharge).
+        ParticleTypes::typesVector = c.types;
+        ParticleTypes::types = nullptr;
+        ParticleTypes::numTypes = (int)c.types.size();
         dt_ = c.dt;
         grid_.ctx_ = ctx_; grid_.n_ = c.numCells; grid_.h_ = c.step;
         const size_t nodes = (size_t)c.numCells.x * c.numCells.y * c.numCells.z;

@@ -1,0 +1,101 @@
+// pica's particle and constants known-answer checks (test/src/particles/ParticleTests.cpp:37-164,
+// test/src/math/ConstantsTests.cpp:15-28) restated against the C++ mirror: Constants<T>
+// equals the cast namespace value for float and double; a particle built from a momentum
+// returns it, with gamma = sqrt(1 + |P|^2 / (m c)^2) to 1e-12; momentum and velocity
+// round-trip to 1e-12; mass and charge come from the type table.  Host-only, no GPU.
+// Prints "ok" or the first failing check.
+#include <cmath>
+#include <cstdio>
+
+#include "pica_gb300.hpp"
+
+using namespace pica_gb300;
+
+static int fails = 0;
+
+static void near(const char* what, double want, double got, double rel = 1e-12) {
+    const double err = std::fabs(want - got), scale = std::fmax(std::fabs(want), 1e-300);
+    if (!(err <= rel * scale)) {
+        std::printf("%s: want %.17g got %.17g\n", what, want, got);
+        fails++;
+    }
+}
+
+static void nearVec(const char* what, const FP3& want, const FP3& got) {
+    // relative to the vector's norm, as pica's ASSERT_NEAR_VECTOR
+    const double err = (want - got).norm(), scale = std::fmax(want.norm(), 1e-300);
+    if (!(err <= 1e-12 * scale)) {
+        std::printf("%s: error %.3g of %.3g\n", what, err, scale);
+        fails++;
+    }
+}
+
+template <typename T>
+static void constantsOf(const char* name) {
+    const bool ok = Constants<T>::pi() == static_cast<T>(constants::pi) && Constants<T>::c() == static_cast<T>(constants::c) &&
+                    Constants<T>::lightVelocity() == static_cast<T>(constants::lightVelocity) &&
+                    Constants<T>::electronCharge() == static_cast<T>(constants::electronCharge) &&
+                    Constants<T>::electronMass() == static_cast<T>(constants::electronMass) &&
+                    Constants<T>::protonMass() == static_cast<T>(constants::protonMass) &&
+                    Constants<T>::planck() == static_cast<T>(constants::planck) &&
+                    Constants<T>::eV() == static_cast<T>(constants::eV) && Constants<T>::meV() == static_cast<T>(constants::meV);
+    if (!ok) {
+        std::printf("Constants<%s> differ from the namespace values\n", name);
+        fails++;
+    }
+}
+
+int main() {
+    constantsOf<float>("float");
+    constantsOf<double>("double");
+
+    ParticleTypes::typesVector = {{constants::electronMass, constants::electronCharge},
+                                  {constants::protonMass, -constants::electronCharge}};
+    ParticleTypes::types = nullptr;
+    ParticleTypes::numTypes = 2;
+
+    Particle3d def;
+    if (def.getGamma() != 1.0 || def.getFactor() != 1.0 || def.getVelocity().norm2() != 0.0) {
+        std::printf("default particle\n");
+        fails++;
+    }
+
+    const FP3 pos(3.1, -32.1, 4.3e-5), mom(-231.3e9, 0.0, 1.23e-5);
+    Particle3d q(pos, mom, 1.4e2, 0);
+    if (q.getPosition().x != pos.x || q.getPosition().y != pos.y || q.getPosition().z != pos.z) {
+        std::printf("position\n");
+        fails++;
+    }
+    nearVec("momentum from the constructor", mom, q.getMomentum());
+    near("mass", constants::electronMass, q.getMass(), 0);
+    near("charge", constants::electronCharge, q.getCharge(), 0);
+    near("factor", 1.4e2, q.getFactor(), 0);
+    const double mc = q.getMass() * Constants<double>::c();
+    near("gamma", std::sqrt(1.0 + mom.norm2() / (mc * mc)), q.getGamma());
+
+    const FP3 m2(54.12e+4, -543.63e-2, 643.165e5);
+    q.setMomentum(m2);
+    nearVec("set / get momentum", m2, q.getMomentum());
+    near("gamma after setMomentum", std::sqrt(1.0 + m2.norm2() / (mc * mc)), q.getGamma());
+
+    const FP3 v(5243.1654, -56.23e5, -65.237e-4);
+    q.setVelocity(v);
+    nearVec("set / get velocity", v, q.getVelocity());
+
+    Particle3d ion(pos, mom, 2.0, 1);
+    near("ion mass", constants::protonMass, ion.getMass(), 0);
+    near("ion charge", -constants::electronCharge, ion.getCharge(), 0);
+    const double mci = constants::protonMass * constants::c;
+    near("ion gamma", std::sqrt(1.0 + mom.norm2() / (mci * mci)), ion.getGamma());
+    ion.setType(0);
+    near("mass after setType", constants::electronMass, ion.getMass(), 0);
+
+    // p is pica's normalised momentum: setP / getP, and P = p m c
+    Particle3d r;
+    r.setP(FP3(0.3, -0.4, 1.2));
+    nearVec("momentum from p", FP3(0.3, -0.4, 1.2) * mc, r.getMomentum());
+    near("gamma from p", std::sqrt(1.0 + 0.09 + 0.16 + 1.44), r.getGamma());
+
+    std::printf(fails ? "failed\n" : "ok\n");
+    return fails ? 1 : 0;
+}

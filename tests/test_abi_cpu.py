@@ -99,3 +99,46 @@ def test_cpp_mirror_compiles_and_links_against_the_library(tmp_path):
                         os.path.join(ROOT, "tests", "cpp", src), so] + extra + ["-o", exe,
                         "-Wl,-rpath," + os.path.dirname(so), "-lpthread"], check=True)
         assert os.path.exists(exe)
+
+
+def test_particle_and_constants_known_answers_of_the_cpp_mirror(tmp_path):
+    """pica's Particle and Constants known answers (ParticleTests.cpp:37-164,
+    ConstantsTests.cpp:15-28) against the C++ mirror, host only."""
+    import subprocess
+    exe = str(tmp_path / "particle_known_answers")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "particle_known_answers.cpp"), "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout
+
+
+CONSTANT_NAMES = ("pi", "c", "lightVelocity", "electronCharge", "electronMass", "protonMass", "planck", "eV", "meV")
+PICA_HEADERS = "/root/reference/include"   # pica's own headers, where this checkout has them
+
+
+def _print_constants(tmp_path, name, include, namespace):
+    import subprocess
+    src = tmp_path / f"{name}.cpp"
+    body = "".join(f'    std::printf("%.17g\\n", {namespace}::constants::{c});\n' for c in CONSTANT_NAMES)
+    src.write_text(f'#include <cstdio>\n#include "{include}"\nint main() {{\n{body}    return 0;\n}}\n')
+    exe = str(tmp_path / name)
+    inc = PICA_HEADERS if namespace == "pica" else os.path.join(ROOT, "include")
+    subprocess.run(["g++", "-std=c++17", "-I", inc, str(src), "-o", exe], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    return [float(v) for v in out]
+
+
+def test_constants_equal_picas(tmp_path):
+    """The mirror's constants table (and the Python module's) equals pica's
+    math/Constants.h value for value; compiled against pica's own header when it is
+    present in this checkout."""
+    import pytest
+    ours = _print_constants(tmp_path, "ours", "pica_gb300.hpp", "pica_gb300")
+    py = dict(pi=pica_gb300.PI, c=pica_gb300.LIGHT_VELOCITY, electronCharge=pica_gb300.ELECTRON_CHARGE,
+              electronMass=pica_gb300.ELECTRON_MASS)
+    for name, v in py.items():
+        assert ours[CONSTANT_NAMES.index(name)] == v, name
+    if not os.path.isdir(os.path.join(PICA_HEADERS, "pica")):
+        pytest.skip("pica's headers are not in this checkout")
+    theirs = _print_constants(tmp_path, "theirs", "pica/math/Constants.h", "pica")
+    assert ours == theirs
