@@ -47,11 +47,16 @@ inline FP3 operator-(const FP3& a, const FP3& b) { return FP3(a.x - b.x, a.y - b
 inline FP3 operator*(const FP3& a, double s) { return FP3(a.x * s, a.y * s, a.z * s); }
 inline FP3 operator*(double s, const FP3& a) { return a * s; }
 inline FP3 operator/(const FP3& a, double s) { return FP3(a.x / s, a.y / s, a.z / s); }
+// Component-wise, as pica's Vector3 (math/Vectors.h).
+inline FP3 operator*(const FP3& a, const FP3& b) { return FP3(a.x * b.x, a.y * b.y, a.z * b.z); }
+inline FP3 operator/(const FP3& a, const FP3& b) { return FP3(a.x / b.x, a.y / b.y, a.z / b.z); }
+inline bool operator==(const FP3& a, const FP3& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
 struct Int3 {
     int x = 0, y = 0, z = 0;
     Int3() = default;
     Int3(int a, int b, int c) : x(a), y(b), z(c) {}
 };
+inline bool operator==(const Int3& a, const Int3& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
 
 // Constants of pica math/Constants.h:9-18 (CGS, pi truncated as in pica), and the
 // Constants<Real> accessors of Constants.h:23-34: each the namespace value cast to Real.
@@ -161,33 +166,82 @@ struct Config {
 class Simulation;
 class YeeSolver;
 
-// Host mirror of the device grid: pica's YeeGrid accessors on host arrays,
-// moved to / from the device with upload() / download().
+// pica's Array3d (utility/Array.h:119-167): a 3D array with z fastest, index
+// (i * ny + j) * nz + k, addressed by (i, j, k) or an Int3.
+class Array3d {
+public:
+    Array3d() = default;
+    explicit Array3d(const Int3& size) : n_(size), v_((size_t)size.x * size.y * size.z, 0.0) {}
+    double& operator()(int i, int j, int k) { return v_[idx(i, j, k)]; }
+    double operator()(int i, int j, int k) const { return v_[idx(i, j, k)]; }
+    double& operator()(const Int3& n) { return v_[idx(n.x, n.y, n.z)]; }
+    double operator()(const Int3& n) const { return v_[idx(n.x, n.y, n.z)]; }
+    Int3 getSize() const { return n_; }
+    size_t size() const { return v_.size(); }
+    double* data() { return v_.data(); }
+    const double* data() const { return v_.data(); }
+
+private:
+    size_t idx(int i, int j, int k) const { return ((size_t)i * n_.y + j) * n_.z + k; }
+    Int3 n_;
+    std::vector<double> v_;
+};
+
+// Host mirror of the device grid: pica's YeeGrid<Three> accessors (grid/YeeGrid.h:193-256,
+// grid/Grid.h:13-83) on host arrays, moved to / from the device with upload() / download().
+// The grid a Simulation owns is periodic with origin 0; a grid built with pica's
+// constructor is a host container only (upload / download throw).
 class YeeGrid {
 public:
-    double& ex(int i, int j, int k) { return f_[0][idx(i, j, k)]; }
-    double& ey(int i, int j, int k) { return f_[1][idx(i, j, k)]; }
-    double& ez(int i, int j, int k) { return f_[2][idx(i, j, k)]; }
-    double& bx(int i, int j, int k) { return f_[3][idx(i, j, k)]; }
-    double& by(int i, int j, int k) { return f_[4][idx(i, j, k)]; }
-    double& bz(int i, int j, int k) { return f_[5][idx(i, j, k)]; }
-    double& jx(int i, int j, int k) { return f_[6][idx(i, j, k)]; }
-    double& jy(int i, int j, int k) { return f_[7][idx(i, j, k)]; }
-    double& jz(int i, int j, int k) { return f_[8][idx(i, j, k)]; }
+    YeeGrid() = default;
+    YeeGrid(const FP3& origin, const FP3& step, const Int3& size) : n_(size), h_(step), o_(origin) {
+        for (auto& a : f_) a = Array3d(size);
+    }
+#define PICA_GB300_COMPONENT(name, c)                                              \
+    double& name(int i, int j, int k) { return f_[c](i, j, k); }                   \
+    double name(int i, int j, int k) const { return f_[c](i, j, k); }              \
+    double& name(const Int3& n) { return f_[c](n); }                               \
+    double name(const Int3& n) const { return f_[c](n); }                          \
+    Array3d& name() { return f_[c]; }                                              \
+    const Array3d& name() const { return f_[c]; }
+    PICA_GB300_COMPONENT(ex, 0)
+    PICA_GB300_COMPONENT(ey, 1)
+    PICA_GB300_COMPONENT(ez, 2)
+    PICA_GB300_COMPONENT(bx, 3)
+    PICA_GB300_COMPONENT(by, 4)
+    PICA_GB300_COMPONENT(bz, 5)
+    PICA_GB300_COMPONENT(jx, 6)
+    PICA_GB300_COMPONENT(jy, 7)
+    PICA_GB300_COMPONENT(jz, 8)
+#undef PICA_GB300_COMPONENT
     Int3 getSize() const { return n_; }
     FP3 getStep() const { return h_; }
-    FP3 getOrigin() const { return FP3(0, 0, 0); }
+    FP3 getOrigin() const { return o_; }
+    // Cell of a position: (position - origin) / step truncated toward zero (Grid.h:37).
+    Int3 getCellIndex(const FP3& r) const {
+        const FP3 q = (r - o_) / h_;
+        return Int3((int)std::trunc(q.x), (int)std::trunc(q.y), (int)std::trunc(q.z));
+    }
+    // Offset of each component's node from the cell corner: pica's staggering (YeeGrid.h:11-14, 247-255).
+    FP3 getShiftEx() const { return FP3(0, 0.5 * h_.y, 0.5 * h_.z); }
+    FP3 getShiftEy() const { return FP3(0.5 * h_.x, 0, 0.5 * h_.z); }
+    FP3 getShiftEz() const { return FP3(0.5 * h_.x, 0.5 * h_.y, 0); }
+    FP3 getShiftBx() const { return FP3(0.5 * h_.x, 0, 0); }
+    FP3 getShiftBy() const { return FP3(0, 0.5 * h_.y, 0); }
+    FP3 getShiftBz() const { return FP3(0, 0, 0.5 * h_.z); }
+    FP3 getShiftJx() const { return getShiftEx(); }
+    FP3 getShiftJy() const { return getShiftEy(); }
+    FP3 getShiftJz() const { return getShiftEz(); }
     inline void upload();
     inline void download();
 
 private:
     friend class Simulation;
     friend class YeeSolver;
-    size_t idx(int i, int j, int k) const { return ((size_t)i * n_.y + j) * n_.z + k; }
     pica_ctx* ctx_ = nullptr;
     Int3 n_;
-    FP3 h_;
-    std::array<std::vector<double>, 9> f_;
+    FP3 h_, o_;
+    std::array<Array3d, 9> f_;
 };
 
 // Host staging of the device ensemble: add() collects particles, upload()
@@ -242,8 +296,7 @@ public:
         ParticleTypes::numTypes = (int)c.types.size();
         dt_ = c.dt;
         grid_.ctx_ = ctx_; grid_.n_ = c.numCells; grid_.h_ = c.step;
-        const size_t nodes = (size_t)c.numCells.x * c.numCells.y * c.numCells.z;
-        for (auto& a : grid_.f_) a.assign(nodes, 0.0);
+        for (auto& a : grid_.f_) a = Array3d(c.numCells);
         ens_.ctx_ = ctx_; ens_.ntypes_ = cfg.nspecies; ens_.S_ = c.numCellsPerSupercell;
         ens_.nsc_ = Int3(c.numCells.x / c.numCellsPerSupercell.x, c.numCells.y / c.numCellsPerSupercell.y,
                          c.numCells.z / c.numCellsPerSupercell.z);
@@ -343,11 +396,13 @@ private:
 };
 
 void YeeGrid::upload() {
+    if (!ctx_) throw Error(PICA_ERR_INVALID, "this grid belongs to no Simulation");
     const double* p[9];
     for (int c = 0; c < 9; c++) p[c] = f_[c].data();
     check(ctx_, pica_upload_fields(ctx_, p));
 }
 void YeeGrid::download() {
+    if (!ctx_) throw Error(PICA_ERR_INVALID, "this grid belongs to no Simulation");
     double* p[9];
     for (int c = 0; c < 9; c++) p[c] = f_[c].data();
     check(ctx_, pica_download_fields(ctx_, p));

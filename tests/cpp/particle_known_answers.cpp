@@ -1,9 +1,11 @@
-// pica's particle and constants known-answer checks (test/src/particles/ParticleTests.cpp:37-164,
-// test/src/math/ConstantsTests.cpp:15-28) restated against the C++ mirror: Constants<T>
-// equals the cast namespace value for float and double; a particle built from a momentum
-// returns it, with gamma = sqrt(1 + |P|^2 / (m c)^2) to 1e-12; momentum and velocity
-// round-trip to 1e-12; mass and charge come from the type table.  Host-only, no GPU.
-// Prints "ok" or the first failing check.
+// pica's particle, constants and grid known-answer checks (test/src/particles/ParticleTests.cpp:37-164,
+// test/src/math/ConstantsTests.cpp:15-28, test/src/grid/YeeGridTests.cpp:115-134) restated
+// against the C++ mirror: Constants<T> equals the cast namespace value for float and double;
+// a particle built from a momentum returns it, with gamma = sqrt(1 + |P|^2 / (m c)^2) to
+// 1e-12; momentum and velocity round-trip to 1e-12; mass and charge come from the type
+// table; a YeeGrid returns its step and size, the cell of every cell centre, its values by
+// every accessor in z-fastest order, and pica's staggering shifts.  Host-only, no GPU.
+// Prints "ok", or each failing check and "failed".
 #include <cmath>
 #include <cstdio>
 
@@ -95,6 +97,48 @@ int main() {
     r.setP(FP3(0.3, -0.4, 1.2));
     nearVec("momentum from p", FP3(0.3, -0.4, 1.2) * mc, r.getMomentum());
     near("gamma from p", std::sqrt(1.0 + 0.09 + 0.16 + 1.44), r.getGamma());
+
+    // YeeGrid<Three> (grid/Grid.h:13-83, grid/YeeGrid.h:193-256) as a host container
+    const FP3 origin(1.25, -4.5, 0.75), step(0.1, 0.2, 0.05);
+    const Int3 size(5, 6, 7);
+    YeeGrid g(origin, step, size);
+    if (!(g.getStep() == step) || !(g.getSize() == size) || !(g.getOrigin() == origin)) {
+        std::printf("grid step / size / origin\n");
+        fails++;
+    }
+    for (int i = 0; i < size.x; i++)
+        for (int j = 0; j < size.y; j++)
+            for (int k = 0; k < size.z; k++) {
+                const FP3 centre = origin + step * FP3(i + 0.5, j + 0.5, k + 0.5);
+                if (!(g.getCellIndex(centre) == Int3(i, j, k))) {
+                    std::printf("cell index of centre %d %d %d\n", i, j, k);
+                    fails++;
+                }
+                g.ey(i, j, k) = 100.0 * i + 10.0 * j + k;
+            }
+    const YeeGrid& cg = g;
+    const Int3 n(3, 2, 5);
+    const double want = 100.0 * 3 + 10.0 * 2 + 5;
+    if (cg.ey(3, 2, 5) != want || cg.ey(n) != want || g.ey()(3, 2, 5) != want || g.ey()(n) != want ||
+        cg.ey().data()[(3 * size.y + 2) * size.z + 5] != want || g.ex(n) != 0.0) {
+        std::printf("grid accessors\n");
+        fails++;
+    }
+    if (!(g.getShiftEx() == FP3(0, 0.1, 0.025)) || !(g.getShiftBz() == FP3(0, 0, 0.025)) ||
+        !(g.getShiftJy() == FP3(0.05, 0, 0.025)) || !(g.getShiftBx() == FP3(0.05, 0, 0))) {
+        std::printf("staggering shifts\n");
+        fails++;
+    }
+    try {
+        g.upload();
+        std::printf("upload of a grid without a Simulation did not throw\n");
+        fails++;
+    } catch (const Error& e) {
+        if (e.status != PICA_ERR_INVALID) {
+            std::printf("upload of a grid without a Simulation: status %d\n", e.status);
+            fails++;
+        }
+    }
 
     std::printf(fails ? "failed\n" : "ok\n");
     return fails ? 1 : 0;

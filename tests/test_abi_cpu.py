@@ -102,12 +102,16 @@ def test_cpp_mirror_compiles_and_links_against_the_library(tmp_path):
 
 
 def test_particle_and_constants_known_answers_of_the_cpp_mirror(tmp_path):
-    """pica's Particle and Constants known answers (ParticleTests.cpp:37-164,
-    ConstantsTests.cpp:15-28) against the C++ mirror, host only."""
+    """pica's Particle, Constants and YeeGrid known answers (ParticleTests.cpp:37-164,
+    ConstantsTests.cpp:15-28, YeeGridTests.cpp:115-134) against the C++ mirror, host only
+    (linked against the library, which a grid without a Simulation never calls)."""
     import subprocess
+    so = _lib.lib_path()
+    _lib.load()
     exe = str(tmp_path / "particle_known_answers")
     subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
-                    os.path.join(ROOT, "tests", "cpp", "particle_known_answers.cpp"), "-o", exe], check=True)
+                    os.path.join(ROOT, "tests", "cpp", "particle_known_answers.cpp"), so, "-o", exe,
+                    "-Wl,-rpath," + os.path.dirname(so)], check=True)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout
 
