@@ -29,6 +29,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "pica_gb300.h"
@@ -248,6 +249,16 @@ private:
 // routes them to supercells (EnsembleSupercells::add, EnsembleSupercells.h:41-45).
 class EnsembleSupercells {
 public:
+    EnsembleSupercells() = default;
+    // pica's constructor (EnsembleSupercells.h:25-34): a host-only container over
+    // [minPosition, maxPosition) with numCells cells in supercells of numCellsPerSupercell
+    // (add and getSupercellIndex work; upload and the device calls throw).  The
+    // ensemble of a Simulation spans [0, numCells * step).
+    EnsembleSupercells(const FP3& minPosition, const FP3& maxPosition, const Int3& numCells,
+                       const Int3& numCellsPerSupercell)
+        : S_(numCellsPerSupercell), min_(minPosition), max_(maxPosition), n_(numCells) {
+        nsc_ = Int3((n_.x + S_.x - 1) / S_.x, (n_.y + S_.y - 1) / S_.y, (n_.z + S_.z - 1) / S_.z);
+    }
     void add(const Particle3d& p) {
         x_.push_back(p.position.x); y_.push_back(p.position.y); z_.push_back(p.position.z);
         ux_.push_back(p.p.x); uy_.push_back(p.p.y); uz_.push_back(p.p.z);
@@ -259,6 +270,22 @@ public:
     inline std::vector<int32_t> counts() const;
     Int3 getNumSupercells() const { return nsc_; }
     Int3 getNumCellsPerSupercell() const { return S_; }
+    Int3 getNumCells() const { return n_; }
+    FP3 getMinPosition() const { return min_; }
+    FP3 getMaxPosition() const { return max_; }
+    // pica's routing rule (EnsembleSupercells.h:54-57): floor((position - min) / supercell size),
+    // supercell size = numCellsPerSupercell * (max - min) / numCells.
+    Int3 getSupercellIndex(const Particle3d& p) const {
+        const FP3 cell = (max_ - min_) / FP3(n_.x, n_.y, n_.z);
+        const FP3 inv = FP3(1, 1, 1) / (FP3(S_.x, S_.y, S_.z) * cell);
+        const FP3 q = (p.position - min_) * inv;
+        return Int3((int)std::floor(q.x), (int)std::floor(q.y), (int)std::floor(q.z));
+    }
+    // The particles of one supercell (EnsembleSupercells.h:51-52), type by type in
+    // slot order: a downloaded copy (the device holds the ensemble).
+    inline std::vector<Particle3d> getParticles(const Int3& supercellIdx) const;
+    // Number of particles on the device (pica's size() throws "not implemented").
+    inline int64_t size() const;
     inline void migrate();
     // Sort every supercell by cell now (EnsembleOrdered::reorder, EnsembleOrdered.h:61-71).
     inline void reorder();
@@ -268,6 +295,9 @@ private:
     pica_ctx* ctx_ = nullptr;
     int ntypes_ = 1;
     Int3 nsc_, S_;
+    FP3 min_, max_;
+    Int3 n_;
+    inline std::vector<Particle3d> download(std::vector<int32_t>* supercell) const;
     std::vector<double> x_, y_, z_, ux_, uy_, uz_, w_;
     std::vector<int32_t> t_;
 };
@@ -300,6 +330,8 @@ public:
         ens_.ctx_ = ctx_; ens_.ntypes_ = cfg.nspecies; ens_.S_ = c.numCellsPerSupercell;
         ens_.nsc_ = Int3(c.numCells.x / c.numCellsPerSupercell.x, c.numCells.y / c.numCellsPerSupercell.y,
                          c.numCells.z / c.numCellsPerSupercell.z);
+        ens_.n_ = c.numCells;
+        ens_.max_ = FP3(c.numCells.x * c.step.x, c.numCells.y * c.step.y, c.numCells.z * c.step.z);
     }
     ~Simulation() { if (ctx_) pica_ctx_destroy(ctx_); }
     Simulation(const Simulation&) = delete;
@@ -409,11 +441,29 @@ void YeeGrid::download() {
 }
 
 void EnsembleSupercells::upload() {
+    if (!ctx_) throw Error(PICA_ERR_INVALID, "this ensemble belongs to no Simulation");
     check(ctx_, pica_upload_particles(ctx_, (int64_t)w_.size(), x_.data(), y_.data(), z_.data(), ux_.data(),
                                       uy_.data(), uz_.data(), w_.data(), t_.data()));
     x_.clear(); y_.clear(); z_.clear(); ux_.clear(); uy_.clear(); uz_.clear(); w_.clear(); t_.clear();
 }
-std::vector<Particle3d> EnsembleSupercells::particles() const {
+std::vector<Particle3d> EnsembleSupercells::particles() const { return download(nullptr); }
+std::vector<Particle3d> EnsembleSupercells::getParticles(const Int3& idx) const {
+    std::vector<int32_t> s;
+    const std::vector<Particle3d> all = download(&s);
+    const int32_t want = (idx.x * nsc_.y + idx.y) * nsc_.z + idx.z;
+    std::vector<Particle3d> out;
+    for (size_t i = 0; i < all.size(); i++)
+        if (s[i] == want) out.push_back(all[i]);
+    return out;
+}
+int64_t EnsembleSupercells::size() const {
+    if (!ctx_) throw Error(PICA_ERR_INVALID, "this ensemble belongs to no Simulation");
+    const int64_t n = pica_num_particles(ctx_);
+    if (n < 0) check(ctx_, (int)n);
+    return n;
+}
+std::vector<Particle3d> EnsembleSupercells::download(std::vector<int32_t>* supercell) const {
+    if (!ctx_) throw Error(PICA_ERR_INVALID, "this ensemble belongs to no Simulation");
     const int64_t n = pica_num_particles(ctx_);
     if (n < 0) check(ctx_, (int)n);
     std::vector<double> a[7];
@@ -428,6 +478,7 @@ std::vector<Particle3d> EnsembleSupercells::particles() const {
         out[i].factor = a[6][i];
         out[i].typeIndex = (short)t[i];
     }
+    if (supercell) *supercell = std::move(s);
     return out;
 }
 std::vector<int32_t> EnsembleSupercells::counts() const {

@@ -4,7 +4,8 @@
 // a particle built from a momentum returns it, with gamma = sqrt(1 + |P|^2 / (m c)^2) to
 // 1e-12; momentum and velocity round-trip to 1e-12; mass and charge come from the type
 // table; a YeeGrid returns its step and size, the cell of every cell centre, its values by
-// every accessor in z-fastest order, and pica's staggering shifts.  Host-only, no GPU.
+// every accessor in z-fastest order, and pica's staggering shifts; an EnsembleSupercells
+// routes every supercell centre to its supercell (floor rule).  Host-only, no GPU.
 // Prints "ok", or each failing check and "failed".
 #include <cmath>
 #include <cstdio>
@@ -136,6 +137,45 @@ int main() {
     } catch (const Error& e) {
         if (e.status != PICA_ERR_INVALID) {
             std::printf("upload of a grid without a Simulation: status %d\n", e.status);
+            fails++;
+        }
+    }
+
+    // EnsembleSupercells routing (particles/EnsembleSupercells.h:25-57): the supercell of
+    // every supercell centre, for an offset domain with uneven cell sizes
+    const FP3 lo(-1.0, 2.0, 0.5), hi(0.6, 2.8, 1.3);
+    const Int3 cells(16, 8, 8), per(4, 2, 4);
+    EnsembleSupercells ens(lo, hi, cells, per);
+    if (!(ens.getNumSupercells() == Int3(4, 4, 2)) || !(ens.getNumCells() == cells) ||
+        !(ens.getMinPosition() == lo) || !(ens.getMaxPosition() == hi)) {
+        std::printf("ensemble geometry\n");
+        fails++;
+    }
+    const FP3 scSize = FP3(per.x, per.y, per.z) * ((hi - lo) / FP3(cells.x, cells.y, cells.z));
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+            for (int k = 0; k < 2; k++) {
+                Particle3d q;
+                q.position = lo + scSize * FP3(i + 0.5, j + 0.5, k + 0.5);
+                if (!(ens.getSupercellIndex(q) == Int3(i, j, k))) {
+                    std::printf("supercell of centre %d %d %d\n", i, j, k);
+                    fails++;
+                }
+            }
+    Particle3d below;
+    below.position = lo - FP3(1e-9, 0, 0);   // floor, not truncation: one supercell down
+    if (ens.getSupercellIndex(below).x != -1) {
+        std::printf("supercell below the minimum\n");
+        fails++;
+    }
+    ens.add(below);
+    try {
+        ens.upload();
+        std::printf("upload of an ensemble without a Simulation did not throw\n");
+        fails++;
+    } catch (const Error& e) {
+        if (e.status != PICA_ERR_INVALID) {
+            std::printf("upload of an ensemble without a Simulation: status %d\n", e.status);
             fails++;
         }
     }
