@@ -141,6 +141,83 @@ private:
     double invGamma() const { return 1.0 / std::sqrt(1.0 + p.norm2()); }
 };
 
+// pica's ParticleArraySoA<Particle3d> (particles/ParticleArray.h:46-203): a host
+// container of particles, one array per component (position, normalised momentum,
+// factor, 1/gamma, type), whose elements are reached through ConstParticleRef /
+// ParticleRef proxies with the accessors of Particle3d.  A host loop fills one and
+// hands its particles to EnsembleSupercells::add.
+class ParticleArraySoA {
+public:
+    typedef Particle3d Particle;
+
+    class ConstParticleRef {
+    public:
+        ConstParticleRef(const ParticleArraySoA& a, int i) : a_(&a), i_(i) {}
+        FP3 getPosition() const { return FP3(a_->x_[i_], a_->y_[i_], a_->z_[i_]); }
+        FP3 getP() const { return FP3(a_->px_[i_], a_->py_[i_], a_->pz_[i_]); }
+        FP3 getMomentum() const { return getP() * Constants<double>::c() * getMass(); }
+        FP3 getVelocity() const { return getP() * Constants<double>::c() * a_->invGamma_[i_]; }
+        double getGamma() const { return 1.0 / a_->invGamma_[i_]; }
+        double getMass() const { return ParticleTypes::at(getType()).mass; }
+        double getCharge() const { return ParticleTypes::at(getType()).charge; }
+        double getFactor() const { return a_->factor_[i_]; }
+        short getType() const { return a_->type_[i_]; }
+        // The element as a Particle3d value.
+        operator Particle3d() const {
+            Particle3d q;
+            q.position = getPosition();
+            q.p = getP();
+            q.factor = getFactor();
+            q.typeIndex = getType();
+            return q;
+        }
+
+    private:
+        const ParticleArraySoA* a_;
+        int i_;
+    };
+
+    class ParticleRef : public ConstParticleRef {
+    public:
+        ParticleRef(ParticleArraySoA& a, int i) : ConstParticleRef(a, i), m_(&a), j_(i) {}
+        void setPosition(const FP3& r) { m_->x_[j_] = r.x; m_->y_[j_] = r.y; m_->z_[j_] = r.z; }
+        void setP(const FP3& p) {
+            m_->px_[j_] = p.x; m_->py_[j_] = p.y; m_->pz_[j_] = p.z;
+            m_->invGamma_[j_] = 1.0 / std::sqrt(1.0 + p.norm2());
+        }
+        void setMomentum(const FP3& m) { setP(m / (Constants<double>::c() * this->getMass())); }
+        void setVelocity(const FP3& v) { setP(v / std::sqrt(constants::c * constants::c - v.norm2())); }
+        void setFactor(double f) { m_->factor_[j_] = f; }
+        void setType(short t) { m_->type_[j_] = t; }
+
+    private:
+        ParticleArraySoA* m_;
+        int j_;
+    };
+
+    int size() const { return (int)type_.size(); }
+    ParticleRef operator[](int i) { return ParticleRef(*this, i); }
+    ConstParticleRef operator[](int i) const { return ConstParticleRef(*this, i); }
+    ParticleRef back() { return (*this)[size() - 1]; }
+    ConstParticleRef back() const { return (*this)[size() - 1]; }
+    void pushBack(const Particle3d& q) {
+        x_.push_back(q.position.x); y_.push_back(q.position.y); z_.push_back(q.position.z);
+        px_.push_back(q.p.x); py_.push_back(q.p.y); pz_.push_back(q.p.z);
+        factor_.push_back(q.factor);
+        invGamma_.push_back(1.0 / std::sqrt(1.0 + q.p.norm2()));
+        type_.push_back(q.typeIndex);
+    }
+    void pushBack(const ConstParticleRef& r) { pushBack(static_cast<Particle3d>(r)); }
+    void popBack() {
+        for (auto* v : {&x_, &y_, &z_, &px_, &py_, &pz_, &factor_, &invGamma_}) v->pop_back();
+        type_.pop_back();
+    }
+
+private:
+    std::vector<double> x_, y_, z_, px_, py_, pz_, factor_, invGamma_;
+    std::vector<short> type_;
+};
+
 class Error : public std::runtime_error {
 public:
     Error(int status, const std::string& msg) : std::runtime_error(msg), status(status) {}
@@ -259,6 +336,7 @@ public:
         : S_(numCellsPerSupercell), min_(minPosition), max_(maxPosition), n_(numCells) {
         nsc_ = Int3((n_.x + S_.x - 1) / S_.x, (n_.y + S_.y - 1) / S_.y, (n_.z + S_.z - 1) / S_.z);
     }
+    void add(const ParticleArraySoA::ConstParticleRef& r) { add(static_cast<Particle3d>(r)); }
     void add(const Particle3d& p) {
         x_.push_back(p.position.x); y_.push_back(p.position.y); z_.push_back(p.position.z);
         ux_.push_back(p.p.x); uy_.push_back(p.p.y); uz_.push_back(p.p.z);

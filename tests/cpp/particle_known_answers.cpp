@@ -1,14 +1,18 @@
 // pica's particle, constants and grid known-answer checks (test/src/particles/ParticleTests.cpp:37-164,
-// test/src/math/ConstantsTests.cpp:15-28, test/src/grid/YeeGridTests.cpp:115-134) restated
+// test/src/math/ConstantsTests.cpp:15-28, test/src/grid/YeeGridTests.cpp:115-134,
+// test/src/particles/ParticleArrayTests.cpp:38-136) restated
 // against the C++ mirror: Constants<T> equals the cast namespace value for float and double;
 // a particle built from a momentum returns it, with gamma = sqrt(1 + |P|^2 / (m c)^2) to
 // 1e-12; momentum and velocity round-trip to 1e-12; mass and charge come from the type
 // table; a YeeGrid returns its step and size, the cell of every cell centre, its values by
 // every accessor in z-fastest order, and pica's staggering shifts; an EnsembleSupercells
-// routes every supercell centre to its supercell (floor rule).  Host-only, no GPU.
+// routes every supercell centre to its supercell (floor rule); a ParticleArraySoA keeps
+// every particle as pushed through index access, back, copies and popBack, and its
+// references set momentum and velocity like a particle.  Host-only, no GPU.
 // Prints "ok", or each failing check and "failed".
 #include <cmath>
 #include <cstdio>
+#include <vector>
 
 #include "pica_gb300.hpp"
 
@@ -141,6 +145,55 @@ int main() {
         }
     }
 
+    // ParticleArraySoA (particles/ParticleArray.h:46-203; ParticleArrayTests.cpp:38-136):
+    // size, index access, back, copies and popBack keep every particle as pushed
+    {
+        auto same = [](const Particle3d& a, const Particle3d& b) {
+            return a.position == b.position && a.p == b.p && a.factor == b.factor && a.typeIndex == b.typeIndex;
+        };
+        auto particle = [](int i) {
+            Particle3d q;
+            q.position = FP3(0.1 * i, -2.5 + i, 3.0 / (i + 1));
+            q.p = FP3(0.01 * (i % 7) - 0.03, 0.5 * std::sin(i), -0.2 + 0.05 * i);
+            q.factor = 10.0 + i;
+            q.typeIndex = (short)(i % 2);
+            return q;
+        };
+        ParticleArraySoA arr;
+        if (arr.size() != 0) { std::printf("empty array size\n"); fails++; }
+        std::vector<Particle3d> pushed;
+        for (int i = 0; i < 33; i++) {
+            pushed.push_back(particle(i));
+            arr.pushBack(pushed.back());
+            if (!same(pushed.back(), arr.back())) { std::printf("back after push %d\n", i); fails++; }
+        }
+        const ParticleArraySoA copy = arr;
+        if (arr.size() != 33 || copy.size() != 33) { std::printf("array size\n"); fails++; }
+        for (int i = 0; i < 33; i++) {
+            if (!same(pushed[i], arr[i]) || !same(pushed[i], copy[i])) { std::printf("element %d\n", i); fails++; }
+            near("element gamma", pushed[i].getGamma(), arr[i].getGamma());
+            nearVec("element velocity", pushed[i].getVelocity(), arr[i].getVelocity());
+        }
+        for (int n = 33; n > 0; n--) {
+            arr.popBack();
+            if (arr.size() != n - 1 || (n > 1 && !same(pushed[n - 2], arr.back()))) { std::printf("popBack %d\n", n); fails++; }
+        }
+        ParticleArraySoA one;
+        one.pushBack(copy[5]);   // from a reference
+        auto r = one[0];
+        r.setMomentum(m2);
+        nearVec("reference set / get momentum", m2, r.getMomentum());
+        r.setVelocity(v);
+        nearVec("reference set / get velocity", v, r.getVelocity());
+        r.setPosition(FP3(1, 2, 3));
+        r.setFactor(7.5);
+        r.setType(1);
+        if (!(one[0].getPosition() == FP3(1, 2, 3)) || one[0].getFactor() != 7.5 || one[0].getMass() != constants::protonMass) {
+            std::printf("reference setters\n");
+            fails++;
+        }
+    }
+
     // EnsembleSupercells routing (particles/EnsembleSupercells.h:25-57): the supercell of
     // every supercell centre, for an offset domain with uneven cell sizes
     const FP3 lo(-1.0, 2.0, 0.5), hi(0.6, 2.8, 1.3);
@@ -169,6 +222,9 @@ int main() {
         fails++;
     }
     ens.add(below);
+    ParticleArraySoA some;
+    some.pushBack(below);
+    ens.add(some[0]);   // from a reference, as pica's templated add
     try {
         ens.upload();
         std::printf("upload of an ensemble without a Simulation did not throw\n");
