@@ -95,7 +95,7 @@ def test_cpp_mirror_compiles_and_links_against_the_library(tmp_path):
     for src in ("host_loop.cpp", "driver_checkpoint.cpp", "host_resident_loop.cpp"):
         exe = str(tmp_path / src.replace(".cpp", ""))
         extra = runtime if src == "host_resident_loop.cpp" else []
-        subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+        subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Wpedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
                         os.path.join(ROOT, "tests", "cpp", src), so] + extra + ["-o", exe,
                         "-Wl,-rpath," + os.path.dirname(so), "-lpthread"], check=True)
         assert os.path.exists(exe)
@@ -109,7 +109,7 @@ def test_particle_and_constants_known_answers_of_the_cpp_mirror(tmp_path):
     so = _lib.lib_path()
     _lib.load()
     exe = str(tmp_path / "particle_known_answers")
-    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Wpedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "particle_known_answers.cpp"), so, "-o", exe,
                     "-Wl,-rpath," + os.path.dirname(so)], check=True)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
