@@ -65,6 +65,40 @@ def test_port_matches_reference_headers(n, sc, ppc, steps, resort):
     assert np.array_equal(ca, cb) and np.array_equal(ma, mb)
 
 
+@pytest.mark.skipif(not REFERENCE_AVAILABLE, reason="pica sources not mounted here")
+@pytest.mark.parametrize("n,sc,ppc,steps,resort,u_sigma,hscale,nspecies,drift", [
+    ((16, 12, 8), (4, 4, 4), 4, 4, 2, 0.1, (1.0, 1.0, 1.0), 2, None),            # electrons and ions, 4^3 supercells
+    ((8, 8, 8), (2, 2, 2), 3, 6, 3, 0.3, (1.0, 0.7, 1.3), 1, (0.2, 0.0, -0.1)),  # hot drifting plasma, uneven cells
+])
+def test_port_matches_reference_headers_species_and_fast_particles(n, sc, ppc, steps, resort, u_sigma, hscale,
+                                                                    nspecies, drift):
+    """The restatement against the harness over pica's headers with two species (ions
+    of 100 electron masses, species interleaved in the input) and with a hot drifting
+    plasma on uneven cells, where many particles migrate every step: equal bit for bit,
+    particles, fields, counts and migration lists."""
+    po.build(reference=True)
+    d = thermal_inputs(n, ppc, seed=23, u_sigma=u_sigma, hscale=hscale, nspecies=nspecies, drift=drift)
+    species = ((ME, E), (100 * ME, -E))[:nspecies]   # electrons (E < 0), ions
+    res = []
+    for kind in ("port", "reference"):
+        o = po.Oracle(n, sc, d["h"], d["dt"], kind=kind, resort_every=resort, species=species)
+        o.load(d["x"], d["y"], d["z"], d["ux"], d["uy"], d["uz"], d["w"], d["species"])
+        rng = np.random.default_rng(4)
+        o.set_fields([2e3 * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3)
+        migrated = 0
+        for _ in range(steps):
+            o.step(1)
+            migrated += len(o.migrations())
+        res.append((o.particles(), o.get_fields(), o.counts(), o.migrations(), migrated))
+    (pa, fa, ca, ma, na), (pb, fb, cb, mb, nb) = res
+    for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species", "supercell"):
+        assert np.array_equal(pa[k], pb[k]), k
+    for c in range(9):
+        assert np.array_equal(fa[c], fb[c]), c
+    assert np.array_equal(ca, cb) and np.array_equal(ma, mb) and na == nb
+    assert na > 0.02 * len(d["x"]) * steps if u_sigma >= 0.3 else na > 0
+
+
 def div_faces(jx, jy, jz, h):
     return ((np.roll(jx, -1, 0) - jx) / h[0] + (np.roll(jy, -1, 1) - jy) / h[1] + (np.roll(jz, -1, 2) - jz) / h[2])
 
