@@ -220,3 +220,29 @@ def test_oracle_one_cell_thick_grid_matches_pica_1d_classes():
         assert rel_err(f[c], g["out_fields"][c]) <= 1e-12, c
     for k in ("x", "ux", "uy", "uz"):
         assert rel_err(got[k], ref[k]) <= 1e-12, k
+
+
+@pytest.mark.parametrize("form,tol", [(po.FORM_FP64_PLAIN, 1e-11), (po.FORM_FP32_CELL, 2e-5)])
+def test_yee_vacuum_plane_wave_follows_the_discrete_dispersion(form, tol):
+    """A standing Ey mode cos(k x) in vacuum (pica's staggering: Ey at x = (i + 1/2) h,
+    YeeGrid.h:11-14), advanced by B(dt/2), E(dt), B(dt/2) per step, keeps its shape and
+    its amplitude follows cos(w n dt) with Yee's discrete dispersion
+    sin(w dt / 2) = (c dt / h) sin(k h / 2), not w = c k."""
+    n, m, h = (32, 2, 2), 3, 1e-3
+    dt = 0.5 * h / (C * np.sqrt(3.0))
+    k = 2 * np.pi * m / (n[0] * h)
+    o = po.Oracle(n, (2, 2, 2), (h, h, h), dt, form=form)
+    o.load(np.zeros(0), np.zeros(0), np.zeros(0), np.zeros(0), np.zeros(0), np.zeros(0), np.zeros(0))
+    mode = np.broadcast_to(np.cos(k * (np.arange(n[0]) + 0.5) * h)[:, None, None], n)
+    f = [np.zeros(n) for _ in range(9)]
+    f[1] = 100.0 * mode
+    o.set_fields(f)
+    w = 2.0 / dt * np.arcsin(C * dt / h * np.sin(k * h / 2))
+    assert abs(w / (C * k) - 1) > 1e-3   # the discrete frequency is measurably not c k
+    steps = 40
+    for s in range(1, steps + 1):
+        o.step(1)
+        ey = o.get_fields()[1]
+        a = np.sum(ey * mode) / np.sum(mode * mode)
+        assert abs(a / 100.0 - np.cos(w * s * dt)) < tol, s
+        assert np.max(np.abs(ey - a * mode)) < tol * 100.0   # still the same mode
