@@ -246,3 +246,33 @@ def test_yee_vacuum_plane_wave_follows_the_discrete_dispersion(form, tol):
         a = np.sum(ey * mode) / np.sum(mode * mode)
         assert abs(a / 100.0 - np.cos(w * s * dt)) < tol, s
         assert np.max(np.abs(ey - a * mode)) < tol * 100.0   # still the same mode
+
+
+@pytest.mark.parametrize("form,shape,deposit,tol", [
+    (po.FORM_FP64_PLAIN, po.SHAPE_CIC, po.DEPOSIT_DIRECT, 1e-12),
+    (po.FORM_FP64_PLAIN, po.SHAPE_TSC, po.DEPOSIT_ESIRKEPOV, 1e-12),
+    (po.FORM_FP32_CELL, po.SHAPE_CIC, po.DEPOSIT_ESIRKEPOV, 2e-5),
+    (po.FORM_FP32_CELL, po.SHAPE_TSC, po.DEPOSIT_ESIRKEPOV, 2e-5),
+])
+def test_uniform_field_is_interpolated_exactly(form, shape, deposit, tol):
+    """Constant-field interpolation is exact: in a uniform E with B = 0, one step
+    changes every particle's normalised momentum by q E dt / (m c) (Boris without
+    rotation), wherever it sits in its cell -- the CIC and TSC weights of every
+    staggered component sum to one."""
+    n = (8, 8, 8)
+    d = thermal_inputs(n, 5, seed=31, u_sigma=0.05)
+    npart = len(d["x"])
+    w = np.mean(d["w"]) * (1.0 + np.arange(npart) / npart)   # unique (also in FP32): identify particles after the step
+    o = po.Oracle(n, (4, 4, 4), d["h"], d["dt"], form=form, shape=shape, deposit=deposit)
+    o.load(d["x"], d["y"], d["z"], d["ux"], d["uy"], d["uz"], w)
+    e = (3.0e6, -1.5e6, 2.0e6)   # du ~ 1e-2, well above the rounding of u ~ 0.05
+    o.set_fields([np.full(n, v) for v in e] + [np.zeros(n)] * 6)
+    before = o.particles()
+    o.step(1)
+    after = o.particles()
+    ib, ia = np.argsort(before["w"]), np.argsort(after["w"])
+    assert np.array_equal(before["w"][ib], after["w"][ia])
+    for c, k in enumerate(("ux", "uy", "uz")):
+        du = after[k][ia] - before[k][ib]
+        want = E * e[c] * d["dt"] / (ME * C)
+        assert np.max(np.abs(du - want)) < tol * abs(want), k
