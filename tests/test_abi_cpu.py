@@ -146,3 +146,16 @@ def test_constants_equal_picas(tmp_path):
         pytest.skip("pica's headers are not in this checkout")
     theirs = _print_constants(tmp_path, "theirs", "pica/math/Constants.h", "pica")
     assert ours == theirs
+
+
+def test_cpp_mirror_plumbing_against_a_host_fake_of_the_abi(tmp_path):
+    """The C++ mirror's host code (field order and round trip, particle conversion,
+    per-supercell selection) against tests/cpp/fake_abi.cpp, a host stand-in for the
+    entry points it calls that returns the ABI's documented ensemble order."""
+    import subprocess
+    exe = str(tmp_path / "mirror_plumbing")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Wpedantic", "-Werror",
+                    "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "mirror_plumbing.cpp"),
+                    os.path.join(ROOT, "tests", "cpp", "fake_abi.cpp"), "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout
