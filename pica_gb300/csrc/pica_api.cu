@@ -351,6 +351,12 @@ int pica_ctx_create(const pica_config* cfg, pica_ctx** out) {
         if (!(cfg->h[d] > 0)) return PICA_ERR_INVALID;
     }
     if (cfg->form == PICA_FORM_FP32_CELL && (cfg->n[0] > 2048 || cfg->n[1] > 2048 || cfg->n[2] > 1024)) return PICA_ERR_LIMIT;
+    // No CUDA device (or no driver): a CUDA error, not an allocation failure.  There is no CPU path.
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return PICA_ERR_CUDA;
+    }
     ctx = new pica_ctx();
     ctx->cfg = *cfg;
     ctx->fp64 = cfg->form == PICA_FORM_FP64_PLAIN;

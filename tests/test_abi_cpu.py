@@ -159,3 +159,51 @@ def test_cpp_mirror_plumbing_against_a_host_fake_of_the_abi(tmp_path):
                     os.path.join(ROOT, "tests", "cpp", "fake_abi.cpp"), "-o", exe], check=True)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout
+
+
+def _config(**kw):
+    c = _lib.PicaConfig()
+    for d in range(3):
+        c.n[d], c.sc[d], c.h[d] = 8, 2, 1e-3
+    c.dt, c.form, c.shape, c.deposit, c.nspecies = 1e-14, 0, 1, 0, 1
+    c.mass[0], c.charge[0] = pica_gb300.ELECTRON_MASS, pica_gb300.ELECTRON_CHARGE
+    for k, v in kw.items():
+        if isinstance(v, tuple):
+            getattr(c, k)[v[0]] = v[1]
+        else:
+            setattr(c, k, v)
+    return c
+
+
+def test_context_creation_rejects_bad_configurations_before_touching_the_device():
+    """Statuses, not exceptions, cross the ABI: every malformed configuration is
+    PICA_ERR_INVALID (a grid beyond the FP32 form's packed cell index, PICA_ERR_LIMIT)
+    and leaves the output handle NULL; validation runs before any CUDA call, so this
+    holds on a machine without a GPU."""
+    lib = _lib.load()
+    bad = [dict(form=7), dict(shape=0), dict(deposit=3), dict(nspecies=0), dict(nspecies=9), dict(dt=0.0),
+           dict(dt=float("nan")), dict(n=(0, 9)), dict(n=(1, 0)), dict(sc=(1, 3)), dict(sc=(2, 0)), dict(h=(2, -1.0)),
+           dict(h=(0, float("nan")))]
+    for kw in bad:
+        out = C.c_void_p(123)
+        assert lib.pica_ctx_create(C.byref(_config(**kw)), C.byref(out)) == -1, kw
+        assert out.value is None, kw
+    out = C.c_void_p(123)
+    assert lib.pica_ctx_create(C.byref(_config(form=1, n=(0, 4096))), C.byref(out)) == -8
+    assert out.value is None
+    assert lib.pica_ctx_create(None, C.byref(out)) == -1
+
+
+def test_context_creation_without_a_device_is_a_cuda_error():
+    """With no CUDA device there is no CPU path: a valid configuration returns
+    PICA_ERR_CUDA, and the Python binding raises."""
+    import pytest
+    lib = _lib.load()
+    out = C.c_void_p(123)
+    rc = lib.pica_ctx_create(C.byref(_config()), C.byref(out))
+    if rc == 0:   # a GPU is present: nothing to check here
+        lib.pica_ctx_destroy(out)
+        pytest.skip("a CUDA device is present")
+    assert rc == -2 and out.value is None
+    with pytest.raises(pica_gb300.PicaError):
+        pica_gb300.Simulation((8, 8, 8), (1e-3,) * 3, 1e-14, supercell=(2, 2, 2))
