@@ -276,3 +276,54 @@ def test_uniform_field_is_interpolated_exactly(form, shape, deposit, tol):
         du = after[k][ia] - before[k][ib]
         want = E * e[c] * d["dt"] / (ME * C)
         assert np.max(np.abs(du - want)) < tol * abs(want), k
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(po.REF_SO), "libpica_ref1d.so")),
+                    reason="the harness over pica's 1D classes is not built here")
+@pytest.mark.parametrize("n,sc,ppc,steps,seed,nspecies,u_sigma,field_amp", [
+    (48, 4, 3, 30, 41, 2, 0.1, 2.0e3),    # electrons and ions (4 electron masses), longer run
+    (20, 2, 6, 12, 42, 1, 0.25, 5.0e2),   # hot plasma, supercell edge 2
+])
+def test_oracle_matches_pica_1d_classes_live(n, sc, ppc, steps, seed, nspecies, u_sigma, field_amp):
+    """The oracle on a grid one cell thick along y and z against pica's own 1D path
+    (oracle/ref_harness_1d.cpp over YeeGrid<One>, FieldInterpolatorCIC and
+    CurrentDepositorCIC of YeeGrid<One>, the 1D YeeSolver), run here on new inputs:
+    fields and particles within 1e-12."""
+    import ctypes as CT
+    lib = CT.CDLL(os.path.join(os.path.dirname(po.REF_SO), "libpica_ref1d.so"))
+    dp = CT.POINTER(CT.c_double)
+    lib.ref1d_run.argtypes = [CT.c_int32, CT.c_double, CT.c_double, CT.c_double, CT.c_int32, dp, dp, CT.c_int64, dp,
+                              dp, dp, dp, dp, CT.POINTER(CT.c_int32), dp, CT.c_int32]
+    rng = np.random.default_rng(seed)
+    h = 0.05 * C / np.sqrt(4 * np.pi * 1e18 * E * E / ME)
+    dt = 0.5 * h / (C * np.sqrt(3.0))
+    npart = n * ppc
+    x = (np.repeat(np.arange(n), ppc) + rng.random(npart)) * h
+    u = rng.normal(0.0, u_sigma, (3, npart))
+    w = np.full(npart, 1e18 * h ** 3 / ppc) * (1.0 + 0.1 * rng.random(npart))
+    sp = rng.integers(0, nspecies, npart).astype(np.int32)
+    f = np.stack([field_amp * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3)
+    mass, charge = np.array([ME, 4 * ME][:nspecies]), np.array([E, -E][:nspecies])
+    xo, uo, fo = x.copy(), u.copy(), f.copy()
+
+    def ptr(a):
+        return a.ctypes.data_as(dp)
+
+    ux, uy, uz = (np.ascontiguousarray(uo[i]) for i in range(3))
+    assert lib.ref1d_run(n, h, h * h, dt, nspecies, ptr(mass), ptr(charge), npart, ptr(xo), ptr(ux), ptr(uy), ptr(uz),
+                         ptr(w), sp.ctypes.data_as(CT.POINTER(CT.c_int32)), ptr(fo), steps) == 0
+
+    o = po.Oracle((n, 1, 1), (sc, 1, 1), (h, h, h), dt, form=po.FORM_FP64_PLAIN, shape=po.SHAPE_CIC,
+                  deposit=po.DEPOSIT_DIRECT, species=tuple(zip(mass, charge)))
+    yz = np.full(npart, 0.5 * h)
+    o.load(x, yz, yz, u[0], u[1], u[2], w, sp)
+    o.set_fields([a.reshape(n, 1, 1) for a in f[:6]] + [np.zeros((n, 1, 1))] * 3)
+    o.step(steps)
+    got = o.get_fields()
+    for c in range(9):
+        assert rel_err(got[c].reshape(-1), fo[c]) <= 1e-12, c
+    p = o.particles()
+    mine, theirs = np.argsort(p["x"]), np.argsort(xo)
+    for k, ref in (("x", xo), ("ux", ux), ("uy", uy), ("uz", uz)):
+        assert rel_err(p[k][mine], ref[theirs]) <= 1e-12, k
+    assert np.array_equal(p["species"][mine], sp[theirs])
