@@ -18,8 +18,11 @@ two-stream (256x256x128, 8.4e8 electrons, CIC) and Weibel (256^3, 2.1e9
 electrons and ions, TSC) plasmas instead, generated on the device; their
 lines carry `value`, the push roofline and the clocks only.
 
-`--impl reference` times the CPU implementation of the same step instead
-(the oracle restatement built from this tree, all host cores).
+`--impl reference` times the CPU implementation of the same step instead: the
+oracle restatement of the headline workload at its full size on all host cores
+(plasma drawn by the oracle's own generator; nothing of the pica_gb300 package
+is imported), with pica's own FP64 CIC/direct arithmetic on the same plasma
+beside it.
 """
 import argparse
 import json
@@ -126,7 +129,6 @@ def parse():
     ap.add_argument("--e2e-split", type=int, default=1,
                     help="1: e2e host copies on copy streams of their own, gather / scatter kernels on two more")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--edge", type=int, default=None,
                     help="grid edge in cells (thermal: 128; two_stream: 256, grid edge x edge x edge/2; weibel: 256)")
@@ -200,18 +202,6 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic_per_particle():
-    """DRAM bytes per particle of the push kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "push_fp32_tsc_esirkepov.md")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_particle:"):
-                return float(line.split(":")[1])
-    except OSError:
-        pass
-    return None
-
-
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -272,6 +262,27 @@ def make_workload(edge, form):
     return wl
 
 
+def workload_description(name, edge=None):
+    """One-line description of a workload (the same for both arms of the bench)."""
+    if name == "thermal":
+        e = edge or 128
+        return (f"thermal electron plasma {e}^3 cells x 100 ppc, FP32 cell+offset form, TSC, Esirkepov, "
+                "supercell 4^3, Boris, periodic")
+    e = edge or 256
+    if name == "two_stream":
+        return (f"two-stream {e}x{e}x{e // 2} cells, two electron beams +-0.2c along x, density "
+                "1 + 0.9 cos(2 pi x / Lx) (10-190 ppc), FP32 cell+offset form, CIC, Esirkepov, supercell 4^3")
+    return (f"Weibel {e}^3 cells, electrons and ions (m_i = 100 m_e), beams +-0.3c along z, 32 ppc per "
+            "species per beam, FP32 cell+offset form, TSC, Esirkepov, supercell 4^3")
+
+
+def bench_config(desc, npart, ncells, world):
+    """The `config` object of a bench line (the same for both arms)."""
+    return {"workload": f"{desc} ({npart} particles per GPU)", "particles_per_gpu": npart, "cells": ncells,
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (particle state %.1f GB)" % (npart * 32 / 1e9)}
+
+
 def named_workload(name, edge=None):
     """The two-stream (256x256x128, CIC) and Weibel (256^3, TSC, two species) plasmas;
     `edge` scales the grid (a smaller case of the same plasma for profiling)."""
@@ -280,83 +291,143 @@ def named_workload(name, edge=None):
     e = edge or 256
     if name == "two_stream":
         wl = workloads.two_stream(n=(e, e, e // 2))
-        desc = (f"two-stream {e}x{e}x{e // 2} cells, two electron beams +-0.2c along x, density "
-                "1 + 0.9 cos(2 pi x / Lx) (10-190 ppc), FP32 cell+offset form, CIC, Esirkepov, supercell 4^3")
     else:
         wl = workloads.weibel(n=(e, e, e))
-        desc = (f"Weibel {e}^3 cells, electrons and ions (m_i = 100 m_e), beams +-0.3c along z, 32 ppc per "
-                "species per beam, FP32 cell+offset form, TSC, Esirkepov, supercell 4^3")
-    return wl, desc
+    return wl, workload_description(name, edge)
 
 
-def cpu_sample(args, steps=None, seconds=None, pica_path=False, workload="thermal", warmup=1):
-    """Oracle restatement of the workload's step on a small block of it (32^3 cells; the
-    two-stream plasma 32x32x16; same ppc, species, supercell, form factor and
-    deposition), all host cores.  With `pica_path`, the same block through pica's own
-    arithmetic instead: FP64 positions, CIC, Boris, direct deposition (the oracle form
-    equal bit for bit to a harness over pica's headers).  `warmup` untimed steps, then
-    `steps` timed ones (or as many as fill `seconds`).  Returns (value, cores, sample,
-    seconds)."""
-    import pica_gb300 as pg
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle only; nothing here loads the pica_gb300 library)
+# ---------------------------------------------------------------------------
+# pica's CGS constants (math/Constants.h:10-14) and the workloads' physical set-up,
+# equal to pica_gb300.workloads (tests/test_bench_cpu.py checks that they agree):
+# n0 = 1e18 cm^-3, h = 0.05 c / omega_p, dt = 0.5 h / (c sqrt 3), weight n0 h^3 / ppc.
+_PI, _C, _QE, _ME, _N0 = 3.14159265358, 29979245800.0, -4.80320427e-10, 9.10938215e-28, 1e18
+_SEED = 20261203
+
+
+def _cell_size():
+    return 0.05 * _C / math.sqrt(4.0 * _PI * _N0 * _QE ** 2 / _ME)
+
+
+def oracle_workload(name, edge=None, resort_every=None):
+    """The oracle's description of workload `name` ("thermal", "two_stream", "weibel";
+    `edge` scales the grid): Oracle keyword arguments, the oracle generator's
+    populations, the resort cadence and a short description.  FP32 cell form."""
     from oracle import pic_oracle as po
 
-    edge = 32
-    if workload == "thermal":
-        wl = make_workload(edge, pg.FORM_FP32_CELL)
-        what = f"{edge}^3 cells x 100 ppc"
+    h = _cell_size()
+    hh = (h, h, h)
+    dt = 0.5 * h / (_C * math.sqrt(3.0))
+    beta_u = lambda b: b / math.sqrt(1.0 - b * b)   # noqa: E731
+    if name == "thermal":
+        e = edge or 128
+        n = (e, e, e)
+        specs = [po.plasma(n, hh, 100, 0.05, _N0 * h ** 3 / 100, _SEED)]
+        species, shape, resort = ((_ME, _QE),), po.SHAPE_TSC, 2
+        what = f"thermal {e}^3 cells x 100 ppc"
+    elif name == "two_stream":
+        e = edge or 256
+        n = (e, e, e // 2)
+        specs = [po.plasma(n, hh, 100, 0.01, _N0 * h ** 3 / 100, _SEED, density_mod=0.9, nbeams=2,
+                           drift_u=beta_u(0.2), drift_axis=0)]
+        species, shape, resort = ((_ME, _QE),), po.SHAPE_CIC, 4
+        what = f"two-stream {e}x{e}x{e // 2} cells"
     else:
-        wl, what = named_workload(workload, edge)
-        what = what.split(",")[0]
-    sim = wl["sim"]
-    parts = [pg.generate_plasma(spec) for spec in wl["specs"]]
-    p = {k: np.concatenate([q[k] for q in parts]) for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species")}
-    cores = os.cpu_count() or 1
+        e = edge or 256
+        n = (e, e, e)
+        w = _N0 * h ** 3 / 64
+        u = beta_u(0.3)
+        specs = [po.plasma(n, hh, 64, 0.01, w, _SEED, species=0, nbeams=2, drift_u=u, drift_axis=2),
+                 po.plasma(n, hh, 64, 0.01 / math.sqrt(100.0), w, _SEED + 1, species=1, nbeams=2, drift_u=u,
+                           drift_axis=2)]
+        species, shape, resort = ((_ME, _QE), (_ME * 100.0, -_QE)), po.SHAPE_TSC, 1
+        what = f"Weibel {e}^3 cells, electrons and ions"
+    if resort_every is not None:
+        resort = resort_every
+    kw = dict(n=n, sc=(4, 4, 4), h=hh, dt=dt, form=po.FORM_FP32_CELL, shape=shape, deposit=po.DEPOSIT_ESIRKEPOV,
+              species=species, resort_every=resort)
+    return kw, specs, what
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_sample(workload="thermal", edge=None, steps=2, warmup=1, pica_path=False, resort_every=None):
+    """The CPU step of a workload in the oracle, all host cores: the restatement of its
+    own step (FP32 cell form, its form factor, Esirkepov), or with `pica_path` pica's own
+    arithmetic on the same plasma (FP64 positions, CIC, Boris, direct deposition: the
+    oracle form equal bit for bit to a harness over pica's headers).  The plasma is
+    drawn by the oracle's generator.  `warmup` untimed steps, then `steps` timed ones.
+    Returns (particle-steps/s, cores, sample description, timed seconds)."""
+    from oracle import pic_oracle as po
+
+    kw, specs, what = oracle_workload(workload, edge, resort_every)
+    cores = host_cores()
+    p = po.generate(specs, threads=cores)
     if pica_path:
-        kw = dict(form=po.FORM_FP64_PLAIN, shape=po.SHAPE_CIC, deposit=po.DEPOSIT_DIRECT)
-    else:
-        kw = dict(form=po.FORM_FP32_CELL, shape=sim["shape"], deposit=sim["deposit"])
-    species = sim.get("species", ((pg.ELECTRON_MASS, pg.ELECTRON_CHARGE),))
-    o = po.Oracle(sim["n"], sim["supercell"], sim["h"], sim["dt"], threads=cores, species=species, **kw)
-    o.load(p["x"], p["y"], p["z"], p["ux"], p["uy"], p["uz"], p["w"], p["species"])
-    o.set_fields([np.zeros(sim["n"])] * 9)
+        kw = dict(kw, form=po.FORM_FP64_PLAIN, shape=po.SHAPE_CIC, deposit=po.DEPOSIT_DIRECT)
+    n, sc, h, dt = kw.pop("n"), kw.pop("sc"), kw.pop("h"), kw.pop("dt")
+    o = po.Oracle(n, sc, h, dt, threads=cores, **kw)
+    o.load(*[p[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species")])
     npart = len(p["x"])
+    del p
+    o.set_fields([np.zeros(n)] * 9)
+    if warmup > 0:
+        o.step(int(warmup))
     t = time.perf_counter()
-    o.step(max(1, int(warmup)))
-    t1 = (time.perf_counter() - t) / max(1, int(warmup))
-    if steps is None:
-        steps = int(max(1, min(50, math.ceil((seconds or 12.0) / max(t1, 1e-3)))))
-    t = time.perf_counter()
-    o.step(steps)
+    o.step(int(steps))
     el = time.perf_counter() - t
-    shape = "TSC" if sim["shape"] == pg.SHAPE_TSC else "CIC"
+    del o
     if pica_path:
         sample = (f"{what} ({npart} particles), pica's path: FP64 positions, CIC, Boris, direct deposition, "
-                  f"supercell 4^3, {steps} steps, oracle form equal bit for bit to pica's headers, OpenMP {cores} threads")
+                  f"supercell 4^3, {steps} steps after {warmup} warm-up, oracle form equal bit for bit to pica's "
+                  f"headers, OpenMP {cores} threads")
     else:
-        sample = (f"{what} ({npart} particles), {shape}, Esirkepov, supercell 4^3, FP32 cell form, {steps} steps, "
-                  f"oracle restatement (pica has no Esirkepov{'' if shape == 'CIC' else ' or TSC'}), "
-                  f"OpenMP {cores} threads")
+        shape = "TSC" if kw["shape"] == po.SHAPE_TSC else "CIC"
+        sample = (f"{what} ({npart} particles), {shape}, Esirkepov, supercell 4^3, FP32 cell form, {steps} steps "
+                  f"after {warmup} warm-up, oracle restatement (pica has no Esirkepov"
+                  f"{'' if shape == 'CIC' else ' or TSC'}), OpenMP {cores} threads")
     return npart * steps / el, cores, sample, el
 
 
 def run_reference(args):
+    """The CPU implementation of the path on this machine's host cores: the thermal
+    headline workload at its full size (128^3 x 100 ppc unless --edge), K timed steps
+    after W warm-up steps of the oracle restatement of its own step (FP32, TSC,
+    Esirkepov; pica has neither), plus pica's own FP64 CIC/direct arithmetic on the
+    same plasma (a few steps).  The two-stream and Weibel plasmas (8.4e8 and 2.1e9
+    particles) do not fit a CPU run of minutes: for them, a block of the plasma."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    # W untimed warm-up steps, then exactly K timed steps of the CPU step on the bounded sample
-    import pica_gb300 as pg  # noqa: F401  (host-side plasma generator only)
-    value, cores, sample, el = cpu_sample(args, steps=args.steps, warmup=args.warmup, workload=args.workload)
     if args.workload == "thermal":
-        what = (f"thermal electron plasma {args.edge or 128}^3 x 100 ppc, TSC, Esirkepov, supercell 4^3 "
-                f"(CPU step on a 32^3 block of it)")
+        edge = args.edge or 128
     else:
-        what = named_workload(args.workload, args.edge)[1] + " (CPU step on a small block of it)"
+        edge = 32
+    resort = args.resort_every
+    value, cores, sample, el = cpu_sample(args.workload, edge, steps=args.steps, warmup=args.warmup,
+                                          resort_every=resort)
+    pk = max(1, min(args.steps, 3))
+    pv, _, psample, _ = cpu_sample(args.workload, edge, steps=pk, warmup=min(1, args.warmup), pica_path=True,
+                                   resort_every=resort)
+    if args.workload == "thermal":
+        ncells = edge ** 3
+        config = bench_config(workload_description("thermal", edge), 100 * ncells, ncells, 1)
+    else:
+        config = {"workload": workload_description(args.workload, args.edge) + " (CPU step on a block of it: "
+                  + sample.split(" (")[0] + ")", "parallelism": "OpenMP over supercells"}
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / max(1, args.steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": what, "parallelism": "OpenMP over supercells"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "config": config,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                         "pica_path": {"value": pv, "unit": UNIT, "cores": cores, "sample": psample}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -393,8 +464,7 @@ def main():
     if headline:
         args.edge = args.edge or 128
         wl = make_workload(args.edge, pg.FORM_FP32_CELL)
-        desc = (f"thermal electron plasma {args.edge}^3 cells x 100 ppc, FP32 cell+offset form, TSC, Esirkepov, "
-                "supercell 4^3, Boris, periodic")
+        desc = workload_description("thermal", args.edge)
         resort = 2 if args.resort_every is None else args.resort_every
     else:
         wl, desc = named_workload(args.workload, args.edge)
@@ -456,11 +526,10 @@ def main():
     peak, peak_kind = measured_hbm_peak()
     alg_bytes = BYTES_PER_PARTICLE_FP32 * npart + PUSH_GRID_BYTES_PER_CELL_FP32 * ncells
     achieved = alg_bytes / push_avg / 1e9
-    tpp = profiled_traffic_per_particle() if headline else None
     kname = "CIC" if wl["sim"]["shape"] == pg.SHAPE_CIC else "TSC"
     roofline = {"bound": "hbm", "kernel": f"k_push_cell_esirkepov<{kname}>", "achieved": achieved, "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None if tpp is None else tpp * npart,
+                "traffic": None,   # DRAM bytes come from ncu only, never from a run that is timed
                 "algorithmic_bytes_per_launch": alg_bytes, "push_ms": 1e3 * push_avg,
                 "step_fraction_in_push": push_avg * K / elapsed}
     step_alg = BYTES_PER_PARTICLE_FP32 * npart + 120 * ncells
@@ -607,17 +676,21 @@ def main():
         return
     cpu = None
     if not args.no_cpu_baseline:
-        v, cores, sample, _ = cpu_sample(args, seconds=args.cpu_seconds, workload=args.workload)
+        # A bounded sample: the headline plasma at its full size for 2 steps (the
+        # two-stream and Weibel plasmas on a 32-cell-edge block for 3).
+        parts = None
+        edge = args.edge if headline else 32
+        k = 2 if headline else 3
+        v, cores, sample, _ = cpu_sample(args.workload, edge, steps=k, warmup=1, resort_every=resort)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
-        v, cores, sample, _ = cpu_sample(args, seconds=0.5 * args.cpu_seconds, pica_path=True, workload=args.workload)
+        v, cores, sample, _ = cpu_sample(args.workload, edge, steps=k - 1, warmup=1, pica_path=True,
+                                         resort_every=resort)
         cpu["pica_path"] = {"value": v, "unit": UNIT, "cores": cores, "sample": sample}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": 1e3 * elapsed / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": f"{desc} ({npart} particles per GPU)",
-                   "particles_per_gpu": npart, "cells": ncells, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (particle state %.1f GB)" % (npart * 32 / 1e9)},
+        "config": bench_config(desc, npart, ncells, world),
         "roofline": roofline,
         "step_hbm_frac": step_alg / (elapsed / K) / 1e9 / peak,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,

@@ -7,8 +7,8 @@
  * the supercell ensemble.  Per-particle calls cannot be fast on a GPU, so this
  * ABI exposes the same operators at ensemble granularity: one call advances
  * every particle of every supercell.  A host loop that used the reference
- * classes calls these entry points once per step instead (see INTEGRATION.md
- * for the header-level C++ mirror and the ctypes binding).
+ * classes calls these entry points once per step instead; pica_gb300.hpp is
+ * the header-level C++ mirror of pica's class names over them.
  *
  * Conventions
  *  - Every function returns a status (PICA_OK = 0, negative = error); no C++
@@ -131,6 +131,23 @@ int     pica_download_particles(pica_ctx* ctx, double* x, double* y, double* z, 
                                 double* uz, double* w, int32_t* species, int32_t* supercell);
 /* Per-supercell particle counts, counts[species * nsupercells + s]. */
 int     pica_get_counts(pica_ctx* ctx, int32_t* counts);
+
+/* Migration lists.  pica routes a particle by floor((x - min) / supercellSize)
+ * (particles/EnsembleSupercells.h:54-57) and has no step that moves particles
+ * between supercells; a host loop over it pops a particle whose route changed and
+ * adds it to its new supercell.  With recording on (enable = 1; off by default),
+ * every pica_migrate keeps the list of its moves: one entry per particle that
+ * changed supercell, (species, source supercell, slot in the source supercell
+ * before the move, destination supercell), ordered by species, then source
+ * supercell, then slot.  pica_num_migrations gives the length of the last step's
+ * list (0 before the first recorded step, -1 for a NULL context) and
+ * pica_get_migrations copies it out (each pointer may be NULL).  Recording reads
+ * the leaver lists back to the host once per step, so it is for checks and
+ * debugging, not for timed runs.  Steps of a batch (pica_batch_step) are not
+ * recorded. */
+int     pica_record_migrations(pica_ctx* ctx, int32_t enable);
+int64_t pica_num_migrations(pica_ctx* ctx);
+int     pica_get_migrations(pica_ctx* ctx, int32_t* species, int32_t* src, int32_t* slot, int32_t* dst);
 
 /* Fields: f9 = {ex, ey, ez, bx, by, bz, jx, jy, jz}, each N^3 doubles.
  * Replaces element access YeeGrid::ex(i,j,k) ... (grid/YeeGrid.h:293-333). */

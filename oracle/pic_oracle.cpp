@@ -356,52 +356,101 @@ void Sim<R, Store>::resort() {
     }
 }
 
-// ---- plain FP64 form helpers ------------------------------------------------
-template <>
-int Sim<double, PlainStore>::load(int64_t n, const double* x, const double* y, const double* z,
-                                  const double* ux, const double* uy, const double* uz,
-                                  const double* w, const int32_t* sp) {
-    for (auto& v : parts) for (auto& s : v) s.clear();
-    for (int64_t i = 0; i < n; i++) {
-        int q = sp ? sp[i] : 0;
-        if (q < 0 || q >= cfg.nspecies) return -2;
-        double p[3] = {x[i], y[i], z[i]};
-        int c[3];
-        for (int d = 0; d < 3; d++) {
-            c[d] = (int)std::floor((p[d] - 0.0) * scInv[d]);  // EnsembleSupercells.h:56
-            c[d] = std::min(std::max(c[d], 0), nsc[d] - 1);
-        }
-        PlainStore& st = parts[q][scLinear(c[0], c[1], c[2])];
-        st.x.push_back(x[i]); st.y.push_back(y[i]); st.z.push_back(z[i]);
-        st.ux.push_back(ux[i]); st.uy.push_back(uy[i]); st.uz.push_back(uz[i]); st.w.push_back(w[i]);
+// ---- loading ---------------------------------------------------------------
+// Routing of one input particle (EnsembleSupercells.h:56 for the supercell).
+inline int routePlain(const SimBase& S, double x, double y, double z) {
+    const double p[3] = {x, y, z};
+    int c[3];
+    for (int d = 0; d < 3; d++) {
+        c[d] = (int)std::floor((p[d] - 0.0) * S.scInv[d]);  // EnsembleSupercells.h:56
+        c[d] = std::min(std::max(c[d], 0), S.nsc[d] - 1);
     }
-    resort();
-    return 0;
+    return S.scLinear(c[0], c[1], c[2]);
+}
+// FP32 form: integer cell and FP32 offset of a position (FP64 arithmetic).
+inline void toCell(const SimBase& S, double x, double y, double z, int* c, float* o) {
+    const double p[3] = {x, y, z};
+    for (int d = 0; d < 3; d++) {
+        double xi = p[d] * S.invh[d];
+        double fl = std::floor(xi);
+        c[d] = (int)fl;
+        o[d] = (float)(xi - fl);
+        if (o[d] >= 1.0f) { o[d] = 0.0f; c[d] += 1; }
+        c[d] = wrapi(c[d], S.cfg.n[d]);
+    }
+}
+inline int routeCell(const SimBase& S, double x, double y, double z) {
+    int c[3]; float o[3];
+    toCell(S, x, y, z, c, o);
+    return S.scLinear(c[0] / S.cfg.sc[0], c[1] / S.cfg.sc[1], c[2] / S.cfg.sc[2]);
+}
+inline int routeOf(const SimBase& S, const PlainStore*, double x, double y, double z) { return routePlain(S, x, y, z); }
+inline int routeOf(const SimBase& S, const CellStore*, double x, double y, double z) { return routeCell(S, x, y, z); }
+inline void putParticle(const SimBase&, PlainStore& st, size_t k, double x, double y, double z, double ux, double uy,
+                        double uz, double w) {
+    st.x[k] = x; st.y[k] = y; st.z[k] = z; st.ux[k] = ux; st.uy[k] = uy; st.uz[k] = uz; st.w[k] = w;
+}
+inline void putParticle(const SimBase& S, CellStore& st, size_t k, double x, double y, double z, double ux, double uy,
+                        double uz, double w) {
+    int c[3]; float o[3];
+    toCell(S, x, y, z, c, o);
+    st.cx[k] = c[0]; st.cy[k] = c[1]; st.cz[k] = c[2];
+    st.ox[k] = o[0]; st.oy[k] = o[1]; st.oz[k] = o[2];
+    st.ux[k] = (float)ux; st.uy[k] = (float)uy; st.uz[k] = (float)uz; st.w[k] = (float)w;
+}
+inline void resizeStore(PlainStore& st, size_t n) {
+    st.x.resize(n); st.y.resize(n); st.z.resize(n); st.ux.resize(n); st.uy.resize(n); st.uz.resize(n); st.w.resize(n);
+}
+inline void resizeStore(CellStore& st, size_t n) {
+    st.cx.resize(n); st.cy.resize(n); st.cz.resize(n); st.ox.resize(n); st.oy.resize(n); st.oz.resize(n);
+    st.ux.resize(n); st.uy.resize(n); st.uz.resize(n); st.w.resize(n);
 }
 
-template <>
-int Sim<float, CellStore>::load(int64_t n, const double* x, const double* y, const double* z,
-                                const double* ux, const double* uy, const double* uz,
-                                const double* w, const int32_t* sp) {
-    for (auto& v : parts) for (auto& s : v) s.clear();
-    for (int64_t i = 0; i < n; i++) {
-        int q = sp ? sp[i] : 0;
-        if (q < 0 || q >= cfg.nspecies) return -2;
-        double p[3] = {x[i], y[i], z[i]};
-        int c[3]; float o[3];
-        for (int d = 0; d < 3; d++) {
-            double xi = p[d] * invh[d];
-            double fl = std::floor(xi);
-            c[d] = (int)fl;
-            o[d] = (float)(xi - fl);
-            if (o[d] >= 1.0f) { o[d] = 0.0f; c[d] += 1; }
-            c[d] = wrapi(c[d], cfg.n[d]);
+// Every particle goes to the supercell its position routes to, in input order
+// (a stable counting sort over contiguous chunks of the input, one per thread),
+// then each supercell is sorted by cell, stably (resort).
+template <typename R, typename Store>
+int Sim<R, Store>::load(int64_t n, const double* x, const double* y, const double* z, const double* ux,
+                        const double* uy, const double* uz, const double* w, const int32_t* sp) {
+    for (int64_t i = 0; i < n; i++)
+        if (sp && (sp[i] < 0 || sp[i] >= cfg.nspecies)) return -2;
+    const int ns = cfg.nspecies;
+    const size_t bins = (size_t)ns * nscTot;
+    std::vector<int32_t> route(n);
+    int nt = 1;
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    std::vector<std::vector<int64_t>> hist(nt, std::vector<int64_t>(bins, 0));
+    auto chunkOf = [&](int t, int64_t& a, int64_t& b) { a = n * t / nt; b = n * (t + 1) / nt; };
+    const Store* tag = nullptr;   // selects the form's routing
+#pragma omp parallel for schedule(static, 1) num_threads(nt)
+    for (int t = 0; t < nt; t++) {
+        int64_t a, b;
+        chunkOf(t, a, b);
+        for (int64_t i = a; i < b; i++) {
+            const int q = sp ? sp[i] : 0;
+            route[i] = routeOf(*this, tag, x[i], y[i], z[i]);
+            hist[t][(size_t)q * nscTot + route[i]]++;
         }
-        CellStore& st = parts[q][scLinear(c[0] / cfg.sc[0], c[1] / cfg.sc[1], c[2] / cfg.sc[2])];
-        st.cx.push_back(c[0]); st.cy.push_back(c[1]); st.cz.push_back(c[2]);
-        st.ox.push_back(o[0]); st.oy.push_back(o[1]); st.oz.push_back(o[2]);
-        st.ux.push_back((float)ux[i]); st.uy.push_back((float)uy[i]); st.uz.push_back((float)uz[i]);
-        st.w.push_back((float)w[i]);
+    }
+    // Thread t writes bin k from offset sum over t' < t of hist[t'][k].
+    for (size_t k = 0; k < bins; k++) {
+        int64_t tot = 0;
+        for (int t = 0; t < nt; t++) { const int64_t c = hist[t][k]; hist[t][k] = tot; tot += c; }
+        Store& st = parts[k / nscTot][k % nscTot];
+        st.clear();
+        resizeStore(st, (size_t)tot);
+    }
+#pragma omp parallel for schedule(static, 1) num_threads(nt)
+    for (int t = 0; t < nt; t++) {
+        int64_t a, b;
+        chunkOf(t, a, b);
+        for (int64_t i = a; i < b; i++) {
+            const int q = sp ? sp[i] : 0;
+            const size_t k = (size_t)q * nscTot + route[i];
+            putParticle(*this, parts[q][route[i]], (size_t)hist[t][k]++, x[i], y[i], z[i], ux[i], uy[i], uz[i], w[i]);
+        }
     }
     resort();
     return 0;
@@ -988,6 +1037,33 @@ double gaussResidual(S* s, const std::vector<double>& rho, double bg, double* rh
     return gmax;
 }
 
+// ----------------------------------------------------------------------------
+// Synthetic plasma (the draws of the product's host generator, restated so that
+// the CPU baseline needs nothing but this file).  Draw d of particle p of cell c
+// is the SplitMix64 output function (S. Vigna, "Further scramblings of
+// Marsaglia's xorshift generators", 2014) applied to the mixed seed xor a key of
+// (c, p, d); normals by Box-Muller (1958) from draws d and d + 1.
+// ----------------------------------------------------------------------------
+inline uint64_t splitmixOut(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+inline double uniformDraw(uint64_t seed, int64_t cell, int64_t p, int d) {
+    const uint64_t key = ((uint64_t)cell << 24) ^ ((uint64_t)p << 4) ^ (uint64_t)d;
+    return (double)(splitmixOut(splitmixOut(seed) ^ key) >> 11) * 0x1.0p-53;   // 53 bits in [0, 1)
+}
+inline double gaussianDraw(uint64_t seed, int64_t cell, int64_t p, int d) {
+    const double u1 = 1.0 - uniformDraw(seed, cell, p, d), u2 = uniformDraw(seed, cell, p, d + 1);
+    return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2);
+}
+// Particles per cell of x-plane i: round(ppc (1 + a cos(2 pi (i + 1/2) / nx))).
+inline int planeCount(const orc_plasma* s, int i) {
+    const double f = 1.0 + s->density_mod * std::cos(2.0 * 3.14159265358979323846 * (i + 0.5) / s->n[0]);
+    return (int)std::lround(s->ppc * f);
+}
+
 }  // namespace
 
 // ============================================================================
@@ -1168,6 +1244,54 @@ int orc_diagnostics(void* sim, double bg, orc_diag* out) {
         for (int sp = 0; sp < c.nspecies; sp++) for (auto& st : s->parts[sp]) for (size_t p = 0; p < st.size(); p++) if (st.alive(p)) out->total_charge += c.charge[sp] * (double)st.w[p];
     }
     out->field_energy = fe * vol / (8.0 * kPi);
+    return 0;
+}
+
+
+int64_t orc_plasma_count(const orc_plasma* s) {
+    if (!s || s->n[0] <= 0 || s->n[1] <= 0 || s->n[2] <= 0 || !(s->ppc >= 0)) return -1;
+    int64_t tot = 0;
+    for (int i = 0; i < s->n[0]; i++) {
+        const int c = planeCount(s, i);
+        if (c < 0) return -1;
+        tot += (int64_t)c * s->n[1] * s->n[2];
+    }
+    return tot;
+}
+
+int orc_plasma_generate(const orc_plasma* s, int32_t threads, double* x, double* y, double* z, double* ux,
+                        double* uy, double* uz, double* w, int32_t* species) {
+    if (orc_plasma_count(s) < 0 || !x || !y || !z || !ux || !uy || !uz || !w) return -1;
+    const int nx = s->n[0], ny = s->n[1], nz = s->n[2];
+    std::vector<int64_t> first(nx + 1, 0);
+    for (int i = 0; i < nx; i++) first[i + 1] = first[i] + (int64_t)planeCount(s, i) * ny * nz;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+    // Order: x-plane, then y, z, then particle index within the cell.
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < nx; i++) {
+        const int per = planeCount(s, i);
+        int64_t o = first[i];
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                const int64_t cell = ((int64_t)i * ny + j) * nz + k;
+                for (int p = 0; p < per; p++, o++) {
+                    x[o] = ((double)i + uniformDraw(s->seed, cell, p, 0)) * s->h[0];
+                    y[o] = ((double)j + uniformDraw(s->seed, cell, p, 1)) * s->h[1];
+                    z[o] = ((double)k + uniformDraw(s->seed, cell, p, 2)) * s->h[2];
+                    double u[3] = {s->sigma_u * gaussianDraw(s->seed, cell, p, 3),
+                                   s->sigma_u * gaussianDraw(s->seed, cell, p, 5),
+                                   s->sigma_u * gaussianDraw(s->seed, cell, p, 7)};
+                    // two beams: even particles drift at +drift_u, odd ones at -drift_u
+                    const double drift = s->nbeams == 2 ? (p % 2 == 0 ? s->drift_u : -s->drift_u) : s->drift_u;
+                    u[s->drift_axis] = u[s->drift_axis] + drift;
+                    ux[o] = u[0]; uy[o] = u[1]; uz[o] = u[2];
+                    w[o] = s->weight;
+                    if (species) species[o] = s->species;
+                }
+            }
+    }
     return 0;
 }
 

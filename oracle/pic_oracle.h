@@ -89,6 +89,27 @@ int     orc_charge_density(void* sim, double* rho);
 /* bg_density: neutralising background charge density (statC/cm^3) added to rho. */
 int     orc_diagnostics(void* sim, double bg_density, orc_diag* out);
 
+/* Synthetic plasma: the particles the product's host generator draws for the
+ * same description (same counter-based draws, same order), so that the timed
+ * CPU baseline needs no product code.  Layout equal to pica_plasma_spec. */
+typedef struct orc_plasma {
+    int32_t n[3];          /* cells                                              */
+    int32_t species;       /* species index written for every particle           */
+    double h[3];           /* cell size, cm                                      */
+    double ppc;            /* mean particles per cell                            */
+    double density_mod;    /* per-cell count round(ppc (1 + a cos(2 pi (i+1/2)/nx)))  */
+    double drift_u;        /* beam drift u along drift_axis                      */
+    double sigma_u;        /* Maxwellian spread of each u component              */
+    double weight;         /* macro-particle factor                              */
+    uint64_t seed;
+    int32_t nbeams;        /* 1 or 2 (beams at +drift_u and -drift_u)            */
+    int32_t drift_axis;    /* 0, 1, 2                                            */
+} orc_plasma;
+int64_t orc_plasma_count(const orc_plasma* spec);
+/* Order: x-plane, y, z, then particle in the cell.  threads 0 = OpenMP default. */
+int     orc_plasma_generate(const orc_plasma* spec, int32_t threads, double* x, double* y, double* z,
+                            double* ux, double* uy, double* uz, double* w, int32_t* species);
+
 /* The same API over pica's own headers (oracle/ref_harness.cpp). */
 void*   ref_create(const orc_config* cfg);
 void    ref_destroy(void* sim);

@@ -34,6 +34,57 @@ class OrcDiag(C.Structure):
                 ("gauss_max", C.c_double), ("rho_max", C.c_double), ("pad_", C.c_double * 3)]
 
 
+class OrcPlasma(C.Structure):
+    """orc_plasma (oracle/pic_oracle.h): one synthetic population."""
+    _fields_ = [
+        ("n", C.c_int32 * 3), ("species", C.c_int32), ("h", C.c_double * 3), ("ppc", C.c_double),
+        ("density_mod", C.c_double), ("drift_u", C.c_double), ("sigma_u", C.c_double), ("weight", C.c_double),
+        ("seed", C.c_uint64), ("nbeams", C.c_int32), ("drift_axis", C.c_int32),
+    ]
+
+
+def plasma(n, h, ppc, sigma, weight, seed, species=0, density_mod=0.0, drift_u=0.0, drift_axis=0, nbeams=1):
+    s = OrcPlasma()
+    for d in range(3):
+        s.n[d], s.h[d] = int(n[d]), float(h[d])
+    s.species, s.ppc, s.density_mod, s.drift_u, s.sigma_u = int(species), float(ppc), float(density_mod), \
+        float(drift_u), float(sigma)
+    s.weight, s.seed, s.nbeams, s.drift_axis = float(weight), int(seed), int(nbeams), int(drift_axis)
+    return s
+
+
+def generate(specs, threads=0):
+    """The populations `specs` (OrcPlasma) drawn on the host by the oracle's generator,
+    concatenated in order: a dict of x y z ux uy uz w (FP64) and species (int32)."""
+    lib, _ = _lib("port")
+    counts = [int(lib.orc_plasma_count(C.byref(s))) for s in specs]
+    if min(counts, default=0) < 0:
+        raise ValueError("bad plasma description")
+    n = sum(counts)
+    out = {k: np.empty(n) for k in ("x", "y", "z", "ux", "uy", "uz", "w")}
+    out["species"] = np.empty(n, np.int32)
+    o = 0
+    for s, c in zip(specs, counts):
+        ptr = [out[k][o:].ctypes.data_as(C.POINTER(C.c_double)) for k in ("x", "y", "z", "ux", "uy", "uz", "w")]
+        if lib.orc_plasma_generate(C.byref(s), int(threads), *ptr, out["species"][o:].ctypes.data_as(C.POINTER(C.c_int32))):
+            raise RuntimeError("plasma generation failed")
+        o += c
+    return out
+
+
+def pica_include_dir():
+    """pica's include directory when the pica sources are mounted (the recipe in
+    oracle/Makefile knows where: PICA_REF), else None."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "include-dir"], capture_output=True, text=True)
+    d = r.stdout.strip()
+    return d if r.returncode == 0 and d and os.path.isdir(os.path.join(d, "pica")) else None
+
+
+def reference_available():
+    """True when the harness over pica's headers is built or can be built here."""
+    return os.path.exists(REF_SO) or pica_include_dir() is not None
+
+
 def build(reference=True):
     """Compile the restatement (and, where the pica sources exist, the harness)."""
     targets = ["oracle"] + (["ref"] if reference else [])
@@ -63,6 +114,8 @@ def _lib(kind):
         if kind == "port":
             fp = C.POINTER(C.c_float)
             sig.update({
+                "plasma_count": (i64, [C.POINTER(OrcPlasma)]),
+                "plasma_generate": (C.c_int, [C.POINTER(OrcPlasma), C.c_int32] + [dp] * 7 + [ip]),
                 "get_particles_cell": (C.c_int, [vp, ip] + [fp] * 7),
                 "charge_density": (C.c_int, [vp, dp]),
                 "diagnostics": (C.c_int, [vp, C.c_double, C.POINTER(OrcDiag)]),

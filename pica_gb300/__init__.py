@@ -150,6 +150,20 @@ class Simulation:
         self._check(self.lib.pica_get_counts(self.ctx, _ip(c)))
         return c.reshape(self.nspecies, -1)
 
+    def record_migrations(self, enable=True):
+        """Keep each step's migration list (pica_record_migrations)."""
+        self._check(self.lib.pica_record_migrations(self.ctx, int(bool(enable))))
+
+    def migrations(self):
+        """The last recorded step's moves as an (m, 4) int32 array of (species, source
+        supercell, source slot, destination supercell), ordered by species, source, slot."""
+        m = int(self.lib.pica_num_migrations(self.ctx))
+        if m < 0:
+            self._check(m)
+        cols = [np.empty(m, np.int32) for _ in range(4)]
+        self._check(self.lib.pica_get_migrations(self.ctx, *[_ip(c) for c in cols]))
+        return np.stack(cols, axis=1) if m else np.zeros((0, 4), np.int32)
+
     def upload_fields(self, f9):
         arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in f9]
         ptrs = (C.POINTER(C.c_double) * 9)(*[_dp(a) for a in arrs])

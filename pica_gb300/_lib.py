@@ -51,6 +51,9 @@ SIGNATURES = {
     "pica_num_particles": (_i64, [_vp]),
     "pica_download_particles": (C.c_int, [_vp] + [_dp] * 7 + [_ip, _ip]),
     "pica_get_counts": (C.c_int, [_vp, _ip]),
+    "pica_record_migrations": (C.c_int, [_vp, _i32]),
+    "pica_num_migrations": (_i64, [_vp]),
+    "pica_get_migrations": (C.c_int, [_vp, _ip, _ip, _ip, _ip]),
     "pica_upload_fields": (C.c_int, [_vp, C.POINTER(_dp)]),
     "pica_download_fields": (C.c_int, [_vp, C.POINTER(_dp)]),
     "pica_push_deposit": (C.c_int, [_vp]),

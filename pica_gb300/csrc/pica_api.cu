@@ -90,6 +90,8 @@ struct pica_ctx {
     int64_t epoch = 0;      // bumped by every step and every change of layout (packed-image validity)
     int threads = 1;
     cudaEvent_t copyOrder = nullptr;   // orders a host copy on a caller's copy stream against the context stream
+    bool recordMig = false;            // keep each step's migration list (pica_record_migrations)
+    std::vector<int32_t> mig;          // last step's list: (species, src, slot, dst) per entry
 };
 
 namespace {
@@ -1075,12 +1077,44 @@ static int resortNow(pica_ctx* ctx) {
     return resortFinish(ctx);
 }
 
+// The migration list of the step whose device part has just finished: the leaver
+// lists (slots sorted ascending by the leaver sort) and the direction code of each
+// leaver's slot, read back and expanded to (species, src, slot, dst).  Runs before
+// a rebuild or resort changes the layout the lists refer to.
+static int recordMigrations(pica_ctx* ctx) {
+    ctx->mig.clear();
+    const int n = ctx->nscTot;
+    for (int q = 0; q < ctx->cfg.nspecies; q++) {
+        SpeciesState& S = ctx->sp[q];
+        std::vector<int32_t> nl(n), ll(S.layoutSlots);
+        std::vector<uint32_t> dir(S.layoutSlots);
+        CK(cudaMemcpy(nl.data(), S.d_nleave, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(ll.data(), S.llist, (size_t)S.layoutSlots * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(dir.data(), S.dir, (size_t)S.layoutSlots * 4, cudaMemcpyDeviceToHost));
+        for (int s = 0; s < n; s++) {
+            const int sz = s % ctx->nsc[2], sy = (s / ctx->nsc[2]) % ctx->nsc[1], sx = s / (ctx->nsc[1] * ctx->nsc[2]);
+            const int64_t st = S.h_start[s];
+            for (int k = 0; k < nl[s]; k++) {
+                const int slot = ll[st + k];
+                const int code = (int)(dir[st + slot] & 31u);
+                if (code == 13) continue;
+                const int dx = code / 9 - 1, dy = (code / 3) % 3 - 1, dz = code % 3 - 1;
+                const int nx = (sx + dx + ctx->nsc[0]) % ctx->nsc[0], ny = (sy + dy + ctx->nsc[1]) % ctx->nsc[1],
+                          nz = (sz + dz + ctx->nsc[2]) % ctx->nsc[2];
+                ctx->mig.insert(ctx->mig.end(), {q, s, slot, scLinear(ctx, nx, ny, nz)});
+            }
+        }
+    }
+    return PICA_OK;
+}
+
 template <class P>
 static int migrateImpl(pica_ctx* ctx) {
     int rc = migrateDevice<P>(ctx);
     if (rc) return rc;
     CK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->recordMig && !ctx->h_flags[0] && (rc = recordMigrations(ctx))) return rc;
     if ((rc = migrateFinish<P>(ctx))) return rc;
     return resortDue(ctx) ? resortNow<P>(ctx) : PICA_OK;
 }
@@ -1092,6 +1126,25 @@ int pica_migrate(pica_ctx* ctx) {
     if (!ctx->pending) return fail(ctx, PICA_ERR_STATE, "migrate without push_deposit");
     ctx->pending = false;
     return ctx->fp64 ? migrateImpl<PlainPtrs>(ctx) : migrateImpl<CellPtrs>(ctx);
+}
+
+int pica_record_migrations(pica_ctx* ctx, int32_t enable) {
+    if (!ctx) return PICA_ERR_INVALID;
+    ctx->recordMig = enable != 0;
+    ctx->mig.clear();
+    return PICA_OK;
+}
+
+int64_t pica_num_migrations(pica_ctx* ctx) { return ctx ? (int64_t)(ctx->mig.size() / 4) : -1; }
+
+int pica_get_migrations(pica_ctx* ctx, int32_t* species, int32_t* src, int32_t* slot, int32_t* dst) {
+    if (!ctx) return PICA_ERR_INVALID;
+    int32_t* out[4] = {species, src, slot, dst};
+    const size_t m = ctx->mig.size() / 4;
+    for (int c = 0; c < 4; c++)
+        if (out[c])
+            for (size_t i = 0; i < m; i++) out[c][i] = ctx->mig[4 * i + c];
+    return PICA_OK;
 }
 
 int pica_reorder(pica_ctx* ctx) {

@@ -12,12 +12,29 @@ PI = 3.14159265358
 
 
 def rel_err(a, b):
-    """max |a - b| / max |b| (0 when both are zero)."""
+    """Norm-wise relative error max |a - b| / max |b| (the infinity-norm relative
+    error of the whole array; 0 when both are zero).  This is the metric of every
+    "relative" tolerance in these tests unless a test says otherwise: a field or
+    momentum component has values that cross zero, where an element-wise ratio
+    measures cancellation rather than the error of the step."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     den = np.max(np.abs(b)) if b.size else 0.0
     num = np.max(np.abs(a - b)) if b.size else 0.0
     return 0.0 if num == 0.0 else num / max(den, 1e-300)
+
+
+def elem_err(a, b, floor=1e-3):
+    """Element-wise relative error max |a - b| / max(|b|, floor max |b|): each
+    element against its own magnitude, with an absolute floor at `floor` of the
+    array's largest magnitude for elements near zero."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if not b.size:
+        return 0.0
+    den = np.maximum(np.abs(b), floor * np.max(np.abs(b)))
+    num = np.abs(a - b)
+    return float(np.max(np.where(num == 0.0, 0.0, num / np.maximum(den, 1e-300))))
 
 
 def periodic_err(a, b, L):

@@ -7,6 +7,7 @@ import re
 import numpy as np
 
 import pica_gb300
+from oracle import pic_oracle as po
 from pica_gb300 import _lib, workloads
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
@@ -117,7 +118,6 @@ def test_particle_and_constants_known_answers_of_the_cpp_mirror(tmp_path):
 
 
 CONSTANT_NAMES = ("pi", "c", "lightVelocity", "electronCharge", "electronMass", "protonMass", "planck", "eV", "meV")
-PICA_HEADERS = "/root/reference/include"   # pica's own headers, where this checkout has them
 
 
 def _print_constants(tmp_path, name, include, namespace):
@@ -126,7 +126,7 @@ def _print_constants(tmp_path, name, include, namespace):
     body = "".join(f'    std::printf("%.17g\\n", {namespace}::constants::{c});\n' for c in CONSTANT_NAMES)
     src.write_text(f'#include <cstdio>\n#include "{include}"\nint main() {{\n{body}    return 0;\n}}\n')
     exe = str(tmp_path / name)
-    inc = PICA_HEADERS if namespace == "pica" else os.path.join(ROOT, "include")
+    inc = po.pica_include_dir() if namespace == "pica" else os.path.join(ROOT, "include")
     subprocess.run(["g++", "-std=c++17", "-I", inc, str(src), "-o", exe], check=True)
     out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
     return [float(v) for v in out]
@@ -142,7 +142,7 @@ def test_constants_equal_picas(tmp_path):
               electronMass=pica_gb300.ELECTRON_MASS)
     for name, v in py.items():
         assert ours[CONSTANT_NAMES.index(name)] == v, name
-    if not os.path.isdir(os.path.join(PICA_HEADERS, "pica")):
+    if po.pica_include_dir() is None:
         pytest.skip("pica's headers are not in this checkout")
     theirs = _print_constants(tmp_path, "theirs", "pica/math/Constants.h", "pica")
     assert ours == theirs

@@ -11,7 +11,7 @@ import pytest
 
 import pica_gb300 as pg
 from oracle import pic_oracle as po
-from tests.helpers import load_golden, particle_args, periodic_err, rel_err, run_1d_golden, species_of, thermal_inputs
+from tests.helpers import elem_err, load_golden, particle_args, periodic_err, rel_err, run_1d_golden, species_of, thermal_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -61,10 +61,12 @@ def run_pair(n, sc, d, steps, form, shape, deposit, species=(pg.ELECTRON,), fiel
     f9 = fields if fields is not None else [np.zeros(n)] * 9
     s.upload_fields(f9)
     o.set_fields(f9)
-    for _ in range(steps):
+    s.record_migrations(True)
+    for st in range(steps):
         s.step(1)
         o.step(1)
-        assert np.array_equal(s.counts(), o.counts())
+        assert np.array_equal(s.counts(), o.counts()), st
+        assert np.array_equal(s.migrations(), o.migrations()), st
     return s, o
 
 
@@ -85,7 +87,9 @@ def test_fp64_forms_match_oracle(shape, deposit):
 
 
 def test_fp64_thermal_32cube_100_steps():
-    """The plain FP64 32^3 x 50 ppc electron plasma (CIC, Boris, direct, supercell 2^3) for 100 steps."""
+    """The plain FP64 32^3 x 50 ppc electron plasma (CIC, Boris, direct, supercell 2^3) for 100 steps:
+    per-supercell counts and the migration list (species, source supercell, source slot,
+    destination) exactly equal after every step; particles and fields within 1e-12."""
     from pica_gb300 import workloads
     wl = workloads.config1()
     p = pg.generate_plasma(wl["specs"][0])
@@ -98,12 +102,21 @@ def test_fp64_thermal_32cube_100_steps():
     zeros = [np.zeros(sim["n"])] * 9
     s.upload_fields(zeros)
     o.set_fields(zeros)
-    for chunk in range(10):
-        s.step(10)
-        o.step(10)
-        assert np.array_equal(s.counts(), o.counts()), chunk
+    s.record_migrations(True)
+    moved = 0
+    for st in range(100):
+        s.step(1)
+        o.step(1)
+        assert np.array_equal(s.counts(), o.counts()), st
+        m = s.migrations()
+        assert np.array_equal(m, o.migrations()), st
+        moved += len(m)
+    assert moved > 0
     L = [sim["n"][k] * sim["h"][k] for k in range(3)]
-    compare_particles(s.particles(), o.particles(), L, FP64_TOL, FP64_TOL)
+    ps, po_ = s.particles(), o.particles()
+    compare_particles(ps, po_, L, FP64_TOL, FP64_TOL)
+    for k in ("ux", "uy", "uz"):   # also element by element, floor 1e-3 of the largest |u|
+        assert elem_err(ps[k], po_[k]) < FP64_TOL, k
     fs, fo = s.fields(), o.get_fields()
     for c in range(9):
         assert rel_err(fs[c], fo[c]) < FP64_TOL, c

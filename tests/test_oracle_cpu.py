@@ -9,7 +9,7 @@ import pytest
 from oracle import pic_oracle as po
 from tests.helpers import C, E, ME, load_golden, rel_err, run_1d_golden, species_of, thermal_inputs
 
-REFERENCE_AVAILABLE = os.path.isdir("/root/reference/include/pica") or os.path.exists(po.REF_SO)
+REFERENCE_AVAILABLE = po.reference_available()
 
 
 def run_fixture(kind, g):
