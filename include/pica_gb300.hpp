@@ -5,30 +5,52 @@
 // ParticleArraySoA<Particle3d>, a BorisPusher, and per supercell a
 // FieldInterpolatorCICSupercell and a CurrentDepositorCICSupercell, then calls
 // get / push / deposit per particle and YeeSolver::updateB/updateE per step.
-// Here the same names stand for device-resident objects and each operator
-// acts on every particle at once:
+// This header keeps those type names, template parameters and constructors.
+// The grid and the ensemble are host containers that bind to one device
+// context the first time an operator acts on them; the per-particle inner loop
+// becomes one bulk call:
 //
-//   pica:                                            pica_gb300:
-//   YeeGrid<Three,double> grid(origin, step, size)   Simulation sim(config); auto& grid = sim.grid();
-//   grid.ex(i,j,k) = v                               grid.ex(i,j,k) = v; ...; grid.upload();
-//   EnsembleSupercells<PA> ens(min, max, N, S)        auto& ens = sim.ensemble();
-//   ens.add(particle)                                 ens.add(particle); ...; ens.upload();
-//   BorisPusher<Particle3d,double> pusher(dt)         (dt and ParticleTypes are in the config)
-//   for each supercell, particle: fi.get; pusher.push;  pushSupercells(sim);      // one call
-//     cd.deposit; ~cd                                 ens.migrate();
-//   YeeSolver().updateB(grid, dt)                      YeeSolver().updateB(grid, dt);
+//   pica:                                             pica_gb300 (this header):
+//   #include "pica/..."                               #include "pica_gb300.hpp"
+//   using namespace pica;                             using namespace pica_gb300;
+//   YeeGrid<Three, double> grid(origin, step, size);  (same)
+//   EnsembleSupercells<ParticleArraySoA<Particle3d>>  (same)
+//       ens(min, max, numCells, numCellsPerSupercell);
+//   ens.add(particle);                                (same)
+//   BorisPusher<Particle3d, double> pusher(dt);        (same)
+//   FieldInterpolatorCICSupercell<double> fi(grid, min, S);   (same)
+//   CurrentDepositorCICSupercell<double> cd(grid, min, S);    (same)
+//   for each supercell, particle:                     pushSupercells(ens, fi, pusher, cd);
+//       fi.get(...); pusher.push(...); cd.deposit(...);
+//   YeeSolver solver; solver.updateB(grid, dt / 2);   (same)
+//   grid.ex(i, j, k), ens.getParticles(idx)           (same: read back from the device on demand)
+//
+// Host and device copies are kept in step by the library: element writes and
+// added particles go to the device before the next operator; after an operator
+// the next host read fetches the device state (one copy of all arrays).  The
+// device grid is periodic over the ensemble's domain [min, max) with no guard
+// layers, so the grid's size must equal the ensemble's numCells; the supercell
+// migration that a pica host loop writes by hand happens inside the library
+// before the next push or read.  double operators run the FP64 plain form
+// (pica's own arithmetic), float operators the FP32 cell form.
+//
+// The explicit form of the same API (Simulation with a Config, explicit
+// upload / download / migrate) is below as well.
 //
 // Errors: every call that fails throws pica_gb300::Error (status + message);
-// the C ABI itself never throws.
+// the C ABI itself never throws.  There is no CPU implementation of any
+// operator: without a GPU, binding a context throws.
 #pragma once
 
 #include <algorithm>
 #include <array>
 #include <cmath>
-#include <functional>
 #include <cstdint>
+#include <functional>
+#include <memory>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -58,6 +80,9 @@ struct Int3 {
     Int3(int a, int b, int c) : x(a), y(b), z(c) {}
 };
 inline bool operator==(const Int3& a, const Int3& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+
+// pica's Dimension (math/Dimension.h): only Three has device operators here.
+enum Dimension { One = 1, Two = 2, Three = 3 };
 
 // Constants of pica math/Constants.h:9-18 (CGS, pi truncated as in pica), and the
 // Constants<Real> accessors of Constants.h:23-34: each the namespace value cast to Real.
@@ -91,9 +116,9 @@ struct ParticleType {
     double mass, charge;
 };
 
-// pica's global particle type table (particles/Particle.h:26-31).  Simulation fills
-// it from Config::types; a host loop may set it itself before creating particles,
-// as a pica host loop does.
+// pica's global particle type table (particles/Particle.h:26-31).  A host loop
+// fills it before creating particles, as a pica host loop does; Simulation fills
+// it from Config::types.  The device context takes its species from it.
 namespace ParticleTypes {
 inline std::vector<ParticleType> typesVector{{constants::electronMass, constants::electronCharge}};
 inline const ParticleType* types = nullptr;   // nullptr: typesVector
@@ -141,14 +166,22 @@ private:
     double invGamma() const { return 1.0 / std::sqrt(1.0 + p.norm2()); }
 };
 
-// pica's ParticleArraySoA<Particle3d> (particles/ParticleArray.h:46-203): a host
+template <class PA>
+class EnsembleSupercells;
+
+// pica's ParticleArraySoA<ParticleType> (particles/ParticleArray.h:46-203): a host
 // container of particles, one array per component (position, normalised momentum,
 // factor, 1/gamma, type), whose elements are reached through ConstParticleRef /
-// ParticleRef proxies with the accessors of Particle3d.  A host loop fills one and
-// hands its particles to EnsembleSupercells::add.
+// ParticleRef proxies with the accessors of Particle3d.  The device ensemble holds
+// 3D particles, so ParticleType is Particle3d.  An array that an ensemble hands
+// out (getParticles) reports writes through its references to that ensemble,
+// which sends them to the device before the next operator.
+template <class ParticleType>
 class ParticleArraySoA {
+    static_assert(std::is_same<ParticleType, Particle3d>::value, "the device ensemble holds Particle3d particles");
+
 public:
-    typedef Particle3d Particle;
+    typedef ParticleType Particle;
 
     class ConstParticleRef {
     public:
@@ -180,20 +213,33 @@ public:
     class ParticleRef : public ConstParticleRef {
     public:
         ParticleRef(ParticleArraySoA& a, int i) : ConstParticleRef(a, i), m_(&a), j_(i) {}
-        void setPosition(const FP3& r) { m_->x_[j_] = r.x; m_->y_[j_] = r.y; m_->z_[j_] = r.z; }
+        void setPosition(const FP3& r) { m_->x_[j_] = r.x; m_->y_[j_] = r.y; m_->z_[j_] = r.z; m_->touch(); }
         void setP(const FP3& p) {
             m_->px_[j_] = p.x; m_->py_[j_] = p.y; m_->pz_[j_] = p.z;
             m_->invGamma_[j_] = 1.0 / std::sqrt(1.0 + p.norm2());
+            m_->touch();
         }
         void setMomentum(const FP3& m) { setP(m / (Constants<double>::c() * this->getMass())); }
         void setVelocity(const FP3& v) { setP(v / std::sqrt(constants::c * constants::c - v.norm2())); }
-        void setFactor(double f) { m_->factor_[j_] = f; }
-        void setType(short t) { m_->type_[j_] = t; }
+        void setFactor(double f) { m_->factor_[j_] = f; m_->touch(); }
+        void setType(short t) { m_->type_[j_] = t; m_->touch(); }
 
     private:
         ParticleArraySoA* m_;
         int j_;
     };
+
+    ParticleArraySoA() = default;
+    // A copy is a plain host array: it reports to no ensemble.
+    ParticleArraySoA(const ParticleArraySoA& o)
+        : x_(o.x_), y_(o.y_), z_(o.z_), px_(o.px_), py_(o.py_), pz_(o.pz_), factor_(o.factor_),
+          invGamma_(o.invGamma_), type_(o.type_) {}
+    ParticleArraySoA& operator=(const ParticleArraySoA& o) {
+        x_ = o.x_; y_ = o.y_; z_ = o.z_; px_ = o.px_; py_ = o.py_; pz_ = o.pz_;
+        factor_ = o.factor_; invGamma_ = o.invGamma_; type_ = o.type_;
+        touch();
+        return *this;
+    }
 
     int size() const { return (int)type_.size(); }
     ParticleRef operator[](int i) { return ParticleRef(*this, i); }
@@ -206,16 +252,32 @@ public:
         factor_.push_back(q.factor);
         invGamma_.push_back(1.0 / std::sqrt(1.0 + q.p.norm2()));
         type_.push_back(q.typeIndex);
+        touch();
     }
     void pushBack(const ConstParticleRef& r) { pushBack(static_cast<Particle3d>(r)); }
     void popBack() {
         for (auto* v : {&x_, &y_, &z_, &px_, &py_, &pz_, &factor_, &invGamma_}) v->pop_back();
         type_.pop_back();
+        touch();
     }
 
 private:
+    template <class PA>
+    friend class EnsembleSupercells;
+    void touch() { if (owner_) *owner_ = true; }
+    bool* owner_ = nullptr;   // the "host copy changed" flag of the ensemble that handed this array out
     std::vector<double> x_, y_, z_, px_, py_, pz_, factor_, invGamma_;
     std::vector<short> type_;
+};
+
+// pica's ParticleArray<Particle, representation>::Type (particles/ParticleArray.h:217-231);
+// the device ensemble is structure-of-arrays only.
+enum ParticleRepresentation { ParticleRepresentation_AoS, ParticleRepresentation_SoA };
+template <class Particle, ParticleRepresentation storage>
+struct ParticleArray;
+template <class Particle>
+struct ParticleArray<Particle, ParticleRepresentation_SoA> {
+    typedef ParticleArraySoA<Particle> Type;
 };
 
 class Error : public std::runtime_error {
@@ -223,6 +285,10 @@ public:
     Error(int status, const std::string& msg) : std::runtime_error(msg), status(status) {}
     int status;
 };
+
+inline void check(pica_ctx* ctx, int rc) {
+    if (rc != PICA_OK) throw Error(rc, std::string(pica_status_string(rc)) + ": " + (ctx ? pica_last_error(ctx) : ""));
+}
 
 enum class Form { FP64Plain = PICA_FORM_FP64_PLAIN, FP32Cell = PICA_FORM_FP32_CELL };
 enum class Shape { CIC = PICA_SHAPE_CIC, TSC = PICA_SHAPE_TSC };
@@ -241,47 +307,93 @@ struct Config {
     int resortEvery = 0;
 };
 
-class Simulation;
-class YeeSolver;
-
-// pica's Array3d (utility/Array.h:119-167): a 3D array with z fastest, index
+// pica's Array3d<T> (utility/Array.h:119-167): a 3D array with z fastest, index
 // (i * ny + j) * nz + k, addressed by (i, j, k) or an Int3.
+template <typename T>
 class Array3d {
 public:
+    typedef T ValueType;
     Array3d() = default;
-    explicit Array3d(const Int3& size) : n_(size), v_((size_t)size.x * size.y * size.z, 0.0) {}
-    double& operator()(int i, int j, int k) { return v_[idx(i, j, k)]; }
-    double operator()(int i, int j, int k) const { return v_[idx(i, j, k)]; }
-    double& operator()(const Int3& n) { return v_[idx(n.x, n.y, n.z)]; }
-    double operator()(const Int3& n) const { return v_[idx(n.x, n.y, n.z)]; }
+    explicit Array3d(const Int3& size) : n_(size), v_((size_t)size.x * size.y * size.z, T(0)) {}
+    T& operator()(int i, int j, int k) { return v_[idx(i, j, k)]; }
+    T operator()(int i, int j, int k) const { return v_[idx(i, j, k)]; }
+    T& operator()(const Int3& n) { return v_[idx(n.x, n.y, n.z)]; }
+    T operator()(const Int3& n) const { return v_[idx(n.x, n.y, n.z)]; }
     Int3 getSize() const { return n_; }
     size_t size() const { return v_.size(); }
-    double* data() { return v_.data(); }
-    const double* data() const { return v_.data(); }
+    T* data() { return v_.data(); }
+    const T* data() const { return v_.data(); }
 
 private:
     size_t idx(int i, int j, int k) const { return ((size_t)i * n_.y + j) * n_.z + k; }
     Int3 n_;
-    std::vector<double> v_;
+    std::vector<T> v_;
 };
 
-// Host mirror of the device grid: pica's YeeGrid<Three> accessors (grid/YeeGrid.h:193-256,
-// grid/Grid.h:13-83) on host arrays, moved to / from the device with upload() / download().
-// The grid a Simulation owns is periodic with origin 0; a grid built with pica's
-// constructor is a host container only (upload / download throw).
-class YeeGrid {
-public:
-    YeeGrid() = default;
-    YeeGrid(const FP3& origin, const FP3& step, const Int3& size) : n_(size), h_(step), o_(origin) {
-        for (auto& a : f_) a = Array3d(size);
+namespace detail {
+// One device context shared by a grid and an ensemble, and what its host copies
+// know of it.
+struct Binding {
+    pica_ctx* ctx = nullptr;
+    pica_config cfg{};
+    bool fieldsStale = false;     // the device changed the fields since the grid's host copy was read
+    bool pending = false;         // a push awaits its migration
+    uint64_t particleEpoch = 1;   // bumped by every call that changes the device particles
+    Binding() = default;
+    Binding(const Binding&) = delete;
+    Binding& operator=(const Binding&) = delete;
+    ~Binding() { if (ctx) pica_ctx_destroy(ctx); }
+    // The migration of the last push, before anything reads or replaces the ensemble.
+    void settle() {
+        if (pending) {
+            pending = false;
+            check(ctx, pica_migrate(ctx));
+            particleEpoch++;
+        }
     }
-#define PICA_GB300_COMPONENT(name, c)                                              \
-    double& name(int i, int j, int k) { return f_[c](i, j, k); }                   \
-    double name(int i, int j, int k) const { return f_[c](i, j, k); }              \
-    double& name(const Int3& n) { return f_[c](n); }                               \
-    double name(const Int3& n) const { return f_[c](n); }                          \
-    Array3d& name() { return f_[c]; }                                              \
-    const Array3d& name() const { return f_[c]; }
+};
+inline bool sameConfig(const pica_config& a, const pica_config& b) {
+    for (int d = 0; d < 3; d++)
+        if (a.n[d] != b.n[d] || a.sc[d] != b.sc[d] || a.h[d] != b.h[d]) return false;
+    if (a.dt != b.dt || a.form != b.form || a.shape != b.shape || a.deposit != b.deposit || a.nspecies != b.nspecies ||
+        a.slack != b.slack || a.resort_every != b.resort_every || a.threads != b.threads)
+        return false;
+    for (int q = 0; q < a.nspecies; q++)
+        if (a.mass[q] != b.mass[q] || a.charge[q] != b.charge[q]) return false;
+    return true;
+}
+struct Access;
+}  // namespace detail
+
+// pica's YeeGrid<Dimension, Real> (grid/YeeGrid.h:193-256, grid/Grid.h:13-83).  The
+// device operators work on YeeGrid<Three, Real>.
+template <Dimension D, typename Real = double>
+class YeeGrid;
+
+// Host copy of the grid with pica's accessors.  Once bound to a device context
+// (by pushSupercells, a YeeSolver update or a Simulation), element writes reach
+// the device before the next operator, and the first read after an operator
+// fetches the device fields (all nine arrays, once).
+template <typename Real>
+class YeeGrid<Three, Real> {
+public:
+    typedef Int3 IndexType;
+    typedef FP3 PositionType;
+    typedef Real ValueType;
+    typedef Array3d<Real> ArrayType;
+
+    YeeGrid(const FP3& origin, const FP3& step, const Int3& size) : n_(size), h_(step), o_(origin) {
+        for (auto& a : f_) a = ArrayType(size);
+    }
+    YeeGrid(const YeeGrid&) = delete;
+    YeeGrid& operator=(const YeeGrid&) = delete;
+#define PICA_GB300_COMPONENT(name, c)                                                      \
+    Real& name(int i, int j, int k) { write(); return f_[c](i, j, k); }                    \
+    Real name(int i, int j, int k) const { read(); return f_[c](i, j, k); }                \
+    Real& name(const Int3& n) { write(); return f_[c](n); }                                \
+    Real name(const Int3& n) const { read(); return f_[c](n); }                            \
+    ArrayType& name() { write(); return f_[c]; }                                           \
+    const ArrayType& name() const { read(); return f_[c]; }
     PICA_GB300_COMPONENT(ex, 0)
     PICA_GB300_COMPONENT(ey, 1)
     PICA_GB300_COMPONENT(ez, 2)
@@ -310,42 +422,108 @@ public:
     FP3 getShiftJx() const { return getShiftEx(); }
     FP3 getShiftJy() const { return getShiftEy(); }
     FP3 getShiftJz() const { return getShiftEz(); }
-    inline void upload();
-    inline void download();
+    // Explicit copies (bound grids only; PICA_ERR_INVALID before the grid is bound).
+    void upload() { need(); push(); }
+    void download() { need(); pull(); }
 
 private:
-    friend class Simulation;
-    friend class YeeSolver;
-    pica_ctx* ctx_ = nullptr;
+    friend struct detail::Access;
+    void need() const {
+        if (!b_) throw Error(PICA_ERR_INVALID, "this grid is bound to no device context yet");
+    }
+    void read() const {
+        if (b_ && b_->fieldsStale && !dirty_) const_cast<YeeGrid*>(this)->pull();
+    }
+    void write() {
+        read();
+        dirty_ = true;
+    }
+    void pull() {
+        std::array<std::vector<double>, 9> t;
+        double* p[9];
+        for (int c = 0; c < 9; c++) {
+            if (std::is_same<Real, double>::value) {
+                p[c] = reinterpret_cast<double*>(f_[c].data());
+            } else {
+                t[c].resize(f_[c].size());
+                p[c] = t[c].data();
+            }
+        }
+        check(b_->ctx, pica_download_fields(b_->ctx, p));
+        if (!std::is_same<Real, double>::value)
+            for (int c = 0; c < 9; c++) std::copy(t[c].begin(), t[c].end(), f_[c].data());
+        b_->fieldsStale = false;
+        dirty_ = false;
+    }
+    void push() {
+        std::array<std::vector<double>, 9> t;
+        const double* p[9];
+        for (int c = 0; c < 9; c++) {
+            if (std::is_same<Real, double>::value) {
+                p[c] = reinterpret_cast<const double*>(f_[c].data());
+            } else {
+                t[c].assign(f_[c].data(), f_[c].data() + f_[c].size());
+                p[c] = t[c].data();
+            }
+        }
+        check(b_->ctx, pica_upload_fields(b_->ctx, p));
+        b_->fieldsStale = false;
+        dirty_ = false;
+    }
+    void flush() {
+        if (dirty_) push();
+    }
+    std::shared_ptr<detail::Binding> b_;
+    bool dirty_ = false;   // the host copy changed since the device received it
     Int3 n_;
     FP3 h_, o_;
-    std::array<Array3d, 9> f_;
+    std::array<ArrayType, 9> f_;
 };
 
-// Host staging of the device ensemble: add() collects particles, upload()
-// routes them to supercells (EnsembleSupercells::add, EnsembleSupercells.h:41-45).
+// pica's EnsembleSupercells<ParticleArray> (particles/EnsembleSupercells.h:15-69):
+// particles routed to supercells of numCellsPerSupercell cells over [min, max)
+// by floor((position - min) / supercellSize).  The host copy keeps one
+// ParticleArray per supercell (its particles type by type); once bound to a
+// device context, added or modified particles reach the device before the next
+// operator, and the first read after an operator fetches the device ensemble.
+// Positions outside [min, max) wrap periodically on the device.
+template <class PA>
 class EnsembleSupercells {
 public:
-    EnsembleSupercells() = default;
-    // pica's constructor (EnsembleSupercells.h:25-34): a host-only container over
-    // [minPosition, maxPosition) with numCells cells in supercells of numCellsPerSupercell
-    // (add and getSupercellIndex work; upload and the device calls throw).  The
-    // ensemble of a Simulation spans [0, numCells * step).
+    typedef PA ParticleArray;
+    typedef typename PA::Particle Particle;
+    typedef typename PA::ParticleRef ParticleRef;
+    typedef typename PA::ConstParticleRef ConstParticleRef;
+    typedef FP3 PositionType;
+    typedef Int3 IndexType;
+
+    // pica's constructor (EnsembleSupercells.h:25-34).
     EnsembleSupercells(const FP3& minPosition, const FP3& maxPosition, const Int3& numCells,
                        const Int3& numCellsPerSupercell)
         : S_(numCellsPerSupercell), min_(minPosition), max_(maxPosition), n_(numCells) {
         nsc_ = Int3((n_.x + S_.x - 1) / S_.x, (n_.y + S_.y - 1) / S_.y, (n_.z + S_.z - 1) / S_.z);
+        cells_.resize((size_t)nsc_.x * nsc_.y * nsc_.z);
+        own();
     }
-    void add(const ParticleArraySoA::ConstParticleRef& r) { add(static_cast<Particle3d>(r)); }
-    void add(const Particle3d& p) {
-        x_.push_back(p.position.x); y_.push_back(p.position.y); z_.push_back(p.position.z);
-        ux_.push_back(p.p.x); uy_.push_back(p.p.y); uz_.push_back(p.p.z);
-        w_.push_back(p.factor); t_.push_back(p.typeIndex);
+    EnsembleSupercells(const EnsembleSupercells&) = delete;
+    EnsembleSupercells& operator=(const EnsembleSupercells&) = delete;
+
+    // EnsembleSupercells::add (EnsembleSupercells.h:41-45): a Particle3d or a reference.
+    template <class P>
+    void add(const P& particle) {
+        const Particle3d q = static_cast<Particle3d>(particle);
+        ensureHost();
+        cells_[linear(wrapped(getSupercellIndex(q)))].pushBack(q);
     }
-    inline void upload();
-    // All particles in ensemble order (type, supercell, slot).
-    inline std::vector<Particle3d> particles() const;
-    inline std::vector<int32_t> counts() const;
+    // The particles of one supercell (EnsembleSupercells.h:49-52), type by type.
+    PA& getParticles(const Int3& idx) {
+        ensureHost();
+        return cells_[linear(idx)];
+    }
+    const PA& getParticles(const Int3& idx) const {
+        ensureHost();
+        return cells_[linear(idx)];
+    }
     Int3 getNumSupercells() const { return nsc_; }
     Int3 getNumCellsPerSupercell() const { return S_; }
     Int3 getNumCells() const { return n_; }
@@ -353,40 +531,349 @@ public:
     FP3 getMaxPosition() const { return max_; }
     // pica's routing rule (EnsembleSupercells.h:54-57): floor((position - min) / supercell size),
     // supercell size = numCellsPerSupercell * (max - min) / numCells.
-    Int3 getSupercellIndex(const Particle3d& p) const {
+    template <class P>
+    Int3 getSupercellIndex(const P& particle) const {
+        const Particle3d p = static_cast<Particle3d>(particle);
         const FP3 cell = (max_ - min_) / FP3(n_.x, n_.y, n_.z);
         const FP3 inv = FP3(1, 1, 1) / (FP3(S_.x, S_.y, S_.z) * cell);
         const FP3 q = (p.position - min_) * inv;
         return Int3((int)std::floor(q.x), (int)std::floor(q.y), (int)std::floor(q.z));
     }
-    // The particles of one supercell (EnsembleSupercells.h:51-52), type by type in
-    // slot order: a downloaded copy (the device holds the ensemble).
-    inline std::vector<Particle3d> getParticles(const Int3& supercellIdx) const;
-    // Number of particles on the device (pica's size() throws "not implemented").
-    inline int64_t size() const;
-    inline void migrate();
-    // Sort every supercell by cell now (EnsembleOrdered::reorder, EnsembleOrdered.h:61-71).
-    inline void reorder();
+    // Number of particles (pica's size() throws "not implemented").
+    int64_t size() const {
+        if (b_ && !dirty_) {
+            const int64_t n = pica_num_particles(b_->ctx);
+            if (n < 0) check(b_->ctx, (int)n);
+            return n;
+        }
+        int64_t n = 0;
+        for (auto& a : cells_) n += a.size();
+        return n;
+    }
+    // All particles in ensemble order (type, supercell, slot) and the per-supercell
+    // counts (counts[type * supercells + s]), read from the device.
+    inline std::vector<Particle3d> particles() const;
+    inline std::vector<int32_t> counts() const;
+    // Explicit calls of the Simulation form: send the host copy now; finish the
+    // push's migration now; sort every supercell by cell now
+    // (EnsembleOrdered::reorder, EnsembleOrdered.h:61-71).
+    void upload() { need(); flush(true); }
+    void migrate() {
+        need();
+        b_->pending = false;
+        check(b_->ctx, pica_migrate(b_->ctx));
+        b_->particleEpoch++;
+    }
+    void reorder() {
+        need();
+        b_->settle();
+        flush(false);
+        check(b_->ctx, pica_reorder(b_->ctx));
+        b_->particleEpoch++;
+    }
+    // In-supercell sort by cell every resortEvery steps on the device (-1: 0 for
+    // double operators, 2 for float operators).  Read when the ensemble is bound.
+    int resortEvery = -1;
 
 private:
-    friend class Simulation;
-    pica_ctx* ctx_ = nullptr;
-    int ntypes_ = 1;
+    friend struct detail::Access;
+    void need() const {
+        if (!b_) throw Error(PICA_ERR_INVALID, "this ensemble is bound to no device context yet");
+    }
+    size_t linear(const Int3& i) const { return ((size_t)i.x * nsc_.y + i.y) * nsc_.z + i.z; }
+    Int3 wrapped(const Int3& i) const {
+        auto w = [](int a, int n) { a %= n; return a < 0 ? a + n : a; };
+        return Int3(w(i.x, nsc_.x), w(i.y, nsc_.y), w(i.z, nsc_.z));
+    }
+    void own() {
+        for (auto& a : cells_) a.owner_ = &dirty_;
+    }
+    inline std::vector<Particle3d> download(std::vector<int32_t>* supercell) const;
+    // Bring the host copy up to date (after a device operator).
+    void ensureHost() const {
+        if (b_ && !dirty_ && epoch_ != b_->particleEpoch) const_cast<EnsembleSupercells*>(this)->pull();
+    }
+    void pull() {
+        std::vector<int32_t> s;
+        const std::vector<Particle3d> all = download(&s);
+        for (auto& a : cells_) a = PA();
+        for (size_t i = 0; i < all.size(); i++) cells_[(size_t)s[i]].pushBack(all[i]);
+        own();
+        dirty_ = false;
+        epoch_ = b_->particleEpoch;
+    }
+    // Send the host copy to the device if it changed (or always).
+    void flush(bool always) {
+        if (!dirty_ && !always) return;
+        b_->settle();
+        int64_t n = 0;
+        for (auto& a : cells_) n += a.size();
+        std::vector<double> v[7];
+        for (auto& x : v) x.reserve((size_t)n);
+        std::vector<int32_t> t;
+        t.reserve((size_t)n);
+        for (auto& a : cells_)
+            for (int i = 0; i < a.size(); i++) {
+                const Particle3d q = static_cast<Particle3d>(a[i]);
+                v[0].push_back(q.position.x - min_.x); v[1].push_back(q.position.y - min_.y);
+                v[2].push_back(q.position.z - min_.z);
+                v[3].push_back(q.p.x); v[4].push_back(q.p.y); v[5].push_back(q.p.z);
+                v[6].push_back(q.factor);
+                t.push_back(q.typeIndex);
+            }
+        check(b_->ctx, pica_upload_particles(b_->ctx, n, v[0].data(), v[1].data(), v[2].data(), v[3].data(),
+                                             v[4].data(), v[5].data(), v[6].data(), t.data()));
+        dirty_ = false;
+        b_->particleEpoch++;   // the device holds them in its own order now
+    }
+    std::shared_ptr<detail::Binding> b_;
     Int3 nsc_, S_;
     FP3 min_, max_;
     Int3 n_;
-    inline std::vector<Particle3d> download(std::vector<int32_t>* supercell) const;
-    std::vector<double> x_, y_, z_, ux_, uy_, uz_, w_;
-    std::vector<int32_t> t_;
+    mutable std::vector<PA> cells_;   // host copy: one array per supercell
+    mutable bool dirty_ = true;       // the host copy changed since the device received it
+    mutable uint64_t epoch_ = 0;      // the binding's particle epoch the host copy reflects
 };
 
-inline void check(pica_ctx* ctx, int rc) {
-    if (rc != PICA_OK) throw Error(rc, std::string(pica_status_string(rc)) + ": " + (ctx ? pica_last_error(ctx) : ""));
+// ---------------------------------------------------------------------------
+// Operators.  Each carries the configuration of the bulk call that replaces its
+// per-particle method (no per-particle get / push / deposit: they would run on
+// the CPU, and there is no CPU path).
+// ---------------------------------------------------------------------------
+
+// pica's BorisPusher<Particle, Real> (particlePush/BorisPusher.h:13-30): dt and the
+// per-type coefficients q dt / (2 m c) from the ParticleTypes table.
+template <class Particle, typename Real>
+struct BorisPusher {
+    std::vector<Real> coeffVector;
+    Real* coeff;
+    Real dt;
+    explicit BorisPusher(Real dt) : dt(dt) {
+        coeffVector.resize((size_t)ParticleTypes::numTypes);
+        coeff = coeffVector.data();
+        for (int i = 0; i < ParticleTypes::numTypes; i++)
+            coeff[i] = static_cast<Real>(ParticleTypes::at(i).charge * dt /
+                                         (2.0 * ParticleTypes::at(i).mass * Constants<double>::c()));
+    }
+};
+
+#define PICA_GB300_INTERPOLATOR(Name, SHAPE)                                                         \
+    template <class GridType>                                                                        \
+    class Name;                                                                                      \
+    template <typename Real>                                                                         \
+    class Name<YeeGrid<Three, Real>> {                                                               \
+    public:                                                                                          \
+        typedef YeeGrid<Three, Real> GridType;                                                       \
+        typedef Real RealType;                                                                       \
+        static constexpr int shape = SHAPE;                                                          \
+        explicit Name(const GridType& g) : grid(g) {}                                                \
+        const GridType& grid;                                                                        \
+    };                                                                                               \
+    template <typename Real>                                                                         \
+    class Name##Supercell {                                                                          \
+    public:                                                                                          \
+        typedef YeeGrid<Three, Real> GridType;                                                       \
+        typedef Real RealType;                                                                       \
+        static constexpr int shape = SHAPE;                                                          \
+        Name##Supercell(const GridType& g, const FP3& minPos, const Int3& cellsPerSupercell)          \
+            : grid(g), minPosition(minPos), numCellsPerSupercell(cellsPerSupercell) {}               \
+        const GridType& grid;                                                                        \
+        FP3 minPosition;                                                                             \
+        Int3 numCellsPerSupercell;                                                                   \
+    };
+// pica's FieldInterpolatorCIC<YeeGrid<Three, Real>> and FieldInterpolatorCICSupercell<Real>
+// (fieldInterpolation/FieldInterpolatorYeeGrid.h:137-187, 188-283), and their TSC
+// siblings (quadratic B-spline form factor; no counterpart in pica).
+PICA_GB300_INTERPOLATOR(FieldInterpolatorCIC, PICA_SHAPE_CIC)
+PICA_GB300_INTERPOLATOR(FieldInterpolatorTSC, PICA_SHAPE_TSC)
+#undef PICA_GB300_INTERPOLATOR
+
+#define PICA_GB300_DEPOSITOR(Name, SHAPE, KIND)                                                      \
+    template <class GridType>                                                                        \
+    class Name;                                                                                      \
+    template <typename Real>                                                                         \
+    class Name<YeeGrid<Three, Real>> {                                                               \
+    public:                                                                                          \
+        typedef YeeGrid<Three, Real> GridType;                                                       \
+        typedef Real RealType;                                                                       \
+        static constexpr int shape = SHAPE;                                                          \
+        static constexpr int deposit = KIND;                                                         \
+        explicit Name(GridType& g) : grid(g) {}                                                      \
+        GridType& grid;                                                                              \
+    };                                                                                               \
+    template <typename Real>                                                                         \
+    class Name##Supercell {                                                                          \
+    public:                                                                                          \
+        typedef YeeGrid<Three, Real> GridType;                                                       \
+        typedef Real RealType;                                                                       \
+        static constexpr int shape = SHAPE;                                                          \
+        static constexpr int deposit = KIND;                                                         \
+        Name##Supercell(GridType& g, const FP3& minPos, const Int3& cellsPerSupercell)                \
+            : grid(g), minPosition(minPos), numCellsPerSupercell(cellsPerSupercell) {}               \
+        GridType& grid;                                                                              \
+        FP3 minPosition;                                                                             \
+        Int3 numCellsPerSupercell;                                                                   \
+    };
+// pica's CurrentDepositorCIC<YeeGrid<Three, Real>> and CurrentDepositorCICSupercell<Real>
+// (currentDeposition/CurrentDepositorYeeGrid.h:126-163, 169-264): direct deposition of
+// q w v at the new position.  The TSC siblings deposit directly with the TSC form
+// factor, and the Esirkepov depositors conserve charge exactly (T. Zh. Esirkepov,
+// Comput. Phys. Commun. 135 (2001) 144) with the interpolator's form factor; pica has
+// neither.
+PICA_GB300_DEPOSITOR(CurrentDepositorCIC, PICA_SHAPE_CIC, PICA_DEPOSIT_DIRECT)
+PICA_GB300_DEPOSITOR(CurrentDepositorTSC, PICA_SHAPE_TSC, PICA_DEPOSIT_DIRECT)
+PICA_GB300_DEPOSITOR(CurrentDepositorEsirkepov, 0, PICA_DEPOSIT_ESIRKEPOV)
+#undef PICA_GB300_DEPOSITOR
+
+namespace detail {
+struct Access {
+    template <typename Real, class PA>
+    static void attach(YeeGrid<Three, Real>& g, EnsembleSupercells<PA>& e, const std::shared_ptr<Binding>& b) {
+        g.b_ = b;
+        g.dirty_ = false;
+        e.b_ = b;
+        e.dirty_ = false;
+        e.epoch_ = b->particleEpoch;
+    }
+    template <typename Real>
+    static void flush(YeeGrid<Three, Real>& g) { g.flush(); }
+    template <class PA>
+    static void flush(EnsembleSupercells<PA>& e) { e.flush(false); }
+    template <class PA>
+    static void replaced(EnsembleSupercells<PA>& e) { e.dirty_ = false; }
+
+    static pica_config base(const Int3& n, const FP3& h, double dt, bool fp64) {
+        pica_config cfg{};
+        cfg.n[0] = n.x; cfg.n[1] = n.y; cfg.n[2] = n.z;
+        cfg.h[0] = h.x; cfg.h[1] = h.y; cfg.h[2] = h.z;
+        cfg.dt = dt;
+        cfg.form = fp64 ? PICA_FORM_FP64_PLAIN : PICA_FORM_FP32_CELL;
+        if (ParticleTypes::numTypes < 1 || ParticleTypes::numTypes > 4)
+            throw Error(PICA_ERR_INVALID, "the ParticleTypes table must hold 1 to 4 types");
+        cfg.nspecies = ParticleTypes::numTypes;
+        for (int q = 0; q < cfg.nspecies; q++) {
+            cfg.mass[q] = ParticleTypes::at(q).mass;
+            cfg.charge[q] = ParticleTypes::at(q).charge;
+        }
+        cfg.slack = 0.15;
+        return cfg;
+    }
+    // The configuration of a bulk push over (grid, ensemble).
+    template <typename Real, class PA>
+    static pica_config configFor(const YeeGrid<Three, Real>& g, const EnsembleSupercells<PA>& e, double dt, int shape,
+                                 int deposit) {
+        if (!(g.n_ == e.n_))
+            throw Error(PICA_ERR_INVALID, "the grid's size must equal the ensemble's numCells (the device grid is "
+                                          "periodic over the ensemble's domain, with no guard layers)");
+        const FP3 cell = (e.max_ - e.min_) / FP3(e.n_.x, e.n_.y, e.n_.z);
+        if (std::fabs(cell.x - g.h_.x) > 1e-9 * g.h_.x || std::fabs(cell.y - g.h_.y) > 1e-9 * g.h_.y ||
+            std::fabs(cell.z - g.h_.z) > 1e-9 * g.h_.z)
+            throw Error(PICA_ERR_INVALID, "the grid's step differs from the ensemble's cell size");
+        const bool fp64 = std::is_same<Real, double>::value;
+        pica_config cfg = base(g.n_, g.h_, dt, fp64);
+        cfg.sc[0] = e.S_.x; cfg.sc[1] = e.S_.y; cfg.sc[2] = e.S_.z;
+        cfg.shape = shape;
+        cfg.deposit = deposit;
+        cfg.resort_every = e.resortEvery >= 0 ? e.resortEvery : (fp64 ? 0 : 2);
+        return cfg;
+    }
+    static std::shared_ptr<Binding> make(const pica_config& cfg) {
+        auto b = std::make_shared<Binding>();
+        b->cfg = cfg;
+        check(nullptr, pica_ctx_create(&cfg, &b->ctx));
+        return b;
+    }
+    // A context of the grid alone (a field solve before any push): one-cell supercells.
+    template <typename Real>
+    static void bindFields(YeeGrid<Three, Real>& g) {
+        pica_config cfg = base(g.n_, g.h_, 1.0, std::is_same<Real, double>::value);
+        cfg.sc[0] = cfg.sc[1] = cfg.sc[2] = 1;
+        cfg.shape = PICA_SHAPE_CIC;
+        cfg.deposit = PICA_DEPOSIT_DIRECT;
+        g.b_ = make(cfg);
+        g.dirty_ = true;
+    }
+    // One context for grid and ensemble with this configuration: reused when it is
+    // already theirs; otherwise both host copies are brought up to date under their
+    // old contexts and go to a new one.
+    template <typename Real, class PA>
+    static Binding& bind(YeeGrid<Three, Real>& g, EnsembleSupercells<PA>& e, const pica_config& cfg) {
+        if (g.b_ && g.b_ == e.b_ && sameConfig(g.b_->cfg, cfg)) return *g.b_;
+        g.read();
+        e.ensureHost();
+        auto b = make(cfg);
+        g.b_ = b;
+        g.dirty_ = true;
+        e.b_ = b;
+        e.dirty_ = true;
+        return *b;
+    }
+    template <typename Real, class PA>
+    static void push(YeeGrid<Three, Real>& g, EnsembleSupercells<PA>& e, const pica_config& cfg) {
+        Binding& b = bind(g, e, cfg);
+        b.settle();
+        g.flush();
+        e.flush(false);
+        check(b.ctx, pica_push_deposit(b.ctx));
+        b.pending = true;
+        b.fieldsStale = true;
+        b.particleEpoch++;
+    }
+    template <typename Real>
+    static void fieldUpdate(YeeGrid<Three, Real>& g, double dt, bool electric) {
+        if (!g.b_) bindFields(g);
+        g.flush();
+        check(g.b_->ctx, electric ? pica_update_e(g.b_->ctx, dt) : pica_update_b(g.b_->ctx, dt));
+        g.b_->fieldsStale = true;
+    }
+};
+}  // namespace detail
+
+// One step's gather + Boris push + current deposit for every particle of every
+// supercell: the supercell loop of a pica host loop, with its per-particle
+// fi.get / pusher.push / cd.deposit calls (FieldInterpolatorYeeGrid.h:197-242,
+// BorisPusher.h:33-47, CurrentDepositorYeeGrid.h:178-226) replaced by one call.
+// The interpolator and the depositor act on one grid; the grid's size equals the
+// ensemble's numCells.  J is cleared first.  The migration of the particles that
+// left their supercell runs before the next push or read of the ensemble.
+template <class PA, class Interpolator, class Particle, typename Real, class Depositor>
+void pushSupercells(EnsembleSupercells<PA>& ens, const Interpolator& fi, const BorisPusher<Particle, Real>& pusher,
+                    Depositor& cd) {
+    static_assert(std::is_same<typename Interpolator::RealType, Real>::value &&
+                      std::is_same<typename Depositor::RealType, Real>::value,
+                  "the interpolator, the pusher and the depositor take one Real");
+    if (static_cast<const void*>(&fi.grid) != static_cast<const void*>(&cd.grid))
+        throw Error(PICA_ERR_INVALID, "the interpolator and the depositor act on different grids");
+    if (Depositor::shape != 0 && Depositor::shape != Interpolator::shape)
+        throw Error(PICA_ERR_INVALID, "the depositor's form factor differs from the interpolator's");
+    detail::Access::push(cd.grid, ens,
+                         detail::Access::configFor(cd.grid, ens, (double)pusher.dt, Interpolator::shape,
+                                                   Depositor::deposit));
 }
 
+// pica YeeSolver (fieldSolver/YeeSolver.h:11-38) on the periodic device grid.  A
+// grid that no push has bound yet gets a context of its own (fields only).
+class YeeSolver {
+public:
+    template <typename Real>
+    void updateE(YeeGrid<Three, Real>& g, double dt) { detail::Access::fieldUpdate(g, dt, true); }
+    template <typename Real>
+    void updateB(YeeGrid<Three, Real>& g, double dt) { detail::Access::fieldUpdate(g, dt, false); }
+};
+
+// ---------------------------------------------------------------------------
+// Explicit form: a Simulation built from a Config owns the context; its grid and
+// ensemble are bound to it from the start.
+// ---------------------------------------------------------------------------
 class Simulation {
 public:
-    explicit Simulation(const Config& c) {
+    typedef YeeGrid<Three, double> Grid;
+    typedef EnsembleSupercells<ParticleArraySoA<Particle3d>> Ensemble;
+
+    explicit Simulation(const Config& c)
+        : grid_(FP3(0, 0, 0), c.step, c.numCells),
+          ens_(FP3(0, 0, 0), FP3(c.numCells.x * c.step.x, c.numCells.y * c.step.y, c.numCells.z * c.step.z),
+               c.numCells, c.numCellsPerSupercell) {
         pica_config cfg{};
         cfg.n[0] = c.numCells.x; cfg.n[1] = c.numCells.y; cfg.n[2] = c.numCells.z;
         cfg.sc[0] = c.numCellsPerSupercell.x; cfg.sc[1] = c.numCellsPerSupercell.y; cfg.sc[2] = c.numCellsPerSupercell.z;
@@ -397,83 +884,115 @@ public:
         for (size_t i = 0; i < c.types.size() && i < 4; i++) { cfg.mass[i] = c.types[i].mass; cfg.charge[i] = c.types[i].charge; }
         cfg.slack = c.slack;
         cfg.resort_every = c.resortEvery;
-        check(nullptr, pica_ctx_create(&cfg, &ctx_));
+        b_ = detail::Access::make(cfg);
         // The configured species become pica's global type table (Particle3d::getMass / getCharge).
         ParticleTypes::typesVector = c.types;
         ParticleTypes::types = nullptr;
         ParticleTypes::numTypes = (int)c.types.size();
         dt_ = c.dt;
-        grid_.ctx_ = ctx_; grid_.n_ = c.numCells; grid_.h_ = c.step;
-        for (auto& a : grid_.f_) a = Array3d(c.numCells);
-        ens_.ctx_ = ctx_; ens_.ntypes_ = cfg.nspecies; ens_.S_ = c.numCellsPerSupercell;
-        ens_.nsc_ = Int3(c.numCells.x / c.numCellsPerSupercell.x, c.numCells.y / c.numCellsPerSupercell.y,
-                         c.numCells.z / c.numCellsPerSupercell.z);
-        ens_.n_ = c.numCells;
-        ens_.max_ = FP3(c.numCells.x * c.step.x, c.numCells.y * c.step.y, c.numCells.z * c.step.z);
+        detail::Access::attach(grid_, ens_, b_);
     }
-    ~Simulation() { if (ctx_) pica_ctx_destroy(ctx_); }
     Simulation(const Simulation&) = delete;
     Simulation& operator=(const Simulation&) = delete;
 
-    YeeGrid& grid() { return grid_; }
-    EnsembleSupercells& ensemble() { return ens_; }
-    pica_ctx* handle() { return ctx_; }
+    Grid& grid() { return grid_; }
+    Ensemble& ensemble() { return ens_; }
+    pica_ctx* handle() { return b_->ctx; }
     double dt() const { return dt_; }
-    void setStream(void* cudaStream) { check(ctx_, pica_set_stream(ctx_, cudaStream)); }
+    void setStream(void* cudaStream) { check(b_->ctx, pica_set_stream(b_->ctx, cudaStream)); }
     // One full step: push + deposit, B(dt/2), E(dt), B(dt/2), migrate.
-    void step(int n = 1) { check(ctx_, pica_step(ctx_, n)); }
+    void step(int n = 1) {
+        ready();
+        check(b_->ctx, pica_step(b_->ctx, n));
+        changed();
+    }
+    // Push + deposit of every particle (the ensemble then awaits its migration).
+    void pushDeposit() {
+        ready();
+        check(b_->ctx, pica_push_deposit(b_->ctx));
+        b_->pending = true;
+        changed();
+    }
     pica_diag diagnostics(double bgDensity = 0.0) {
+        ready();
         pica_diag d{};
-        check(ctx_, pica_diagnostics(ctx_, bgDensity, &d));
+        check(b_->ctx, pica_diagnostics(b_->ctx, bgDensity, &d));
         return d;
     }
-    int64_t stepCount() { return pica_step_count(ctx_); }
-    // Synthetic plasma generated on the device in place of ensemble().upload()
+    int64_t stepCount() { return pica_step_count(b_->ctx); }
+    // Synthetic plasma generated on the device in place of ensemble() particles
     // (FP32 cell form; see pica_generate_plasma).
     void generatePlasma(const std::vector<pica_plasma_spec>& specs) {
-        check(ctx_, pica_generate_plasma(ctx_, specs.data(), (int32_t)specs.size()));
+        b_->settle();
+        check(b_->ctx, pica_generate_plasma(b_->ctx, specs.data(), (int32_t)specs.size()));
+        detail::Access::replaced(ens_);
+        b_->particleEpoch++;
     }
     // Packed particle state of one species (used slots only; see pica_state_packed_slots):
     // statePackedSlots() lays the image out, copyStatePacked() moves one component of
     // it (host: pinned memory of statePackedSlots() x 4 or 8 bytes).
     int64_t statePackedSlots(int species = 0) {
-        const int64_t n = pica_state_packed_slots(ctx_, species);
-        if (n < 0) check(ctx_, (int)n);
+        const int64_t n = pica_state_packed_slots(b_->ctx, species);
+        if (n < 0) check(b_->ctx, (int)n);
         return n;
     }
     void copyStatePacked(int species, int comp, void* host, bool toDevice) {
-        check(ctx_, pica_state_copy_packed(ctx_, species, comp, host, toDevice ? 1 : 0));
+        check(b_->ctx, pica_state_copy_packed(b_->ctx, species, comp, host, toDevice ? 1 : 0));
+        if (toDevice) b_->particleEpoch++;
     }
     // The image part of supercells [scBegin, scEnd) (host: start of the whole image);
     // copyStream: the host copy on that cudaStream_t, the gather / scatter kernel on
     // the context stream (pica_state_copy_packed_range_on).
     void copyStatePackedRange(int species, int comp, void* host, bool toDevice, int scBegin, int scEnd,
                               void* copyStream = nullptr) {
-        check(ctx_, pica_state_copy_packed_range_on(ctx_, species, comp, host, toDevice ? 1 : 0, scBegin, scEnd,
-                                                    copyStream));
+        check(b_->ctx, pica_state_copy_packed_range_on(b_->ctx, species, comp, host, toDevice ? 1 : 0, scBegin, scEnd,
+                                                       copyStream));
+        if (toDevice) b_->particleEpoch++;
     }
     // The push in waitEvents.size() supercell ranges, range r after a wait for
     // waitEvents[r] (cudaEvent_t or nullptr); the rest of the step follows as in a
     // pica host loop: YeeSolver updateB(dt/2), updateE(dt), updateB(dt/2), ensemble().migrate().
     void pushDepositChunked(const std::vector<void*>& waitEvents) {
-        check(ctx_, pica_push_deposit_chunked(ctx_, (int32_t)waitEvents.size(), waitEvents.data()));
+        check(b_->ctx, pica_push_deposit_chunked(b_->ctx, (int32_t)waitEvents.size(), waitEvents.data()));
+        b_->pending = true;
+        changed();
     }
     // The same over supercell ranges [bounds[r], bounds[r+1]) of the caller's choice
     // (bounds.size() == waitEvents.size() + 1, from 0 to the supercell count).
     void pushDepositRanges(const std::vector<int32_t>& bounds, const std::vector<void*>& waitEvents) {
         if (bounds.size() != waitEvents.size() + 1) throw Error(PICA_ERR_INVALID, "one more bound than wait events");
-        check(ctx_, pica_push_deposit_ranges(ctx_, (int32_t)waitEvents.size(), bounds.data(), waitEvents.data()));
+        check(b_->ctx, pica_push_deposit_ranges(b_->ctx, (int32_t)waitEvents.size(), bounds.data(), waitEvents.data()));
+        b_->pending = true;
+        changed();
     }
     // Complete state between steps; a Simulation of the same Config loaded from it
     // continues like this one (FP32 form: bit for bit).
-    void saveCheckpoint(const std::string& path) { check(ctx_, pica_checkpoint_save(ctx_, path.c_str())); }
-    void loadCheckpoint(const std::string& path) { check(ctx_, pica_checkpoint_load(ctx_, path.c_str())); }
+    void saveCheckpoint(const std::string& path) {
+        ready();
+        check(b_->ctx, pica_checkpoint_save(b_->ctx, path.c_str()));
+    }
+    void loadCheckpoint(const std::string& path) {
+        b_->settle();
+        check(b_->ctx, pica_checkpoint_load(b_->ctx, path.c_str()));
+        detail::Access::replaced(ens_);
+        changed();
+    }
 
 private:
-    pica_ctx* ctx_ = nullptr;
+    // Host changes to the device, the last migration done.
+    void ready() {
+        b_->settle();
+        detail::Access::flush(grid_);
+        detail::Access::flush(ens_);
+    }
+    void changed() {
+        b_->fieldsStale = true;
+        b_->particleEpoch++;
+    }
+    std::shared_ptr<detail::Binding> b_;
     double dt_ = 0;
-    YeeGrid grid_;
-    EnsembleSupercells ens_;
+    Grid grid_;
+    Ensemble ens_;
 };
 
 // Host loop around a Simulation (the PICADOR driver's role; periodic boundaries):
@@ -505,53 +1024,39 @@ private:
     Simulation& sim_;
 };
 
-void YeeGrid::upload() {
-    if (!ctx_) throw Error(PICA_ERR_INVALID, "this grid belongs to no Simulation");
-    const double* p[9];
-    for (int c = 0; c < 9; c++) p[c] = f_[c].data();
-    check(ctx_, pica_upload_fields(ctx_, p));
-}
-void YeeGrid::download() {
-    if (!ctx_) throw Error(PICA_ERR_INVALID, "this grid belongs to no Simulation");
-    double* p[9];
-    for (int c = 0; c < 9; c++) p[c] = f_[c].data();
-    check(ctx_, pica_download_fields(ctx_, p));
-}
+// Push + deposit of a Simulation's whole ensemble (pushSupercells with the
+// Simulation's own configuration).
+inline void pushSupercells(Simulation& sim) { sim.pushDeposit(); }
 
-void EnsembleSupercells::upload() {
-    if (!ctx_) throw Error(PICA_ERR_INVALID, "this ensemble belongs to no Simulation");
-    check(ctx_, pica_upload_particles(ctx_, (int64_t)w_.size(), x_.data(), y_.data(), z_.data(), ux_.data(),
-                                      uy_.data(), uz_.data(), w_.data(), t_.data()));
-    x_.clear(); y_.clear(); z_.clear(); ux_.clear(); uy_.clear(); uz_.clear(); w_.clear(); t_.clear();
+template <class PA>
+std::vector<Particle3d> EnsembleSupercells<PA>::particles() const {
+    need();
+    const_cast<EnsembleSupercells*>(this)->flush(false);
+    return download(nullptr);
 }
-std::vector<Particle3d> EnsembleSupercells::particles() const { return download(nullptr); }
-std::vector<Particle3d> EnsembleSupercells::getParticles(const Int3& idx) const {
-    std::vector<int32_t> s;
-    const std::vector<Particle3d> all = download(&s);
-    const int32_t want = (idx.x * nsc_.y + idx.y) * nsc_.z + idx.z;
-    std::vector<Particle3d> out;
-    for (size_t i = 0; i < all.size(); i++)
-        if (s[i] == want) out.push_back(all[i]);
-    return out;
+template <class PA>
+std::vector<int32_t> EnsembleSupercells<PA>::counts() const {
+    need();
+    b_->settle();
+    const_cast<EnsembleSupercells*>(this)->flush(false);
+    std::vector<int32_t> c((size_t)b_->cfg.nspecies * nsc_.x * nsc_.y * nsc_.z);
+    check(b_->ctx, pica_get_counts(b_->ctx, c.data()));
+    return c;
 }
-int64_t EnsembleSupercells::size() const {
-    if (!ctx_) throw Error(PICA_ERR_INVALID, "this ensemble belongs to no Simulation");
-    const int64_t n = pica_num_particles(ctx_);
-    if (n < 0) check(ctx_, (int)n);
-    return n;
-}
-std::vector<Particle3d> EnsembleSupercells::download(std::vector<int32_t>* supercell) const {
-    if (!ctx_) throw Error(PICA_ERR_INVALID, "this ensemble belongs to no Simulation");
-    const int64_t n = pica_num_particles(ctx_);
-    if (n < 0) check(ctx_, (int)n);
+template <class PA>
+std::vector<Particle3d> EnsembleSupercells<PA>::download(std::vector<int32_t>* supercell) const {
+    need();
+    b_->settle();
+    const int64_t n = pica_num_particles(b_->ctx);
+    if (n < 0) check(b_->ctx, (int)n);
     std::vector<double> a[7];
-    for (auto& v : a) v.resize(n);
-    std::vector<int32_t> t(n), s(n);
-    check(ctx_, pica_download_particles(ctx_, a[0].data(), a[1].data(), a[2].data(), a[3].data(), a[4].data(),
-                                        a[5].data(), a[6].data(), t.data(), s.data()));
-    std::vector<Particle3d> out(n);
+    for (auto& v : a) v.resize((size_t)n);
+    std::vector<int32_t> t((size_t)n), s((size_t)n);
+    check(b_->ctx, pica_download_particles(b_->ctx, a[0].data(), a[1].data(), a[2].data(), a[3].data(), a[4].data(),
+                                           a[5].data(), a[6].data(), t.data(), s.data()));
+    std::vector<Particle3d> out((size_t)n);
     for (int64_t i = 0; i < n; i++) {
-        out[i].position = FP3(a[0][i], a[1][i], a[2][i]);
+        out[i].position = FP3(a[0][i], a[1][i], a[2][i]) + min_;
         out[i].p = FP3(a[3][i], a[4][i], a[5][i]);
         out[i].factor = a[6][i];
         out[i].typeIndex = (short)t[i];
@@ -559,23 +1064,5 @@ std::vector<Particle3d> EnsembleSupercells::download(std::vector<int32_t>* super
     if (supercell) *supercell = std::move(s);
     return out;
 }
-std::vector<int32_t> EnsembleSupercells::counts() const {
-    std::vector<int32_t> c((size_t)ntypes_ * nsc_.x * nsc_.y * nsc_.z);
-    check(ctx_, pica_get_counts(ctx_, c.data()));
-    return c;
-}
-void EnsembleSupercells::migrate() { check(ctx_, pica_migrate(ctx_)); }
-void EnsembleSupercells::reorder() { check(ctx_, pica_reorder(ctx_)); }
-
-// pica YeeSolver (fieldSolver/YeeSolver.h:11-38) on the periodic device grid.
-class YeeSolver {
-public:
-    void updateE(YeeGrid& g, double dt) { check(g.ctx_, pica_update_e(g.ctx_, dt)); }
-    void updateB(YeeGrid& g, double dt) { check(g.ctx_, pica_update_b(g.ctx_, dt)); }
-};
-
-// FieldInterpolator::get + BorisPusher::push + CurrentDepositor::deposit for
-// every particle of every supercell (the supercell loop of a pica host loop).
-inline void pushSupercells(Simulation& sim) { check(sim.handle(), pica_push_deposit(sim.handle())); }
 
 }  // namespace pica_gb300

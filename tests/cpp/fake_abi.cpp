@@ -1,5 +1,5 @@
 // A host-only stand-in for the few C ABI entry points that the C++ mirror's
-// plumbing calls (context, field and particle upload / download), so that the
+// plumbing calls (context, field and particle upload / download, migration), so that the
 // mirror's host code -- field index order, particle conversion, per-supercell
 // selection -- is tested without a GPU.  The fake keeps what is uploaded and
 // returns it in the ABI's documented ensemble order (species, then linear
@@ -69,6 +69,9 @@ int pica_upload_particles(pica_ctx* ctx, int64_t n, const double* x, const doubl
 }
 
 int64_t pica_num_particles(pica_ctx* ctx) { return (int64_t)ctx->species.size(); }
+
+// The fake moves no particles, so a migration has nothing to do.
+int pica_migrate(pica_ctx*) { return PICA_OK; }
 
 int pica_download_particles(pica_ctx* ctx, double* x, double* y, double* z, double* ux, double* uy, double* uz,
                             double* w, int32_t* species, int32_t* supercell) {

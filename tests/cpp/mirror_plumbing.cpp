@@ -57,7 +57,7 @@ int main() {
 
     // particles: half through a ParticleArraySoA, half as values
     auto& ens = sim.ensemble();
-    ParticleArraySoA arr;
+    ParticleArraySoA<Particle3d> arr;
     std::vector<Particle3d> all;
     for (int q = 0; q < 60; q++) {
         Particle3d p;
@@ -92,7 +92,9 @@ int main() {
                 for (int t = 0; t < 2; t++)
                     for (const auto& p : uploaded)
                         if (p.typeIndex == t && ens.getSupercellIndex(p) == Int3(a, b, c)) want.push_back(p);
-                const std::vector<Particle3d> got = ens.getParticles(Int3(a, b, c));
+                const auto& arrOf = ens.getParticles(Int3(a, b, c));
+                std::vector<Particle3d> got;
+                for (int i = 0; i < arrOf.size(); i++) got.push_back(arrOf[i]);
                 seen += got.size();
                 bool ok = got.size() == want.size();
                 for (size_t i = 0; ok && i < got.size(); i++) ok = same(got[i], want[i]);

@@ -106,7 +106,7 @@ int main() {
     // YeeGrid<Three> (grid/Grid.h:13-83, grid/YeeGrid.h:193-256) as a host container
     const FP3 origin(1.25, -4.5, 0.75), step(0.1, 0.2, 0.05);
     const Int3 size(5, 6, 7);
-    YeeGrid g(origin, step, size);
+    YeeGrid<Three, double> g(origin, step, size);
     if (!(g.getStep() == step) || !(g.getSize() == size) || !(g.getOrigin() == origin)) {
         std::printf("grid step / size / origin\n");
         fails++;
@@ -121,7 +121,7 @@ int main() {
                 }
                 g.ey(i, j, k) = 100.0 * i + 10.0 * j + k;
             }
-    const YeeGrid& cg = g;
+    const YeeGrid<Three, double>& cg = g;
     const Int3 n(3, 2, 5);
     const double want = 100.0 * 3 + 10.0 * 2 + 5;
     if (cg.ey(3, 2, 5) != want || cg.ey(n) != want || g.ey()(3, 2, 5) != want || g.ey()(n) != want ||
@@ -159,7 +159,7 @@ int main() {
             q.typeIndex = (short)(i % 2);
             return q;
         };
-        ParticleArraySoA arr;
+        ParticleArraySoA<Particle3d> arr;
         if (arr.size() != 0) { std::printf("empty array size\n"); fails++; }
         std::vector<Particle3d> pushed;
         for (int i = 0; i < 33; i++) {
@@ -167,7 +167,7 @@ int main() {
             arr.pushBack(pushed.back());
             if (!same(pushed.back(), arr.back())) { std::printf("back after push %d\n", i); fails++; }
         }
-        const ParticleArraySoA copy = arr;
+        const ParticleArraySoA<Particle3d> copy = arr;
         if (arr.size() != 33 || copy.size() != 33) { std::printf("array size\n"); fails++; }
         for (int i = 0; i < 33; i++) {
             if (!same(pushed[i], arr[i]) || !same(pushed[i], copy[i])) { std::printf("element %d\n", i); fails++; }
@@ -178,7 +178,7 @@ int main() {
             arr.popBack();
             if (arr.size() != n - 1 || (n > 1 && !same(pushed[n - 2], arr.back()))) { std::printf("popBack %d\n", n); fails++; }
         }
-        ParticleArraySoA one;
+        ParticleArraySoA<Particle3d> one;
         one.pushBack(copy[5]);   // from a reference
         auto r = one[0];
         r.setMomentum(m2);
@@ -198,7 +198,7 @@ int main() {
     // every supercell centre, for an offset domain with uneven cell sizes
     const FP3 lo(-1.0, 2.0, 0.5), hi(0.6, 2.8, 1.3);
     const Int3 cells(16, 8, 8), per(4, 2, 4);
-    EnsembleSupercells ens(lo, hi, cells, per);
+    EnsembleSupercells<ParticleArraySoA<Particle3d>> ens(lo, hi, cells, per);
     if (!(ens.getNumSupercells() == Int3(4, 4, 2)) || !(ens.getNumCells() == cells) ||
         !(ens.getMinPosition() == lo) || !(ens.getMaxPosition() == hi)) {
         std::printf("ensemble geometry\n");
@@ -222,7 +222,7 @@ int main() {
         fails++;
     }
     ens.add(below);
-    ParticleArraySoA some;
+    ParticleArraySoA<Particle3d> some;
     some.pushBack(below);
     ens.add(some[0]);   // from a reference, as pica's templated add
     try {

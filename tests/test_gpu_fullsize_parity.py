@@ -15,6 +15,15 @@ momenta and all nine fields within 1e-4 norm-wise relative error (max |a - b| /
 max |b|).  The two sides differ only in FP32 rounding: the GPU contracts a*b + c
 into fused multiply-adds and sums currents in exact fixed point, the oracle sums
 them in FP32 in its own order.
+
+Particles are compared slot by slot.  One rounding difference is allowed to move
+a particle, not to change it: an offset that rounds to the cell face (1.0) on one
+side and just below it on the other puts the particle in neighbouring cells of the
+same supercell, and the next resort (by cell) then shifts the slots of the
+particles between its two places by one.  Where a supercell's slots disagree, its
+particles are matched one to one by nearest neighbour in (position, momentum)
+instead, every match within the same tolerances; at most 1e-3 of the supercells
+may need this, and none may differ in count.
 """
 import os
 
@@ -24,7 +33,7 @@ import pytest
 import pica_gb300 as pg
 from oracle import pic_oracle as po
 from pica_gb300 import workloads
-from tests.helpers import periodic_err, rel_err
+from tests.helpers import rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -38,6 +47,35 @@ CASES = {
 def host_plasma(specs):
     parts = [pg.generate_plasma(s) for s in specs]
     return [np.concatenate([p[k] for p in parts]) for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species")]
+
+
+TOL_X, TOL_U = 1e-6, 1e-4
+
+
+def compare_ensembles(ps, pr, L, nsc):
+    """Slot by slot; supercells whose slots disagree are matched one to one by nearest
+    neighbour instead (see the module docstring)."""
+    umax = [max(np.max(np.abs(pr[k])), 1e-300) for k in ("ux", "uy", "uz")]
+    bad = np.zeros(len(ps["x"]), bool)
+    for d, k in enumerate(("x", "y", "z")):
+        dd = np.abs(ps[k] - pr[k])
+        bad |= np.minimum(dd, L[d] - dd) >= TOL_X * L[d]
+    for k, m in zip(("ux", "uy", "uz"), umax):
+        bad |= np.abs(ps[k] - pr[k]) >= TOL_U * m
+    if not bad.any():
+        return
+    key = pr["species"].astype(np.int64) * (1 << 32) + pr["supercell"]
+    groups = np.unique(key[bad])
+    assert len(groups) <= max(2, 1e-3 * nsc), f"{len(groups)} supercells disagree slot by slot"
+    from scipy.spatial import cKDTree
+    scale = np.array([TOL_X * L[0], TOL_X * L[1], TOL_X * L[2]] + [TOL_U * m for m in umax])
+    for g in groups:
+        idx = np.nonzero(key == g)[0]
+        a = np.stack([ps[k][idx] for k in ("x", "y", "z", "ux", "uy", "uz")], axis=1) / scale
+        b = np.stack([pr[k][idx] for k in ("x", "y", "z", "ux", "uy", "uz")], axis=1) / scale
+        dist, j = cKDTree(b).query(a, p=np.inf)   # tolerance units: every component below 1
+        assert np.all(dist < 1.0), f"supercell {g}: a particle has no counterpart within the tolerances"
+        assert len(np.unique(j)) == len(idx), f"supercell {g}: the nearest-neighbour match is not one to one"
 
 
 def cores():
@@ -79,10 +117,7 @@ def test_workload_at_its_own_size_matches_oracle(name):
     assert np.array_equal(ps["supercell"], pr["supercell"])
     assert np.array_equal(ps["species"], pr["species"])
     L = [sim["n"][d] * sim["h"][d] for d in range(3)]
-    for d, k in enumerate(("x", "y", "z")):
-        assert periodic_err(ps[k], pr[k], L[d]) < 1e-6, k
-    for k in ("ux", "uy", "uz"):
-        assert rel_err(ps[k], pr[k]) < 1e-4, k
+    compare_ensembles(ps, pr, L, nsc=int(np.prod(s.nsc)) * s.nspecies)
     del ps, pr
     fs, fo = s.fields(), o.get_fields()
     for c in range(9):
