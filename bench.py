@@ -46,7 +46,8 @@ PUSH_GRID_BYTES_PER_CELL_FP32 = 36  # E/B gather 6 words + J write 3 words, FP32
 
 def batched_measure(args, rank=0, world=1, dist=None):
     """The batching form on independent thermal plasmas of uneven size (members drawn
-    as in pica_gb300.workloads.batched_members; by default every edge halved).  Timed
+    as in pica_gb300.workloads.batched_members, at full size unless --batched-half),
+    with the supercell edge and resort cadence tuned on a sample of them.  Timed
     with the host clock: every batch step ends with a stream synchronisation (the
     host reads each member's migration flags).  On N ranks the plasmas are binned
     over the ranks by particle count (no communication on the data path); the job's
@@ -57,7 +58,26 @@ def batched_measure(args, rank=0, world=1, dist=None):
     import pica_gb300 as pg
     from pica_gb300 import autotune, workloads
     from pica_gb300.replicas import bin_members, job_throughput_binned
-    members = workloads.batched_members(count=args.batched, half=not args.batched_full)
+    full = not args.batched_half
+    # Supercell edge and resort cadence of the whole batch, tuned on a sample (the
+    # first 8 members of the draw; part of the warm-up).
+    def make_sample(sc, every):
+        sample = workloads.batched_members(count=min(8, args.batched), half=not full, resort_every=every,
+                                           supercell=sc)
+        sb = pg.Batch([m["sim"] for m in sample])
+        for sim, wl in zip(sb.members, sample):
+            sim.generate_plasma(wl["specs"])
+            sim.upload_fields([np.zeros(wl["sim"]["n"])] * 9)
+        sb.reorder()
+        return sb
+
+    cfg_tune = autotune.tune_batch_config(make_sample)
+    if dist is not None:   # every rank takes rank 0's choice
+        box = [cfg_tune]
+        dist.broadcast_object_list(box, src=0)
+        cfg_tune = box[0]
+    members = workloads.batched_members(count=args.batched, half=not full, resort_every=cfg_tune["resort_every"],
+                                        supercell=cfg_tune["supercell"])
     edges = [m["sim"]["n"][0] for m in members]
     nall = len(members)
     if world > 1:
@@ -77,7 +97,7 @@ def batched_measure(args, rank=0, world=1, dist=None):
         sim.upload_fields([np.zeros(wl["sim"]["n"])] * 9)
     b.reorder()
     npart = b.num_particles()
-    tune = autotune.tune_batch(b, steps=2)
+    tune = autotune.tune_batch(b, steps=3)
     best = min(tune, key=tune.get)
     b.step(3)
     if dist is not None:
@@ -101,9 +121,11 @@ def batched_measure(args, rank=0, world=1, dist=None):
     b.close()
     if rank != 0:
         return None
+    sc = "x".join(str(v) for v in cfg_tune["supercell"])
     return {"workload": f"{nall} thermal plasmas, edges {min(edges)}-{max(edges)} cells"
-                        f"{'' if args.batched_full else ' (member edges halved)'}, 16-128 ppc, CIC, Esirkepov, "
-                        "supercell 4^3, FP32 cell form",
+                        f"{'' if full else ' (member edges halved)'}, 16-128 ppc, CIC, Esirkepov, "
+                        f"supercell {sc} and resort every {cfg_tune['resort_every']} (autotuned), FP32 cell form",
+            "autotune": {k: v for k, v in cfg_tune.items()},
             "ranks": world, "members_on_rank0": len(members),
             "sharding": "plasmas binned over the ranks by particle count, no communication" if world > 1 else None,
             "particles": int(round(value * el / K)), "steps": K, "value": value, "unit": UNIT,
@@ -139,8 +161,9 @@ def parse():
                     help="in-supercell cell sort cadence (steps; default 2, two_stream 4)")
     ap.add_argument("--variant", type=int, default=-1, help="push-kernel launch variant (-1: autotune)")
     ap.add_argument("--batched", type=int, default=64, help="members of the batching-form run (0: skip)")
-    ap.add_argument("--batched-full", action="store_true",
-                    help="batching form at the full member sizes (grids 32^3-96^3, ~1.5e9 particles)")
+    ap.add_argument("--batched-half", action="store_true",
+                    help="batching form with every member edge halved (default: the full member sizes, grids "
+                         "32^3-96^3, 1.85e9 particles)")
     ap.add_argument("--batched-steps", type=int, default=10)
     ap.add_argument("--validate-steps", type=int, default=1000,
                     help="steps of the FP32-vs-FP64 error run on a 32^3 block (0: skip)")
@@ -499,7 +522,7 @@ def main():
     # Launch variant of the push kernel chosen on this workload (part of the warm-up).
     from pica_gb300 import autotune
     if args.variant < 0:
-        tune = autotune.tune_variant(sim, steps=1)
+        tune = autotune.tune_variant(sim, steps=3)
     else:
         sim.set_variant(args.variant)
         tune = {}

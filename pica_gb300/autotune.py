@@ -17,7 +17,8 @@ not bit for bit).
 ``tune_config`` searches the last two on a sample of the workload (a block of
 the grid with the same particles per cell) through a caller-supplied factory
 and caches the answer in a JSON file keyed by grid, particles per cell, form,
-shape and depositor.
+shape and depositor.  ``tune_batch_config`` does the same for the batching form
+(one supercell edge for every member, one cadence), on a sample of the members.
 """
 import json
 import os
@@ -34,9 +35,11 @@ def _timed_steps(sim, steps):
     return (time.perf_counter() - t) / steps
 
 
-def tune_variant(sim, steps=2):
+def tune_variant(sim, steps=3):
     """Time every launch variant for `steps` steps (the simulation advances by
-    variants x (steps + 1) steps) and keep the fastest.  Returns {variant: s/step}."""
+    variants x (steps + 1) steps) and keep the fastest.  Returns {variant: s/step}.
+    With a resort cadence of k, steps >= k times both the pushes right after a
+    resort (particles in cell order) and those between resorts."""
     _, count = sim.variant()
     times = {}
     for v in range(count):
@@ -94,4 +97,31 @@ def tune_config(make_sim, key, supercells=((4, 4, 4), (2, 2, 2)), cadences=(4, 8
         known[key] = best
         with open(cache, "w") as f:
             json.dump(known, f, indent=1)
+    return best
+
+
+def tune_batch_config(make_batch, supercells=((4, 4, 4), (2, 2, 2)), cadences=(2, 4, 8), steps=3):
+    """Supercell edge and resort cadence of the batching form.  make_batch(supercell,
+    resort_every) -> Batch with its members' particles and fields loaded (a sample of
+    the workload's members).  Each combination: the fastest push variant
+    (tune_batch), then `steps` timed steps after a resort-cadence's worth of warm-up
+    (so that sorted and unsorted pushes are both timed).  Returns the best
+    {"supercell", "resort_every", "variant", "s_per_step"} and every combination's
+    time under "tried"."""
+    best, tried = None, {}
+    for sc in supercells:
+        for every in cadences:
+            b = make_batch(sc, every)
+            vt = tune_batch(b, steps=2)
+            v = min(vt, key=vt.get)
+            b.set_options(use_graph=True, variant=v)
+            b.step(every)
+            t0 = time.perf_counter()
+            b.step(max(steps, every))
+            t = (time.perf_counter() - t0) / max(steps, every)
+            b.close()
+            tried[f"{sc[0]}x{sc[1]}x{sc[2]}/every{every}"] = t
+            if best is None or t < best["s_per_step"]:
+                best = {"supercell": list(sc), "resort_every": every, "variant": v, "s_per_step": t}
+    best["tried"] = tried
     return best

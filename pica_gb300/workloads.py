@@ -95,11 +95,12 @@ def config5():
     return weibel()
 
 
-def batched_members(count=64, seed_base=0, half=False, resort_every=4):
+def batched_members(count=64, seed_base=0, half=False, resort_every=4, supercell=(4, 4, 4)):
     """64 independent thermal plasmas: plasma k seeded by k; edge in {32, 36, ..., 96}, ppc in
     16..128, sigma in [0.02, 0.1].  Uses a SplitMix64 stream so the draws are reproducible.
     half=True halves every edge (rounded to a multiple of 4): the same members at 1/8 of
-    the cells."""
+    the cells.  `supercell` and `resort_every` apply to every member (the batching form
+    takes one supercell edge for all)."""
     def mix(z):
         z = (z + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
         z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
@@ -114,7 +115,7 @@ def batched_members(count=64, seed_base=0, half=False, resort_every=4):
             edge = 4 * round(edge / 8)
         ppc = 16 + r[1] % 113
         sigma = 0.02 + 0.08 * (r[2] >> 11) / float(1 << 53)
-        wl = thermal(n=(edge, edge, edge), ppc=ppc, sigma=sigma, supercell=(4, 4, 4), form=FORM_FP32_CELL,
+        wl = thermal(n=(edge, edge, edge), ppc=ppc, sigma=sigma, supercell=tuple(supercell), form=FORM_FP32_CELL,
                      shape=SHAPE_CIC, deposit=DEPOSIT_ESIRKEPOV, steps=200, seed=1000 + k)
         wl["sim"]["resort_every"] = resort_every
         out.append(wl)

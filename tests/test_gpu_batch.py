@@ -94,3 +94,28 @@ def test_batch_rejects_mixed_forms():
         pg.Batch([ok, dict(ok, form=pg.FORM_FP64_PLAIN)])
     with pytest.raises(pg.PicaError):
         pg.Batch([ok, dict(ok, supercell=(2, 2, 2))])
+
+
+def test_batch_config_tuner_picks_a_measured_combination():
+    """autotune.tune_batch_config on a small sample: every (supercell edge, cadence)
+    combination is built and timed, the choice is the fastest of them, and a batch
+    built with the choice steps."""
+    from pica_gb300 import autotune, workloads
+
+    def make(sc, every):
+        ms = workloads.batched_members(count=3, half=True, resort_every=every, supercell=sc)
+        b = pg.Batch([m["sim"] for m in ms])
+        for sim, wl in zip(b.members, ms):
+            sim.generate_plasma(wl["specs"])
+            sim.upload_fields([np.zeros(wl["sim"]["n"])] * 9)
+        return b
+
+    best = autotune.tune_batch_config(make, supercells=((4, 4, 4), (2, 2, 2)), cadences=(2, 4), steps=2)
+    assert set(best["tried"]) == {"4x4x4/every2", "4x4x4/every4", "2x2x2/every2", "2x2x2/every4"}
+    assert best["s_per_step"] == min(best["tried"].values())
+    b = make(tuple(best["supercell"]), best["resort_every"])
+    n0 = b.num_particles()
+    b.set_options(use_graph=True, variant=best["variant"])
+    b.step(3)
+    assert b.num_particles() == n0
+    b.close()
