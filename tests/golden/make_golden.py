@@ -7,7 +7,8 @@ mounted.  Inputs are seeded numpy draws and are
 stored in the fixture, so the GPU tests need neither the sources nor the
 generator.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py            (every fixture)
+        python tests/golden/make_golden.py config1    (the 32^3 x 50 ppc run only)
 """
 import os
 import sys
@@ -95,7 +96,37 @@ def case_1d(name, n, ppc, steps, seed, field_amp=1.0e3, u_sigma=0.1):
     print(out, npart, "particles")
 
 
-if __name__ == "__main__":
+def case_config1(name="config1_pica_100steps", steps=100, sample_every=1009):
+    """The plain FP64 electron plasma at its own size (tests.helpers.config1_plasma:
+    32^3 cells, 50 ppc, CIC, Boris, direct deposition, supercell 2^3) run 100 steps
+    through pica's headers.  The fixture keeps checksums, not the 1.6e6 particles: per
+    step the number of moves, sum of count * (s + 1) and sum over moves of src * 7 +
+    slot * 3 + dst; at the end the per-supercell counts, per field component the sum,
+    sum of |.| and sum of squares, per particle component the sum and sum of squares,
+    and every sample_every-th particle in ensemble order."""
+    from tests.helpers import config1_plasma, run_checksums
+    sim, p = config1_plasma()
+    o = Oracle(sim["n"], sim["supercell"], sim["h"], sim["dt"], kind="reference")
+    o.load(*[p[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species")])
+    o.set_fields([np.zeros(sim["n"])] * 9)
+    nm, cs, ms = run_checksums(lambda: o.step(1), o.counts, o.migrations, steps)
+    q = o.particles()
+    f = o.get_fields()
+    comps = ("x", "y", "z", "ux", "uy", "uz")
+    idx = np.arange(0, len(q["x"]), sample_every)
+    out = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(
+        out, steps=steps, n_moves=nm, count_sums=cs, move_sums=ms, counts=o.counts().astype(np.int32),
+        field_sum=np.array([np.sum(a) for a in f]), field_abs=np.array([np.sum(np.abs(a)) for a in f]),
+        field_sq=np.array([np.sum(a * a) for a in f]),
+        part_sum=np.array([np.sum(q[k]) for k in comps]), part_sq=np.array([np.sum(q[k] * q[k]) for k in comps]),
+        sample_index=idx, sample=np.stack([q[k][idx] for k in comps], axis=1), sample_supercell=q["supercell"][idx])
+    print(out, len(q["x"]), "particles,", int(nm.sum()), "moves over", steps, "steps")
+
+
+if __name__ == "__main__" and sys.argv[1:] == ["config1"]:
+    case_config1()
+elif __name__ == "__main__":
     # The plain FP64 32^3 electron plasma reduced to 8^3 x 4 ppc x 5 steps.
     case("cic_direct_8cube", (8, 8, 8), (2, 2, 2), 4, 5, seed=1)
     # Non-cubic grid and supercell, two species, non-zero initial E and B.
@@ -103,3 +134,5 @@ if __name__ == "__main__":
          species=((ME, E), (ME * 4.0, -E)), field_amp=2.0e3, u_sigma=0.08, resort_every=2)
     # pica's 1D classes: 32 cells x 4 ppc x 20 steps, non-zero initial E and B.
     case_1d("pica_1d_cic_direct", 32, 4, 20, seed=3)
+    # The plain FP64 32^3 x 50 ppc plasma itself, 100 steps (checksums and a sample).
+    case_config1()

@@ -95,3 +95,64 @@ def run_1d_golden(make_sim, g, sc=(4, 1, 1)):
     got = {k: p[k][order] for k in ("x", "ux", "uy", "uz")}
     ref = {k: g["out_" + k][ref_order] for k in ("x", "ux", "uy", "uz")}
     return f, got, ref
+
+
+def _splitmix(z):
+    """SplitMix64 output function (S. Vigna) on uint64 arrays (modular, exact)."""
+    with np.errstate(over="ignore"):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+CONFIG1_SEED = 20261203
+
+
+def config1_plasma():
+    """The plain FP64 electron plasma at its own size: 32^3 cells (h = the Debye length of
+    n0 = 1e18 cm^-3 at u_th = 0.05), 50 electrons per cell uniformly random in the cell,
+    momenta Maxwellian with sigma 0.05 (u = p / (m c)), dt = 0.5 Courant.  Drawn with
+    integer hashing and exact sums so that every machine gets the same bits: offsets
+    are 53-bit uniforms, each momentum component is the Irwin-Hall sum of twelve 32-bit
+    uniforms minus 6 (variance 1, support +-6) times sigma.  Returns (sim keyword
+    arguments, particle arrays in cell order)."""
+    n, ppc, sigma = (32, 32, 32), 50, 0.05
+    n0 = 1e18
+    wp = np.sqrt(4 * PI * n0 * E * E / ME)
+    h = 0.05 * C / wp
+    dt = 0.5 * h / (C * np.sqrt(3.0))
+    cells = np.repeat(np.arange(np.prod(n), dtype=np.uint64), ppc)
+    part = np.tile(np.arange(ppc, dtype=np.uint64), int(np.prod(n)))
+    base = _splitmix(np.uint64(CONFIG1_SEED)) ^ (cells << np.uint64(24)) ^ (part << np.uint64(8))
+    ijk = np.stack(np.unravel_index(cells.astype(np.int64), n), axis=1).astype(np.float64)
+    pos = np.empty((len(cells), 3))
+    for d in range(3):
+        u = (_splitmix(base ^ np.uint64(d)) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+        pos[:, d] = (ijk[:, d] + u) * h
+    mom = np.empty((len(cells), 3))
+    for d in range(3):
+        s = np.zeros(len(cells))
+        for k in range(12):
+            s += (_splitmix(base ^ np.uint64(16 + 12 * d + k)) >> np.uint64(32)).astype(np.float64) * 2.0 ** -32
+        mom[:, d] = sigma * (s - 6.0)
+    w = np.full(len(cells), n0 * h ** 3 / ppc)
+    sim = dict(n=n, h=(h, h, h), dt=dt, supercell=(2, 2, 2))
+    parts = dict(x=pos[:, 0], y=pos[:, 1], z=pos[:, 2], ux=mom[:, 0], uy=mom[:, 1], uz=mom[:, 2], w=w,
+                 species=np.zeros(len(cells), np.int32))
+    return sim, parts
+
+
+def run_checksums(step, counts, migrations, steps):
+    """Per-step checksums of a run: step(1) advances it, counts() and migrations() read
+    it.  Returns (number of moves per step, sum over supercells of count * (s + 1) per
+    step, sum over moves of src * 7 + slot * 3 + dst per step), all int64."""
+    nm, cs, ms = [], [], []
+    for _ in range(steps):
+        step()
+        c = np.asarray(counts(), np.int64).reshape(-1)
+        m = np.asarray(migrations(), np.int64).reshape(-1, 4)
+        nm.append(len(m))
+        cs.append(int(np.sum(c * (np.arange(len(c)) + 1))))
+        ms.append(int(np.sum(m[:, 1] * 7 + m[:, 2] * 3 + m[:, 3])) if len(m) else 0)
+    return np.array(nm, np.int64), np.array(cs, np.int64), np.array(ms, np.int64)

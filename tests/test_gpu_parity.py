@@ -328,3 +328,41 @@ def test_fp64_one_cell_thick_grid_matches_pica_1d_classes():
     for k in ("x", "ux", "uy", "uz"):
         assert rel_err(got[k], ref[k]) <= FP64_TOL, k
     sims[0].close()
+
+
+def test_fp64_config1_matches_pica_headers_fixture():
+    """The plain FP64 32^3 x 50 ppc plasma (CIC, Boris, direct, supercell 2^3) for 100
+    steps on the GPU against tests/golden/config1_pica_100steps.npz, which pica's own
+    headers made from the same plasma: number of moves, count checksum and move-list
+    checksum equal after every step, final per-supercell counts and the supercell of
+    every sampled particle equal; field and particle sums and the particle sample
+    within 1e-12 (norm-wise; only the order of the FP64 current sums differs)."""
+    from tests.helpers import config1_plasma, run_checksums
+    g = load_golden("config1_pica_100steps")
+    sim, p = config1_plasma()
+    s = pg.Simulation(**sim)
+    s.upload_particles(*[p[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species")])
+    s.upload_fields([np.zeros(sim["n"])] * 9)
+    s.record_migrations(True)
+    nm, cs, ms = run_checksums(lambda: s.step(1), s.counts, s.migrations, int(g["steps"]))
+    assert np.array_equal(nm, g["n_moves"])
+    assert np.array_equal(cs, g["count_sums"])
+    assert np.array_equal(ms, g["move_sums"])
+    assert np.array_equal(s.counts(), g["counts"])
+    q, f = s.particles(), s.fields()
+    comps = ("x", "y", "z", "ux", "uy", "uz")
+    # Sums are compared against the sum of magnitudes (a mean field or momentum near
+    # zero cancels, and its sum carries the rounding of the terms, not of the total).
+    fabs = [np.sum(np.abs(a)) for a in f]
+    pabs = [np.sum(np.abs(q[k])) for k in comps]
+    for name, got, want, scale in (("field_sum", [np.sum(a) for a in f], g["field_sum"], fabs),
+                                   ("field_abs", fabs, g["field_abs"], fabs),
+                                   ("field_sq", [np.sum(a * a) for a in f], g["field_sq"], g["field_sq"]),
+                                   ("part_sum", [np.sum(q[k]) for k in comps], g["part_sum"], pabs),
+                                   ("part_sq", [np.sum(q[k] * q[k]) for k in comps], g["part_sq"], g["part_sq"])):
+        for c, (a, b, sc) in enumerate(zip(got, want, scale)):
+            assert abs(a - b) <= FP64_TOL * abs(sc) or a == b, (name, c)
+    idx = g["sample_index"]
+    assert np.array_equal(q["supercell"][idx], g["sample_supercell"])
+    for c, k in enumerate(comps):
+        assert rel_err(q[k][idx], g["sample"][:, c]) < FP64_TOL, k

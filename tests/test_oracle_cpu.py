@@ -327,3 +327,60 @@ def test_oracle_matches_pica_1d_classes_live(n, sc, ppc, steps, seed, nspecies, 
     for k, ref in (("x", xo), ("ux", ux), ("uy", uy), ("uz", uz)):
         assert rel_err(p[k][mine], ref[theirs]) <= 1e-12, k
     assert np.array_equal(p["species"][mine], sp[theirs])
+
+
+def run_config1(kind, steps=100):
+    from tests.helpers import config1_plasma, run_checksums
+    sim, p = config1_plasma()
+    o = po.Oracle(sim["n"], sim["supercell"], sim["h"], sim["dt"], kind=kind)
+    o.load(*[p[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species")])
+    o.set_fields([np.zeros(sim["n"])] * 9)
+    return o, run_checksums(lambda: o.step(1), o.counts, o.migrations, steps)
+
+
+def test_config1_restatement_reproduces_pica_fixture():
+    """The plain FP64 32^3 x 50 ppc plasma, 100 steps, through the restatement: every
+    checksum of tests/golden/config1_pica_100steps.npz (made by pica's own headers)
+    equal bit for bit -- moves, counts and move lists every step, and the final
+    counts, fields, particle sums and particle sample."""
+    g = load_golden("config1_pica_100steps")
+    o, (nm, cs, ms) = run_config1("port", int(g["steps"]))
+    assert np.array_equal(nm, g["n_moves"]) and np.array_equal(cs, g["count_sums"])
+    assert np.array_equal(ms, g["move_sums"])
+    assert np.array_equal(o.counts(), g["counts"])
+    q, f = o.particles(), o.get_fields()
+    comps = ("x", "y", "z", "ux", "uy", "uz")
+    assert np.array_equal([np.sum(a) for a in f], g["field_sum"])
+    assert np.array_equal([np.sum(a * a) for a in f], g["field_sq"])
+    assert np.array_equal([np.sum(q[k]) for k in comps], g["part_sum"])
+    idx = g["sample_index"]
+    assert np.array_equal(np.stack([q[k][idx] for k in comps], axis=1), g["sample"])
+    assert np.array_equal(q["supercell"][idx], g["sample_supercell"])
+
+
+@pytest.mark.skipif(not REFERENCE_AVAILABLE, reason="pica sources not mounted here")
+def test_config1_restatement_matches_pica_headers_every_step():
+    """The same 100 steps side by side, the restatement against the harness over pica's
+    headers: per-supercell counts and migration lists equal after every step, particles
+    and fields equal bit for bit at the end."""
+    from tests.helpers import config1_plasma
+    po.build(reference=True)
+    sim, p = config1_plasma()
+    pair = []
+    for kind in ("port", "reference"):
+        o = po.Oracle(sim["n"], sim["supercell"], sim["h"], sim["dt"], kind=kind)
+        o.load(*[p[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species")])
+        o.set_fields([np.zeros(sim["n"])] * 9)
+        pair.append(o)
+    a, b = pair
+    for st in range(100):
+        a.step(1)
+        b.step(1)
+        assert np.array_equal(a.counts(), b.counts()), st
+        assert np.array_equal(a.migrations(), b.migrations()), st
+    pa, pb = a.particles(), b.particles()
+    for k in ("x", "y", "z", "ux", "uy", "uz", "w", "supercell"):
+        assert np.array_equal(pa[k], pb[k]), k
+    fa, fb = a.get_fields(), b.get_fields()
+    for c in range(9):
+        assert np.array_equal(fa[c], fb[c]), c
