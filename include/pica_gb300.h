@@ -149,6 +149,39 @@ int     pica_record_migrations(pica_ctx* ctx, int32_t enable);
 int64_t pica_num_migrations(pica_ctx* ctx);
 int     pica_get_migrations(pica_ctx* ctx, int32_t* species, int32_t* src, int32_t* slot, int32_t* dst);
 
+/* Domain decomposition of one plasma into slabs along x, each slab a context whose
+ * grid holds its own cells plus guard layers on both x faces (pica reserves the
+ * fields of a domain decomposition in Parameters.h:16-27 and plans one in
+ * README.md:21; it has none).  All device buffers below are the caller's device
+ * memory on this context's device; the copies run on the context stream.
+ *
+ * pica_field_slab: x-layers [x0, x0 + nx) of field component comp (0..8 = ex ey ez
+ *   bx by bz jx jy jz; double in the FP64 form, float in the FP32 form) to the
+ *   buffer (mode 0), from it (mode 1), or the buffer added to them (mode 2: the
+ *   current a neighbour deposited into its guard layers).  A run of x-layers is
+ *   contiguous (z fastest), so each call is one copy or one add kernel.  Allowed
+ *   while a migration is pending (after push_deposit the FP32 form's J holds the
+ *   step's current).
+ * pica_take_supercells: moves the particles of supercells [sc_begin, sc_end) of one
+ *   species out of the context: their slots, supercell by supercell, packed into
+ *   the component buffers dev[0..ncomp) (components as for pica_state_copy), and
+ *   those supercells left empty.  counts (host, may be NULL) receives each
+ *   supercell's number.  Returns the total (>= 0) or a status.  dev == NULL
+ *   returns the total and counts without taking anything.  PICA_ERR_LIMIT when the
+ *   total exceeds capacity; PICA_ERR_STATE for supercells holding dead slots
+ *   (the guard supercells a migration has just filled hold none).
+ * pica_append_to_supercells: appends counts[i] packed particles (the layout
+ *   pica_take_supercells writes) to the end of supercell sc_begin + i, shifting
+ *   the FP32 form's cell x (or the FP64 form's x) by dx_cells cells into this
+ *   context's frame.  PICA_ERR_OVERFLOW, with nothing written, when the arrivals
+ *   exceed a supercell's spare slots (the caller then re-uploads the ensemble).
+ * Both particle calls return PICA_ERR_STATE between push_deposit and migrate. */
+int     pica_field_slab(pica_ctx* ctx, int32_t comp, int32_t x0, int32_t nx, void* dev, int32_t mode);
+int64_t pica_take_supercells(pica_ctx* ctx, int32_t species, int32_t sc_begin, int32_t sc_end, void* const* dev,
+                             int64_t capacity, int32_t* counts);
+int     pica_append_to_supercells(pica_ctx* ctx, int32_t species, int32_t sc_begin, int32_t sc_end,
+                                  const int32_t* counts, const void* const* dev, int32_t dx_cells);
+
 /* Fields: f9 = {ex, ey, ez, bx, by, bz, jx, jy, jz}, each N^3 doubles.
  * Replaces element access YeeGrid::ex(i,j,k) ... (grid/YeeGrid.h:293-333). */
 int     pica_upload_fields(pica_ctx* ctx, const double* const* f9);
@@ -212,9 +245,15 @@ int     pica_field_energy(pica_ctx* ctx, double* out);
  * array of 16384 partial sums (128 KB), so grids above 512^3 = 134,217,728
  * nodes return PICA_ERR_LIMIT.  The first call on each device looks the
  * scratch address up (cudaGetSymbolAddress) with that device current: make it
- * before any stream capture.  Calls that can overlap on the GPU (other streams,
- * other host threads) race on the one scratch: serialise them.  Runs on
- * `stream` (a cudaStream_t, 0 for the legacy stream) and synchronises it.
+ * before any stream capture.  With CUDA's lazy module loading, the first call of
+ * each precision on a device also loads its kernels and the static array, which
+ * is an allocation: make one call per precision used at start-up; later calls
+ * allocate nothing.  The address is kept for the life of the process, so a
+ * process that resets the device (cudaDeviceReset) must not call this again.
+ * Calls that can overlap on the GPU (other streams, other host threads) race on
+ * the one scratch: serialise them.  Runs on `stream` (a cudaStream_t of the
+ * current device, 0 for the legacy stream) and synchronises it; an error left
+ * by earlier unrelated work surfaces here as PICA_ERR_CUDA.
  * No counterpart in the reference. */
 int     pica_field_energy_noalloc(const void* const* fields, int32_t fp64, const int32_t* n, const double* h,
                                   void* stream, double* out);

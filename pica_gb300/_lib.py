@@ -84,6 +84,9 @@ SIGNATURES = {
     "pica_push_deposit_chunked": (C.c_int, [_vp, _i32, C.POINTER(_vp)]),
     "pica_push_deposit_ranges": (C.c_int, [_vp, _i32, C.POINTER(_i32), C.POINTER(_vp)]),
     "pica_reorder": (C.c_int, [_vp]),
+    "pica_field_slab": (C.c_int, [_vp, _i32, _i32, _i32, _vp, _i32]),
+    "pica_take_supercells": (_i64, [_vp, _i32, _i32, _i32, C.POINTER(_vp), _i64, _ip]),
+    "pica_append_to_supercells": (C.c_int, [_vp, _i32, _i32, _i32, _ip, C.POINTER(_vp), _i32]),
     "pica_generate_plasma": (C.c_int, [_vp, C.POINTER(PicaPlasmaSpec), _i32]),
     "pica_plasma_count": (_i64, [C.POINTER(PicaPlasmaSpec)]),
     "pica_plasma_generate": (C.c_int, [C.POINTER(PicaPlasmaSpec), _i32] + [_dp] * 7 + [_ip]),

@@ -24,6 +24,7 @@ UNITS = [
     ("grid_kernels.cu", ["--fmad=false"]),
     ("noalloc.cu", ["--fmad=false"]),
     ("plasma_gen.cu", ["--fmad=false"]),
+    ("domain_kernels.cu", ["--fmad=false"]),
 ]
 
 

@@ -1147,6 +1147,118 @@ int pica_get_migrations(pica_ctx* ctx, int32_t* species, int32_t* src, int32_t* 
     return PICA_OK;
 }
 
+int pica_field_slab(pica_ctx* ctx, int32_t comp, int32_t x0, int32_t nx, void* dev, int32_t mode) {
+    if (!ctx || !dev || comp < 0 || comp > 8 || mode < 0 || mode > 2) return PICA_ERR_INVALID;
+    const pica_config& c = ctx->cfg;
+    if (x0 < 0 || nx < 0 || x0 + nx > c.n[0]) return fail(ctx, PICA_ERR_INVALID, "x-layers outside the grid");
+    const size_t es = ctx->fp64 ? 8 : 4;
+    const int64_t layer = (int64_t)c.n[1] * c.n[2];
+    char* f = static_cast<char*>(ctx->f[comp]) + (size_t)x0 * (size_t)layer * es;
+    const int64_t n = (int64_t)nx * layer;
+    if (mode == 0) CK(cudaMemcpyAsync(dev, f, (size_t)n * es, cudaMemcpyDeviceToDevice, ctx->stream));
+    else if (mode == 1) CK(cudaMemcpyAsync(f, dev, (size_t)n * es, cudaMemcpyDeviceToDevice, ctx->stream));
+    else {
+        CKL(launchAddSlab(ctx->fp64, f, dev, n, ctx->stream));
+        ctx->launches++;
+    }
+    return PICA_OK;
+}
+
+// Counts and live counts of supercells [b, e) of species q, read back to the host.
+static int rangeCounts(pica_ctx* ctx, int q, int b, int e, std::vector<int32_t>& cnt, std::vector<int32_t>& alive) {
+    SpeciesState& S = ctx->sp[q];
+    cnt.resize(e - b);
+    alive.resize(e - b);
+    CK(cudaMemcpyAsync(cnt.data(), S.d_count + b, (size_t)(e - b) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(alive.data(), S.d_alive + b, (size_t)(e - b) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PICA_OK;
+}
+
+int64_t pica_take_supercells(pica_ctx* ctx, int32_t species, int32_t sc_begin, int32_t sc_end, void* const* dev,
+                             int64_t capacity, int32_t* counts) {
+    if (!ctx || species < 0 || species >= ctx->cfg.nspecies || sc_begin < 0 || sc_end < sc_begin ||
+        sc_end > ctx->nscTot)
+        return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "take while a migration is pending");
+    SpeciesState& S = ctx->sp[species];
+    const int m = sc_end - sc_begin;
+    std::vector<int32_t> cnt, alive;
+    int rc = rangeCounts(ctx, species, sc_begin, sc_end, cnt, alive);
+    if (rc) return rc;
+    std::vector<int64_t> off(m);
+    int64_t tot = 0;
+    for (int i = 0; i < m; i++) {
+        if (cnt[i] != alive[i]) return fail(ctx, PICA_ERR_STATE, "supercells with dead slots: reorder first");
+        off[i] = tot;
+        tot += cnt[i];
+    }
+    if (counts) std::copy(cnt.begin(), cnt.end(), counts);
+    if (!dev) return tot;   // sizes only
+    if (tot > capacity) return fail(ctx, PICA_ERR_LIMIT, "the buffers hold fewer slots than the supercells");
+    for (int k = 0; k < ctx->ncomp; k++)
+        if (!dev[k]) return PICA_ERR_INVALID;
+    // From pageable memory: staged before the call returns, ordered on the stream.
+    CK(cudaMemcpyAsync(S.d_outOff + sc_begin, off.data(), (size_t)m * 8, cudaMemcpyHostToDevice, ctx->stream));
+    for (int k = 0; k < ctx->ncomp; k++) {
+        CKL(launchPackCopy(S.buf[ctx->cur][k], dev[k], S.d_start, S.d_count, S.d_outOff, sc_begin, sc_end,
+                           (int)(ctx->compBytes[k] / 4), true, ctx->stream));
+        ctx->launches++;
+    }
+    CK(cudaMemsetAsync(S.d_count + sc_begin, 0, (size_t)m * 4, ctx->stream));
+    CK(cudaMemsetAsync(S.d_alive + sc_begin, 0, (size_t)m * 4, ctx->stream));
+    ctx->epoch++;
+    return tot;
+}
+
+int pica_append_to_supercells(pica_ctx* ctx, int32_t species, int32_t sc_begin, int32_t sc_end,
+                              const int32_t* counts, const void* const* dev, int32_t dx_cells) {
+    if (!ctx || !counts || species < 0 || species >= ctx->cfg.nspecies || sc_begin < 0 || sc_end < sc_begin ||
+        sc_end > ctx->nscTot)
+        return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "append while a migration is pending");
+    SpeciesState& S = ctx->sp[species];
+    const int m = sc_end - sc_begin;
+    int64_t tot = 0;
+    for (int i = 0; i < m; i++) {
+        if (counts[i] < 0) return PICA_ERR_INVALID;
+        tot += counts[i];
+    }
+    if (tot == 0) return PICA_OK;
+    if (!dev) return PICA_ERR_INVALID;
+    for (int k = 0; k < ctx->ncomp; k++)
+        if (!dev[k]) return PICA_ERR_INVALID;
+    std::vector<int32_t> cnt, alive;
+    int rc = rangeCounts(ctx, species, sc_begin, sc_end, cnt, alive);
+    if (rc) return rc;
+    std::vector<int64_t> off(m), st(m);
+    int64_t o = 0;
+    for (int i = 0; i < m; i++) {
+        if ((int64_t)cnt[i] + counts[i] > S.h_cap[sc_begin + i])
+            return fail(ctx, PICA_ERR_OVERFLOW, "arrivals exceed the spare slots of a supercell");
+        off[i] = o;
+        o += counts[i];
+        st[i] = S.h_start[sc_begin + i] + cnt[i];
+        cnt[i] += counts[i];
+        alive[i] += counts[i];
+    }
+    CK(cudaMemcpyAsync(S.d_outOff + sc_begin, off.data(), (size_t)m * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.d_start2 + sc_begin, st.data(), (size_t)m * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.d_cap2 + sc_begin, counts, (size_t)m * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CKL(launchAppendPositions(ctx->fp64, dev[0], S.buf[ctx->cur][0], S.d_start2, S.d_cap2, S.d_outOff, sc_begin,
+                              sc_end, dx_cells, ctx->cfg.n[0], dx_cells * ctx->cfg.h[0], ctx->stream));
+    ctx->launches++;
+    for (int k = 1; k < ctx->ncomp; k++) {
+        CKL(launchPackCopy(dev[k], S.buf[ctx->cur][k], S.d_start2, S.d_cap2, S.d_outOff, sc_begin, sc_end,
+                           (int)(ctx->compBytes[k] / 4), false, ctx->stream));
+        ctx->launches++;
+    }
+    CK(cudaMemcpyAsync(S.d_count + sc_begin, cnt.data(), (size_t)m * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(S.d_alive + sc_begin, alive.data(), (size_t)m * 4, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->epoch++;
+    return PICA_OK;
+}
+
 int pica_reorder(pica_ctx* ctx) {
     if (!ctx) return PICA_ERR_INVALID;
     if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "reorder between push_deposit and migrate");

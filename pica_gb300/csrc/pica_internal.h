@@ -297,6 +297,14 @@ int launchGenerate(const GenArgs& a, int nscTot, cudaStream_t s);
 // (src = image, dst = slot array).
 int launchPackCopy(const void* src, void* dst, const int64_t* start, const int32_t* count, const int64_t* off,
                    int scBegin, int scEnd, int words, bool gather, cudaStream_t s);
+// Domain decomposition (domain_kernels.cu): dst += src over n elements (double if fp64
+// else float); the position component of packed arrivals into supercells [scBegin,
+// scEnd) (slots from start[s], count[s] of them from image offset off[s]), the FP32
+// form's cell x shifted by dxCells (wrapped into [0, nx)), the FP64 form's x by dxLength.
+int launchAddSlab(bool fp64, void* dst, const void* src, int64_t n, cudaStream_t s);
+int launchAppendPositions(bool fp64, const void* src, void* dst, const int64_t* start, const int32_t* count,
+                          const int64_t* off, int scBegin, int scEnd, int dxCells, int nx, double dxLength,
+                          cudaStream_t s);
 // Gauss residual: max |div E - 4 pi (rho + bg)| and max |rho|; partial: 2*kReduceBlocks doubles.
 int launchGauss(bool fp64, void* const* f, const double* rho, const int* n, const double* h, double bg,
                 double* partial, double* out2, cudaStream_t s);

@@ -544,42 +544,52 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                         for (int d = 0; d < 3; d++) { ln[d] = lc[d]; on[d] = o[d]; }
                     }
                     const float kq[3] = {kqs[0] * wgt, kqs[1] * wgt, kqs[2] * wgt};
-                    // Old and new shapes on the rho-lattice nodes lc-1 .. lc+1 of the old cell (used
-                    // when the particle stays in its cell).  TSC: weights of o - 1/2 on all three.
-                    // CIC: nodes base, base+1 with base = lc or lc-1 by o >= 1/2, the third weight 0.
-                    float w0[3][NWn], w1[3][NWn];
-#pragma unroll
-                    for (int d = 0; d < 3; d++) {
-                        if constexpr (SHAPE == PICA_SHAPE_TSC) {
-                            tscWeights(o[d] - 0.5f, w0[d]);
-                            tscWeights(on[d] - 0.5f, w1[d]);
-                        } else {
-                            const bool h0 = o[d] >= 0.5f, h1 = on[d] >= 0.5f;
-                            const float d0 = h0 ? o[d] - 0.5f : o[d] + 0.5f, d1 = h1 ? on[d] - 0.5f : on[d] + 0.5f;
-                            w0[d][0] = h0 ? 0.0f : 1.0f - d0; w0[d][1] = h0 ? 1.0f - d0 : d0; w0[d][2] = h0 ? d0 : 0.0f;
-                            w1[d][0] = h1 ? 0.0f : 1.0f - d1; w1[d][1] = h1 ? 1.0f - d1 : d1; w1[d][2] = h1 ? d1 : 0.0f;
-                        }
-                    }
                     const bool sameWindow = !lone && inRange && ln[0] == lc[0] && ln[1] == lc[1] && ln[2] == lc[2];
                     if (sameWindow) {
-                        // a = S0, dd = S1 - S0; p = a + d/2, q = a/2 + d/3; yz = a_y p_z + d_y q_z.
+                        // Old shape S0 and its change dd = S1 - S0 on the rho-lattice nodes lc-1 ..
+                        // lc+1 of the cell.  TSC: weights of o - 1/2 on all three.  CIC: nodes base,
+                        // base+1 with base = lc or lc-1 by o >= 1/2, the third weight 0.  dd is
+                        // written in factored form from the displacement D = on - o, not as the
+                        // difference of two shapes: a step moves a particle by about 1% of a cell,
+                        // and S1 - S0 in FP32 would keep only the bits of D above 2^-24 of the
+                        // weights, a few 1e-6 of dd (the charge-conservation residual).
+                        // p = a + d/2, q = a/2 + d/3; yz = a_y p_z + d_y q_z.
                         float aa[3][NWn], dd[3][NWn], pp[3][NWn], qq[3][NWn];
 #pragma unroll
-                        for (int d = 0; d < 3; d++)
+                        for (int d = 0; d < 3; d++) {
+                            const float D = on[d] - o[d];
+                            if constexpr (SHAPE == PICA_SHAPE_TSC) {
+                                const float dl = o[d] - 0.5f;
+                                tscWeights(dl, aa[d]);
+                                dd[d][0] = D * (0.5f * D + dl - 0.5f);
+                                dd[d][1] = -D * (2.0f * dl + D);
+                                dd[d][2] = D * (0.5f + dl + 0.5f * D);
+                            } else {
+                                const bool h0 = o[d] >= 0.5f, h1 = on[d] >= 0.5f;
+                                const float d0 = h0 ? o[d] - 0.5f : o[d] + 0.5f;
+                                aa[d][0] = h0 ? 0.0f : 1.0f - d0; aa[d][1] = h0 ? 1.0f - d0 : d0; aa[d][2] = h0 ? d0 : 0.0f;
+                                // Same half: the shape slides by D.  Across the centre: a = o - 1/2 and
+                                // b = on - 1/2 are both near zero and exact.
+                                const float a = o[d] - 0.5f, b = on[d] - 0.5f;
+                                if (h0 == h1) {
+                                    dd[d][0] = h0 ? 0.0f : -D; dd[d][1] = h0 ? -D : D; dd[d][2] = h0 ? D : 0.0f;
+                                } else {
+                                    dd[d][0] = h1 ? a : -b; dd[d][2] = h1 ? b : -a; dd[d][1] = h1 ? -(a + b) : a + b;
+                                }
+                            }
 #pragma unroll
                             for (int k = 0; k < NWn; k++) {
-                                aa[d][k] = w0[d][k];
-                                dd[d][k] = w1[d][k] - w0[d][k];
                                 pp[d][k] = aa[d][k] + 0.5f * dd[d][k];
                                 qq[d][k] = 0.5f * aa[d][k] + (float)kThird * dd[d][k];
                             }
-                        // e[d][f]: -(q w) h_d/dt times the running sum of dd over faces 0..f.
+                        }
+                        // e[d][f]: -(q w) h_d/dt times the running sum of dd over faces 0..f, that is
+                        // dd[0] and dd[0] + dd[1] = -dd[2] (the sum of dd is zero; no cancellation).
                         float e[3][NWn - 1];
 #pragma unroll
                         for (int d = 0; d < 3; d++) {
-                            float run = 0.0f;
-#pragma unroll
-                            for (int f = 0; f < NWn - 1; f++) { run += dd[d][f]; e[d][f] = kq[d] * run; }
+                            e[d][0] = kq[d] * dd[d][0];
+                            e[d][1] = -(kq[d] * dd[d][2]);
                         }
                         // Jx and Jy share the z factors (pp2, qq2): their terms and sums go in
                         // packed FP32x2 pairs (each half rounds as the scalar form); Jz alone.

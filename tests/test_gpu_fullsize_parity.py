@@ -13,17 +13,23 @@ exactly equal.  At the end: the supercell and species of every particle exactly
 equal (so the ensemble order is the same); positions within 1e-6 of the box edge;
 momenta and all nine fields within 1e-4 norm-wise relative error (max |a - b| /
 max |b|).  The two sides differ only in FP32 rounding: the GPU contracts a*b + c
-into fused multiply-adds and sums currents in exact fixed point, the oracle sums
-them in FP32 in its own order.
+into fused multiply-adds, takes 1/sqrt from the hardware and sums currents in
+exact fixed point, the oracle rounds every operation and sums currents in FP32.
 
-Particles are compared slot by slot.  One rounding difference is allowed to move
-a particle, not to change it: an offset that rounds to the cell face (1.0) on one
-side and just below it on the other puts the particle in neighbouring cells of the
-same supercell, and the next resort (by cell) then shifts the slots of the
-particles between its two places by one.  Where a supercell's slots disagree, its
-particles are matched one to one by nearest neighbour in (position, momentum)
-instead, every match within the same tolerances; at most 1e-3 of the supercells
-may need this, and none may differ in count.
+One rounding difference is allowed to move a particle, not to change it: an
+offset that rounds to the cell face (1.0) on one side and just below it on the
+other (a tie) puts the particle in neighbouring cells.  Measured on the two-stream
+block (1.05e8 particles): one such particle in its fifth step, x = 99.99999994
+cells on the GPU and 100.0 in the oracle, which is also a supercell face.  So:
+  * counts and migration lists are compared exactly until a step where the counts
+    differ; a difference must be a tie: supercells that differ come in pairs of
+    +1 / -1, at most TIES of them over the run;
+  * after the first tie, the migration lists are compared as the number of moves
+    per (species, source, destination), with the same budget;
+  * particles are compared slot by slot; where a supercell's slots disagree (a tie
+    particle, or the slots a later resort shifted around it), its particles and
+    those of the supercells around it are matched one to one by nearest neighbour in
+    (position, momentum) instead, every match within the tolerances above.
 """
 import os
 
@@ -50,32 +56,65 @@ def host_plasma(specs):
 
 
 TOL_X, TOL_U = 1e-6, 1e-4
+TIES = 8   # face ties allowed over a run (measured: 0 or 1)
 
 
-def compare_ensembles(ps, pr, L, nsc):
-    """Slot by slot; supercells whose slots disagree are matched one to one by nearest
-    neighbour instead (see the module docstring)."""
+def compare_ensembles(ps, pr, L, nsc3):
+    """Slot by slot; the supercells whose slots disagree are matched one to one by
+    nearest neighbour instead, together with their neighbours (see the module
+    docstring)."""
+    comps = ("x", "y", "z", "ux", "uy", "uz")
     umax = [max(np.max(np.abs(pr[k])), 1e-300) for k in ("ux", "uy", "uz")]
-    bad = np.zeros(len(ps["x"]), bool)
-    for d, k in enumerate(("x", "y", "z")):
-        dd = np.abs(ps[k] - pr[k])
-        bad |= np.minimum(dd, L[d] - dd) >= TOL_X * L[d]
-    for k, m in zip(("ux", "uy", "uz"), umax):
-        bad |= np.abs(ps[k] - pr[k]) >= TOL_U * m
+    same_len = len(ps["x"]) == len(pr["x"])
+    bad = np.ones(len(pr["x"]), bool) if not same_len else np.zeros(len(pr["x"]), bool)
+    if same_len:
+        bad |= ps["supercell"] != pr["supercell"]
+        bad |= ps["species"] != pr["species"]
+        for d, k in enumerate(("x", "y", "z")):
+            dd = np.abs(ps[k] - pr[k])
+            bad |= np.minimum(dd, L[d] - dd) >= TOL_X * L[d]
+        for k, m in zip(("ux", "uy", "uz"), umax):
+            bad |= np.abs(ps[k] - pr[k]) >= TOL_U * m
     if not bad.any():
-        return
-    key = pr["species"].astype(np.int64) * (1 << 32) + pr["supercell"]
-    groups = np.unique(key[bad])
-    assert len(groups) <= max(2, 1e-3 * nsc), f"{len(groups)} supercells disagree slot by slot"
+        return 0
+    groups = np.unique(pr["supercell"][bad])
+    nsc = int(np.prod(nsc3))
+    assert len(groups) <= max(8, 1e-3 * nsc), f"{len(groups)} supercells disagree slot by slot"
+    # the disagreeing supercells and their 26 neighbours (a tie particle sits across a face)
+    sx, sy, sz = np.unravel_index(groups, nsc3)
+    near = set()
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dz in (-1, 0, 1):
+                near.update(np.ravel_multi_index(((sx + dx) % nsc3[0], (sy + dy) % nsc3[1], (sz + dz) % nsc3[2]),
+                                                 nsc3).tolist())
+    near = np.array(sorted(near))
     from scipy.spatial import cKDTree
     scale = np.array([TOL_X * L[0], TOL_X * L[1], TOL_X * L[2]] + [TOL_U * m for m in umax])
-    for g in groups:
-        idx = np.nonzero(key == g)[0]
-        a = np.stack([ps[k][idx] for k in ("x", "y", "z", "ux", "uy", "uz")], axis=1) / scale
-        b = np.stack([pr[k][idx] for k in ("x", "y", "z", "ux", "uy", "uz")], axis=1) / scale
-        dist, j = cKDTree(b).query(a, p=np.inf)   # tolerance units: every component below 1
-        assert np.all(dist < 1.0), f"supercell {g}: a particle has no counterpart within the tolerances"
-        assert len(np.unique(j)) == len(idx), f"supercell {g}: the nearest-neighbour match is not one to one"
+    ia = np.nonzero(np.isin(ps["supercell"], near))[0]
+    ib = np.nonzero(np.isin(pr["supercell"], near))[0]
+    assert len(ia) == len(ib), "the particles around the disagreeing supercells differ in number"
+    for q in np.unique(pr["species"][ib]):
+        ja, jb = ia[ps["species"][ia] == q], ib[pr["species"][ib] == q]
+        assert len(ja) == len(jb)
+        # In tolerance units (every component of a match below 1); positions periodic
+        # (a tie at a domain face puts the particle at L - eps on one side, 0 on the other).
+        box = np.array([1.0 / TOL_X] * 3 + [1e12] * 3)
+        shift = np.array([0.0] * 3 + [0.5e12] * 3)
+        a = np.mod(np.stack([ps[k][ja] for k in comps], axis=1) / scale + shift, box)
+        b = np.mod(np.stack([pr[k][jb] for k in comps], axis=1) / scale + shift, box)
+        dist, j = cKDTree(b, boxsize=box).query(a, p=np.inf)
+        assert np.all(dist < 1.0), "a particle has no counterpart within the tolerances"
+        assert len(np.unique(j)) == len(ja), "the nearest-neighbour match is not one to one"
+    return len(groups)
+
+
+def move_counts(m):
+    """Number of moves per (species, source, destination)."""
+    if len(m) == 0:
+        return {}
+    keys, n = np.unique(m[:, [0, 1, 3]], axis=0, return_counts=True)
+    return {tuple(k): int(c) for k, c in zip(keys.tolist(), n.tolist())}
 
 
 def cores():
@@ -103,21 +142,30 @@ def test_workload_at_its_own_size_matches_oracle(name):
     o.set_fields(zeros)
     assert np.array_equal(s.counts(), o.counts())
     s.record_migrations(True)
-    moved = 0
+    moved, ties = 0, 0
     for st in range(steps):
         s.step(1)
         o.step(1)
-        assert np.array_equal(s.counts(), o.counts()), f"counts differ after step {st + 1}"
-        m = s.migrations()
-        assert np.array_equal(m, o.migrations()), f"migration lists differ after step {st + 1}"
+        cs, co = s.counts(), o.counts()
+        m, mo = s.migrations(), o.migrations()
         moved += len(m)
+        if ties == 0 and np.array_equal(cs, co):
+            assert np.array_equal(m, mo), f"migration lists differ after step {st + 1}"
+            continue
+        d = (cs - co).reshape(-1)
+        nd = int(np.count_nonzero(d))
+        ties += nd // 2
+        assert np.all(np.abs(d) <= 1) and int(d.sum()) == 0 and nd % 2 == 0, f"counts differ after step {st + 1}"
+        assert ties <= TIES, f"{ties} ties by step {st + 1}"
+        ma, mb = move_counts(m), move_counts(mo)
+        off = sum(abs(ma.get(k, 0) - mb.get(k, 0)) for k in set(ma) | set(mb))
+        assert off <= 2 * TIES, f"moves differ by {off} after step {st + 1}"
     assert moved > 0
     s.record_migrations(False)
     ps, pr = s.particles(), o.particles()
-    assert np.array_equal(ps["supercell"], pr["supercell"])
-    assert np.array_equal(ps["species"], pr["species"])
     L = [sim["n"][d] * sim["h"][d] for d in range(3)]
-    compare_ensembles(ps, pr, L, nsc=int(np.prod(s.nsc)) * s.nspecies)
+    nsc3 = tuple(sim["n"][d] // sim["supercell"][d] for d in range(3))
+    compare_ensembles(ps, pr, L, nsc3)
     del ps, pr
     fs, fo = s.fields(), o.get_fields()
     for c in range(9):

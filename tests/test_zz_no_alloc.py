@@ -61,6 +61,16 @@ def test_noalloc_field_energy_matches_context_entry_point(form):
     host = sum(np.sum(np.asarray(f, dtype=npdt).astype(np.float64) ** 2) for f in f9[:6])
     assert rel_err(e1, host * h[0] * h[1] * h[2] / (8.0 * PI)) < 1e-12
     assert sim.field_energy() == ref     # the context entry point is unchanged by the static scratch
+    # After the first calls (which load the kernels), a call allocates nothing: the
+    # device's free memory and the caching allocator's counters stay as they were.
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    stats0 = torch.cuda.memory_stats().get("allocation.all.allocated", 0)
+    rc3, e3 = _call(fn, dev, fp64, n, h, stream)
+    torch.cuda.synchronize()
+    assert rc3 == 0 and e3 == e1
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_stats().get("allocation.all.allocated", 0) == stats0
     sim.close()
 
 
