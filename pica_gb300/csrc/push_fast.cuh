@@ -51,20 +51,39 @@ __device__ __forceinline__ int windowIdx(int TT, int T1, int T2, const int* b, i
 
 // Boris rotation of BorisPusher.h:33-43 in FP32 with the hardware reciprocal
 // square root and fast division (a few ulp; the FP32 form is checked against
-// the FP32 oracle within 1e-4).  Returns 1/gamma of the new u.
+// the FP32 oracle within 1e-4).  Returns 1/gamma of the new u.  This unit is
+// compiled without implicit contraction, so every multiply-add below is written
+// out (_rn intrinsics and fused multiply-adds): each instantiation of the push --
+// launch variants, the batching form -- then rounds alike.
+__device__ __forceinline__ float sumsq3(const float* v) {
+    return __fmaf_rn(v[2], v[2], __fmaf_rn(v[1], v[1], __fmul_rn(v[0], v[0])));
+}
+// a*b - c*d as one fused multiply-add on a rounded product.
+__device__ __forceinline__ float mulSub(float a, float b, float c, float d) { return __fmaf_rn(a, b, -__fmul_rn(c, d)); }
+
 __device__ __forceinline__ float borisFast(float ec, const float* eb, float* u) {
-    const float em[3] = {eb[0] * ec, eb[1] * ec, eb[2] * ec};
-    const float um[3] = {u[0] + em[0], u[1] + em[1], u[2] + em[2]};
-    const float tc = ec * rsqrtf(1.0f + (um[0] * um[0] + um[1] * um[1] + um[2] * um[2]));
-    const float t[3] = {eb[3] * tc, eb[4] * tc, eb[5] * tc};
-    const float up[3] = {um[0] + (um[1] * t[2] - um[2] * t[1]), um[1] + (um[2] * t[0] - um[0] * t[2]),
-                         um[2] + (um[0] * t[1] - um[1] * t[0])};
-    const float sc = __fdividef(2.0f, 1.0f + (t[0] * t[0] + t[1] * t[1] + t[2] * t[2]));
-    const float s[3] = {t[0] * sc, t[1] * sc, t[2] * sc};
-    u[0] = um[0] + (up[1] * s[2] - up[2] * s[1]) + em[0];
-    u[1] = um[1] + (up[2] * s[0] - up[0] * s[2]) + em[1];
-    u[2] = um[2] + (up[0] * s[1] - up[1] * s[0]) + em[2];
-    return rsqrtf(1.0f + (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
+    const float em[3] = {__fmul_rn(eb[0], ec), __fmul_rn(eb[1], ec), __fmul_rn(eb[2], ec)};
+    const float um[3] = {__fadd_rn(u[0], em[0]), __fadd_rn(u[1], em[1]), __fadd_rn(u[2], em[2])};
+    const float tc = __fmul_rn(ec, rsqrtf(__fadd_rn(1.0f, sumsq3(um))));
+    const float t[3] = {__fmul_rn(eb[3], tc), __fmul_rn(eb[4], tc), __fmul_rn(eb[5], tc)};
+    const float up[3] = {__fadd_rn(um[0], mulSub(um[1], t[2], um[2], t[1])),
+                         __fadd_rn(um[1], mulSub(um[2], t[0], um[0], t[2])),
+                         __fadd_rn(um[2], mulSub(um[0], t[1], um[1], t[0]))};
+    const float sc = __fdividef(2.0f, __fadd_rn(1.0f, sumsq3(t)));
+    const float s[3] = {__fmul_rn(t[0], sc), __fmul_rn(t[1], sc), __fmul_rn(t[2], sc)};
+    u[0] = __fadd_rn(__fadd_rn(um[0], mulSub(up[1], s[2], up[2], s[1])), em[0]);
+    u[1] = __fadd_rn(__fadd_rn(um[1], mulSub(up[2], s[0], up[0], s[2])), em[1]);
+    u[2] = __fadd_rn(__fadd_rn(um[2], mulSub(up[0], s[1], up[1], s[0])), em[2]);
+    return rsqrtf(__fadd_rn(1.0f, sumsq3(u)));
+}
+
+// TSC weights of the three nodes around an offset d in [-1/2, 1/2] (FP32, the
+// roundings written out): 1/2 (1/2 - d)^2, 3/4 - d^2, 1/2 (1/2 + d)^2.
+__device__ __forceinline__ void tscWeightsF(float d, float* w) {
+    const float a = __fsub_rn(0.5f, d), b = __fadd_rn(0.5f, d);
+    w[0] = __fmul_rn(0.5f, __fmul_rn(a, a));
+    w[1] = __fmaf_rn(-d, d, 0.75f);
+    w[2] = __fmul_rn(0.5f, __fmul_rn(b, b));
 }
 
 // Two field components gathered together with packed FP32x2 arithmetic (each half
@@ -109,56 +128,50 @@ __device__ __forceinline__ float pickN(const float* a, int i) {
     return v;
 }
 
-// esirkepov() (push_kernels.cuh) in FP32 with the loop over the transverse node
-// pair rolled: the same values from the same expressions, in about a tenth of
+// esirkepov() (push_kernels.cuh) in FP32 with the loops over transverse node
+// pairs rolled: the same values from the same expressions, in about a tenth of
 // the code.  The general window runs once per queue drain, straight through, so
 // its unrolled form is fetched from the instruction cache hierarchy at every
-// call; the selects of the rolled loop cost less than those fetch stalls.  A node
-// pair outside both shapes (zero transverse factor) adds nothing and is skipped.
+// call; the selects of the rolled loops cost less than those fetch stalls.
+// len[d] is the number of window nodes the two shapes cover along d (NW, or NW-1
+// when the particle stays in its cell along d): pairs and faces beyond it carry
+// exactly zero and are not visited, nor is a pair whose transverse factor is zero.
 template <int NW, typename Tile>
 __device__ __forceinline__ void esirkepovRolled(const Tile& jt, int TT, int T1, int T2, const int* b,
-                                                const float (*s0)[NW], const float (*s1)[NW], const float* k) {
+                                                const float (*s0)[NW], const float (*s1)[NW], const float* k,
+                                                const int* len) {
     float ds[3][NW];
 #pragma unroll
     for (int d = 0; d < 3; d++)
 #pragma unroll
-        for (int i = 0; i < NW; i++) ds[d][i] = s1[d][i] - s0[d][i];
+        for (int i = 0; i < NW; i++) ds[d][i] = __fsub_rn(s1[d][i], s0[d][i]);
     const float hf = 0.5f, th = (float)kThird;
+    // Transverse factor a b + (d_a b + a d_b) / 2 + d_a d_b / 3 of a node pair.
+    auto factor = [hf, th](float a, float da, float b, float db) {
+        return __fmaf_rn(th, __fmul_rn(da, db), __fmaf_rn(hf, __fmaf_rn(da, b, __fmul_rn(a, db)), __fmul_rn(a, b)));
+    };
+    // Component c along dimension c: transverse dimensions t1 < t2, faces along c.
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const int t1 = c == 0 ? 1 : 0, t2 = c == 2 ? 1 : 2;
+        const int n2 = len[t2], np = len[t1] * n2, nf = len[c] - 1;
 #pragma unroll 1
-    for (int q = 0; q < NW * NW; q++) {
-        const int u = q / NW, v = q - u * NW;
-        const float a0u = pickN<NW>(s0[0], u), d0u = pickN<NW>(ds[0], u);
-        const float a1u = pickN<NW>(s0[1], u), d1u = pickN<NW>(ds[1], u);
-        const float a1v = pickN<NW>(s0[1], v), d1v = pickN<NW>(ds[1], v);
-        const float a2v = pickN<NW>(s0[2], v), d2v = pickN<NW>(ds[2], v);
-        // Jx on transverse nodes (j, l) = (u, v).
-        const float yz = a1u * a2v + hf * (d1u * a2v + a1u * d2v) + th * (d1u * d2v);
-        if (yz != 0.f) {
-            float acc = 0.f;
+        for (int q = 0; q < np; q++) {
+            const int u = q / n2, v = q - u * n2;
+            const float f = factor(pickN<NW>(s0[t1], u), pickN<NW>(ds[t1], u), pickN<NW>(s0[t2], v), pickN<NW>(ds[t2], v));
+            if (f != 0.f) {
+                int n[3];
+                n[t1] = b[t1] + u;
+                n[t2] = b[t2] + v;
+                float acc = 0.f;
 #pragma unroll
-            for (int i = 0; i < NW - 1; i++) {
-                acc = acc + ds[0][i] * yz;
-                jt.add(((b[0] + i + 1) * T1 + (b[1] + u)) * T2 + (b[2] + v), acc * k[0]);
-            }
-        }
-        // Jy on (i, l) = (u, v).
-        const float xz = a0u * a2v + hf * (d0u * a2v + a0u * d2v) + th * (d0u * d2v);
-        if (xz != 0.f) {
-            float acc = 0.f;
-#pragma unroll
-            for (int j = 0; j < NW - 1; j++) {
-                acc = acc + ds[1][j] * xz;
-                jt.add(TT + ((b[0] + u) * T1 + (b[1] + j + 1)) * T2 + (b[2] + v), acc * k[1]);
-            }
-        }
-        // Jz on (i, j) = (u, v).
-        const float xy = a0u * a1v + hf * (d0u * a1v + a0u * d1v) + th * (d0u * d1v);
-        if (xy != 0.f) {
-            float acc = 0.f;
-#pragma unroll
-            for (int l = 0; l < NW - 1; l++) {
-                acc = acc + ds[2][l] * xy;
-                jt.add(2 * TT + ((b[0] + u) * T1 + (b[1] + v)) * T2 + (b[2] + l + 1), acc * k[2]);
+                for (int i = 0; i < NW - 1; i++) {
+                    if (i < nf) {
+                        acc = __fmaf_rn(ds[c][i], f, acc);
+                        n[c] = b[c] + i + 1;
+                        jt.add(c * TT + (n[0] * T1 + n[1]) * T2 + n[2], __fmul_rn(acc, k[c]));
+                    }
+                }
             }
         }
     }
@@ -172,14 +185,14 @@ __device__ __forceinline__ void generalWindow(const Tile& jt, int TT, int T1, in
     constexpr int NWn = SHAPE == PICA_SHAPE_TSC ? 3 : 2;
     constexpr int NW4 = NWn + 1;
     float s0[3][NW4], s1[3][NW4];
-    int b[3];
+    int b[3], len[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         float w0[NWn], w1[NWn];
         int lo0, lo1;
         if constexpr (SHAPE == PICA_SHAPE_TSC) {
-            tscWeights(o[d] - 0.5f, w0);
-            tscWeights(on[d] - 0.5f, w1);
+            tscWeightsF(__fsub_rn(o[d], 0.5f), w0);
+            tscWeightsF(__fsub_rn(on[d], 0.5f), w1);
             lo0 = lc[d] - 1;
             lo1 = ln[d] - 1;
         } else {
@@ -194,8 +207,9 @@ __device__ __forceinline__ void generalWindow(const Tile& jt, int TT, int T1, in
         placeShape<float, NW4, NWn>(s0[d], lo0, base, w0);
         placeShape<float, NW4, NWn>(s1[d], lo1, base, w1);
         b[d] = base + kG;
+        len[d] = lo0 == lo1 ? NWn : NW4;   // |lo1 - lo0| <= 1: at most a third of a cell per step
     }
-    esirkepovRolled<NW4>(jt, TT, T1, T2, b, s0, s1, kq);
+    esirkepovRolled<NW4>(jt, TT, T1, T2, b, s0, s1, kq, len);
 }
 
 // Fixed-point tile addressed by shared-window byte addresses, for code that is
@@ -274,17 +288,35 @@ __device__ __forceinline__ void reduceRows(const float* red, const int* keys, in
         const unsigned mP = __ballot_sync(0xffffffffu, kp == ref) & pendP;
         pendL &= ~mL;
         pendP &= ~mP;
-        float s0 = 0.0f, s1 = 0.0f;
-        for (unsigned m = mL; m; m &= m - 1) {
-            const int r = (__ffs(m) - 1) * kRowStride;
-            if (lane < NV) s0 += c0[r];
-            if (lane + 32 < NV) s1 += c1[r];
+        // The member rows in a fixed order (lane rows ascending, then park rows in the
+        // order taken), row k into partial sum k mod 4: four independent chains of
+        // loads and adds instead of one, combined as (p0 + p1) + (p2 + p3).
+        float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f, q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f;
+        const bool hasHigh = lane + 32 < NV;
+        unsigned mm[2] = {mL, mP};
+#pragma unroll
+        for (int part = 0; part < 2; part++) {
+            unsigned m = mm[part];
+            const int base = part == 0 ? 0 : 32;
+            while (m) {
+                int r[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    r[k] = m ? (base + __ffs(m) - 1) * kRowStride : -1;
+                    m &= m - 1;
+                }
+                float v[4], w[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    v[k] = r[k] >= 0 ? c0[r[k]] : 0.f;
+                    w[k] = r[k] >= 0 && hasHigh ? c1[r[k]] : 0.f;
+                }
+                p0 = __fadd_rn(p0, v[0]); p1 = __fadd_rn(p1, v[1]); p2 = __fadd_rn(p2, v[2]); p3 = __fadd_rn(p3, v[3]);
+                q0 = __fadd_rn(q0, w[0]); q1 = __fadd_rn(q1, w[1]); q2 = __fadd_rn(q2, w[2]); q3 = __fadd_rn(q3, w[3]);
+            }
         }
-        for (unsigned m = mP; m; m &= m - 1) {
-            const int r = (32 + __ffs(m) - 1) * kRowStride;
-            if (lane < NV) s0 += c0[r];
-            if (lane + 32 < NV) s1 += c1[r];
-        }
+        const float s0 = __fadd_rn(__fadd_rn(p0, p1), __fadd_rn(p2, p3));
+        const float s1 = __fadd_rn(__fadd_rn(q0, q1), __fadd_rn(q2, q3));
         const int b[3] = {(ref >> 16) - 4 + kG, ((ref >> 8) & 0xff) - 4 + kG, (ref & 0xff) - 4 + kG};
         if (lane < NV) jt.add(windowIdx<NWn>(TT, T1, T2, b, lane), s0);
         if (lane + 32 < NV) jt.add(windowIdx<NWn>(TT, T1, T2, b, lane + 32), s1);
@@ -502,8 +534,8 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
 #pragma unroll
                         for (int d = 0; d < 3; d++) {
                             const bool hi = o[d] >= 0.5f;
-                            bc[d] = lc[d] + (hi ? 1 : 0); tscWeights(hi ? o[d] - 1.0f : o[d], wc[d]);
-                            bs[d] = lc[d]; tscWeights(o[d] - 0.5f, ws[d]);
+                            bc[d] = lc[d] + (hi ? 1 : 0); tscWeightsF(hi ? __fsub_rn(o[d], 1.0f) : o[d], wc[d]);
+                            bs[d] = lc[d]; tscWeightsF(__fsub_rn(o[d], 0.5f), ws[d]);
                         }
 #pragma unroll
                         for (int cp = 0; cp < 6; cp += 2) {   // (Ex, Ey), (Ez, Bx), (By, Bz)
@@ -526,7 +558,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     float on[3];
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
-                        float onew = o[d] + (u[d] * ig) * cdth[d];
+                        float onew = __fmaf_rn(__fmul_rn(u[d], ig), cdth[d], o[d]);
                         const float fl = floorf(onew);
                         ln[d] = lc[d] + (int)fl;
                         onew = onew - fl;
@@ -543,7 +575,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
 #pragma unroll
                         for (int d = 0; d < 3; d++) { ln[d] = lc[d]; on[d] = o[d]; }
                     }
-                    const float kq[3] = {kqs[0] * wgt, kqs[1] * wgt, kqs[2] * wgt};
+                    const float kq[3] = {__fmul_rn(kqs[0], wgt), __fmul_rn(kqs[1], wgt), __fmul_rn(kqs[2], wgt)};
                     const bool sameWindow = !lone && inRange && ln[0] == lc[0] && ln[1] == lc[1] && ln[2] == lc[2];
                     if (sameWindow) {
                         // Old shape S0 and its change dd = S1 - S0 on the rho-lattice nodes lc-1 ..
@@ -556,31 +588,35 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                         // p = a + d/2, q = a/2 + d/3; yz = a_y p_z + d_y q_z.
                         float aa[3][NWn], dd[3][NWn], pp[3][NWn], qq[3][NWn];
 #pragma unroll
+                        // Every rounding is spelled out (_rn intrinsics, which the compiler does not
+                        // contract), so that every instantiation of this code -- launch variants,
+                        // the batching form -- rounds the same way.
                         for (int d = 0; d < 3; d++) {
-                            const float D = on[d] - o[d];
+                            const float D = __fsub_rn(on[d], o[d]);
                             if constexpr (SHAPE == PICA_SHAPE_TSC) {
-                                const float dl = o[d] - 0.5f;
-                                tscWeights(dl, aa[d]);
-                                dd[d][0] = D * (0.5f * D + dl - 0.5f);
-                                dd[d][1] = -D * (2.0f * dl + D);
-                                dd[d][2] = D * (0.5f + dl + 0.5f * D);
+                                const float dl = __fsub_rn(o[d], 0.5f);
+                                tscWeightsF(dl, aa[d]);
+                                dd[d][0] = __fmul_rn(D, __fadd_rn(__fmaf_rn(0.5f, D, dl), -0.5f));
+                                dd[d][1] = -__fmul_rn(D, __fmaf_rn(2.0f, dl, D));
+                                dd[d][2] = __fmul_rn(D, __fmaf_rn(0.5f, D, __fadd_rn(0.5f, dl)));
                             } else {
                                 const bool h0 = o[d] >= 0.5f, h1 = on[d] >= 0.5f;
                                 const float d0 = h0 ? o[d] - 0.5f : o[d] + 0.5f;
                                 aa[d][0] = h0 ? 0.0f : 1.0f - d0; aa[d][1] = h0 ? 1.0f - d0 : d0; aa[d][2] = h0 ? d0 : 0.0f;
                                 // Same half: the shape slides by D.  Across the centre: a = o - 1/2 and
                                 // b = on - 1/2 are both near zero and exact.
-                                const float a = o[d] - 0.5f, b = on[d] - 0.5f;
+                                const float a = __fsub_rn(o[d], 0.5f), b = __fsub_rn(on[d], 0.5f);
+                                const float ab = __fadd_rn(a, b);
                                 if (h0 == h1) {
                                     dd[d][0] = h0 ? 0.0f : -D; dd[d][1] = h0 ? -D : D; dd[d][2] = h0 ? D : 0.0f;
                                 } else {
-                                    dd[d][0] = h1 ? a : -b; dd[d][2] = h1 ? b : -a; dd[d][1] = h1 ? -(a + b) : a + b;
+                                    dd[d][0] = h1 ? a : -b; dd[d][2] = h1 ? b : -a; dd[d][1] = h1 ? -ab : ab;
                                 }
                             }
 #pragma unroll
                             for (int k = 0; k < NWn; k++) {
-                                pp[d][k] = aa[d][k] + 0.5f * dd[d][k];
-                                qq[d][k] = 0.5f * aa[d][k] + (float)kThird * dd[d][k];
+                                pp[d][k] = __fmaf_rn(0.5f, dd[d][k], aa[d][k]);
+                                qq[d][k] = __fmaf_rn((float)kThird, dd[d][k], __fmul_rn(0.5f, aa[d][k]));
                             }
                         }
                         // e[d][f]: -(q w) h_d/dt times the running sum of dd over faces 0..f, that is
@@ -588,8 +624,8 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                         float e[3][NWn - 1];
 #pragma unroll
                         for (int d = 0; d < 3; d++) {
-                            e[d][0] = kq[d] * dd[d][0];
-                            e[d][1] = -(kq[d] * dd[d][2]);
+                            e[d][0] = __fmul_rn(kq[d], dd[d][0]);
+                            e[d][1] = -__fmul_rn(kq[d], dd[d][2]);
                         }
                         // Jx and Jy share the z factors (pp2, qq2): their terms and sums go in
                         // packed FP32x2 pairs (each half rounds as the scalar form); Jz alone.
@@ -623,7 +659,9 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                             for (int y = 0; y < NWn; y++)
 #pragma unroll
                                 for (int z = 0; z < NWn; z++)
-                                    acc[2 * P + y * NWn * (NWn - 1) + z * (NWn - 1) + f] += e[2][f] * (aa[0][y] * pp[1][z] + dd[0][y] * qq[1][z]);
+                                    acc[2 * P + y * NWn * (NWn - 1) + z * (NWn - 1) + f] =
+                                        __fmaf_rn(e[2][f], __fmaf_rn(dd[0][y], qq[1][z], __fmul_rn(aa[0][y], pp[1][z])),
+                                                  acc[2 * P + y * NWn * (NWn - 1) + z * (NWn - 1) + f]);
                     } else if (inRange) {
                         needQ = true;
 #pragma unroll

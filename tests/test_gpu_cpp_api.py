@@ -134,7 +134,7 @@ def python_drop_in(steps, fp32):
         if st == 1:
             q = s.particles()
             sc27 = np.nonzero(q["supercell"] == 27)[0]
-            first = sc27[np.argmin(q["species"][sc27] * (1 << 40) + sc27)]   # species 0 first, then slot order
+            first = sc27[np.argmin(q["species"][sc27].astype(np.int64) * (1 << 40) + sc27)]   # species 0 first
             q["ux"][first] += 0.05
             q["uy"][first] += 0.0
             q["uz"][first] += -0.02

@@ -60,28 +60,32 @@ TIES = 8   # face ties allowed over a run (measured: 0 or 1)
 
 
 def compare_ensembles(ps, pr, L, nsc3):
-    """Slot by slot; the supercells whose slots disagree are matched one to one by
-    nearest neighbour instead, together with their neighbours (see the module
-    docstring)."""
+    """Slot by slot within each (species, supercell); the supercells whose particles
+    disagree (a different count after a tie, or slots shifted around a tie particle)
+    are matched one to one by nearest neighbour instead, together with their
+    neighbours (see the module docstring).  Returns the number of such supercells."""
     comps = ("x", "y", "z", "ux", "uy", "uz")
     umax = [max(np.max(np.abs(pr[k])), 1e-300) for k in ("ux", "uy", "uz")]
-    same_len = len(ps["x"]) == len(pr["x"])
-    bad = np.ones(len(pr["x"]), bool) if not same_len else np.zeros(len(pr["x"]), bool)
-    if same_len:
-        bad |= ps["supercell"] != pr["supercell"]
-        bad |= ps["species"] != pr["species"]
-        for d, k in enumerate(("x", "y", "z")):
-            dd = np.abs(ps[k] - pr[k])
-            bad |= np.minimum(dd, L[d] - dd) >= TOL_X * L[d]
-        for k, m in zip(("ux", "uy", "uz"), umax):
-            bad |= np.abs(ps[k] - pr[k]) >= TOL_U * m
-    if not bad.any():
-        return 0
-    groups = np.unique(pr["supercell"][bad])
     nsc = int(np.prod(nsc3))
+    nsp = int(max(ps["species"].max(initial=0), pr["species"].max(initial=0))) + 1
+    ks = ps["species"].astype(np.int64) * nsc + ps["supercell"]
+    kr = pr["species"].astype(np.int64) * nsc + pr["supercell"]
+    cs, cr = np.bincount(ks, minlength=nsp * nsc), np.bincount(kr, minlength=nsp * nsc)
+    ss, sr = np.cumsum(cs) - cs, np.cumsum(cr) - cr
+    ir = np.nonzero(cs[kr] == cr[kr])[0]            # particles of supercells with equal counts
+    ia = ss[kr[ir]] + (ir - sr[kr[ir]])             # the same slot on the other side
+    bad = np.zeros(len(ir), bool)
+    for d, k in enumerate(("x", "y", "z")):
+        dd = np.abs(ps[k][ia] - pr[k][ir])
+        bad |= np.minimum(dd, L[d] - dd) >= TOL_X * L[d]
+    for k, m in zip(("ux", "uy", "uz"), umax):
+        bad |= np.abs(ps[k][ia] - pr[k][ir]) >= TOL_U * m
+    groups = np.union1d(np.nonzero(cs != cr)[0], kr[ir[bad]])
+    if len(groups) == 0:
+        return 0
     assert len(groups) <= max(8, 1e-3 * nsc), f"{len(groups)} supercells disagree slot by slot"
     # the disagreeing supercells and their 26 neighbours (a tie particle sits across a face)
-    sx, sy, sz = np.unravel_index(groups, nsc3)
+    sx, sy, sz = np.unravel_index(groups % nsc, nsc3)
     near = set()
     for dx in (-1, 0, 1):
         for dy in (-1, 0, 1):
@@ -91,16 +95,14 @@ def compare_ensembles(ps, pr, L, nsc3):
     near = np.array(sorted(near))
     from scipy.spatial import cKDTree
     scale = np.array([TOL_X * L[0], TOL_X * L[1], TOL_X * L[2]] + [TOL_U * m for m in umax])
-    ia = np.nonzero(np.isin(ps["supercell"], near))[0]
-    ib = np.nonzero(np.isin(pr["supercell"], near))[0]
-    assert len(ia) == len(ib), "the particles around the disagreeing supercells differ in number"
-    for q in np.unique(pr["species"][ib]):
-        ja, jb = ia[ps["species"][ia] == q], ib[pr["species"][ib] == q]
-        assert len(ja) == len(jb)
-        # In tolerance units (every component of a match below 1); positions periodic
-        # (a tie at a domain face puts the particle at L - eps on one side, 0 on the other).
-        box = np.array([1.0 / TOL_X] * 3 + [1e12] * 3)
-        shift = np.array([0.0] * 3 + [0.5e12] * 3)
+    # In tolerance units (every component of a match below 1); positions periodic
+    # (a tie at a domain face puts the particle at L - eps on one side, 0 on the other).
+    box = np.array([1.0 / TOL_X] * 3 + [1e12] * 3)
+    shift = np.array([0.0] * 3 + [0.5e12] * 3)
+    for q in range(nsp):
+        ja = np.nonzero(np.isin(ps["supercell"], near) & (ps["species"] == q))[0]
+        jb = np.nonzero(np.isin(pr["supercell"], near) & (pr["species"] == q))[0]
+        assert len(ja) == len(jb), "the particles around the disagreeing supercells differ in number"
         a = np.mod(np.stack([ps[k][ja] for k in comps], axis=1) / scale + shift, box)
         b = np.mod(np.stack([pr[k][jb] for k in comps], axis=1) / scale + shift, box)
         dist, j = cKDTree(b, boxsize=box).query(a, p=np.inf)
