@@ -21,8 +21,10 @@ A step of every slab:
    above);
 2. push and deposit (pica_push_deposit);
 3. current fold: the current a slab deposited into its guard layers is added to
-   the owned layers of the neighbour that owns them (a slab's guard current is
-   never read again: it feeds only guard fields, which the next halo overwrites);
+   the owned layers of the neighbour that owns them; then the current halo copies
+   the completed owned current back into the neighbours' guard layers.  The guard
+   current is needed within the step: the E update of a guard layer feeds the
+   second B half step of the owned layer next to it;
 4. B dt/2, E dt, B dt/2 and the migration, each slab on its own;
 5. particle exchange: the particles that migrated into a slab's guard supercells
    are taken out (pica_take_supercells) and appended to the neighbour's supercells
@@ -205,12 +207,12 @@ class LocalTransport:
     def __init__(self, domains):
         self.domains = domains
 
-    def halo(self, plan):
+    def halo(self, plan, comps=E_B):
         for r, d in enumerate(self.domains):
             lo, hi = self.domains[plan.low(r)], self.domains[plan.high(r)]
             src_lo, dst_lo = plan.halo_low(r)
             src_hi, dst_hi = plan.halo_high(r)
-            for c in E_B:
+            for c in comps:
                 d.put_slab(c, dst_lo, lo.slab(c, src_lo, plan.G))
                 d.put_slab(c, dst_hi, hi.slab(c, src_hi, plan.G))
 
@@ -264,16 +266,16 @@ class DistTransport:
             for w in dist.batch_isend_irecv(ops):
                 w.wait()
 
-    def halo(self, plan):
+    def halo(self, plan, comps=E_B):
         d, r, G = self.d, self.r, plan.G
-        send_lo = [d.slab(c, G, G) for c in E_B]                  # my bottom owned layers -> low neighbour's high guard
-        send_hi = [d.slab(c, plan.w[r], G) for c in E_B]          # my top owned layers -> high neighbour's low guard
-        recv_lo = [d.slab(c, 0, G) for c in E_B]                  # buffers of the right size
-        recv_hi = [d.slab(c, G + plan.w[r], G) for c in E_B]
+        send_lo = [d.slab(c, G, G) for c in comps]                  # my bottom owned layers -> low neighbour's high guard
+        send_hi = [d.slab(c, plan.w[r], G) for c in comps]          # my top owned layers -> high neighbour's low guard
+        recv_lo = [d.slab(c, 0, G) for c in comps]                  # buffers of the right size
+        recv_hi = [d.slab(c, G + plan.w[r], G) for c in comps]
         self._sendrecv(plan, send_lo, send_hi, recv_lo, recv_hi)
-        for c, t in zip(E_B, recv_lo):
+        for c, t in zip(comps, recv_lo):
             d.put_slab(c, 0, t)
-        for c, t in zip(E_B, recv_hi):
+        for c, t in zip(comps, recv_hi):
             d.put_slab(c, G + plan.w[r], t)
 
     def fold(self, plan):
@@ -328,6 +330,7 @@ class SlabDecomposition:
             for d in self.domains:
                 d.sim.push_deposit()
             self.t.fold(self.plan)
+            self.t.halo(self.plan, J)   # the completed current back into the guard layers
             for d in self.domains:
                 d.sim.update_b(0.5 * self.dt)
                 d.sim.update_e(self.dt)

@@ -8,7 +8,9 @@ in its guard layers, and particles in its guard supercells tagged with their
 global cell.  One halo, fold and particle exchange must then leave:
 
 * every guard layer equal to the function at the global cell it stands for;
-* the owned current next to each face raised by the neighbour's guard current;
+* the owned current next to each face raised by the neighbour's guard current,
+  and, after the current halo, every guard current equal to the completed
+  current of the cell it stands for;
 * every particle in the owned supercell of the slab that owns its global cell, at
   the local cell that stands for it.
 
@@ -120,6 +122,8 @@ def check(plan, r, d):
             if c >= 6 and G <= l < G + plan.w[r]:
                 near = l < 2 * G or l >= plan.w[r]
                 assert np.array_equal(a[l], want + (7.0 if near else 0.0)), (r, c, l)   # fold
+            if c >= 6 and (l < G or l >= G + plan.w[r]):
+                assert np.array_equal(a[l], want + 7.0), (r, c, l)    # current halo: the owner's completed value
     got = 0
     for s, rows in enumerate(d.parts):
         sx = s // (d.nsc3[1] * d.nsc3[2])
@@ -158,6 +162,7 @@ def test_local_transport_moves_layers_current_and_particles(slabs):
     t = domain.LocalTransport(doms)
     t.halo(plan)
     t.fold(plan)
+    t.halo(plan, domain.J)
     t.exchange(plan)
     assert sum(check(plan, r, d) for r, d in enumerate(doms)) == sent
 
@@ -181,6 +186,7 @@ def _rank(rank, world, port, q):
         t = domain.DistTransport(d, rank, world, dist)
         t.halo(plan)
         t.fold(plan)
+        t.halo(plan, domain.J)
         t.exchange(plan)
         q.put((rank, sent, check(plan, rank, d), None))
     except Exception as e:   # report to the parent
