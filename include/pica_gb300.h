@@ -43,6 +43,7 @@ extern "C" {
 #define PICA_ERR_STATE (-6)     /* call out of order (e.g. push twice without migrate) */
 #define PICA_ERR_NOT_BUILT (-7) /* form / shape / depositor combination not compiled */
 #define PICA_ERR_LIMIT (-8)     /* size beyond a documented fixed limit   */
+#define PICA_ERR_TIMEOUT (-9)   /* a bounded wait on the device gave up (an asynchronous copy never completed) */
 
 /* Precision forms. */
 #define PICA_FORM_FP64_PLAIN 0  /* FP64 absolute positions; pica's own arithmetic */
@@ -114,7 +115,11 @@ const char* pica_last_error(pica_ctx* ctx);
 /* Kernels this context has launched since creation (for launch accounting). */
 int64_t     pica_launch_count(pica_ctx* ctx);
 /* Launch shape of the FP32 charge-conserving push kernel (no counterpart in pica,
- * which has no GPU path): 0..count-1, chosen by pica_gb300.autotune. */
+ * which has no GPU path): 0..count-1, chosen by pica_gb300.autotune.  All variants
+ * give bit-identical results.  Variant 4 stages the E/B tile of interior
+ * supercells with tensor-memory-accelerator copies (supercells of 4^3 cells on
+ * grids of at least 12 cells per side; elsewhere, and in the batching form, it
+ * launches as variant 0). */
 int         pica_set_variant(pica_ctx* ctx, int32_t variant);
 int         pica_get_variant(pica_ctx* ctx, int32_t* variant, int32_t* count);
 

@@ -92,6 +92,8 @@ struct pica_ctx {
     cudaEvent_t copyOrder = nullptr;   // orders a host copy on a caller's copy stream against the context stream
     bool recordMig = false;            // keep each step's migration list (pica_record_migrations)
     std::vector<int32_t> mig;          // last step's list: (species, src, slot, dst) per entry
+    TmaFieldMaps tmaps{};              // tensor maps of ex..bz for push variant 4 (FP32 form, supercells 4^3)
+    bool hasTmaps = false;
 };
 
 namespace {
@@ -286,6 +288,38 @@ void parallelFor(int threads, int64_t n, const std::function<void(int64_t, int64
 }
 }  // namespace
 
+// Tensor maps of the six FP32 E/B arrays for push variant 4: a 3D tiled map over
+// (nz, ny, nx) floats per component, box (kTmaBoxZ, 7, 7), no swizzle, zero fill
+// outside the grid (the kernel copies only boxes whose used nodes lie inside).
+// The encoder is the driver's cuTensorMapEncodeTiled, reached through the runtime.
+// False, and no maps, for other supercell shapes, grids narrower than 12 cells, or
+// a driver without the encoder: variant 4 then launches as variant 0.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static bool encodeFieldMaps(pica_ctx* ctx) {
+    const pica_config& c = ctx->cfg;
+    for (int d = 0; d < 3; d++)
+        if (c.sc[d] != kTmaS || c.n[d] < 12) return false;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return false;
+    }
+    const cuuint64_t dims[3] = {(cuuint64_t)c.n[2], (cuuint64_t)c.n[1], (cuuint64_t)c.n[0]};
+    const cuuint64_t strides[2] = {(cuuint64_t)c.n[2] * 4, (cuuint64_t)c.n[1] * c.n[2] * 4};
+    const cuuint32_t box[3] = {kTmaBoxZ, kTmaS + 3, kTmaS + 3}, unit[3] = {1, 1, 1};
+    for (int k = 0; k < 6; k++)
+        if (reinterpret_cast<EncodeTiledFn>(fn)(&ctx->tmaps.m[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, ctx->f[k], dims,
+                                                 strides, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                                 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    return true;
+}
+
 // Kernel arguments of the push for the context's current layout (the buffers
 // themselves are set by the caller).
 template <class A>
@@ -305,6 +339,7 @@ static void fillPushArgs(pica_ctx* ctx, A& a) {
     a.tileSplit = ctx->tileSplit;
     a.norm = 1.0 / (c.h[0] * c.h[1] * c.h[2]);   // CurrentDepositorYeeGrid.h:203
     a.flags = ctx->d_flags;
+    if constexpr (std::is_same<A, PushArgs<CellPtrs>>::value) a.tmaps = ctx->hasTmaps ? &ctx->tmaps : nullptr;
     for (int q = 0; q < c.nspecies; q++) {
         SpeciesState& S = ctx->sp[q];
         auto& sa = a.sp[q];
@@ -332,6 +367,7 @@ const char* pica_status_string(int s) {
         case PICA_ERR_STATE: return "call out of order";
         case PICA_ERR_NOT_BUILT: return "combination not built";
         case PICA_ERR_LIMIT: return "size beyond a fixed limit";
+        case PICA_ERR_TIMEOUT: return "a bounded device wait gave up";
         default: return "unknown status";
     }
 }
@@ -409,6 +445,7 @@ int pica_ctx_create(const pica_config* cfg, pica_ctx** out) {
         cudaMalloc(&ctx->d_red, ctx->redCount * 8) || cudaMalloc(&ctx->d_out, 8 * 8) || cudaMallocHost(&ctx->h_out, 8 * 8))
         return bail(PICA_ERR_OOM);
     cudaMemset(ctx->d_flags, 0, 4 * sizeof(int));
+    if (!ctx->fp64) ctx->hasTmaps = encodeFieldMaps(ctx);
     if (cudaDeviceSynchronize() != cudaSuccess) return bail(PICA_ERR_CUDA);
     *out = ctx;
     return PICA_OK;
@@ -957,7 +994,10 @@ template <class P>
 static int migrateFinish(pica_ctx* ctx) {
     const pica_config& c = ctx->cfg;
     const int A = ctx->cur, B = 1 - ctx->cur;
-    if (ctx->h_flags[0]) return fail(ctx, ctx->h_flags[0], "a particle crossed more than one supercell in one step");
+    if (ctx->h_flags[0])
+        return fail(ctx, ctx->h_flags[0],
+                    ctx->h_flags[0] == PICA_ERR_TIMEOUT ? "the push's tensor copies of the E/B tile never completed"
+                                                         : "a particle crossed more than one supercell in one step");
     if (ctx->h_flags[1]) {
         // Overflow (the fill did nothing): gather the leavers into the outbox (B is then
         // free), rebuild A + arrivals into B with capacities for the new counts, and swap.

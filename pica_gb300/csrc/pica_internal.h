@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <cuda.h>   // CUtensorMap (types only; the encoder is reached through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 #include "../../include/pica_gb300.h"
@@ -114,7 +115,19 @@ struct PushArgs {
     double norm;        // FP64 form: 1 / (hx hy hz)
     int* flags;         // flags[0]: error code (0 = ok)
     int scBegin, scEnd; // FP32 Esirkepov push: supercells [scBegin, scEnd) (scEnd 0: all)
+    const struct TmaFieldMaps* tmaps;   // FP32 form, host: tensor maps of ex..bz (nullptr: none)
     SpeciesArgs<P> sp[kMaxSpecies];
+};
+// Tensor maps of the six E/B arrays for the TMA-staged push (launch variant 4): a
+// 3D tiled map per component over (nz, ny, nx) floats, box (kTmaBoxZ, S+3, S+3).
+// The box starts 4 nodes below the supercell in z, so that its innermost
+// coordinate is a multiple of 4 floats (16 bytes), and covers nodes m-4 .. m+7.
+constexpr int kTmaS = 4;          // supercell edge of the TMA variant
+constexpr int kTmaBoxZ = 12;      // z extent of the box (48 bytes)
+constexpr int kTmaZOff = 3;       // tile node m-1 sits at box index 3
+constexpr int kTmaCompFloats = 608;   // (S+3)^2 x 12 = 588 floats, padded to a multiple of 128 bytes
+struct alignas(64) TmaFieldMaps {
+    CUtensorMap m[6];
 };
 
 // Arguments of the FP32 Esirkepov push: only the fields it reads, FP64 factors
@@ -223,7 +236,7 @@ struct MigrateArgs {
 // Push launchers (push_fp64.cu / push_fp32.cu).  Return cudaError_t as int.
 int launchPushPlain(const PushArgs<PlainPtrs>& a, int shape, int deposit, cudaStream_t s);
 // variant: launch shape of the FP32 Esirkepov kernel (0..kPushVariants-1), see push_fp32.cu.
-constexpr int kPushVariants = 4;
+constexpr int kPushVariants = 5;
 int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int deposit, int variant, cudaStream_t s);
 // Persistent push over a batch (FP32 cell form, Esirkepov; S = supercell edges shared
 // by every plasma).  grid <= 0: one CTA per resident slot on every SM.

@@ -1,4 +1,6 @@
-// FP32 cell form: push and migration kernels (FMA contraction allowed).
+// FP32 cell form: push and migration kernels.  Compiled without implicit FMA
+// contraction: every fused multiply-add is written out, so that each template
+// instantiation (launch variant, batch member) rounds the same way.
 #include <algorithm>
 
 #include "push_fast.cuh"
@@ -37,13 +39,35 @@ int launchEsirkepovV(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     return (int)cudaGetLastError();
 }
 
+// Variant 4: 128 threads, >= 3 CTAs/SM, the E/B tile of interior supercells staged
+// by TMA (cubic supercells of edge 4 with tensor maps; variant 0 otherwise).
+template <int SHAPE, int K, int THREADS, int MINB>
+int launchEsirkepovTma(const PushArgs<CellPtrs>& a, cudaStream_t s) {
+    const int TT = a.T[0] * a.T[1] * a.T[2];
+    const size_t smem = (size_t)esirkepovSmemWords(TT, kTmaCompFloats, THREADS / 32, kRedRowsTma, true) * 4;
+    auto k = k_push_cell_esirkepov_tma<SHAPE, K, THREADS, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return (int)e;
+    const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
+    const int n = a.scEnd > a.scBegin ? a.scEnd - a.scBegin : nscTot;
+    PushArgsSlim<kMaxSpecies> sl;
+    slimArgs(a, sl);
+    k<<<n, THREADS, smem, s>>>(sl, *a.tmaps);
+    return (int)cudaGetLastError();
+}
+
 // Launch variants of the Esirkepov kernel.  All keep K = 8 particles per lane, so the
 // particles summed together in registers (and hence every rounding) are the same and
 // the variants give bit-identical results; they differ in CTA size and occupancy:
 // 0: 128 threads, >= 3 CTAs/SM   1: 128 threads, >= 2 CTAs/SM
-// 2: 64 threads, >= 6 CTAs/SM    3: 256 threads, >= 1 CTA/SM.
+// 2: 64 threads, >= 6 CTAs/SM    3: 256 threads, >= 1 CTA/SM
+// 4: as 0, E/B tile by TMA.
 template <int SHAPE, int SC>
 int launchEsirkepovS(const PushArgs<CellPtrs>& a, int variant, cudaStream_t s) {
+    if constexpr (SC == kTmaS) {
+        if (variant == 4 && a.tmaps) return launchEsirkepovTma<SHAPE, 8, 128, 3>(a, s);
+    }
     switch (variant) {
         case 1: return launchEsirkepovV<SHAPE, SC, 8, 128, 2>(a, s);
         case 2: return launchEsirkepovV<SHAPE, SC, 8, 64, 6>(a, s);

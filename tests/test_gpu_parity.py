@@ -273,20 +273,27 @@ def test_error_paths_do_not_fault():
     assert s.num_particles() == len(d["x"])
 
 
+@pytest.mark.parametrize("n", [(16, 8, 8), (16, 16, 24)])
 @pytest.mark.parametrize("shape", [pg.SHAPE_CIC, pg.SHAPE_TSC])
-def test_push_variants_give_identical_results(shape):
+def test_push_variants_give_identical_results(shape, n):
     """Every launch variant of the FP32 charge-conserving push kernel gives the same
-    particles and fields bit for bit (the J sums are exact integers)."""
-    n, sc = (16, 8, 8), (4, 4, 4)
+    particles and fields bit for bit (the J sums are exact integers), from random
+    E and B.  On the 16 x 16 x 24 grid the TMA variant (4) copies the E/B tile of
+    the interior supercells (2 x 2 x 4 of 4 x 4 x 6) and loads the others; on the
+    16 x 8 x 8 grid it has no tensor maps and launches as variant 0."""
+    sc = (4, 4, 4)
     d = thermal_inputs(n, 10, seed=77, u_sigma=0.2)
+    rng = np.random.default_rng(9)
+    f9 = [1e3 * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3
     out = []
     _, count = gpu_sim(n, sc, d["h"], d["dt"], form=pg.FORM_FP32_CELL).variant()
+    assert count == 5
     for v in range(count):
         s = gpu_sim(n, sc, d["h"], d["dt"], form=pg.FORM_FP32_CELL, shape=shape, deposit=pg.DEPOSIT_ESIRKEPOV,
                     resort_every=3)
         s.set_variant(v)
         s.upload_particles(*particle_args(d))
-        s.upload_fields([np.zeros(n)] * 9)
+        s.upload_fields(f9)
         s.step(6)
         out.append((s.particles(), s.fields()))
     for p, f in out[1:]:
