@@ -324,14 +324,12 @@ __device__ __forceinline__ void reduceRows(const float* red, const int* keys, in
 }
 
 // Dynamic shared memory of k_push_cell_esirkepov, in 4-byte words.
-// rr: rows of a warp's reduction area; align: the E/B tile starts on a 128-byte
-// boundary (the TMA variant's copy destination).
-constexpr int kRedRowsTma = 40;   // the TMA variant's larger E/B tile leaves room for 8 park rows
-__host__ __device__ constexpr int64_t esirkepovSmemWords(int TT, int ECS, int warps, int rr = kRedRows,
-                                                         bool align = false) {
-    return (align ? 6ll * TT + 32 : 6ll * TT) + 6ll * ECS +
-           (int64_t)warps * (kRing * kQWords + rr * kRowStride + rr);
+__host__ __device__ constexpr int64_t esirkepovSmemWords(int TT, int ETT, int warps) {
+    return 6ll * TT + 6ll * ETT + (int64_t)warps * (kRing * kQWords + kRedRows * kRowStride + kRedRows);
 }
+// The TMA variant's tensor copies land in the warps' reduction rows (free until the
+// particle loop starts), 6 boxes of kTmaCompFloats from a 128-byte boundary.
+static_assert(2 * kRedRows * kRowStride >= 6 * kTmaCompFloats + 31, "TMA staging fits two warps' reduction rows");
 
 // Bounded wait on an mbarrier phase (parity): true once the phase completed, false
 // when `limit` polls passed without it.
@@ -352,11 +350,13 @@ constexpr int kTmaWaitPolls = 1 << 20;
 // edge SC known at compile time (tile strides become constants); SC == 0: edges
 // read from the arguments.
 //
-// TMA != 0 (cubic supercells of edge 4 only): interior supercells stage the E/B tile
-// with one tensor-memory-accelerator copy per component (maps: the six tensor maps,
-// in kernel parameter space); the tile then has z rows of kTmaBoxZ floats, node
-// m-1 at index kTmaZOff.  Supercells whose tile wraps around the periodic domain
-// stage with plain loads into the same layout.
+// TMA != 0 (cubic supercells of edge 4 only): interior supercells fetch the E/B
+// tile with one tensor-memory-accelerator copy per component (maps: the six tensor
+// maps, in kernel parameter space) into the warps' reduction rows, boxes with z
+// rows of kTmaBoxZ floats and node m-1 at z index kTmaZOff; one shared-memory pass
+// then packs them into the tile.  Supercells whose tile wraps around the periodic
+// domain stage with plain loads.  Shared-memory footprint, park rows and so every
+// rounding are those of the plain kernel.
 template <int SHAPE, int K, int THREADS, int SC, class A, int TMA = 0>
 __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned char* smem_raw, int& s_nleave,
                                               const TmaFieldMaps* maps = nullptr) {
@@ -364,8 +364,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
     constexpr int NWn = kStayNodes;                        // stay-in-cell window: nodes lc-1 .. lc+1
     constexpr int NV = kStayValues;                        // 54 face values
     constexpr int kWarps = THREADS / 32;
-    constexpr int RR = TMA ? kRedRowsTma : kRedRows;       // rows of a warp's reduction area
-    constexpr int kPark = RR - 32;
+    constexpr int kPark = kRedRows - 32;
     static_assert(K == 8, "a segment of 32 x 8 particles is staged in the lane-row block");
     constexpr unsigned FULL = 0xffffffffu;
 
@@ -373,9 +372,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
     const int T1 = SC ? SC + 2 * kG + 1 : a.T[1], T2 = SC ? SC + 2 * kG + 1 : a.T[2];
     const int TT = (SC ? SC + 2 * kG + 1 : a.T[0]) * T1 * T2;
     const int Sx = SC ? SC : a.S[0], Sy = SC ? SC : a.S[1], Sz = SC ? SC : a.S[2];
-    // E/B tile: component stride ECS floats, z rows of E2 floats, node m-1 at z index EOFF.
-    const int E1 = Sy + 3, E2 = TMA ? kTmaBoxZ : Sz + 3, ECS = TMA ? kTmaCompFloats : (Sx + 3) * E1 * E2;
-    constexpr int EOFF = TMA ? kTmaZOff : 0;
+    const int E1 = Sy + 3, E2 = Sz + 3, ETT = (Sx + 3) * E1 * E2;
     const int Sv[3] = {Sx, Sy, Sz};
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
@@ -383,14 +380,10 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
     jt.lo = reinterpret_cast<unsigned int*>(smem_raw);
     jt.hi = reinterpret_cast<int*>(jt.lo + 3 * TT);
     jt.setSplit(a.tileSplit);
-    float* eb = reinterpret_cast<float*>(smem_raw) + 6 * TT;
-    if constexpr (TMA != 0) {   // tensor copies land on 128-byte boundaries (32 words of slack)
-        const unsigned e0 = (unsigned)__cvta_generic_to_shared(eb);
-        eb += ((128u - (e0 & 127u)) & 127u) / 4u;
-    }
-    float* ring = eb + 6 * ECS + warp * (kRing * kQWords);
-    float* red = eb + 6 * ECS + kWarps * (kRing * kQWords) + warp * (RR * kRowStride);
-    int* keys = reinterpret_cast<int*>(eb + 6 * ECS + kWarps * (kRing * kQWords + RR * kRowStride)) + warp * RR;
+    float* eb = reinterpret_cast<float*>(jt.hi + 3 * TT);
+    float* ring = eb + 6 * ETT + warp * (kRing * kQWords);
+    float* red = eb + 6 * ETT + kWarps * (kRing * kQWords) + warp * (kRedRows * kRowStride);
+    int* keys = reinterpret_cast<int*>(eb + 6 * ETT + kWarps * (kRing * kQWords + kRedRows * kRowStride)) + warp * kRedRows;
     uint32_t* stage = reinterpret_cast<uint32_t*>(red);   // the lane-row block, while a segment runs
     FixTileS jts;
     jts.lo = (unsigned)__cvta_generic_to_shared(jt.lo);
@@ -410,7 +403,10 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
     bool viaTma = false;
     __shared__ __align__(8) unsigned long long s_mbar;
     const unsigned mbar = (unsigned)__cvta_generic_to_shared(&s_mbar);
+    float* stg = eb + 6 * ETT + kWarps * (kRing * kQWords);   // the reduction rows, 128-byte aligned below
     if constexpr (TMA != 0) {
+        static_assert(kWarps >= 2, "TMA staging uses the reduction rows of two warps");
+        stg += ((128u - ((unsigned)__cvta_generic_to_shared(stg) & 127u)) & 127u) / 4u;
         viaTma = m[0] >= 1 && m[0] + Sx + 1 < a.n[0] && m[1] >= 1 && m[1] + Sy + 1 < a.n[1] && m[2] >= 1 &&
                  m[2] + Sz + 1 < a.n[2];
         if (viaTma && threadIdx.x == 0) {
@@ -420,7 +416,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(kBytes) : "memory");
             for (int c = 0; c < 6; c++) {
-                const unsigned dst = (unsigned)__cvta_generic_to_shared(eb + c * ECS);
+                const unsigned dst = (unsigned)__cvta_generic_to_shared(stg + c * kTmaCompFloats);
                 // Box origin (z, y, x) = (m2 - 4, m1 - 1, m0 - 1): z a multiple of 4 floats.
                 asm volatile(
                     "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
@@ -439,13 +435,11 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
     }
     __syncthreads();
     if (!viaTma) {
-        const int EX = Sz + 3, ETT = (Sx + 3) * E1 * EX;   // the nodes staged
         for (int t = threadIdx.x; t < 6 * ETT; t += THREADS) {
             const int c = t / ETT, r = t - c * ETT;
-            const int i = r / (E1 * EX), jj = (r / EX) % E1, k = r % EX;   // E/B tile origin m - 1
-            eb[c * ECS + (i * E1 + jj) * E2 + k + EOFF] =
-                static_cast<const float*>(a.eb[c])[((int64_t)s_wrap[0][i + 1] * a.n[1] + s_wrap[1][jj + 1]) * a.n[2] +
-                                                   s_wrap[2][k + 1]];
+            const int i = r / (E1 * E2), jj = (r / E2) % E1, k = r % E2;   // E/B tile origin m - 1
+            eb[t] = static_cast<const float*>(a.eb[c])[((int64_t)s_wrap[0][i + 1] * a.n[1] + s_wrap[1][jj + 1]) * a.n[2] +
+                                                       s_wrap[2][k + 1]];
         }
     }
     for (int t = threadIdx.x; t < 3 * TT; t += THREADS) { jt.lo[t] = 0u; jt.hi[t] = 0; }
@@ -462,6 +456,11 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
             ok = mbarWait(mbar, 0, kTmaWaitPolls);
         }
         if (__syncthreads_or(!ok)) return;
+        for (int t = threadIdx.x; t < 6 * ETT; t += THREADS) {
+            const int c = t / ETT, r = t - c * ETT;
+            const int i = r / (E1 * E2), jj = (r / E2) % E1, k = r % E2;
+            eb[t] = stg[c * kTmaCompFloats + (i * E1 + jj) * kTmaBoxZ + k + kTmaZOff];
+        }
     }
     __syncthreads();
 
@@ -595,7 +594,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                                 tb[d] = stag(cp + 1, d) ? bs[d] : bc[d];
                             }
                             const float2 g = gatherPair<2>(
-                                eb + cp * ECS + EOFF, eb + (cp + 1) * ECS + EOFF, E1, E2, ta, tb, stag(cp, 0) ? ws[0] : wc[0],
+                                eb + cp * ETT, eb + (cp + 1) * ETT, E1, E2, ta, tb, stag(cp, 0) ? ws[0] : wc[0],
                                 stag(cp, 1) ? ws[1] : wc[1], stag(cp, 2) ? ws[2] : wc[2], stag(cp + 1, 0) ? ws[0] : wc[0],
                                 stag(cp + 1, 1) ? ws[1] : wc[1], stag(cp + 1, 2) ? ws[2] : wc[2]);
                             eb6[cp] = g.x;
@@ -619,7 +618,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                                 tb[d] = stag(cp + 1, d) ? bs[d] : bc[d];
                             }
                             const float2 g = gatherPair<3>(
-                                eb + cp * ECS + EOFF, eb + (cp + 1) * ECS + EOFF, E1, E2, ta, tb, stag(cp, 0) ? ws[0] : wc[0],
+                                eb + cp * ETT, eb + (cp + 1) * ETT, E1, E2, ta, tb, stag(cp, 0) ? ws[0] : wc[0],
                                 stag(cp, 1) ? ws[1] : wc[1], stag(cp, 2) ? ws[2] : wc[2], stag(cp + 1, 0) ? ws[0] : wc[0],
                                 stag(cp + 1, 1) ? ws[1] : wc[1], stag(cp + 1, 2) ? ws[2] : wc[2]);
                             eb6[cp] = g.x;

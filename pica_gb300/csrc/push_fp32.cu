@@ -44,7 +44,7 @@ int launchEsirkepovV(const PushArgs<CellPtrs>& a, cudaStream_t s) {
 template <int SHAPE, int K, int THREADS, int MINB>
 int launchEsirkepovTma(const PushArgs<CellPtrs>& a, cudaStream_t s) {
     const int TT = a.T[0] * a.T[1] * a.T[2];
-    const size_t smem = (size_t)esirkepovSmemWords(TT, kTmaCompFloats, THREADS / 32, kRedRowsTma, true) * 4;
+    const size_t smem = (size_t)esirkepovSmemWords(TT, (kTmaS + 3) * (kTmaS + 3) * (kTmaS + 3), THREADS / 32) * 4;
     auto k = k_push_cell_esirkepov_tma<SHAPE, K, THREADS, MINB>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);

@@ -8,8 +8,12 @@ all from FP64 reductions on the GPU:
   (W(t) - W(0)) / W(0) of the FP32 form minus that of the FP64 form, largest
   magnitude over the run;
 * RMS momentum error after `rms_steps` steps: sqrt(mean |u32 - u64|^2) /
-  sqrt(mean |u64|^2), particles matched by ensemble slot (valid while both forms
-  keep every particle in the same cell, which is checked);
+  sqrt(mean |u64|^2) over matched particles.  Particles are matched by ensemble
+  slot within each (species, supercell) whose counts and slot-wise positions
+  agree; a rounding difference at a cell face can put a particle in the next
+  cell in one form, which changes the counts or, after a resort, the slot order
+  of the supercells around it, and those supercells are matched by nearest
+  neighbour in (position, momentum) instead (`match_particles`);
 * charge-conservation residual of the FP32 form over one step:
   max |(rho^{n+1} - rho^n)/dt + div J^{n+1/2}| on the cell-centred lattice,
   divided by max |rho^n| / dt, and also by max |(rho^{n+1} - rho^n)/dt|.
@@ -56,13 +60,76 @@ def charge_residual(sim):
     return float(res / (np.max(np.abs(r0)) / sim.dt)), float(res / max(np.max(np.abs(drho)), 1e-300))
 
 
-def rms_momentum_error(a, b):
-    """RMS |u_a - u_b| / RMS |u_b| with particles matched by slot; None if the ensembles differ."""
-    if len(a["x"]) != len(b["x"]) or not np.array_equal(a["supercell"], b["supercell"]):
+def match_particles(a, b, L, nsc3, pos_tol=1e-3):
+    """One-to-one match of two ensembles of the same plasma (particles() dicts).
+
+    Slot by slot within every (species, supercell) whose counts agree and whose
+    slot-wise positions lie within pos_tol of the box edge per axis;
+    the particles of the other supercells and of their 26 neighbours are matched by
+    nearest neighbour in (position, momentum), positions periodic.  Returns index
+    arrays (ia, ib) and the number of particles matched by nearest neighbour; None
+    when the ensembles differ in size per species."""
+    nsc = int(np.prod(nsc3))
+    nsp = int(max(a["species"].max(initial=0), b["species"].max(initial=0))) + 1
+    ka = a["species"].astype(np.int64) * nsc + a["supercell"]
+    kb = b["species"].astype(np.int64) * nsc + b["supercell"]
+    ca, cb = np.bincount(ka, minlength=nsp * nsc), np.bincount(kb, minlength=nsp * nsc)
+    if not np.array_equal(ca.reshape(nsp, nsc).sum(1), cb.reshape(nsp, nsc).sum(1)):
         return None
-    du = sum((a[k] - b[k]) ** 2 for k in ("ux", "uy", "uz"))
-    u2 = sum(b[k] ** 2 for k in ("ux", "uy", "uz"))
-    return float(np.sqrt(np.mean(du) / np.mean(u2)))
+    sa, sb = np.cumsum(ca) - ca, np.cumsum(cb) - cb
+    ib = np.nonzero(ca[kb] == cb[kb])[0]
+    ia = sa[kb[ib]] + (ib - sb[kb[ib]])
+    bad = np.zeros(len(ib), bool)
+    for d, k in enumerate(("x", "y", "z")):
+        dd = np.abs(a[k][ia] - b[k][ib])
+        bad |= np.minimum(dd, L[d] - dd) >= pos_tol * L[d]
+    groups = np.union1d(np.nonzero(ca != cb)[0], kb[ib[bad]])
+    if len(groups) == 0:
+        return ia, ib, 0
+    sx, sy, sz = np.unravel_index(groups % nsc, nsc3)
+    near = set()
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dz in (-1, 0, 1):
+                near.update(np.ravel_multi_index(((sx + dx) % nsc3[0], (sy + dy) % nsc3[1], (sz + dz) % nsc3[2]),
+                                                 nsc3).tolist())
+    near = np.array(sorted(near))
+    keep = ~np.isin(b["supercell"][ib], near)
+    ia, ib = [ia[keep]], [ib[keep]]
+    from scipy.spatial import cKDTree
+    umax = [max(np.max(np.abs(b[k])), 1e-300) for k in ("ux", "uy", "uz")]
+    scale = np.array([pos_tol * L[0], pos_tol * L[1], pos_tol * L[2]] + umax)
+    box = np.array([1.0 / pos_tol] * 3 + [1e12] * 3)
+    shift = np.array([0.0] * 3 + [0.5e12] * 3)
+    nn = 0
+    for q in range(nsp):
+        ja = np.nonzero(np.isin(a["supercell"], near) & (a["species"] == q))[0]
+        jb = np.nonzero(np.isin(b["supercell"], near) & (b["species"] == q))[0]
+        if len(ja) != len(jb):
+            return None
+        comps = ("x", "y", "z", "ux", "uy", "uz")
+        pa = np.mod(np.stack([a[k][ja] for k in comps], axis=1) / scale + shift, box)
+        pb = np.mod(np.stack([b[k][jb] for k in comps], axis=1) / scale + shift, box)
+        _, j = cKDTree(pb, boxsize=box).query(pa)
+        if len(np.unique(j)) != len(ja):
+            return None
+        ia.append(ja)
+        ib.append(jb[j])
+        nn += len(ja)
+    return np.concatenate(ia), np.concatenate(ib), nn
+
+
+def rms_momentum_error(a, b, L, nsc3):
+    """RMS |u_a - u_b| / RMS |u_b| over matched particles (`match_particles`).
+    Returns (error, particles matched by nearest neighbour); (None, 0) when the
+    ensembles cannot be matched one to one."""
+    m = match_particles(a, b, L, nsc3)
+    if m is None:
+        return None, 0
+    ia, ib, nn = m
+    du = sum((a[k][ia] - b[k][ib]) ** 2 for k in ("ux", "uy", "uz"))
+    u2 = sum(b[k][ib] ** 2 for k in ("ux", "uy", "uz"))
+    return float(np.sqrt(np.mean(du) / np.mean(u2))), nn
 
 
 def compare_forms(n=(32, 32, 32), ppc=100, steps=1000, every=10, rms_steps=10, seed=20261203, shape=SHAPE_TSC,
@@ -73,7 +140,9 @@ def compare_forms(n=(32, 32, 32), ppc=100, steps=1000, every=10, rms_steps=10, s
     bg = wl["bg"]
     sims = {f: _make(wl, f, particles) for f in (FORM_FP64_PLAIN, FORM_FP32_CELL)}
     hist = {f: [_energy(s, bg)] for f, s in sims.items()}
-    rms = None
+    rms, rms_nn = None, 0
+    L = [n[d] * wl["sim"]["h"][d] for d in range(3)]
+    nsc3 = tuple(n[d] // supercell[d] for d in range(3))
     done = 0
     while done < steps:
         k = min(every, steps - done)
@@ -84,7 +153,8 @@ def compare_forms(n=(32, 32, 32), ppc=100, steps=1000, every=10, rms_steps=10, s
             hist[f].append(_energy(s, bg))
         done += k
         if done == rms_steps:
-            rms = rms_momentum_error(sims[FORM_FP32_CELL].particles(), sims[FORM_FP64_PLAIN].particles())
+            rms, rms_nn = rms_momentum_error(sims[FORM_FP32_CELL].particles(), sims[FORM_FP64_PLAIN].particles(), L,
+                                             nsc3)
     drift = {f: (np.array(h) - h[0]) / h[0] for f, h in hist.items()}
     res_rho, res_drho = charge_residual(sims[FORM_FP32_CELL])
     for s in sims.values():
@@ -98,6 +168,7 @@ def compare_forms(n=(32, 32, 32), ppc=100, steps=1000, every=10, rms_steps=10, s
         "energy_drift_diff_max": float(np.max(np.abs(dd))),
         "rms_momentum_error": rms,
         "rms_momentum_steps": rms_steps,
+        "rms_momentum_nn_matched": rms_nn,
         "charge_residual": res_rho,
         "charge_residual_vs_drho": res_drho,
     }
