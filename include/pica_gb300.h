@@ -207,11 +207,45 @@ int     pica_download_fields(pica_ctx* ctx, double* const* f9);
  * pica_step: push_deposit; update_b(dt/2); update_e(dt); update_b(dt/2); migrate. */
 int     pica_push_deposit(pica_ctx* ctx);
 /* Sort every supercell by cell now, dropping its dead slots (what the periodic
- * resort does every resort_every steps): the GPU counterpart of
- * EnsembleOrdered::reorder (particles/EnsembleOrdered.h:61-71), which sorts a flat
- * array by position; here the order is (species, supercell, cell, slot).
- * PICA_ERR_STATE between push_deposit and migrate. */
+ * resort does every resort_every steps): the supercell layout's counterpart of
+ * EnsembleOrdered::reorder (particles/EnsembleOrdered.h:61-71); here the order is
+ * (species, supercell, cell, slot).  PICA_ERR_STATE between push_deposit and migrate. */
 int     pica_reorder(pica_ctx* ctx);
+
+/* Flat particle arrays: pica's EnsembleUnordered / EnsembleOrdered layouts
+ * (particles/EnsembleUnordered.h:14-40, EnsembleOrdered.h:17-71), one SoA array of
+ * FP64 particles in caller-owned device memory instead of supercells.
+ *
+ * pica_order_by_position: EnsembleOrdered::reorder on the device.  order[i] (device)
+ *   is the index of the i-th particle in lexicographic position order over the
+ *   first dims coordinates of x, y, z (device; y, z may be NULL below dims 2, 3),
+ *   with pica's comparator (EnsembleOrdered.h:31-41; -0.0 equals +0.0).  Stable:
+ *   ties keep input order, where pica's std::sort leaves them unspecified.
+ *   Positions must not be NaN.  stream: a cudaStream_t (NULL: legacy default
+ *   stream); allocates about 16 bytes per particle of scratch and frees it, and
+ *   synchronises the stream.
+ * pica_push_flat: one push of a flat array in any order, on the context's fields
+ *   (FP64 plain form, direct deposition).  Per particle: the grid-level gather of
+ *   FieldInterpolatorCIC<YeeGrid<Three,Real>> (fieldInterpolation/
+ *   FieldInterpolatorYeeGrid.h:23-38, 137-183) for a pica grid whose origin is
+ *   -guard cells (pica node g = context node g - guard, periodic), or the TSC
+ *   gather on the nearest nodes; BorisPusher::push (particlePush/BorisPusher.h:
+ *   33-47); CurrentDepositorCIC<YeeGrid<Three,Real>>::deposit (currentDeposition/
+ *   CurrentDepositorYeeGrid.h:23-38, 126-163) of the current v (q w) / (hx hy hz)
+ *   at the new position, added to J (zeroed first) with FP64 global atomics, whose
+ *   order varies from run to run.  Positions then wrap periodically; the array
+ *   order never changes.  The caller then runs pica_update_b / pica_update_e.
+ *   species may be NULL (all 0).  Synchronises the context stream.
+ *   PICA_ERR_NOT_BUILT for the FP32 form or the Esirkepov depositor; PICA_ERR_STATE
+ *   between push_deposit and migrate; PICA_ERR_INVALID for a species out of range. */
+int     pica_order_by_position(int64_t n, int32_t dims, const double* x, const double* y, const double* z,
+                               int64_t* order, void* stream);
+/* pica_order_by_position on host arrays (copied to the device and back); for host
+ * containers such as the C++ mirror's EnsembleOrdered. */
+int     pica_order_by_position_host(int64_t n, int32_t dims, const double* x, const double* y, const double* z,
+                                    int64_t* order);
+int     pica_push_flat(pica_ctx* ctx, int64_t n, double* x, double* y, double* z, double* ux, double* uy,
+                       double* uz, const double* w, const int32_t* species, int32_t guard);
 /* pica_push_deposit as nchunks launches over consecutive ranges of supercells
  * (range r: linear supercells [nscTot r / nchunks, nscTot (r+1) / nchunks)), the
  * launch of range r enqueued on the context stream after a wait for

@@ -635,6 +635,76 @@ private:
     mutable uint64_t epoch_ = 0;      // the binding's particle epoch the host copy reflects
 };
 
+// pica's EnsembleUnordered (particles/EnsembleUnordered.h:14-40): one flat host
+// array of particles in insertion order.  A flat array on the device is pushed
+// through pica_push_flat (include/pica_gb300.h).
+template <class PA>
+class EnsembleUnordered {
+public:
+    typedef PA ParticleArray;
+    typedef typename PA::Particle Particle;
+    typedef typename PA::ParticleRef ParticleRef;
+    typedef typename PA::ConstParticleRef ConstParticleRef;
+    typedef FP3 PositionType;
+
+    EnsembleUnordered(const FP3& minPosition, const FP3& maxPosition) : min_(minPosition), max_(maxPosition) {}
+    FP3 getMinPosition() const { return min_; }
+    FP3 getMaxPosition() const { return max_; }
+    int size() const { return particles_.size(); }
+    template <class P>
+    void add(const P& particle) { particles_.pushBack(static_cast<Particle3d>(particle)); }
+    PA& getParticles() { return particles_; }
+    const PA& getParticles() const { return particles_; }
+
+protected:
+    PA particles_;
+    FP3 min_, max_;
+};
+
+// pica's EnsembleOrdered (particles/EnsembleOrdered.h:17-71): reorder() sorts the
+// array lexicographically by position, on the device (pica_order_by_position_host),
+// stably: ties keep their order, where pica's std::sort leaves it unspecified.
+template <class PA>
+class EnsembleOrdered : public EnsembleUnordered<PA> {
+public:
+    EnsembleOrdered(const FP3& minPosition, const FP3& maxPosition) : EnsembleUnordered<PA>(minPosition, maxPosition) {}
+    void reorder() {
+        const PA& a = this->particles_;
+        const int n = a.size();
+        std::vector<double> x((size_t)n), y((size_t)n), z((size_t)n);
+        for (int i = 0; i < n; i++) {
+            const FP3 r = a[i].getPosition();
+            x[(size_t)i] = r.x; y[(size_t)i] = r.y; z[(size_t)i] = r.z;
+        }
+        std::vector<int64_t> order((size_t)n);
+        check(nullptr, pica_order_by_position_host(n, 3, x.data(), y.data(), z.data(), order.data()));
+        PA sorted;
+        for (int i = 0; i < n; i++) sorted.pushBack(a[(int)order[(size_t)i]]);
+        this->particles_ = sorted;
+    }
+};
+
+// pica's representation selector (particles/Ensemble.h:20-53).
+enum EnsembleRepresentation {
+    EnsembleRepresentation_Unordered,
+    EnsembleRepresentation_Ordered,
+    EnsembleRepresentation_Supercells
+};
+template <class PA, EnsembleRepresentation storage>
+struct Ensemble;
+template <class PA>
+struct Ensemble<PA, EnsembleRepresentation_Unordered> {
+    typedef EnsembleUnordered<PA> Type;
+};
+template <class PA>
+struct Ensemble<PA, EnsembleRepresentation_Ordered> {
+    typedef EnsembleOrdered<PA> Type;
+};
+template <class PA>
+struct Ensemble<PA, EnsembleRepresentation_Supercells> {
+    typedef EnsembleSupercells<PA> Type;
+};
+
 // ---------------------------------------------------------------------------
 // Operators.  Each carries the configuration of the bulk call that replaces its
 // per-particle method (no per-particle get / push / deposit: they would run on

@@ -12,6 +12,9 @@
  *   - SoA velocity / inverse gamma           include/pica/particles/ParticleArray.h:122-149,263,311-317
  *   - CIC supercell direct depositor         include/pica/currentDeposition/CurrentDepositorYeeGrid.h:178-262
  *   - supercell routing (floor)              include/pica/particles/EnsembleSupercells.h:25-57
+ *   - flat (unordered) push, grid-level CIC  include/pica/fieldInterpolation/FieldInterpolatorYeeGrid.h:23-38,137-183
+ *                                            include/pica/currentDeposition/CurrentDepositorYeeGrid.h:23-38,126-163
+ *   - ordered ensemble sort                  include/pica/particles/EnsembleOrdered.h:31-41,61-71
  * The FP64 CIC/direct path reproduces the reference's floating-point
  * expressions term by term (compile with -ffp-contract=off) and is checked
  * bit-exactly against oracle/ref_harness.cpp, which drives pica's own headers.
@@ -1291,6 +1294,162 @@ int orc_plasma_generate(const orc_plasma* s, int32_t threads, double* x, double*
                     if (species) species[o] = s->species;
                 }
             }
+    }
+    return 0;
+}
+
+/* EnsembleOrdered::reorder (particles/EnsembleOrdered.h:61-71): indexes sorted by
+ * pica's comparator (lexicographic position order over `dims` coordinates,
+ * EnsembleOrdered.h:31-41), stably, so that ties keep input order. */
+int orc_order_by_position(int64_t n, int32_t dims, const double* x, const double* y, const double* z, int64_t* order) {
+    if (n < 0 || dims < 1 || dims > 3) return -1;
+    const double* key[3] = {x, y, z};
+    for (int64_t i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order, order + n, [&](int64_t a, int64_t b) {
+        for (int d = 0; d < dims; d++) {
+            if (key[d][a] < key[d][b]) return true;
+            if (key[d][a] > key[d][b]) return false;
+        }
+        return false;
+    });
+    return 0;
+}
+
+/* One push of a flat particle array in array order (the unordered layout): pica's
+ * grid-level CIC interpolator and depositor (FieldInterpolatorYeeGrid.h:23-38,
+ * 137-183; CurrentDepositorYeeGrid.h:23-38, 126-163) on a grid with `guard`
+ * layers below the domain (origin -guard h; pica grid node g is domain node
+ * g - guard, periodic), the Boris pusher (BorisPusher.h:33-47) and, for TSC, the
+ * quadratic B-spline on the nodes nearest to the position.  The current added
+ * at the new position is v (q w) / (hx hy hz).  f6: ex ey ez bx by bz, j3: jx jy
+ * jz (added to), N^3 arrays, z fastest.  Positions wrap periodically after the
+ * deposit. */
+int orc_push_flat(const orc_config* c, int32_t guard, int64_t n, double* x, double* y, double* z, double* ux,
+                  double* uy, double* uz, const double* w, const int32_t* species, const double* const* f6,
+                  double* const* j3) {
+    if (!c || c->form != ORC_FORM_FP64_PLAIN || c->deposit != ORC_DEPOSIT_DIRECT || guard < 0) return -1;
+    const int N[3] = {c->n[0], c->n[1], c->n[2]};
+    double invh[3], no[3], nos[3], L[3];
+    for (int d = 0; d < 3; d++) {
+        invh[d] = 1.0 / c->h[d];
+        no[d] = (-(double)guard * c->h[d]) / c->h[d];
+        nos[d] = no[d] + 0.5;
+        L[d] = (double)N[d] * c->h[d];
+    }
+    const double norm = 1.0 / (c->h[0] * c->h[1] * c->h[2]);
+    auto at = [&](int i, int j, int k) {
+        return ((size_t)wrapi(i, N[0]) * N[1] + wrapi(j, N[1])) * N[2] + wrapi(k, N[2]);
+    };
+    const bool cic = c->shape == ORC_SHAPE_CIC;
+    for (int64_t p = 0; p < n; p++) {
+        const int sp = species ? species[p] : 0;
+        if (sp < 0 || sp >= c->nspecies) return -2;
+        const double pos[3] = {x[p], y[p], z[p]};
+        double eb[6];
+        auto indexCoeff = [&](const double* q, int* ic, double* cc, int* is, double* cs) {
+            for (int d = 0; d < 3; d++) {
+                const double np = q[d] * invh[d];
+                double in = np - no[d];
+                ic[d] = (int)in; cc[d] = in - (double)ic[d];
+                in = np - nos[d];
+                is[d] = (int)in; cs[d] = in - (double)is[d];
+            }
+        };
+        auto tsc = [&](const double* q, int* nc, double (*wc)[3], int* ns, double (*ws)[3]) {
+            for (int d = 0; d < 3; d++) {
+                const double xi = q[d] * invh[d];
+                nc[d] = (int)std::floor(xi + 0.5); tscWeights(xi - (double)nc[d], wc[d]);
+                const double xs = xi - 0.5;
+                ns[d] = (int)std::floor(xs + 0.5); tscWeights(xs - (double)ns[d], ws[d]);
+            }
+        };
+        if (cic) {
+            int ic[3], is[3]; double cc[3], cs[3];
+            indexCoeff(pos, ic, cc, is, cs);
+            for (int comp = 0; comp < 6; comp++) {
+                const int* sg = kStag[comp];
+                int b[3]; double cw[3];
+                for (int d = 0; d < 3; d++) { b[d] = (sg[d] ? is[d] : ic[d]) - guard; cw[d] = sg[d] ? cs[d] : cc[d]; }
+                const double* f = f6[comp];
+                auto A = [&](int i, int j, int k) { return f[at(b[0] + i, b[1] + j, b[2] + k)]; };
+                eb[comp] = A(0, 0, 0) * (1.0 - cw[0]) * (1.0 - cw[1]) * (1.0 - cw[2]) +
+                           A(0, 0, 1) * (1.0 - cw[0]) * (1.0 - cw[1]) * cw[2] +
+                           A(0, 1, 0) * (1.0 - cw[0]) * cw[1] * (1.0 - cw[2]) + A(0, 1, 1) * (1.0 - cw[0]) * cw[1] * cw[2] +
+                           A(1, 0, 0) * cw[0] * (1.0 - cw[1]) * (1.0 - cw[2]) + A(1, 0, 1) * cw[0] * (1.0 - cw[1]) * cw[2] +
+                           A(1, 1, 0) * cw[0] * cw[1] * (1.0 - cw[2]) + A(1, 1, 1) * cw[0] * cw[1] * cw[2];
+            }
+        } else {
+            int nc[3], ns[3]; double wc[3][3], ws[3][3];
+            tsc(pos, nc, wc, ns, ws);
+            for (int comp = 0; comp < 6; comp++) {
+                const int* sg = kStag[comp];
+                const double* f = f6[comp];
+                double r = 0.0;
+                for (int a = 0; a < 3; a++) {
+                    double ry = 0.0;
+                    for (int b = 0; b < 3; b++) {
+                        double rz = 0.0;
+                        for (int k = 0; k < 3; k++)
+                            rz += (sg[2] ? ws[2] : wc[2])[k] *
+                                  f[at((sg[0] ? ns[0] : nc[0]) - 1 + a, (sg[1] ? ns[1] : nc[1]) - 1 + b,
+                                       (sg[2] ? ns[2] : nc[2]) - 1 + k)];
+                        ry += (sg[1] ? ws[1] : wc[1])[b] * rz;
+                    }
+                    r += (sg[0] ? ws[0] : wc[0])[a] * ry;
+                }
+                eb[comp] = r;
+            }
+        }
+        const double ec = c->charge[sp] * c->dt / (2.0 * c->mass[sp] * kC);   // BorisPusher.h:29
+        double u[3] = {ux[p], uy[p], uz[p]}, ig;
+        boris<double>(ec, eb, eb + 3, u, ig);
+        double v[3], np[3];
+        for (int d = 0; d < 3; d++) {
+            v[d] = (u[d] * kC) * ig;
+            np[d] = pos[d] + v[d] * c->dt;
+        }
+        const double qw = c->charge[sp] * w[p];
+        const double cur[3] = {(v[0] * qw) * norm, (v[1] * qw) * norm, (v[2] * qw) * norm};
+        if (cic) {
+            int ic[3], is[3]; double cc[3], cs[3];
+            indexCoeff(np, ic, cc, is, cs);
+            for (int comp = 0; comp < 3; comp++) {
+                const int* sg = kStag[comp];
+                int b[3]; double cw[3];
+                for (int d = 0; d < 3; d++) { b[d] = (sg[d] ? is[d] : ic[d]) - guard; cw[d] = sg[d] ? cs[d] : cc[d]; }
+                double* J = j3[comp];
+                auto A = [&](int i, int j, int k) -> double& { return J[at(b[0] + i, b[1] + j, b[2] + k)]; };
+                const double vv = cur[comp];
+                A(0, 0, 0) += (1.0 - cw[0]) * (1.0 - cw[1]) * (1.0 - cw[2]) * vv;
+                A(0, 0, 1) += (1.0 - cw[0]) * (1.0 - cw[1]) * cw[2] * vv;
+                A(0, 1, 0) += (1.0 - cw[0]) * cw[1] * (1.0 - cw[2]) * vv;
+                A(0, 1, 1) += (1.0 - cw[0]) * cw[1] * cw[2] * vv;
+                A(1, 0, 0) += cw[0] * (1.0 - cw[1]) * (1.0 - cw[2]) * vv;
+                A(1, 0, 1) += cw[0] * (1.0 - cw[1]) * cw[2] * vv;
+                A(1, 1, 0) += cw[0] * cw[1] * (1.0 - cw[2]) * vv;
+                A(1, 1, 1) += cw[0] * cw[1] * cw[2] * vv;
+            }
+        } else {
+            int nc[3], ns[3]; double wc[3][3], ws[3][3];
+            tsc(np, nc, wc, ns, ws);
+            for (int comp = 0; comp < 3; comp++) {
+                const int* sg = kStag[comp];
+                double* J = j3[comp];
+                for (int a = 0; a < 3; a++)
+                    for (int b = 0; b < 3; b++) {
+                        const double wxy = (sg[0] ? ws[0] : wc[0])[a] * (sg[1] ? ws[1] : wc[1])[b];
+                        for (int k = 0; k < 3; k++)
+                            J[at((sg[0] ? ns[0] : nc[0]) - 1 + a, (sg[1] ? ns[1] : nc[1]) - 1 + b,
+                                 (sg[2] ? ns[2] : nc[2]) - 1 + k)] += wxy * (sg[2] ? ws[2] : wc[2])[k] * cur[comp];
+                    }
+            }
+        }
+        for (int d = 0; d < 3; d++) {
+            if (np[d] < 0.0) np[d] += L[d];
+            if (np[d] >= L[d]) np[d] -= L[d];
+        }
+        x[p] = np[0]; y[p] = np[1]; z[p] = np[2];
+        ux[p] = u[0]; uy[p] = u[1]; uz[p] = u[2];
     }
     return 0;
 }

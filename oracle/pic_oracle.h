@@ -89,6 +89,25 @@ int     orc_charge_density(void* sim, double* rho);
 /* bg_density: neutralising background charge density (statC/cm^3) added to rho. */
 int     orc_diagnostics(void* sim, double bg_density, orc_diag* out);
 
+/* Flat particle arrays (pica's EnsembleOrdered / EnsembleUnordered).
+ * orc_order_by_position: order[i] = index of the i-th particle in lexicographic
+ *   position order over the first `dims` coordinates, ties in input order.
+ * orc_push_flat: one push of a flat FP64 array in array order with the grid-level
+ *   CIC (or TSC) gather and direct deposit on a periodic grid viewed with `guard`
+ *   layers below the domain; the current v (q w) / (hx hy hz) is added to j3;
+ *   positions and momenta are updated in place and wrapped periodically.
+ *   ref_push_flat does the same through pica's own classes (guard 2, CIC only), and
+ *   ref_order_by_position through EnsembleOrdered::reorder (std::sort: ties unordered). */
+int     orc_order_by_position(int64_t n, int32_t dims, const double* x, const double* y, const double* z,
+                              int64_t* order);
+int     orc_push_flat(const orc_config* cfg, int32_t guard, int64_t n, double* x, double* y, double* z,
+                      double* ux, double* uy, double* uz, const double* w, const int32_t* species,
+                      const double* const* f6, double* const* j3);
+int     ref_order_by_position(int64_t n, int32_t dims, const double* x, const double* y, const double* z,
+                              int64_t* order);
+int     ref_push_flat(const orc_config* cfg, int32_t guard, int64_t n, double* x, double* y, double* z,
+                      double* ux, double* uy, double* uz, const double* w, const int32_t* species,
+                      const double* const* f6, double* const* j3);
 /* Synthetic plasma: the particles the product's host generator draws for the
  * same description (same counter-based draws, same order), so that the timed
  * CPU baseline needs no product code.  Layout equal to pica_plasma_spec. */

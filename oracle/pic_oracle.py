@@ -110,6 +110,9 @@ def _lib(kind):
             "get_particles": (C.c_int, [vp] + [dp] * 7 + [ip, ip]),
             "get_counts": (C.c_int, [vp, ip]), "num_migrations": (i64, [vp]),
             "get_migrations": (C.c_int, [vp, ip, ip, ip, ip]),
+            "order_by_position": (C.c_int, [i64, C.c_int32, dp, dp, dp, C.POINTER(C.c_int64)]),
+            "push_flat": (C.c_int, [C.POINTER(OrcConfig), C.c_int32, i64] + [dp] * 7 + [ip, C.POINTER(dp),
+                                                                                   C.POINTER(dp)]),
         }
         if kind == "port":
             fp = C.POINTER(C.c_float)
@@ -137,6 +140,52 @@ def _ip(a):
 
 def _fp(a):
     return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def order_by_position(x, y=None, z=None, kind="port"):
+    """Indexes of the particles in lexicographic (x, y, z) order, over as many
+    coordinates as are given (EnsembleOrdered::reorder, EnsembleOrdered.h:61-71).
+    "port": stable (ties in input order); "reference": pica's own std::sort."""
+    lib, p = _lib(kind)
+    keys = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z) if a is not None]
+    n = len(keys[0])
+    while len(keys) < 3:
+        keys.append(keys[0])
+    order = np.zeros(n, np.int64)
+    dims = sum(a is not None for a in (x, y, z))
+    rc = getattr(lib, p + "order_by_position")(n, dims, _dp(keys[0]), _dp(keys[1]), _dp(keys[2]),
+                                              order.ctypes.data_as(C.POINTER(C.c_int64)))
+    if rc != 0:
+        raise RuntimeError(f"order_by_position failed: {rc}")
+    return order
+
+
+def push_flat(n, h, dt, particles, f6, shape=SHAPE_CIC, species=((9.10938215e-28, -4.80320427e-10),), guard=2,
+              kind="port"):
+    """One push of a flat particle array (pica's EnsembleUnordered with the grid-level
+    CIC interpolator and depositor).  particles: dict with x y z ux uy uz w species
+    (updated copies are returned); f6: ex ey ez bx by bz.  Returns (particles, j3)."""
+    lib, p = _lib(kind)
+    cfg = OrcConfig()
+    for d in range(3):
+        cfg.n[d], cfg.sc[d], cfg.h[d] = int(n[d]), 1, float(h[d])
+    cfg.dt, cfg.form, cfg.shape, cfg.deposit = float(dt), FORM_FP64_PLAIN, shape, DEPOSIT_DIRECT
+    cfg.nspecies = len(species)
+    for i, (m, q) in enumerate(species):
+        cfg.mass[i], cfg.charge[i] = m, q
+    out = {k: np.array(particles[k], dtype=np.float64) for k in ("x", "y", "z", "ux", "uy", "uz")}
+    w = np.ascontiguousarray(particles["w"], dtype=np.float64)
+    sp = np.ascontiguousarray(particles.get("species", np.zeros(len(w), np.int32)), dtype=np.int32)
+    fs = [np.ascontiguousarray(f, dtype=np.float64).reshape(-1) for f in f6]
+    j3 = [np.zeros(int(np.prod(n))) for _ in range(3)]
+    fa = (C.POINTER(C.c_double) * 6)(*[_dp(f) for f in fs])
+    ja = (C.POINTER(C.c_double) * 3)(*[_dp(j) for j in j3])
+    rc = getattr(lib, p + "push_flat")(C.byref(cfg), int(guard), len(w), *[_dp(out[k]) for k in
+                                       ("x", "y", "z", "ux", "uy", "uz")], _dp(w), _ip(sp), fa, ja)
+    if rc != 0:
+        raise RuntimeError(f"push_flat failed: {rc}")
+    out["w"], out["species"] = w, sp
+    return out, [j.reshape(n) for j in j3]
 
 
 class Oracle:

@@ -27,6 +27,8 @@
 #include "pica/particles/Particle.h"
 #include "pica/particles/ParticleArray.h"
 #include "pica/particles/EnsembleSupercells.h"
+#include "pica/particles/EnsembleOrdered.h"
+#include "pica/particles/EnsembleUnordered.h"
 #include "pica/grid/YeeGrid.h"
 #include "pica/fieldSolver/YeeSolver.h"
 #include "pica/fieldInterpolation/FieldInterpolator.h"
@@ -436,6 +438,98 @@ int ref_get_migrations(void* sim, int32_t* species, int32_t* src, int32_t* slot,
         species[i] = s->migrations[i].sp; src[i] = s->migrations[i].src;
         slot[i] = s->migrations[i].slot; dst[i] = s->migrations[i].dst;
     }
+    return 0;
+}
+
+// EnsembleOrdered::reorder (EnsembleOrdered.h:61-71) on particles whose factor is
+// their input index, so that the reordered factors give the permutation.
+int ref_order_by_position(int64_t n, int32_t dims, const double* x, const double* y, const double* z, int64_t* order) {
+    if (dims != 3) return -1;   // Particle3d: pica compares all three coordinates
+    (void)dims;
+    if (n > (int64_t)1 << 31) return -1;
+    EnsembleOrdered<PArray> e(FP3(-1e300, -1e300, -1e300), FP3(1e300, 1e300, 1e300));
+    for (int64_t i = 0; i < n; i++) {
+        Particle3d p;
+        p.setPosition(FP3(x[i], y[i], z[i]));
+        p.setFactor((double)i);
+        e.add(p);
+    }
+    e.reorder();
+    const PArray& arr = e.getParticles();
+    for (int i = 0; i < arr.size(); i++) order[i] = (int64_t)arr[i].getFactor();
+    return 0;
+}
+
+// One push of a flat array through pica's grid-level classes: EnsembleUnordered,
+// FieldInterpolatorCIC<YeeGrid<Three, double>>, BorisPusher and
+// CurrentDepositorCIC<YeeGrid<Three, double>> on a grid with origin -guard h and
+// periodic guard layers (filled before the gather, folded after the deposit).
+// The current passed to the depositor is v (q w) / (hx hy hz).
+int ref_push_flat(const orc_config* c, int32_t guard, int64_t n, double* x, double* y, double* z, double* ux,
+                  double* uy, double* uz, const double* w, const int32_t* species, const double* const* f6,
+                  double* const* j3) {
+    if (!c || c->shape != ORC_SHAPE_CIC || c->deposit != ORC_DEPOSIT_DIRECT || guard < 2) return -1;
+    const Int3 N(c->n[0], c->n[1], c->n[2]);
+    const FP3 h(c->h[0], c->h[1], c->h[2]);
+    const FP3 L((double)N.x * h.x, (double)N.y * h.y, (double)N.z * h.z);
+    YeeGrid<Three, double> grid(FP3(-(double)guard * h.x, -(double)guard * h.y, -(double)guard * h.z), h,
+                                N + Int3(2 * guard, 2 * guard, 2 * guard));
+    const Int3 sz = grid.getSize();
+    auto img = [&](int i, int j, int k) {
+        return ((size_t)wrapi(i - guard, N.x) * N.y + wrapi(j - guard, N.y)) * N.z + wrapi(k - guard, N.z);
+    };
+    for (int i = 0; i < sz.x; i++)
+        for (int j = 0; j < sz.y; j++)
+            for (int k = 0; k < sz.z; k++) {
+                const size_t o = img(i, j, k);
+                grid.ex(i, j, k) = f6[0][o]; grid.ey(i, j, k) = f6[1][o]; grid.ez(i, j, k) = f6[2][o];
+                grid.bx(i, j, k) = f6[3][o]; grid.by(i, j, k) = f6[4][o]; grid.bz(i, j, k) = f6[5][o];
+                grid.jx(i, j, k) = 0; grid.jy(i, j, k) = 0; grid.jz(i, j, k) = 0;
+            }
+    ParticleTypes::typesVector.resize(c->nspecies);
+    for (int q = 0; q < c->nspecies; q++) {
+        ParticleTypes::typesVector[q].mass = c->mass[q];
+        ParticleTypes::typesVector[q].charge = c->charge[q];
+    }
+    ParticleTypes::types = &ParticleTypes::typesVector[0];
+    ParticleTypes::numTypes = c->nspecies;
+    EnsembleUnordered<PArray> e(FP3(0, 0, 0), L);
+    for (int64_t i = 0; i < n; i++) {
+        Particle3d p;
+        p.setPosition(FP3(x[i], y[i], z[i]));
+        p.setP(FP3(ux[i], uy[i], uz[i]));
+        p.setFactor(w[i]);
+        p.setType((short)(species ? species[i] : 0));
+        e.add(p);
+    }
+    FieldInterpolatorCIC<YeeGrid<Three, double> > fi(grid);
+    CurrentDepositorCIC<YeeGrid<Three, double> > cd(grid);
+    BorisPusher<Particle3d, double> pusher(c->dt);
+    const double norm = 1.0 / (h.x * h.y * h.z);
+    PArray& arr = e.getParticles();
+    for (int i = 0; i < arr.size(); i++) {
+        PArray::ParticleRef ref = arr[i];
+        FP3 ef, bf;
+        fi.get(ref.getPosition(), ef, bf);
+        pusher.push(&ref, ef, bf);
+        const double q = c->charge[ref.getType()];
+        cd.deposit(ref.getPosition(), ref.getVelocity() * (q * ref.getFactor()) * norm);
+        FP3 r = ref.getPosition();
+        for (int d = 0; d < 3; d++) {
+            if (r[d] < 0.0) r[d] += L[d];
+            if (r[d] >= L[d]) r[d] -= L[d];
+        }
+        ref.setPosition(r);
+        x[i] = r.x; y[i] = r.y; z[i] = r.z;
+        const FP3 u = ref.getP();
+        ux[i] = u.x; uy[i] = u.y; uz[i] = u.z;
+    }
+    for (int i = 0; i < sz.x; i++)
+        for (int j = 0; j < sz.y; j++)
+            for (int k = 0; k < sz.z; k++) {
+                const size_t o = img(i, j, k);
+                j3[0][o] += grid.jx(i, j, k); j3[1][o] += grid.jy(i, j, k); j3[2][o] += grid.jz(i, j, k);
+            }
     return 0;
 }
 

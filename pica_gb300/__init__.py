@@ -262,6 +262,22 @@ class Simulation:
         """Sort every supercell by cell now (EnsembleOrdered::reorder's role)."""
         self._check(self.lib.pica_reorder(self.ctx))
 
+    def push_flat(self, x, y, z, ux, uy, uz, w, species=None, guard=2):
+        """One push of a flat particle array on this context's fields (pica_push_flat):
+        float64 CUDA tensors of one length (positions and momenta updated in place),
+        species an int32 CUDA tensor or None; J is replaced by the array's current.
+        FP64 plain form with direct deposition only."""
+        ts = (x, y, z, ux, uy, uz, w)
+        n = int(x.numel())
+        for t in ts:
+            if not (t.is_cuda and t.dtype.itemsize == 8 and t.is_contiguous() and t.numel() == n):
+                raise ValueError("flat arrays: contiguous float64 CUDA tensors of one length")
+        if species is not None and not (species.is_cuda and species.dtype.itemsize == 4 and species.numel() == n):
+            raise ValueError("species: an int32 CUDA tensor of the same length")
+        ptrs = [C.c_void_p(t.data_ptr()) for t in ts]
+        sp = C.c_void_p(species.data_ptr()) if species is not None else None
+        self._check(self.lib.pica_push_flat(self.ctx, n, *ptrs, sp, int(guard)))
+
     def chunk_ranges(self, nchunks):
         """Supercell ranges of pica_push_deposit_chunked: [n r / nchunks, n (r+1) / nchunks)."""
         return supercell_ranges(int(np.prod(self.nsc)), nchunks)
@@ -290,6 +306,91 @@ class Simulation:
                 raise ValueError("ranges must be consecutive")
         arr = (C.c_void_p * len(wait_events))(*[C.c_void_p(int(e)) if e else None for e in wait_events])
         self._check(self.lib.pica_push_deposit_ranges(self.ctx, len(ranges), bounds, arr))
+
+
+def order_by_position(x, y=None, z=None, stream=0):
+    """EnsembleOrdered::reorder's order on the device (pica_order_by_position): an
+    int64 CUDA tensor of indexes that sorts the particles lexicographically by the
+    given coordinates (float64 CUDA tensors), ties in input order."""
+    import torch
+
+    keys = [t for t in (x, y, z) if t is not None]
+    n = int(keys[0].numel())
+    for t in keys:
+        if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous() and t.numel() == n):
+            raise ValueError("positions: contiguous float64 CUDA tensors of one length")
+    order = torch.empty(n, dtype=torch.int64, device=keys[0].device)
+    p = [C.c_void_p(t.data_ptr()) for t in keys] + [None] * (3 - len(keys))
+    rc = load().pica_order_by_position(n, len(keys), p[0], p[1], p[2], C.c_void_p(order.data_ptr()),
+                                       C.c_void_p(int(stream)) if stream else None)
+    if rc:
+        raise PicaError(rc, load().pica_status_string(rc).decode())
+    return order
+
+
+class FlatEnsemble:
+    """pica's EnsembleUnordered (particles/EnsembleUnordered.h:14-40) on the device:
+    one flat SoA array of FP64 particles in insertion order, pushed by one thread per
+    particle on a Simulation's fields (FP64 plain form, direct deposition), with
+    ``reorder()`` as EnsembleOrdered::reorder (EnsembleOrdered.h:61-71).
+
+    The grid-level gather and deposit see the Simulation's periodic grid as a pica
+    YeeGrid whose origin is ``-guard`` cells (``guard`` = 2 as in pica's supercell
+    helpers).  Tensors are float64 (x y z ux uy uz w) and int32 (species)."""
+
+    KEYS = ("x", "y", "z", "ux", "uy", "uz", "w")
+
+    def __init__(self, sim, guard=2):
+        import torch
+
+        if sim.form != FORM_FP64_PLAIN:
+            raise ValueError("flat ensembles hold FP64 positions: an FP64 plain-form Simulation")
+        self.sim, self.guard = sim, int(guard)
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.t = {k: torch.empty(0, dtype=torch.float64, device=dev) for k in self.KEYS}
+        self.species = torch.empty(0, dtype=torch.int32, device=dev)
+        L = [sim.n[d] * sim.h[d] for d in range(3)]
+        self.min_position, self.max_position = (0.0, 0.0, 0.0), tuple(L)
+
+    def size(self):
+        return int(self.t["x"].numel())
+
+    def add(self, x, y, z, ux, uy, uz, w, species=None):
+        """Append particles (EnsembleUnordered::add): host arrays or tensors."""
+        import torch
+
+        dev = self.t["x"].device
+        new = [torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).to(dev) for a in (x, y, z, ux, uy, uz, w)]
+        sp = np.zeros(len(x), np.int32) if species is None else np.ascontiguousarray(species, dtype=np.int32)
+        for k, a in zip(self.KEYS, new):
+            self.t[k] = torch.cat([self.t[k], a])
+        self.species = torch.cat([self.species, torch.as_tensor(sp).to(dev)])
+
+    def particles(self):
+        """The array in its current order (EnsembleUnordered::getParticles)."""
+        out = {k: v.cpu().numpy() for k, v in self.t.items()}
+        out["species"] = self.species.cpu().numpy()
+        return out
+
+    def reorder(self):
+        """EnsembleOrdered::reorder: sort by position (x, then y, then z), stably."""
+        order = order_by_position(self.t["x"], self.t["y"], self.t["z"])
+        for k in self.KEYS:
+            self.t[k] = self.t[k][order].contiguous()
+        self.species = self.species[order].contiguous()
+        return order
+
+    def push(self):
+        """Gather, Boris push and direct deposit of every particle (J replaced)."""
+        self.sim.push_flat(*[self.t[k] for k in self.KEYS], self.species, guard=self.guard)
+
+    def step(self, nsteps=1):
+        """push; update_b(dt/2); update_e(dt); update_b(dt/2) -- pica's step order."""
+        for _ in range(int(nsteps)):
+            self.push()
+            self.sim.update_b(0.5 * self.sim.dt)
+            self.sim.update_e(self.sim.dt)
+            self.sim.update_b(0.5 * self.sim.dt)
 
 
 class Driver:

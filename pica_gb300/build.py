@@ -30,6 +30,7 @@ UNITS = [
     ("noalloc.cu", ["--fmad=false"]),
     ("plasma_gen.cu", ["--fmad=false"]),
     ("domain_kernels.cu", ["--fmad=false"]),
+    ("flat.cu", ["--fmad=false"]),
 ]
 
 

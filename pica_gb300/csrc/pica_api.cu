@@ -906,6 +906,63 @@ int pica_push_deposit_ranges(pica_ctx* ctx, int32_t nranges, const int32_t* boun
     return pushImpl(ctx, nranges, bounds, wait_events);
 }
 
+int pica_order_by_position(int64_t n, int32_t dims, const double* x, const double* y, const double* z, int64_t* order,
+                           void* stream) {
+    if (n < 0 || dims < 1 || dims > 3) return PICA_ERR_INVALID;
+    if (n == 0) return PICA_OK;
+    if (!x || (dims > 1 && !y) || (dims > 2 && !z) || !order) return PICA_ERR_INVALID;
+    if (n > ((int64_t)1 << 40)) return PICA_ERR_LIMIT;
+    const double* key[3] = {x, y, z};
+    const int e = orderByPosition(n, dims, key, order, static_cast<cudaStream_t>(stream));
+    if (e == (int)cudaErrorMemoryAllocation) { cudaGetLastError(); return PICA_ERR_OOM; }
+    return e ? PICA_ERR_CUDA : PICA_OK;
+}
+
+int pica_order_by_position_host(int64_t n, int32_t dims, const double* x, const double* y, const double* z,
+                                int64_t* order) {
+    if (n < 0 || dims < 1 || dims > 3 || (n > 0 && (!x || (dims > 1 && !y) || (dims > 2 && !z) || !order)))
+        return PICA_ERR_INVALID;
+    if (n == 0) return PICA_OK;
+    if (n > ((int64_t)1 << 40)) return PICA_ERR_LIMIT;
+    const double* host[3] = {x, y, z};
+    double* dev[3] = {nullptr, nullptr, nullptr};
+    int64_t* dorder = nullptr;
+    int rc = PICA_OK;
+    for (int d = 0; d < dims && rc == PICA_OK; d++) {
+        if (cudaMalloc(&dev[d], (size_t)n * 8) != cudaSuccess) rc = PICA_ERR_OOM;
+        else if (cudaMemcpy(dev[d], host[d], (size_t)n * 8, cudaMemcpyHostToDevice) != cudaSuccess) rc = PICA_ERR_CUDA;
+    }
+    if (rc == PICA_OK && cudaMalloc(&dorder, (size_t)n * 8) != cudaSuccess) rc = PICA_ERR_OOM;
+    if (rc == PICA_OK) rc = pica_order_by_position(n, dims, dev[0], dev[1], dev[2], dorder, nullptr);
+    if (rc == PICA_OK && cudaMemcpy(order, dorder, (size_t)n * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = PICA_ERR_CUDA;
+    for (double* p : dev) cudaFree(p);
+    cudaFree(dorder);
+    if (rc != PICA_OK) cudaGetLastError();
+    return rc;
+}
+
+int pica_push_flat(pica_ctx* ctx, int64_t n, double* x, double* y, double* z, double* ux, double* uy, double* uz,
+                   const double* w, const int32_t* species, int32_t guard) {
+    if (!ctx || n < 0 || guard < 0 || guard > 1024) return fail(ctx, PICA_ERR_INVALID, "bad flat push arguments");
+    if (n > 0 && (!x || !y || !z || !ux || !uy || !uz || !w))
+        return fail(ctx, PICA_ERR_INVALID, "a flat particle array is missing");
+    if (!ctx->fp64) return fail(ctx, PICA_ERR_NOT_BUILT, "flat particle arrays hold FP64 positions: the plain form only");
+    if (ctx->cfg.deposit != PICA_DEPOSIT_DIRECT)
+        return fail(ctx, PICA_ERR_NOT_BUILT, "flat particle arrays deposit directly (no charge-conserving form)");
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "the context's own push awaits its migration");
+    const int64_t nodes = (int64_t)ctx->cfg.n[0] * ctx->cfg.n[1] * ctx->cfg.n[2];
+    for (int k = 6; k < 9; k++) CK(cudaMemsetAsync(ctx->f[k], 0, nodes * 8, ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_flags, 0, 4 * sizeof(int), ctx->stream));
+    double* xu[6] = {x, y, z, ux, uy, uz};
+    CKL(launchPushFlat(ctx->cfg, ctx->f, guard, n, xu, w, species, ctx->d_flags, ctx->stream));
+    ctx->launches += n > 0 ? 1 : 0;
+    CK(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_flags[0]) return fail(ctx, ctx->h_flags[0], "a particle's species is outside the configuration");
+    return PICA_OK;
+}
+
 int pica_update_b(pica_ctx* ctx, double dt) {
     if (!ctx) return PICA_ERR_INVALID;
     const pica_config& c = ctx->cfg;

@@ -235,6 +235,13 @@ struct MigrateArgs {
 
 // Push launchers (push_fp64.cu / push_fp32.cu).  Return cudaError_t as int.
 int launchPushPlain(const PushArgs<PlainPtrs>& a, int shape, int deposit, cudaStream_t s);
+// Flat particle arrays (flat.cu): stable lexicographic position order of n particles
+// (dims coordinates, key[d] device arrays) into order (device), and one push of a
+// flat FP64 array (xu: x y z ux uy uz, device) on a grid seen with `guard` layers.
+int orderByPosition(int64_t n, int dims, const double* const* key, int64_t* order, cudaStream_t s);
+int launchPushFlat(const pica_config& c, void* const* f, int guard, int64_t n, double* const* xu, const double* w,
+                   const int32_t* species, int* flags, cudaStream_t s);
+
 // variant: launch shape of the FP32 Esirkepov kernel (0..kPushVariants-1), see push_fp32.cu.
 constexpr int kPushVariants = 5;
 int launchPushCell(const PushArgs<CellPtrs>& a, int shape, int deposit, int variant, cudaStream_t s);

@@ -134,8 +134,11 @@ __device__ __forceinline__ float pickN(const float* a, int i) {
 // its unrolled form is fetched from the instruction cache hierarchy at every
 // call; the selects of the rolled loops cost less than those fetch stalls.
 // len[d] is the number of window nodes the two shapes cover along d (NW, or NW-1
-// when the particle stays in its cell along d): pairs and faces beyond it carry
-// exactly zero and are not visited, nor is a pair whose transverse factor is zero.
+// when the particle stays in its cell along d): faces beyond it are not visited
+// (their sum of shape changes is zero but for rounding); a node pair whose
+// transverse factor is zero (every pair beyond the covered nodes) adds nothing and
+// is skipped.  The pair loop keeps a fixed trip count, so that its index split is a
+// division by a constant.
 template <int NW, typename Tile>
 __device__ __forceinline__ void esirkepovRolled(const Tile& jt, int TT, int T1, int T2, const int* b,
                                                 const float (*s0)[NW], const float (*s1)[NW], const float* k,
@@ -154,10 +157,10 @@ __device__ __forceinline__ void esirkepovRolled(const Tile& jt, int TT, int T1, 
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         const int t1 = c == 0 ? 1 : 0, t2 = c == 2 ? 1 : 2;
-        const int n2 = len[t2], np = len[t1] * n2, nf = len[c] - 1;
+        const int nf = len[c] - 1;
 #pragma unroll 1
-        for (int q = 0; q < np; q++) {
-            const int u = q / n2, v = q - u * n2;
+        for (int q = 0; q < NW * NW; q++) {
+            const int u = q / NW, v = q - u * NW;
             const float f = factor(pickN<NW>(s0[t1], u), pickN<NW>(ds[t1], u), pickN<NW>(s0[t2], v), pickN<NW>(ds[t2], v));
             if (f != 0.f) {
                 int n[3];
@@ -536,12 +539,11 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                 }
                 // A lane meeting another window parks its sums in a park row; when the park
                 // rows run out the warp deposits them and goes on parking.
-                // CIC: a lone particle of another window -- the lane's next particle is
-                // back in the lane's window (a particle out of cell order since the last
-                // resort) -- goes to the cell-change queue instead of costing the lane two
-                // parks.  (TSC's general window is 144 candidate values against CIC's 54;
-                // there two parks measured cheaper.)
-                const bool lone = SHAPE == PICA_SHAPE_CIC && act && key != accKey && accKey >= 0 && it + 1 < kk &&
+                // A lone particle of another window -- the lane's next particle is back
+                // in the lane's window (a particle out of cell order since the last
+                // resort) -- goes to the cell-change queue instead of costing the lane
+                // two parks.
+                const bool lone = act && key != accKey && accKey >= 0 && it + 1 < kk &&
                                   i + 1 < segEnd && pc == accCell;
                 const bool sw = act && key != accKey && !lone;
                 const bool park = sw && accKey >= 0;

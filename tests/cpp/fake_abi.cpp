@@ -94,3 +94,18 @@ int pica_download_particles(pica_ctx* ctx, double* x, double* y, double* z, doub
 }
 
 }  // extern "C"
+
+// Stand-in for the device sort: a host stable sort with pica's comparator.
+int pica_order_by_position_host(int64_t n, int32_t dims, const double* x, const double* y, const double* z,
+                                int64_t* order) {
+    const double* key[3] = {x, y, z};
+    for (int64_t i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order, order + n, [&](int64_t a, int64_t b) {
+        for (int d = 0; d < dims; d++) {
+            if (key[d][a] < key[d][b]) return true;
+            if (key[d][a] > key[d][b]) return false;
+        }
+        return false;
+    });
+    return PICA_OK;
+}

@@ -107,6 +107,39 @@ int main() {
         std::printf("supercells hold %zu particles\n", seen);
         fails++;
     }
+
+    // flat ensembles: pica's Ensemble traits, EnsembleUnordered keeps insertion order,
+    // EnsembleOrdered::reorder applies the position order to every component
+    typedef ParticleArray<Particle3d, ParticleRepresentation_SoA>::Type PA;
+    Ensemble<PA, EnsembleRepresentation_Unordered>::Type flat(FP3(0, 0, 0), FP3(1, 1, 1));
+    Ensemble<PA, EnsembleRepresentation_Ordered>::Type ordered(FP3(0, 0, 0), FP3(1, 1, 1));
+    for (int i = 0; i < 40; i++) {
+        Particle3d q;
+        q.position = FP3(0.1 * ((i * 7) % 5), 0.05 * ((i * 3) % 4), 0.01 * i);
+        q.p = FP3(i, -i, 0.5 * i);
+        q.factor = 100.0 + i;
+        q.typeIndex = (short)(i % 2);
+        flat.add(q);
+        ordered.add(q);
+    }
+    if (flat.size() != 40 || flat.getParticles()[7].getFactor() != 107.0) {
+        std::printf("EnsembleUnordered does not keep insertion order\n");
+        fails++;
+    }
+    ordered.reorder();
+    const PA& o = ordered.getParticles();
+    for (int i = 1; i < o.size(); i++) {
+        const FP3 a = o[i - 1].getPosition(), b = o[i].getPosition();
+        const bool le = a.x < b.x || (a.x == b.x && (a.y < b.y || (a.y == b.y && a.z <= b.z)));
+        const int k = (int)o[i].getFactor() - 100;
+        const bool same = o[i].getP().x == (double)k && o[i].getType() == (short)(k % 2) &&
+                          o[i].getPosition().z == 0.01 * k;
+        if (!le || !same) {
+            std::printf("EnsembleOrdered::reorder: element %d out of order or torn\n", i);
+            fails++;
+            break;
+        }
+    }
     std::printf(fails ? "failed\n" : "ok\n");
     return fails ? 1 : 0;
 }

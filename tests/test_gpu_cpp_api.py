@@ -175,3 +175,23 @@ def test_pica_drop_in_loop_matches_python(tmp_path, mode):
         for c in range(2, 8):
             assert np.max(np.abs(rows[:, c] - ref[:, c])) <= 1e-13 * np.max(np.abs(ref[:, c])), c
         np.testing.assert_allclose(last, fref, rtol=1e-11, atol=0)
+
+
+def test_cpp_ensemble_ordered_reorders_on_the_device(tmp_path):
+    """pica's EnsembleOrdered host code on the mirror: reorder() through the device
+    sort gives the stable lexicographic order of the oracle, ties included."""
+    from oracle import pic_oracle as po
+
+    so = pg._lib.lib_path()
+    pg._lib.load()
+    exe = str(tmp_path / "ordered_ensemble")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "ordered_ensemble.cpp"), so, "-o", exe,
+                    "-Wl,-rpath," + os.path.dirname(so), "-lpthread"], check=True)
+    for n, seed in ((1, 1), (1000, 2), (9000, 3)):
+        out = subprocess.run([exe, str(n), str(seed)], capture_output=True, text=True, check=True).stdout
+        rows = np.array([[float(v) for v in line.split()] for line in out.strip().split("\n")])
+        perm = rows[:, 0].astype(np.int64)
+        xyz = np.empty((n, 3))
+        xyz[perm] = rows[:, 1:]                  # positions in input order
+        assert np.array_equal(perm, po.order_by_position(xyz[:, 0], xyz[:, 1], xyz[:, 2]))
