@@ -165,6 +165,9 @@ def parse():
                     help="batching form with every member edge halved (default: the full member sizes, grids "
                          "32^3-96^3, 1.85e9 particles)")
     ap.add_argument("--batched-steps", type=int, default=10)
+    ap.add_argument("--flat-steps", type=int, default=0,
+                    help="pushes per order of the flat-layout leg (pica's EnsembleUnordered / EnsembleOrdered, "
+                         "FP64 CIC direct) against the supercell layout (0: skip)")
     ap.add_argument("--validate-steps", type=int, default=1000,
                     help="steps of the FP32-vs-FP64 error run on a 32^3 block (0: skip)")
     return ap.parse_args()
@@ -416,6 +419,76 @@ def cpu_sample(workload="thermal", edge=None, steps=2, warmup=1, pica_path=False
                   f"after {warmup} warm-up, oracle restatement (pica has no Esirkepov"
                   f"{'' if shape == 'CIC' else ' or TSC'}), OpenMP {cores} threads")
     return npart * steps / el, cores, sample, el
+
+
+def flat_measure(args, parts, stream):
+    """pica's own operators (FP64 positions, CIC, Boris, direct deposition) on the
+    headline plasma in three layouts: supercells (pica_push_deposit, shared-memory
+    current tiles), and one flat array (pica_push_flat, FP64 global atomics) in the
+    generator's cell order, in a random order, and after EnsembleOrdered::reorder
+    (pica_order_by_position).  Milliseconds per push by CUDA events (median of
+    args.flat_steps after one untimed push), and the reorder's time."""
+    import torch
+
+    import pica_gb300 as pg
+
+    keys = ("x", "y", "z", "ux", "uy", "uz", "w")
+    wl = make_workload(args.edge, pg.FORM_FP64_PLAIN)
+    sim = dict(wl["sim"], shape=pg.SHAPE_CIC, deposit=pg.DEPOSIT_DIRECT)
+    n = sim["n"]
+
+    def timed(fn, after=None):
+        ts = []
+        for r in range(args.flat_steps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+            if after:
+                after()
+        return float(np.median(ts[1:]))
+
+    out = {"workload": "the headline plasma, FP64 positions, CIC, Boris, direct deposition, E = B = 0"}
+    s = pg.Simulation(**sim)
+    s.set_stream(stream.cuda_stream)
+    s.upload_particles(*[parts[k] for k in keys], parts["species"])
+    s.upload_fields([np.zeros(n)] * 9)
+
+    def rest():
+        s.update_b(0.5 * s.dt)
+        s.update_e(s.dt)
+        s.update_b(0.5 * s.dt)
+        s.migrate()
+    out["supercell_push_ms"] = timed(s.push_deposit, rest)
+    s.close()
+    f = pg.Simulation(**dict(sim, supercell=(1, 1, 1)))
+    f.set_stream(stream.cuda_stream)
+    f.upload_fields([np.zeros(n)] * 9)
+    e = pg.FlatEnsemble(f)
+    e.add(*[parts[k] for k in keys], parts["species"])
+    out["flat_cell_order_push_ms"] = timed(e.push)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1)
+    perm = torch.randperm(e.size(), device="cuda", generator=g)
+    for k in e.KEYS:
+        e.t[k] = e.t[k][perm].contiguous()
+    e.species = e.species[perm].contiguous()
+    del perm
+    out["flat_random_push_ms"] = timed(e.push)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    e.reorder()
+    b.record(stream)
+    torch.cuda.synchronize()
+    out["reorder_ms"] = a.elapsed_time(b)
+    out["flat_ordered_push_ms"] = timed(e.push)
+    out["pushes"] = args.flat_steps
+    del e
+    f.close()
+    torch.cuda.synchronize()
+    return out
 
 
 def run_reference(args):
@@ -681,6 +754,11 @@ def main():
                 "steps": args.fp64_steps, "dtype": "fp64", "form": "FP64 plain (absolute positions)"}
         s64.close()
 
+    # ---------------- flat layouts (EnsembleUnordered / EnsembleOrdered) ----------------
+    flat = None
+    if headline and args.flat_steps > 0:
+        flat = flat_measure(args, parts, stream)
+
     # ---------------- batching form: many plasmas, persistent push + CUDA graph ----------------
     batched = None
     if headline and args.batched > 0:
@@ -719,6 +797,7 @@ def main():
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
         "fp64_form": fp64, "fp32_over_fp64": (value / world / fp64["value"]) if fp64 else None,
         "fp32_vs_fp64_errors": errors,
+        "flat_layout": flat,
         "batched": batched,
         "tuning": {"push_variant": sim_variant, "variant_s_per_step": {str(k): v for k, v in tune.items()},
                    "resort_every": resort},

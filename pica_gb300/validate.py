@@ -64,11 +64,13 @@ def match_particles(a, b, L, nsc3, pos_tol=1e-3):
     """One-to-one match of two ensembles of the same plasma (particles() dicts).
 
     Slot by slot within every (species, supercell) whose counts agree and whose
-    slot-wise positions lie within pos_tol of the box edge per axis;
-    the particles of the other supercells and of their 26 neighbours are matched by
-    nearest neighbour in (position, momentum), positions periodic.  Returns index
-    arrays (ia, ib) and the number of particles matched by nearest neighbour; None
-    when the ensembles differ in size per species."""
+    slot-wise positions lie within pos_tol of the box edge per axis; the particles of
+    the other supercells (a particle that sits in neighbouring supercells in the two
+    ensembles makes both of them disagree) are matched by nearest neighbour in
+    (position, momentum), positions periodic, across all of them at once.  Returns
+    index arrays (ia, ib) and the number of particles matched by nearest neighbour;
+    None when the ensembles differ in size per species or the match is not one to
+    one."""
     nsc = int(np.prod(nsc3))
     nsp = int(max(a["species"].max(initial=0), b["species"].max(initial=0))) + 1
     ka = a["species"].astype(np.int64) * nsc + a["supercell"]
@@ -86,14 +88,7 @@ def match_particles(a, b, L, nsc3, pos_tol=1e-3):
     groups = np.union1d(np.nonzero(ca != cb)[0], kb[ib[bad]])
     if len(groups) == 0:
         return ia, ib, 0
-    sx, sy, sz = np.unravel_index(groups % nsc, nsc3)
-    near = set()
-    for dx in (-1, 0, 1):
-        for dy in (-1, 0, 1):
-            for dz in (-1, 0, 1):
-                near.update(np.ravel_multi_index(((sx + dx) % nsc3[0], (sy + dy) % nsc3[1], (sz + dz) % nsc3[2]),
-                                                 nsc3).tolist())
-    near = np.array(sorted(near))
+    near = np.unique(groups % nsc)
     keep = ~np.isin(b["supercell"][ib], near)
     ia, ib = [ia[keep]], [ib[keep]]
     from scipy.spatial import cKDTree
