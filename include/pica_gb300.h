@@ -69,11 +69,7 @@ typedef struct pica_config {
     double mass[4];      /* g                                                            */
     double charge[4];    /* statC                                                        */
     double slack;        /* spare slots per supercell as a fraction of its count (0 -> 0.15) */
-    int32_t resort_every;/* compact each supercell, sort it by cell and re-balance capacities every
-                          * k steps (0 = never: capacities on overflow only).  -1 (FP32 cell form,
-                          * Esirkepov): sorted push -- every push writes a supercell's stayers to
-                          * the other buffer in the stable order of their new cell, and the
-                          * migration appends the arrivals in canonical order after them */
+    int32_t resort_every;/* re-balance supercell capacities every k steps (0 = on overflow only) */
     int32_t threads;     /* host threads for upload/download/generation (0 = hardware) */
 } pica_config;
 

@@ -834,30 +834,9 @@ void Sim<R, Store>::migrate() {
                 }
         // Each destination: this step's own leavers leave holes (ascending slots); arrivals
         // in canonical order (direction code, then source slot) fill the holes, then append.
-        // Sorted push (resort_every == -1): the stayers, stably sorted by their new cell,
-        // come first and the arrivals are appended in the same canonical order.
         std::vector<Store> next(nscTot);
-        const bool sorted = cfg.resort_every == -1;
 #pragma omp parallel for schedule(dynamic, 8)
         for (int d = 0; d < nscTot; d++) {
-            if (sorted) {
-                int dc[3]; scCoords(d, dc);
-                const int m[3] = {dc[0] * cfg.sc[0], dc[1] * cfg.sc[1], dc[2] * cfg.sc[2]};
-                std::vector<std::pair<int, size_t>> key;
-                for (size_t p = 0; p < sc[d].size(); p++)
-                    if (dirs[d][p] == 13) key.push_back({cellKey(*this, sc[d], p, m), p});
-                std::stable_sort(key.begin(), key.end(),
-                                 [](const std::pair<int, size_t>& a, const std::pair<int, size_t>& b) { return a.first < b.first; });
-                for (auto& k : key) next[d].append(sc[d], k.second);
-                for (int dir = 0; dir < 27; dir++) {
-                    if (dir == 13) continue;
-                    int ds[3]; dirDelta(dir, ds);
-                    int src = scLinear(wrapi(dc[0] - ds[0], nsc[0]), wrapi(dc[1] - ds[1], nsc[1]), wrapi(dc[2] - ds[2], nsc[2]));
-                    for (size_t p = 0; p < sc[src].size(); p++)
-                        if (dirs[src][p] == dir) next[d].append(sc[src], p);
-                }
-                continue;
-            }
             next[d] = sc[d];
             std::vector<size_t> holes;
             for (size_t p = 0; p < sc[d].size(); p++)

@@ -21,10 +21,7 @@
  *     code 0..26 of the move, then source slot) into the slots its own
  *     leavers vacated in this step (ascending), then appended at the end;
  *   - every resort_every steps: each supercell drops its dead slots and is
- *     re-sorted by cell (stable);
- *   - resort_every == -1 (sorted push; the restatement only): each step a
- *     supercell holds its stayers, stably sorted by their new cell, then its
- *     arrivals in the same canonical order (no dead slots).
+ *     re-sorted by cell (stable).
  * Downloads list the live particles in slot order.
  */
 #ifndef PICA_ORACLE_H
@@ -52,9 +49,7 @@ typedef struct orc_config {
     double mass[4];      /* g                                            */
     double charge[4];    /* statC                                        */
     int32_t threads;     /* OpenMP threads, 0 = runtime default          */
-    int32_t resort_every;/* compact + sort each supercell by cell every k steps (0 = never);
-                          * -1: sorted push -- each step the stayers of a supercell, stably
-                          * sorted by their new cell, then the arrivals in canonical order */
+    int32_t resort_every;/* compact + sort each supercell by cell every k steps (0 = never) */
 } orc_config;
 
 /* Diagnostics, all FP64 sums (see orc_diagnostics). */

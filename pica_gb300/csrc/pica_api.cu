@@ -103,10 +103,6 @@ int fail(pica_ctx* c, int code, const std::string& msg) {
     return code;
 }
 
-// resort_every == -1: the FP32 push writes each supercell's stayers sorted by cell
-// into the other buffer (see SpeciesArgsSlim in pica_internal.h).
-bool sortedPush(const pica_ctx* c) { return !c->fp64 && c->cfg.resort_every == -1; }
-
 #define CK(call)                                                                               \
     do {                                                                                       \
         cudaError_t e_ = (call);                                                               \
@@ -343,14 +339,11 @@ static void fillPushArgs(pica_ctx* ctx, A& a) {
     a.tileSplit = ctx->tileSplit;
     a.norm = 1.0 / (c.h[0] * c.h[1] * c.h[2]);   // CurrentDepositorYeeGrid.h:203
     a.flags = ctx->d_flags;
-    if constexpr (std::is_same<A, PushArgs<CellPtrs>>::value) {
-        a.tmaps = ctx->hasTmaps ? &ctx->tmaps : nullptr;
-        a.sorted = sortedPush(ctx) ? 1 : 0;
-    }
+    if constexpr (std::is_same<A, PushArgs<CellPtrs>>::value) a.tmaps = ctx->hasTmaps ? &ctx->tmaps : nullptr;
     for (int q = 0; q < c.nspecies; q++) {
         SpeciesState& S = ctx->sp[q];
         auto& sa = a.sp[q];
-        sa.start = S.d_start; sa.cap = S.d_cap; sa.count = S.d_count; sa.alive = S.d_alive;
+        sa.start = S.d_start; sa.cap = S.d_cap; sa.count = S.d_count;
         sa.nleave = S.d_nleave; sa.llist = S.llist; sa.dir = S.dir;
         sa.ec = c.charge[q] * c.dt / (2.0 * c.mass[q] * kC);   // BorisPusher.h:29
         sa.q = c.charge[q];
@@ -396,9 +389,6 @@ int pica_ctx_create(const pica_config* cfg, pica_ctx** out) {
         if (!(cfg->h[d] > 0)) return PICA_ERR_INVALID;
     }
     if (cfg->form == PICA_FORM_FP32_CELL && (cfg->n[0] > 2048 || cfg->n[1] > 2048 || cfg->n[2] > 1024)) return PICA_ERR_LIMIT;
-    if (cfg->resort_every < -1) return PICA_ERR_INVALID;
-    if (cfg->resort_every == -1 && (cfg->form != PICA_FORM_FP32_CELL || cfg->deposit != PICA_DEPOSIT_ESIRKEPOV))
-        return PICA_ERR_NOT_BUILT;   // the sorted push is a mode of the FP32 charge-conserving kernel
     // No CUDA device (or no driver): a CUDA error, not an allocation failure.  There is no CPU path.
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
@@ -883,7 +873,6 @@ static int pushImpl(pica_ctx* ctx, int nchunks, const int32_t* bounds, void* con
             }
         }
     }
-    if (sortedPush(ctx)) ctx->cur = 1 - ctx->cur;   // the stayers, sorted, are in the other buffer now
     if (!ctx->fp64) {
         // J = sum / h^3 (CurrentDepositorYeeGrid.h:203), from the exact fixed-point sums.
         const double scale = (ctx->kmax * std::ldexp(1.0, -ctx->jfrac)) * (1.0 / (c.h[0] * c.h[1] * c.h[2]));
@@ -1024,8 +1013,7 @@ static void migrateArgs(pica_ctx* ctx, MigrateArgs<P>& a) {
         SpeciesState& S = ctx->sp[q];
         for (int32_t v : S.h_cap) maxCap = std::max(maxCap, v);
         auto& m = a.sp[q];
-        // After a sorted push the leaver records sit in the current buffer itself.
-        m.a = ptrsOf<P>(S.buf[A]); m.b = ptrsOf<P>(S.buf[sortedPush(ctx) ? A : B]); m.dst = ptrsOf<P>(S.buf[B]);
+        m.a = ptrsOf<P>(S.buf[A]); m.b = ptrsOf<P>(S.buf[B]); m.dst = ptrsOf<P>(S.buf[B]);
         m.outbox = ptrsOf<P>(S.outbox);
         m.start = S.d_start; m.cap = S.d_cap; m.count = S.d_count; m.alive = S.d_alive;
         m.nleave = S.d_nleave; m.llist = S.llist; m.dir = S.dir;
@@ -1034,7 +1022,6 @@ static void migrateArgs(pica_ctx* ctx, MigrateArgs<P>& a) {
         m.lbydir = S.lbydir; m.dirOff = S.d_dirOff;
     }
     a.bitmapWords = (maxCap + 31) / 32;
-    a.sorted = sortedPush(ctx) ? 1 : 0;
 }
 
 template <class P>
@@ -1901,7 +1888,7 @@ int pica_batch_create(const pica_config* cfgs, int32_t count, pica_batch** out) 
     for (int k = 0; k < count; k++) {
         const pica_config& c = cfgs[k];
         if (c.form != PICA_FORM_FP32_CELL || c.deposit != PICA_DEPOSIT_ESIRKEPOV || c.shape != cfgs[0].shape ||
-            c.nspecies > kBatchSpecies || c.resort_every < 0)
+            c.nspecies > kBatchSpecies)
             return PICA_ERR_INVALID;
         for (int d = 0; d < 3; d++)
             if (c.sc[d] != cfgs[0].sc[d]) return PICA_ERR_INVALID;

@@ -88,11 +88,10 @@ __host__ __device__ inline bool aliveX(double x) { return x > -1.0e299; }
 template <class P>
 struct SpeciesArgs {
     P buf;             // A: updated in place
-    P out;             // B: leaver records, packed at start + k (sorted push: at start + cap - 1 - k)
+    P out;             // B: leaver records, packed at start + k
     const int64_t* start;
     const int32_t* cap;
-    int32_t* count;    // sorted push: set to the live count of B's sorted stayers
-    int32_t* alive;
+    const int32_t* count;
     int32_t* nleave;   // leavers per supercell (this step)
     int32_t* llist;    // leaver slots, list of supercell s at [start[s], start[s] + nleave[s])
     uint32_t* dir;     // per slot, valid for leavers: direction code | (packed record index << 5)
@@ -116,7 +115,6 @@ struct PushArgs {
     double norm;        // FP64 form: 1 / (hx hy hz)
     int* flags;         // flags[0]: error code (0 = ok)
     int scBegin, scEnd; // FP32 Esirkepov push: supercells [scBegin, scEnd) (scEnd 0: all)
-    int sorted;         // FP32 Esirkepov push: sorted push (see SpeciesArgsSlim)
     const struct TmaFieldMaps* tmaps;   // FP32 form, host: tensor maps of ex..bz (nullptr: none)
     SpeciesArgs<P> sp[kMaxSpecies];
 };
@@ -137,18 +135,11 @@ struct alignas(64) TmaFieldMaps {
 // those of up to batchMembers<NSP>() plasmas of at most NSP species in its kernel
 // parameters, work item w (one supercell) belonging to plasma k with
 // base[k] <= w < base[k + 1].
-// Sorted push (PushArgsSlim::sorted): after a supercell's particles are pushed in
-// place in buf, its stayers go to out at [start, start + live) in the stable order of
-// their new cell, count and alive become that live count, and the leaver records sit
-// at the top of the supercell's range of out (start + cap - 1 - k); out then becomes
-// the current buffer, and the migration appends arrivals (there are no holes).
 struct SpeciesArgsSlim {
     CellPtrs buf;
     CellPtrs out;
     const int64_t* start;
-    const int32_t* cap;
-    int32_t* count;
-    int32_t* alive;
+    const int32_t* count;
     int32_t* nleave;
     int32_t* llist;
     uint32_t* dir;
@@ -161,7 +152,6 @@ struct PushArgsSlim {
     int nspecies;
     int tileSplit;
     int scOffset;       // first supercell of the launch (block b works on supercell scOffset + b)
-    int sorted;         // sorted push (see SpeciesArgsSlim)
     float cdth[3];
     float invUnit;
     const void* eb[6];
@@ -182,14 +172,13 @@ inline void slimArgs(const PushArgs<CellPtrs>& a, PushArgsSlim<NSP>& o) {
     o.nspecies = a.nspecies;
     o.tileSplit = a.tileSplit;
     o.scOffset = a.scBegin;
-    o.sorted = a.sorted;
     o.invUnit = (float)a.invUnit;
     for (int k = 0; k < 6; k++) o.eb[k] = a.eb[k];
     o.flags = a.flags;
     for (int q = 0; q < a.nspecies && q < NSP; q++) {
         const auto& x = a.sp[q];
         auto& y = o.sp[q];
-        y.buf = x.buf; y.out = x.out; y.start = x.start; y.cap = x.cap; y.count = x.count; y.alive = x.alive;
+        y.buf = x.buf; y.out = x.out; y.start = x.start; y.count = x.count;
         y.nleave = x.nleave; y.llist = x.llist; y.dir = x.dir; y.ec = (float)x.ec;
         for (int d = 0; d < 3; d++) y.kq[d] = (float)x.kq[d];
     }
@@ -215,7 +204,7 @@ constexpr int kDirBuckets = 28;  // 27 direction codes + end
 template <class P>
 struct MigrateSpecies {
     P a;                    // A (current)
-    P b;                    // leaver records: B at start + k (sorted push: A at start + cap - 1 - k)
+    P b;                    // B (leaver records, packed at start + k)
     P dst;                  // rebuild / resort destination (new layout)
     P outbox;               // rebuild: leaver copies gathered per source supercell
     const int64_t* start;
@@ -240,7 +229,6 @@ struct MigrateArgs {
     double invh[3];         // FP64 resort: local cell from x
     int bitmapWords;        // leaver sort: 32-bit words covering the largest count
     int srcMaxCap;          // resort: largest capacity of the source layout (any species)
-    int sorted;             // after a sorted push: no holes, records at the top of each range of A
     int* flags;             // flags[0] error code, flags[1] overflow
     MigrateSpecies<P> sp[kMaxSpecies];
 };

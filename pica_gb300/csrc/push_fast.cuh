@@ -348,88 +348,6 @@ __device__ __forceinline__ bool mbarWait(unsigned mbar, unsigned parity, int lim
 }
 constexpr int kTmaWaitPolls = 1 << 20;
 
-// Sorted push, after a supercell's particles were pushed in place: its live slots
-// [0, count) of A (leavers are dead there) go to B at [start, start + live) in the
-// stable order of their local cell; returns the live count.  A counting sort on the
-// whole CTA: warp w owns the w-th contiguous share of the slots (a multiple of 32),
-// counts the cells of its share, a scan over (cell, warp) gives every warp its first
-// position in each cell, and the warp scatters its share in slot order (ranks among
-// equal cells of a 32-slot step from __match_any_sync).  cnt: shared scratch of at
-// least warps * cells + warps + 1 ints.  A was written by this CTA; its lines are
-// read back mostly from L2.
-template <int THREADS>
-__device__ __forceinline__ int sortStayers(const CellPtrs A, const CellPtrs B, const int64_t start, const int count,
-                                        const int m0, const int m1, const int m2, const int Sx, const int Sy, const int Sz,
-                                        int* cnt) {
-    constexpr int W = THREADS / 32;
-    constexpr unsigned FULL = 0xffffffffu;
-    const int NC = Sx * Sy * Sz;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const unsigned lt = (1u << lane) - 1u;
-    int* wsum = cnt + W * NC;
-    for (int t = threadIdx.x; t < W * NC; t += THREADS) cnt[t] = 0;
-    __syncthreads();
-    const int share = ((count + W - 1) / W + 31) & ~31;
-    const int b0 = min(count, warp * share), b1 = min(count, b0 + share);
-    auto keyOf = [&](int i) {
-        if (i >= b1) return -1;
-        const uint32_t c = A.cell[start + i];
-        if (c == kDeadCell) return -1;
-        int x, y, z;
-        unpackCell(c, x, y, z);
-        return ((x - m0) * Sy + (y - m1)) * Sz + (z - m2);
-    };
-    for (int i0 = b0; i0 < b1; i0 += 32) {
-        const int key = keyOf(i0 + lane);
-        const unsigned peers = __match_any_sync(FULL, key);
-        if (key >= 0 && lane == __ffs(peers) - 1) cnt[warp * NC + key] += __popc(peers);
-        __syncwarp();
-    }
-    __syncthreads();
-    // Exclusive scan over (cell, warp): thread t owns cells [t per, (t + 1) per).
-    const int per = (NC + THREADS - 1) / THREADS;
-    const int c0 = min(NC, threadIdx.x * per), c1 = min(NC, c0 + per);
-    int tot = 0;
-    for (int c = c0; c < c1; c++)
-        for (int w = 0; w < W; w++) tot += cnt[w * NC + c];
-    int incl = tot;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += v;
-    }
-    if (lane == 31) wsum[warp] = incl;
-    __syncthreads();
-    int run = incl - tot;
-    for (int w = 0; w < warp; w++) run += wsum[w];
-    if (threadIdx.x == THREADS - 1) wsum[W] = run + tot;   // the live count
-    for (int c = c0; c < c1; c++)
-        for (int w = 0; w < W; w++) {
-            const int v = cnt[w * NC + c];
-            cnt[w * NC + c] = run;
-            run += v;
-        }
-    __syncthreads();
-    for (int i0 = b0; i0 < b1; i0 += 32) {
-        const int i = i0 + lane;
-        const int key = keyOf(i);
-        const unsigned peers = __match_any_sync(FULL, key);
-        if (key >= 0) {
-            const int64_t src = start + i, dst = start + cnt[warp * NC + key] + __popc(peers & lt);
-            B.cell[dst] = A.cell[src];
-            B.ox[dst] = A.ox[src]; B.oy[dst] = A.oy[src]; B.oz[dst] = A.oz[src];
-            B.ux[dst] = A.ux[src]; B.uy[dst] = A.uy[src]; B.uz[dst] = A.uz[src];
-            B.w[dst] = A.w[src];
-        }
-        __syncwarp();
-        if (key >= 0 && lane == __ffs(peers) - 1) cnt[warp * NC + key] += __popc(peers);
-        __syncwarp();
-    }
-    const int live = wsum[W];
-    __syncthreads();   // every thread has read the live count; cnt may be reused
-    return live;
-}
-
 // One supercell s of the plasma described by a, on the whole CTA (smem_raw: the
 // dynamic shared memory, esirkepovSmemWords words).  SC > 0: cubic supercells of
 // edge SC known at compile time (tile strides become constants); SC == 0: edges
@@ -553,9 +471,6 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
         const auto& sa = a.sp[spi];
         const int64_t start = sa.start[s];
         const int count = sa.count[s];
-        // Leaver record k: out at start + k, or (sorted push) at start + cap - 1 - k.
-        const int64_t recBase = a.sorted ? start + sa.cap[s] - 1 : start;
-        const int64_t recStep = a.sorted ? -1 : 1;
         const float ec = (float)sa.ec;
         const float kqs[3] = {(float)sa.kq[0] * invU, (float)sa.kq[1] * invU, (float)sa.kq[2] * invU};
         if (threadIdx.x == 0) s_nleave = 0;
@@ -860,13 +775,13 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     stage[stageIdx(6, sp)] = __float_as_uint(u[2]);
                     if (code != 13) {
                         const int k = atomicAdd(&s_nleave, 1);
-                        const int64_t o = recBase + recStep * k;   // leaver records are packed (see pica_internal.h)
+                        const int64_t o = start + k;   // leaver records are packed (see pica_internal.h)
                         sa.out.cell[o] = pc2;
                         sa.out.ox[o] = on[0]; sa.out.oy[o] = on[1]; sa.out.oz[o] = on[2];
                         sa.out.ux[o] = u[0]; sa.out.uy[o] = u[1]; sa.out.uz[o] = u[2];
                         sa.out.w[o] = wgt;
                         sa.dir[slot] = (uint32_t)code | ((uint32_t)k << 5);
-                        sa.llist[start + k] = i;
+                        sa.llist[o] = i;
                     }
                 }
                 // Queue window changes in the ring; deposit 32 at a time (one per lane).
@@ -918,12 +833,6 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
         }
         __syncthreads();
         if (threadIdx.x == 0) sa.nleave[s] = s_nleave;
-        if (a.sorted) {
-            // The reduction rows are free between species: scratch of the stayer sort.
-            const int live = sortStayers<THREADS>(sa.buf, sa.out, start, count, m[0], m[1], m[2], Sx, Sy, Sz,
-                                                  reinterpret_cast<int*>(eb + 6 * ETT + kWarps * (kRing * kQWords)));
-            if (threadIdx.x == 0) { sa.count[s] = live; sa.alive[s] = live; }
-        }
         __syncthreads();
     }
     if (qN > 0) drainRing<SHAPE>(ringS, 0, qN, jts, TT, T1, T2);

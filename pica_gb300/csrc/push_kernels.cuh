@@ -730,9 +730,7 @@ __global__ void __launch_bounds__(128) k_sortLeavers(const __grid_constant__ Mig
         const int n = sa.nleave[s];
         const int64_t start = sa.start[s];
         if (n > 1) {   // uniform across the block
-            // Leaver slots are below the pre-push count; after a sorted push count holds
-            // the live stayers, so the capacity bounds the bitmap instead.
-            const int nw = ((a.sorted ? sa.cap[s] : sa.count[s]) + 31) / 32;
+            const int nw = (sa.count[s] + 31) / 32;
             for (int w = threadIdx.x; w < nw; w += blockDim.x) bits[w] = 0u;
             __syncthreads();
             for (int k = threadIdx.x; k < n; k += blockDim.x) {
@@ -863,13 +861,6 @@ __device__ __forceinline__ int forArrivals(const MigrateArgs<P>& a, const Migrat
     return total;
 }
 
-// Slot in the side buffer of record rec of source supercell src (first slot srcStart).
-template <class P>
-__device__ __forceinline__ int64_t recordSlot(const MigrateArgs<P>& a, const MigrateSpecies<P>& sa, int src,
-                                              int64_t srcStart, int rec) {
-    return a.sorted ? srcStart + sa.cap[src] - 1 - rec : srcStart + rec;
-}
-
 template <class P, int STAGE>
 __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ MigrateArgs<P> a) {
     const int nscTot = a.nsc[0] * a.nsc[1] * a.nsc[2];
@@ -880,7 +871,6 @@ __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ Migrate
         const MigrateSpecies<P>& sa = a.sp[spi];
         const int64_t start = sa.start[d];
         const int nh = sa.nleave[d];
-        const int holes = a.sorted ? 0 : nh;   // after a sorted push the leavers left no holes
         const int cnt = sa.count[d];
         int arrivals;
         if constexpr (STAGE == kCountArrivals) {
@@ -888,26 +878,23 @@ __global__ void __launch_bounds__(256) k_migrate(const __grid_constant__ Migrate
             int64_t sst;
             arrivals = arrivalBuckets(a, sa, d, src, sst, b0, pre);
             if (lane == 0) {
-                const int need = cnt + max(0, arrivals - holes);
+                const int need = cnt + max(0, arrivals - nh);
                 sa.needed[d] = need;
-                sa.neededAlive[d] = sa.alive[d] - holes + arrivals;
-                // Sorted push: arrivals must not reach the supercell's own leaver records,
-                // which its neighbours are reading.
-                if (need > sa.cap[d] - (a.sorted ? nh : 0)) atomicExch(a.flags + 1, 1);
+                sa.neededAlive[d] = sa.alive[d] - nh + arrivals;
+                if (need > sa.cap[d]) atomicExch(a.flags + 1, 1);
             }
         } else if constexpr (STAGE == kGatherOutbox) {
             const int64_t off = sa.outOff[d];
-            for (int k = lane; k < nh; k += 32)
-                copyParticle(sa.b, recordSlot(a, sa, d, start, sa.lbydir[start + k]), sa.outbox, off + k);
+            for (int k = lane; k < nh; k += 32) copyParticle(sa.b, start + sa.lbydir[start + k], sa.outbox, off + k);
         } else if constexpr (STAGE == kRebuild) {
             const int64_t ns = sa.newStart[d];
             for (int i = lane; i < cnt; i += 32) copyParticle(sa.a, start + i, sa.dst, ns + i);
             __syncwarp();
             arrivals = forArrivals(a, sa, d, [&](int k, int src, int, int r, int64_t) {
-                const int target = k < holes ? sa.llist[start + k] : cnt + (k - holes);
+                const int target = k < nh ? sa.llist[start + k] : cnt + (k - nh);
                 copyParticle(sa.outbox, sa.outOff[src] + r, sa.dst, ns + target);
             });
-            if (lane == 0) { sa.count[d] = cnt + max(0, arrivals - holes); sa.alive[d] = sa.alive[d] - holes + arrivals; }
+            if (lane == 0) { sa.count[d] = cnt + max(0, arrivals - nh); sa.alive[d] = sa.alive[d] - nh + arrivals; }
         }
     }
 }
@@ -923,14 +910,14 @@ __global__ void __launch_bounds__(kFillWarps * 32) k_fill(const __grid_constant_
     for (int spi = 0; spi < a.nspecies; spi++) {
         const MigrateSpecies<P>& sa = a.sp[spi];
         const int64_t start = sa.start[d];
-        const int nh = a.sorted ? 0 : sa.nleave[d];   // holes (none after a sorted push)
+        const int nh = sa.nleave[d];
         const int cnt = sa.count[d];
         const int alive = sa.alive[d];
         const int arrivals = forArrivals(
             a, sa, d,
-            [&](int k, int src, int rec, int, int64_t srcStart) {
+            [&](int k, int, int slot, int, int64_t srcStart) {
                 const int target = k < nh ? sa.llist[start + k] : cnt + (k - nh);
-                copyParticle(sa.b, recordSlot(a, sa, src, srcStart, rec), sa.a, start + target);
+                copyParticle(sa.b, srcStart + slot, sa.a, start + target);
             },
             warp, kFillWarps);
         __syncthreads();   // every warp has read count and alive

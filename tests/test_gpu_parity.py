@@ -140,62 +140,6 @@ def test_fp32_cell_form_matches_oracle(shape, deposit):
         assert rel_err(fs[c], fo[c]) < 1e-4, c
 
 
-@pytest.mark.parametrize("shape", [pg.SHAPE_CIC, pg.SHAPE_TSC])
-@pytest.mark.parametrize("n,sc", [((16, 16, 8), (4, 4, 4)), ((16, 8, 8), (4, 4, 2))])
-def test_fp32_sorted_push_matches_oracle(shape, n, sc):
-    """resort_every = -1, the sorted push: every step each supercell holds its stayers
-    sorted by their new cell (stable), then its arrivals in canonical order.  Two
-    species and random fields; the per-supercell counts and the migration list are
-    equal to the oracle's after every step, and the final ensemble slot by slot (so
-    the order is the oracle's)."""
-    d = thermal_inputs(n, 6, seed=33, u_sigma=0.15, nspecies=2)
-    species = (pg.ELECTRON, (pg.ELECTRON_MASS * 100.0, -pg.ELECTRON_CHARGE))
-    rng = np.random.default_rng(6)
-    fields = [1e3 * rng.standard_normal(n) for _ in range(6)] + [np.zeros(n)] * 3
-    s, o = run_pair(n, sc, d, 6, pg.FORM_FP32_CELL, shape, pg.DEPOSIT_ESIRKEPOV, species=species, fields=fields,
-                    resort_every=-1)
-    ps, pr = s.particles(), o.particles()
-    L = [n[k] * d["h"][k] for k in range(3)]
-    assert np.array_equal(ps["supercell"], pr["supercell"])
-    assert np.array_equal(ps["species"], pr["species"])
-    for k, key in enumerate(("x", "y", "z")):
-        assert periodic_err(ps[key], pr[key], L[k]) < 1e-6
-    for key in ("ux", "uy", "uz"):
-        assert rel_err(ps[key], pr[key]) < 1e-4
-    fs, fo = s.fields(), o.get_fields()
-    for c in range(9):
-        assert rel_err(fs[c], fo[c]) < 1e-4, c
-    s.close()
-
-
-def test_sorted_push_overflow_rebuild_keeps_order():
-    """The cold beam of test_migration_overflow_rebuild_keeps_order in the FP32 sorted
-    push: arrivals that would reach the destination's own leaver records (kept at the
-    top of its range) overflow, the layout is rebuilt, and the order stays the oracle's."""
-    n, sc = (16, 4, 4), (2, 2, 2)
-    d = thermal_inputs(n, 2, seed=41, u_sigma=1e-4)
-    h = d["h"]
-    m = 120
-    rng = np.random.default_rng(5)
-    x = np.concatenate([d["x"], (1.97 + 0.02 * rng.random(m)) * h[0]])
-    y = np.concatenate([d["y"], 0.5 * h[1] + 0 * rng.random(m)])
-    z = np.concatenate([d["z"], 0.5 * h[2] + rng.random(m) * h[2]])
-    ux = np.concatenate([d["ux"], np.full(m, 0.9)])
-    uy = np.concatenate([d["uy"], np.zeros(m)])
-    uz = np.concatenate([d["uz"], np.zeros(m)])
-    w = np.concatenate([d["w"], np.full(m, d["w"][0])])
-    sp = np.zeros(len(x), np.int32)
-    dd = dict(h=h, dt=d["dt"], x=x, y=y, z=z, ux=ux, uy=uy, uz=uz, w=w, species=sp)
-    s, o = run_pair(n, sc, dd, 4, pg.FORM_FP32_CELL, pg.SHAPE_CIC, pg.DEPOSIT_ESIRKEPOV, slack=1e-9,
-                    resort_every=-1)
-    ps, pr = s.particles(), o.particles()
-    assert np.array_equal(ps["supercell"], pr["supercell"])
-    L = [n[k] * h[k] for k in range(3)]
-    for k, key in enumerate(("x", "y", "z")):
-        assert periodic_err(ps[key], pr[key], L[k]) < 1e-6
-    s.close()
-
-
 def test_fp64_yee_update_bit_exact():
     """With no particles the step is YeeSolver only: bit-exact against the oracle."""
     n = (8, 12, 6)
@@ -329,10 +273,9 @@ def test_error_paths_do_not_fault():
     assert s.num_particles() == len(d["x"])
 
 
-@pytest.mark.parametrize("resort", [3, -1])
 @pytest.mark.parametrize("n", [(16, 8, 8), (16, 16, 24)])
 @pytest.mark.parametrize("shape", [pg.SHAPE_CIC, pg.SHAPE_TSC])
-def test_push_variants_give_identical_results(shape, n, resort):
+def test_push_variants_give_identical_results(shape, n):
     """Every launch variant of the FP32 charge-conserving push kernel gives the same
     particles and fields bit for bit (the J sums are exact integers), from random
     E and B.  On the 16 x 16 x 24 grid the TMA variant (4) copies the E/B tile of
@@ -347,7 +290,7 @@ def test_push_variants_give_identical_results(shape, n, resort):
     assert count == 5
     for v in range(count):
         s = gpu_sim(n, sc, d["h"], d["dt"], form=pg.FORM_FP32_CELL, shape=shape, deposit=pg.DEPOSIT_ESIRKEPOV,
-                    resort_every=resort)
+                    resort_every=3)
         s.set_variant(v)
         s.upload_particles(*particle_args(d))
         s.upload_fields(f9)

@@ -384,36 +384,3 @@ def test_config1_restatement_matches_pica_headers_every_step():
     fa, fb = a.get_fields(), b.get_fields()
     for c in range(9):
         assert np.array_equal(fa[c], fb[c]), c
-
-
-def test_sorted_push_order_in_the_oracle():
-    """resort_every = -1 (sorted push): after every step each supercell holds its
-    stayers in nondecreasing cell order, then exactly its arrivals; the particles are
-    those of the unsorted run (resort_every = 0), up to FP32 rounding of the order."""
-    n, sc = (16, 8, 8), (4, 4, 4)
-    d = thermal_inputs(n, 6, seed=3, u_sigma=0.2)
-    runs = {}
-    for every in (0, -1):
-        o = po.Oracle(n, sc, d["h"], d["dt"], form=po.FORM_FP32_CELL, shape=po.SHAPE_TSC,
-                      deposit=po.DEPOSIT_ESIRKEPOV, resort_every=every)
-        o.load(*[d[k] for k in ("x", "y", "z", "ux", "uy", "uz", "w", "species")])
-        o.set_fields([np.zeros(n)] * 9)
-        for _ in range(3):
-            o.step(1)
-            if every == -1:
-                counts = o.counts().reshape(-1)
-                arr = np.bincount(o.migrations()[:, 3], minlength=counts.size) if len(o.migrations()) else 0
-                cells = o.particles_cell()["cell"]
-                p = o.particles()
-                start = np.concatenate([[0], np.cumsum(counts)])
-                nstay = counts - arr
-                for s in range(counts.size):
-                    seg = cells[start[s]:start[s] + nstay[s]]
-                    assert np.all(np.diff(seg) >= 0), s
-                    assert np.all(p["supercell"][start[s]:start[s + 1]] == s)
-        runs[every] = o.particles()
-    key = lambda p: np.lexsort((p["uz"], p["uy"], p["ux"], p["supercell"]))
-    a, b = runs[0], runs[-1]
-    ia, ib = key(a), key(b)
-    for k in ("x", "ux", "uz"):
-        assert rel_err(a[k][ia], b[k][ib]) < 1e-5, k
