@@ -283,8 +283,8 @@ int     pica_field_energy(pica_ctx* ctx, double* out);
  * owns its fields but has no pica context.  The scratch is one static device
  * array of 16384 partial sums (128 KB), so grids above 512^3 = 134,217,728
  * nodes return PICA_ERR_LIMIT.  The first call on each device looks the
- * scratch address up (cudaGetSymbolAddress) with that device current: make it
- * before any stream capture.  With CUDA's lazy module loading, the first call of
+ * scratch address up (cudaGetSymbolAddress) with that device current.  With
+ * CUDA's lazy module loading, the first call of
  * each precision on a device also loads its kernels and the static array, which
  * is an allocation: make one call per precision used at start-up; later calls
  * allocate nothing.  The address is kept for the life of the process, so a
