@@ -595,7 +595,7 @@ def main():
     # Launch variant of the push kernel chosen on this workload (part of the warm-up).
     from pica_gb300 import autotune
     if args.variant < 0:
-        tune = autotune.tune_variant(sim, steps=3)
+        tune = autotune.tune_variant(sim)
     else:
         sim.set_variant(args.variant)
         tune = {}

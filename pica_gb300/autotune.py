@@ -35,17 +35,29 @@ def _timed_steps(sim, steps):
     return (time.perf_counter() - t) / steps
 
 
-def tune_variant(sim, steps=3):
-    """Time every launch variant for `steps` steps (the simulation advances by
-    variants x (steps + 1) steps) and keep the fastest.  Returns {variant: s/step}.
-    With a resort cadence of k, steps >= k times both the pushes right after a
-    resort (particles in cell order) and those between resorts."""
+def tune_variant(sim, steps=None, rounds=3):
+    """Time every launch variant and keep the fastest.  Returns {variant: s/step},
+    the median over `rounds` rounds.  Each round times every variant for `steps`
+    steps (default: the resort cadence, so that every window holds one resort, the
+    push right after it and those between resorts; 3 without a cadence), in an
+    order rotated from round to round: a plasma that evolves while the variants are
+    timed one after another then biases none of them.  The simulation advances by
+    variants x (1 + rounds x steps) steps."""
     _, count = sim.variant()
-    times = {}
+    if steps is None:
+        cfg = getattr(sim, "cfg", None)
+        every = int(getattr(cfg, "resort_every", 0)) if cfg is not None else 0
+        steps = every if every > 0 else 3
     for v in range(count):
         sim.set_variant(v)
         sim.step(1)  # first launch of a variant sets its attributes
-        times[v] = _timed_steps(sim, steps)
+    samples = {v: [] for v in range(count)}
+    for r in range(rounds):
+        for j in range(count):
+            v = (j + r) % count
+            sim.set_variant(v)
+            samples[v].append(_timed_steps(sim, steps))
+    times = {v: sorted(t)[len(t) // 2] for v, t in samples.items()}
     best = min(times, key=times.get)
     sim.set_variant(best)
     return times
@@ -85,7 +97,7 @@ def tune_config(make_sim, key, supercells=((4, 4, 4), (2, 2, 2)), cadences=(4, 8
     for sc in supercells:
         for every in cadences:
             sim = make_sim(sc, every)
-            vt = tune_variant(sim, steps=1)
+            vt = tune_variant(sim, steps=1, rounds=1)
             v = min(vt, key=vt.get)
             sim.set_variant(v)
             t = _timed_steps(sim, steps)
