@@ -207,3 +207,22 @@ def test_context_creation_without_a_device_is_a_cuda_error():
     assert rc == -2 and out.value is None
     with pytest.raises(pica_gb300.PicaError):
         pica_gb300.Simulation((8, 8, 8), (1e-3,) * 3, 1e-14, supercell=(2, 2, 2))
+
+
+def test_flat_entry_points_reject_bad_arguments_before_touching_the_device():
+    """pica_order_by_position / _host and pica_push_flat check their arguments first:
+    bad dimensions, negative sizes and missing arrays are PICA_ERR_INVALID, and an
+    empty array is a no-op, all without a device."""
+    lib = _lib.load()
+    x = np.zeros(4)
+    order = np.zeros(4, np.int64)
+    dp = x.ctypes.data_as(C.POINTER(C.c_double))
+    op = order.ctypes.data_as(C.POINTER(C.c_int64))
+    assert lib.pica_order_by_position(4, 0, x.ctypes.data, None, None, order.ctypes.data, None) == -1
+    assert lib.pica_order_by_position(4, 4, x.ctypes.data, x.ctypes.data, x.ctypes.data, order.ctypes.data, None) == -1
+    assert lib.pica_order_by_position(-1, 1, x.ctypes.data, None, None, order.ctypes.data, None) == -1
+    assert lib.pica_order_by_position(4, 2, x.ctypes.data, None, None, order.ctypes.data, None) == -1
+    assert lib.pica_order_by_position(0, 3, None, None, None, None, None) == 0
+    assert lib.pica_order_by_position_host(4, 3, dp, dp, None, op) == -1
+    assert lib.pica_order_by_position_host(0, 3, None, None, None, None) == 0
+    assert lib.pica_push_flat(None, 4, *([x.ctypes.data] * 7), None, 2) == -1
