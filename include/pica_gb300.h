@@ -246,6 +246,10 @@ int     pica_order_by_position_host(int64_t n, int32_t dims, const double* x, co
                                     int64_t* order);
 int     pica_push_flat(pica_ctx* ctx, int64_t n, double* x, double* y, double* z, double* ux, double* uy,
                        double* uz, const double* w, const int32_t* species, int32_t guard);
+/* pica_push_flat on host arrays (copied to the device and back, x..uz updated in
+ * place); for host containers such as the C++ mirror's EnsembleUnordered. */
+int     pica_push_flat_host(pica_ctx* ctx, int64_t n, double* x, double* y, double* z, double* ux, double* uy,
+                            double* uz, const double* w, const int32_t* species, int32_t guard);
 /* pica_push_deposit as nchunks launches over consecutive ranges of supercells
  * (range r: linear supercells [nscTot r / nchunks, nscTot (r+1) / nchunks)), the
  * launch of range r enqueued on the context stream after a wait for

@@ -889,6 +889,45 @@ struct Access {
         b.fieldsStale = true;
         b.particleEpoch++;
     }
+    // A context for the grid alone with this configuration (a flat push): reused when
+    // the grid's binding already has it; otherwise the grid's host copy is brought up
+    // to date under its old context and goes to a new one.
+    template <typename Real>
+    static Binding& bindGrid(YeeGrid<Three, Real>& g, const pica_config& cfg) {
+        if (g.b_ && sameConfig(g.b_->cfg, cfg)) return *g.b_;
+        g.read();
+        auto b = make(cfg);
+        g.b_ = b;
+        g.dirty_ = true;
+        return *b;
+    }
+    template <class PA>
+    static void pushFlat(YeeGrid<Three, double>& g, EnsembleUnordered<PA>& e, const pica_config& cfg) {
+        Binding& b = bindGrid(g, cfg);
+        b.settle();
+        g.flush();
+        PA& a = e.getParticles();
+        const int n = a.size();
+        const FP3 lo = e.getMinPosition();
+        std::vector<double> v[7];
+        for (auto& x : v) x.resize((size_t)n);
+        std::vector<int32_t> t((size_t)n);
+        for (int i = 0; i < n; i++) {
+            const Particle3d q = static_cast<Particle3d>(((const PA&)a)[i]);
+            v[0][i] = q.position.x - lo.x; v[1][i] = q.position.y - lo.y; v[2][i] = q.position.z - lo.z;
+            v[3][i] = q.p.x; v[4][i] = q.p.y; v[5][i] = q.p.z;
+            v[6][i] = q.factor;
+            t[(size_t)i] = q.typeIndex;
+        }
+        check(b.ctx, pica_push_flat_host(b.ctx, n, v[0].data(), v[1].data(), v[2].data(), v[3].data(), v[4].data(),
+                                         v[5].data(), v[6].data(), t.data(), 0));
+        b.fieldsStale = true;
+        for (int i = 0; i < n; i++) {
+            typename PA::ParticleRef r = a[i];
+            r.setPosition(FP3(v[0][i] + lo.x, v[1][i] + lo.y, v[2][i] + lo.z));
+            r.setP(FP3(v[3][i], v[4][i], v[5][i]));
+        }
+    }
     template <typename Real>
     static void fieldUpdate(YeeGrid<Three, Real>& g, double dt, bool electric) {
         if (!g.b_) bindFields(g);
@@ -919,6 +958,38 @@ void pushSupercells(EnsembleSupercells<PA>& ens, const Interpolator& fi, const B
     detail::Access::push(cd.grid, ens,
                          detail::Access::configFor(cd.grid, ens, (double)pusher.dt, Interpolator::shape,
                                                    Depositor::deposit));
+}
+
+// One step's gather + Boris push + current deposit for every particle of a flat
+// ensemble (EnsembleUnordered, EnsembleOrdered): a pica host loop's per-particle
+// fi.get / pusher.push / cd.deposit with the grid-level FieldInterpolatorCIC and
+// CurrentDepositorCIC on YeeGrid<Three, double> (FieldInterpolatorYeeGrid.h:137-183,
+// BorisPusher.h:33-47, CurrentDepositorYeeGrid.h:126-163), or their TSC siblings,
+// replaced by one call (pica_push_flat).  FP64 positions, direct deposition.  The
+// grid spans the ensemble's [min, max) (its node 0 at min) and is periodic; each
+// particle adds v (q w) / (hx hy hz) to J, which is cleared first; positions wrap
+// into [min, max).  The array order does not change.
+template <class PA, class Interpolator, class Particle, class Depositor>
+void pushParticles(EnsembleUnordered<PA>& ens, const Interpolator& fi, const BorisPusher<Particle, double>& pusher,
+                   Depositor& cd) {
+    static_assert(std::is_same<typename Interpolator::RealType, double>::value &&
+                      std::is_same<typename Depositor::RealType, double>::value,
+                  "flat ensembles hold FP64 positions: double operators");
+    if (static_cast<const void*>(&fi.grid) != static_cast<const void*>(&cd.grid))
+        throw Error(PICA_ERR_INVALID, "the interpolator and the depositor act on different grids");
+    if (Depositor::deposit != PICA_DEPOSIT_DIRECT || (Depositor::shape != 0 && Depositor::shape != Interpolator::shape))
+        throw Error(PICA_ERR_NOT_BUILT, "flat ensembles deposit directly with the interpolator's form factor");
+    auto& g = cd.grid;
+    const Int3 n = g.getSize();
+    const FP3 h = g.getStep(), span = ens.getMaxPosition() - ens.getMinPosition();
+    if (std::fabs(span.x - n.x * h.x) > 1e-9 * span.x || std::fabs(span.y - n.y * h.y) > 1e-9 * span.y ||
+        std::fabs(span.z - n.z * h.z) > 1e-9 * span.z)
+        throw Error(PICA_ERR_INVALID, "the grid (size times step) must span the ensemble's [min, max)");
+    pica_config cfg = detail::Access::base(n, h, (double)pusher.dt, true);
+    cfg.sc[0] = cfg.sc[1] = cfg.sc[2] = 1;
+    cfg.shape = Interpolator::shape;
+    cfg.deposit = PICA_DEPOSIT_DIRECT;
+    detail::Access::pushFlat(g, ens, cfg);
 }
 
 // pica YeeSolver (fieldSolver/YeeSolver.h:11-38) on the periodic device grid.  A

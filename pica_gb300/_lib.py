@@ -87,6 +87,7 @@ SIGNATURES = {
     "pica_order_by_position": (C.c_int, [_i64, _i32, _vp, _vp, _vp, _vp, _vp]),
     "pica_push_flat": (C.c_int, [_vp, _i64] + [_vp] * 8 + [_i32]),
     "pica_order_by_position_host": (C.c_int, [_i64, _i32, _dp, _dp, _dp, C.POINTER(_i64)]),
+    "pica_push_flat_host": (C.c_int, [_vp, _i64] + [_dp] * 7 + [_ip, _i32]),
     "pica_field_slab": (C.c_int, [_vp, _i32, _i32, _i32, _vp, _i32]),
     "pica_take_supercells": (_i64, [_vp, _i32, _i32, _i32, C.POINTER(_vp), _i64, _ip]),
     "pica_append_to_supercells": (C.c_int, [_vp, _i32, _i32, _i32, _ip, C.POINTER(_vp), _i32]),

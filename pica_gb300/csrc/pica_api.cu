@@ -963,6 +963,36 @@ int pica_push_flat(pica_ctx* ctx, int64_t n, double* x, double* y, double* z, do
     return PICA_OK;
 }
 
+int pica_push_flat_host(pica_ctx* ctx, int64_t n, double* x, double* y, double* z, double* ux, double* uy, double* uz,
+                        const double* w, const int32_t* species, int32_t guard) {
+    if (!ctx || n < 0) return fail(ctx, PICA_ERR_INVALID, "bad flat push arguments");
+    if (n > 0 && (!x || !y || !z || !ux || !uy || !uz || !w))
+        return fail(ctx, PICA_ERR_INVALID, "a flat particle array is missing");
+    double* host[7] = {x, y, z, ux, uy, uz, const_cast<double*>(w)};
+    double* dev[7] = {};
+    int32_t* dsp = nullptr;
+    int rc = PICA_OK;
+    const size_t bytes = (size_t)std::max<int64_t>(n, 1) * 8;
+    for (int k = 0; k < 7 && rc == PICA_OK; k++) {
+        if (cudaMalloc(&dev[k], bytes) != cudaSuccess) rc = fail(ctx, PICA_ERR_OOM, "flat push staging");
+        else if (n > 0 && cudaMemcpy(dev[k], host[k], (size_t)n * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = fail(ctx, PICA_ERR_CUDA, "flat push upload");
+    }
+    if (rc == PICA_OK && species) {
+        if (cudaMalloc(&dsp, bytes / 2) != cudaSuccess) rc = fail(ctx, PICA_ERR_OOM, "flat push staging");
+        else if (n > 0 && cudaMemcpy(dsp, species, (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = fail(ctx, PICA_ERR_CUDA, "flat push upload");
+    }
+    if (rc == PICA_OK) rc = pica_push_flat(ctx, n, dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], dev[6], dsp, guard);
+    for (int k = 0; k < 6 && rc == PICA_OK && n > 0; k++)
+        if (cudaMemcpy(host[k], dev[k], (size_t)n * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = fail(ctx, PICA_ERR_CUDA, "flat push download");
+    for (double* p : dev) cudaFree(p);
+    cudaFree(dsp);
+    if (rc != PICA_OK) cudaGetLastError();
+    return rc;
+}
+
 int pica_update_b(pica_ctx* ctx, double dt) {
     if (!ctx) return PICA_ERR_INVALID;
     const pica_config& c = ctx->cfg;

@@ -195,3 +195,59 @@ def test_cpp_ensemble_ordered_reorders_on_the_device(tmp_path):
         xyz = np.empty((n, 3))
         xyz[perm] = rows[:, 1:]                  # positions in input order
         assert np.array_equal(perm, po.order_by_position(xyz[:, 0], xyz[:, 1], xyz[:, 2]))
+
+
+def python_flat_loop(steps, ordered):
+    n0 = 1e18
+    wp = np.sqrt(4 * pg.PI * n0 * pg.ELECTRON_CHARGE ** 2 / pg.ELECTRON_MASS)
+    h = 0.05 * pg.LIGHT_VELOCITY / wp
+    dt = 0.5 * h / (pg.LIGHT_VELOCITY * np.sqrt(3.0))
+    n = (8, 6, 10)
+    species = (pg.ELECTRON, (PROTON_MASS, -pg.ELECTRON_CHARGE))
+    s = pg.Simulation(n, (h, h, h), dt, supercell=(1, 1, 1), species=species)
+    cols = [[] for _ in range(8)]
+    for i in range(n[0]):
+        for j in range(n[1]):
+            for k in range(n[2]):
+                for p in range(2):
+                    ii = n[0] - 1 - i
+                    vals = ((ii + 0.2 + 0.5 * p) * h, (j + 0.35) * h, (k + 0.7 - 0.4 * p) * h,
+                            0.02 * ((ii + p) % 3 - 1), 0.03 * ((j + k) % 2) - 0.01, -0.015 + 0.01 * p,
+                            n0 * h * h * h / 2, p)
+                    for c, v in zip(cols, vals):
+                        c.append(v)
+    f9 = [np.zeros(n) for _ in range(9)]
+    f9[2][3, 4, 5] = 100.0
+    f9[4][1, 2, 3] = -50.0
+    f9[0][7, 5, 9] = 30.0
+    s.upload_fields(f9)
+    e = pg.FlatEnsemble(s, guard=0)
+    e.add(*[np.array(c) for c in cols[:7]], np.array(cols[7], np.int32))
+    if ordered:
+        e.reorder()
+    e.step(steps)
+    return e.particles(), s.fields()
+
+
+@pytest.mark.parametrize("kind", ["unordered", "ordered"])
+def test_cpp_flat_host_loop_matches_python(tmp_path, kind):
+    """pica's host loop over EnsembleUnordered / EnsembleOrdered with the grid-level
+    CIC operators, on the C++ mirror (pushParticles), against FlatEnsemble: the same
+    particles in the same array order and the same fields (FP64; the atomic current
+    sums may round differently, so 1e-13)."""
+    so = pg._lib.lib_path()
+    pg._lib.load()
+    exe = str(tmp_path / "flat_host_loop")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "flat_host_loop.cpp"), so, "-o", exe,
+                    "-Wl,-rpath," + os.path.dirname(so), "-lpthread"], check=True)
+    out = subprocess.run([exe, "3", kind], capture_output=True, text=True, check=True).stdout.strip().split("\n")
+    m = int(out[0])
+    rows = np.array([[float(v) for v in line.split()] for line in out[1:1 + m]])
+    last = [float(v) for v in out[1 + m].split()[1:]]
+    p, f = python_flat_loop(3, kind == "ordered")
+    assert np.array_equal(rows[:, 0].astype(np.int32), p["species"])
+    for c, k in enumerate(("x", "y", "z", "ux", "uy", "uz", "w")):
+        assert np.max(np.abs(rows[:, 1 + c] - p[k])) <= 1e-13 * np.max(np.abs(p[k])), k
+    for got, want in zip(last, (f[0][3, 4, 5], f[6][2, 2, 2], f[5][4, 4, 4])):
+        assert abs(got - want) <= 1e-13 * max(abs(want), 1e-300)
