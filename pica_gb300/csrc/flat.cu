@@ -6,7 +6,9 @@
 //   sorts the array lexicographically by position.  Here: a stable least-significant-
 //   digit radix sort of an index array, 8 bits per pass, over order-preserving 64-bit
 //   images of the coordinates (z first, x last), so that the result is the (x, y, z)
-//   lexicographic order with ties in input order.
+//   lexicographic order with ties in input order.  For each coordinate the images are
+//   gathered through the index once and then sorted together with it, so the passes
+//   read and write both arrays in order.
 // * pica_push_flat: one thread per particle of a flat array, in any order: pica's
 //   grid-level FieldInterpolatorCIC<YeeGrid<Three>> (fieldInterpolation/
 //   FieldInterpolatorYeeGrid.h:23-38, 137-183) gathers from the periodic device grid,
@@ -36,12 +38,14 @@ __device__ __forceinline__ unsigned long long orderImage(double v) {
     return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
-__device__ __forceinline__ unsigned digitOf(const double* key, const int64_t* idx, int64_t i, int shift) {
-    return (unsigned)(orderImage(key[idx[i]]) >> shift) & 0xFFu;
+// img[i] = the order-preserving image of key[idx[i]].
+__global__ void k_gatherImages(const double* key, const int64_t* idx, int64_t n, unsigned long long* img) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) img[i] = orderImage(key[idx[i]]);
 }
 
 // hist[d * tiles + t]: elements of tile t with digit d.
-__global__ void __launch_bounds__(kSortThreads) k_sortHist(const double* key, const int64_t* idx, int64_t n, int shift,
+__global__ void __launch_bounds__(kSortThreads) k_sortHist(const unsigned long long* img, int64_t n, int shift,
                                                            unsigned* hist, int tiles) {
     __shared__ unsigned h[256];
     h[threadIdx.x] = 0u;
@@ -49,7 +53,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sortHist(const double* key, co
     const int64_t t0 = (int64_t)blockIdx.x * kSortTile;
     for (int r = 0; r < kSortItems; r++) {
         const int64_t i = t0 + (int64_t)r * kSortThreads + threadIdx.x;
-        if (i < n) atomicAdd(&h[digitOf(key, idx, i, shift)], 1u);
+        if (i < n) atomicAdd(&h[(unsigned)(img[i] >> shift) & 0xFFu], 1u);
     }
     __syncthreads();
     hist[(int64_t)threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
@@ -109,8 +113,9 @@ __global__ void __launch_bounds__(kSortThreads) k_sortRowScan(unsigned* hist, in
 // tile order.  Rounds of kSortThreads elements; in a round the warps take
 // consecutive runs of 32, and an element's rank among equal digits is (earlier
 // rounds) + (earlier warps of this round) + (earlier lanes of its warp).
-__global__ void __launch_bounds__(kSortThreads) k_sortScatter(const double* key, const int64_t* idx, int64_t n, int shift,
-                                                              const int64_t* offs, int tiles, int64_t* out) {
+__global__ void __launch_bounds__(kSortThreads) k_sortScatter(const unsigned long long* img, const int64_t* idx, int64_t n,
+                                                              int shift, const int64_t* offs, int tiles,
+                                                              unsigned long long* imgOut, int64_t* out) {
     __shared__ unsigned long long base[256];
     __shared__ unsigned short wc[kSortWarps][256];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -123,7 +128,8 @@ __global__ void __launch_bounds__(kSortThreads) k_sortScatter(const double* key,
         const int64_t i = t0 + (int64_t)r * kSortThreads + threadIdx.x;
         const bool valid = i < n;
         const int64_t v = valid ? idx[i] : 0;
-        const unsigned dg = valid ? (unsigned)(orderImage(key[v]) >> shift) & 0xFFu : 256u;
+        const unsigned long long k = valid ? img[i] : 0ull;
+        const unsigned dg = valid ? (unsigned)(k >> shift) & 0xFFu : 256u;
         const unsigned peers = __match_any_sync(0xffffffffu, dg);
         const int rank = __popc(peers & lt);
         if (valid && rank == 0) wc[warp][dg] = (unsigned short)__popc(peers);
@@ -136,7 +142,11 @@ __global__ void __launch_bounds__(kSortThreads) k_sortScatter(const double* key,
             run += c;
         }
         __syncthreads();
-        if (valid) out[base[dg] + wc[warp][dg] + rank] = v;
+        if (valid) {
+            const unsigned long long o = base[dg] + wc[warp][dg] + rank;
+            out[o] = v;
+            imgOut[o] = k;
+        }
         __syncthreads();
         base[threadIdx.x] += run;
         for (int w = 0; w < kSortWarps; w++) wc[w][threadIdx.x] = 0;
@@ -350,31 +360,40 @@ int orderByPosition(int64_t n, int dims, const double* const* key, int64_t* orde
     if (n <= 0) return 0;
     const int tiles = (int)((n + kSortTile - 1) / kSortTile);
     int64_t* tmp = nullptr;
+    unsigned long long* img[2] = {nullptr, nullptr};
     unsigned* hist = nullptr;
     int64_t* offs = nullptr;
     unsigned long long* total = nullptr;
     cudaError_t e = cudaMalloc(&tmp, (size_t)n * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&img[0], (size_t)n * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&img[1], (size_t)n * 8);
     if (e == cudaSuccess) e = cudaMalloc(&hist, (size_t)256 * tiles * 4);
     if (e == cudaSuccess) e = cudaMalloc(&offs, (size_t)256 * tiles * 8);
     if (e == cudaSuccess) e = cudaMalloc(&total, 256 * 8);
     if (e == cudaSuccess) {
-        k_iota<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(order, n);
-        int64_t* src = order;
-        int64_t* dst = tmp;
-        // Least significant first: z, then y, then x; 8 passes of 8 bits per coordinate.
-        for (int d = dims - 1; d >= 0 && e == cudaSuccess; d--)
+        const unsigned blocks = (unsigned)((n + 255) / 256);
+        k_iota<<<blocks, 256, 0, s>>>(order, n);
+        // Least significant first: z, then y, then x; 8 passes of 8 bits per coordinate,
+        // an even count, so every coordinate's passes end with the index back in `order`.
+        for (int d = dims - 1; d >= 0; d--) {
+            k_gatherImages<<<blocks, 256, 0, s>>>(key[d], order, n, img[0]);
+            int64_t* src = order;
+            int64_t* dst = tmp;
+            unsigned long long* isrc = img[0];
+            unsigned long long* idst = img[1];
             for (int shift = 0; shift < 64; shift += 8) {
-                k_sortHist<<<tiles, kSortThreads, 0, s>>>(key[d], src, n, shift, hist, tiles);
+                k_sortHist<<<tiles, kSortThreads, 0, s>>>(isrc, n, shift, hist, tiles);
                 k_sortTotals<<<256, kSortThreads, 0, s>>>(hist, tiles, total);
                 k_sortRowScan<<<256, kSortThreads, 0, s>>>(hist, tiles, total, offs);
-                k_sortScatter<<<tiles, kSortThreads, 0, s>>>(key[d], src, n, shift, offs, tiles, dst);
+                k_sortScatter<<<tiles, kSortThreads, 0, s>>>(isrc, src, n, shift, offs, tiles, idst, dst);
                 std::swap(src, dst);
+                std::swap(isrc, idst);
             }
-        // 8 passes per coordinate: an even count, so the result is back in `order`.
+        }
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     }
-    cudaFree(tmp); cudaFree(hist); cudaFree(offs); cudaFree(total);
+    cudaFree(tmp); cudaFree(img[0]); cudaFree(img[1]); cudaFree(hist); cudaFree(offs); cudaFree(total);
     return (int)e;
 }
 
