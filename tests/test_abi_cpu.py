@@ -31,6 +31,7 @@ def test_library_exports_every_declared_symbol():
         assert name in _lib.SIGNATURES, name
     assert lib.pica_abi_version() == 1
     assert lib.pica_status_string(-5).decode().startswith("particle crossed")
+    assert "bounded device wait" in lib.pica_status_string(-9).decode()   # PICA_ERR_TIMEOUT
 
 
 def test_config_struct_layout_matches_header():
