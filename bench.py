@@ -148,6 +148,9 @@ def parse():
                     help="the first and last e2e ranges are cut into this many pieces (pica_push_deposit_ranges)")
     ap.add_argument("--e2e-copy-split", type=int, default=1,
                     help="each e2e push range's host copies in this many pieces (upload piece after download piece)")
+    ap.add_argument("--e2e-raw", type=int, default=0,
+                    help="1: e2e copies move the raw slots of each supercell range (layout slack included, one copy "
+                         "per component and range, no gather / scatter kernel) instead of the packed image")
     ap.add_argument("--e2e-split", type=int, default=1,
                     help="1: e2e host copies on copy streams of their own, gather / scatter kernels on two more")
     ap.add_argument("--fp64-steps", type=int, default=2)
@@ -658,11 +661,19 @@ def main():
         # Pinned host buffers are set up once, outside the timed region, with room
         # for the layout to grow at a resort or capacity rebuild.
         torch.cuda.synchronize()
-        slots = sim.state_packed_slots(0)
+        raw = bool(args.e2e_raw)
+        state_slots = (lambda: sim.state_slots(0)) if raw else (lambda: sim.state_packed_slots(0))
+
+        def copy(c, ptr, to_device, rg, cs):
+            if raw:
+                sim.state_copy_range(0, c, ptr, to_device, rg, copy_stream=cs)
+            else:
+                sim.state_copy_packed(0, c, ptr, to_device, sc_range=rg, copy_stream=cs)
+        slots = state_slots()
         alloc = int(slots * 1.25) + 1024
         host = [torch.empty(alloc * 4, dtype=torch.uint8, pin_memory=True) for _ in range(comps)]
         for c in range(comps):
-            sim.state_copy_packed(0, c, host[c].data_ptr(), False)
+            copy(c, host[c].data_ptr(), False, (0, int(np.prod(sim.nsc))), None)
         torch.cuda.synchronize()
         downed = [None] * len(flat)
         te0, te1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -679,7 +690,7 @@ def main():
                     if downed[q] is not None:
                         upc.wait_event(downed[q])
                     for c in range(comps):
-                        sim.state_copy_packed(0, c, host[c].data_ptr(), True, sc_range=flat[q], copy_stream=cs_up)
+                        copy(c, host[c].data_ptr(), True, flat[q], cs_up)
                 ev = torch.cuda.Event()
                 ev.record(up)
                 upped.append(ev)
@@ -690,7 +701,7 @@ def main():
             sim.update_e(dt)
             sim.update_b(0.5 * dt)
             sim.migrate()   # returns once the step's device work is done (it reads the flags)
-            slots = sim.state_packed_slots(0)   # the image of the new layout and counts
+            slots = state_slots()   # the image of the new layout and counts
             if slots > alloc:            # no copy is in flight here
                 torch.cuda.synchronize()
                 host = [torch.empty(slots * 4, dtype=torch.uint8, pin_memory=True) for _ in range(comps)]
@@ -701,7 +712,7 @@ def main():
             sim.set_stream(down.cuda_stream)
             for q, rg in enumerate(flat):
                 for c in range(comps):
-                    sim.state_copy_packed(0, c, host[c].data_ptr(), False, sc_range=rg, copy_stream=cs_down)
+                    copy(c, host[c].data_ptr(), False, rg, cs_down)
                 downed[q] = torch.cuda.Event()
                 downed[q].record(downc)
             sim.set_stream(stream.cuda_stream)
@@ -719,8 +730,12 @@ def main():
                "h2d_bytes_per_step": h2d // max(1, done), "d2h_bytes_per_step": d2h // max(1, done),
                "link_gbs": moved, "host_link": link, "link_frac": moved / link["both_gbs"],
                "steps": done, "ranges": len(ranges), "edge_split": args.e2e_edge_split, "copy_pieces": k,
-               "split_copy_streams": bool(args.e2e_split),
-               "path": "pica_state_copy_packed_range_on (pinned host, per supercell range) -> "
+               "split_copy_streams": bool(args.e2e_split), "raw_slots": raw,
+               "path": "pica_state_copy_range_on (pinned host, the raw slots of each supercell range, no kernel) -> "
+                       "pica_push_deposit_ranges (each range after its upload) -> pica_update_b/update_e/update_b/"
+                       "migrate -> pica_state_slots, pica_state_copy_range_on; uploads and downloads overlapped "
+                       "across steps on copy streams" if raw else
+                       "pica_state_copy_packed_range_on (pinned host, per supercell range) -> "
                        "pica_push_deposit_ranges (each range after its upload) -> pica_update_b/update_e/update_b/"
                        "migrate -> pica_state_packed_slots, pica_state_copy_packed_range_on; uploads and downloads "
                        "overlapped across steps, host copies on copy streams apart from the gather / scatter "

@@ -309,6 +309,16 @@ int     pica_field_energy_noalloc(const void* const* fields, int32_t fp64, const
  * 1..7 = ox oy oz ux uy uz w (float). */
 int64_t pica_state_slots(pica_ctx* ctx, int32_t species);
 int     pica_state_copy(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device);
+/* The raw slots of supercells [sc_begin, sc_end) (one contiguous run of the layout,
+ * slack included: [start[sc_begin], start[sc_end]) of pica_state_slots() entries,
+ * at the same offset in host) with one cudaMemcpyAsync on copy_stream (a
+ * cudaStream_t; NULL: the context stream), ordered against the context stream by
+ * an event: an upload before the context stream's next work, a download after the
+ * context stream's work so far.  No kernel: for host loops whose copies must not
+ * wait for SMs.  The layout is valid until the next step (a resort or capacity
+ * rebuild changes it; pica_state_slots() gives the host buffer size after each step). */
+int     pica_state_copy_range_on(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device,
+                                 int32_t sc_begin, int32_t sc_end, void* copy_stream);
 /* Packed particle state: the used slots of every supercell (dead ones
  * included), back to back in supercell order -- the slot state without the
  * layout's slack.  pica_state_packed_slots() reads the current counts

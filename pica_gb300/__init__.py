@@ -240,6 +240,14 @@ class Simulation:
             self._check(n)
         return n
 
+    def state_copy_range(self, species, comp, host_ptr, to_device, sc_range, copy_stream=None):
+        """Raw slots of the supercells ``sc_range=(begin, end)`` (slack included, one
+        contiguous copy at the same offset of host_ptr as on the device; no kernel),
+        on ``copy_stream`` ordered against the context stream (pica_state_copy_range_on)."""
+        self._check(self.lib.pica_state_copy_range_on(self.ctx, int(species), int(comp), C.c_void_p(int(host_ptr)),
+                                                      1 if to_device else 0, int(sc_range[0]), int(sc_range[1]),
+                                                      C.c_void_p(int(copy_stream)) if copy_stream else None))
+
     def state_copy_packed(self, species, comp, host_ptr, to_device, sc_range=None, copy_stream=None):
         """One component of the packed image; ``sc_range=(begin, end)``: only the part of
         those supercells (host_ptr is still the start of the whole image).  ``copy_stream``

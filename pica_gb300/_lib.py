@@ -81,6 +81,7 @@ SIGNATURES = {
     "pica_state_copy_packed": (C.c_int, [_vp, _i32, _i32, _vp, _i32]),
     "pica_state_copy_packed_range": (C.c_int, [_vp, _i32, _i32, _vp, _i32, _i32, _i32]),
     "pica_state_copy_packed_range_on": (C.c_int, [_vp, _i32, _i32, _vp, _i32, _i32, _i32, _vp]),
+    "pica_state_copy_range_on": (C.c_int, [_vp, _i32, _i32, _vp, _i32, _i32, _i32, _vp]),
     "pica_push_deposit_chunked": (C.c_int, [_vp, _i32, C.POINTER(_vp)]),
     "pica_push_deposit_ranges": (C.c_int, [_vp, _i32, C.POINTER(_i32), C.POINTER(_vp)]),
     "pica_reorder": (C.c_int, [_vp]),

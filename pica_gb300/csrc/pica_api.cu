@@ -1496,6 +1496,38 @@ int pica_state_copy(pica_ctx* ctx, int32_t species, int32_t comp, void* host, in
     return PICA_OK;
 }
 
+int pica_state_copy_range_on(pica_ctx* ctx, int32_t species, int32_t comp, void* host, int32_t to_device,
+                             int32_t sc_begin, int32_t sc_end, void* copy_stream) {
+    if (!ctx || !host || species < 0 || species >= ctx->cfg.nspecies || comp < 0 || comp >= ctx->ncomp ||
+        sc_begin < 0 || sc_end < sc_begin || sc_end > ctx->nscTot)
+        return PICA_ERR_INVALID;
+    if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "state copy while a migration is pending");
+    SpeciesState& S = ctx->sp[species];
+    const int64_t s0 = sc_begin < ctx->nscTot ? S.h_start[sc_begin] : S.layoutSlots;
+    const int64_t s1 = sc_end < ctx->nscTot ? S.h_start[sc_end] : S.layoutSlots;
+    const size_t cb = ctx->compBytes[comp];
+    const size_t bytes = (size_t)(s1 - s0) * cb;
+    if (bytes == 0) return PICA_OK;
+    char* hp = static_cast<char*>(host) + (size_t)s0 * cb;
+    char* dp = static_cast<char*>(S.buf[ctx->cur][comp]) + (size_t)s0 * cb;
+    cudaStream_t cs = copy_stream ? static_cast<cudaStream_t>(copy_stream) : ctx->stream;
+    if (cs != ctx->stream && !ctx->copyOrder) CK(cudaEventCreateWithFlags(&ctx->copyOrder, cudaEventDisableTiming));
+    if (to_device) {
+        CK(cudaMemcpyAsync(dp, hp, bytes, cudaMemcpyHostToDevice, cs));
+        if (cs != ctx->stream) {
+            CK(cudaEventRecord(ctx->copyOrder, cs));
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->copyOrder, 0));
+        }
+    } else {
+        if (cs != ctx->stream) {
+            CK(cudaEventRecord(ctx->copyOrder, ctx->stream));
+            CK(cudaStreamWaitEvent(cs, ctx->copyOrder, 0));
+        }
+        CK(cudaMemcpyAsync(hp, dp, bytes, cudaMemcpyDeviceToHost, cs));
+    }
+    return PICA_OK;
+}
+
 int64_t pica_state_packed_slots(pica_ctx* ctx, int32_t species) {
     if (!ctx || species < 0 || species >= ctx->cfg.nspecies) return PICA_ERR_INVALID;
     if (ctx->pending) return fail(ctx, PICA_ERR_STATE, "packed state while a migration is pending");
