@@ -171,6 +171,10 @@ def parse():
     ap.add_argument("--flat-steps", type=int, default=0,
                     help="pushes per order of the flat-layout leg (pica's EnsembleUnordered / EnsembleOrdered, "
                          "FP64 CIC direct) against the supercell layout (0: skip)")
+    ap.add_argument("--slabs", type=int, default=0,
+                    help="also step the headline plasma as this many x-slab contexts of one domain decomposition "
+                         "on this GPU (halo, current fold, particle exchange; pica_gb300.domain) (0: skip)")
+    ap.add_argument("--slab-steps", type=int, default=6)
     ap.add_argument("--validate-steps", type=int, default=1000,
                     help="steps of the FP32-vs-FP64 error run on a 32^3 block (0: skip)")
     return ap.parse_args()
@@ -422,6 +426,78 @@ def cpu_sample(workload="thermal", edge=None, steps=2, warmup=1, pica_path=False
                   f"after {warmup} warm-up, oracle restatement (pica has no Esirkepov"
                   f"{'' if shape == 'CIC' else ' or TSC'}), OpenMP {cores} threads")
     return npart * steps / el, cores, sample, el
+
+
+def slab_measure(args, parts, resort):
+    """The headline plasma stepped as args.slabs x-slab contexts on this GPU
+    (pica_gb300.domain.local_decomposition: per step an E/B halo, the push of every
+    slab, the current fold and halo, the field update and migration of every slab,
+    and the particle exchange).  Slabs run one after another on the one GPU, so the
+    step time is the sum over slabs plus the exchanges; the bench times whole steps
+    with the host clock (the exchange reads counts back) and, separately, the halo,
+    fold and exchange phases.  Checks that no particle is lost."""
+    import torch
+
+    import pica_gb300 as pg
+    from pica_gb300 import domain
+
+    wl = make_workload(args.edge, pg.FORM_FP32_CELL)
+    sim = dict(wl["sim"])
+    n, sc = sim.pop("n"), sim.pop("supercell")
+    h, dt = sim.pop("h"), sim.pop("dt")
+    dec = domain.local_decomposition(n, h, dt, sc, args.slabs, resort_every=resort, **sim)
+    keys = ("x", "y", "z", "ux", "uy", "uz", "w", "species")
+    total = len(parts["x"])
+    zeros = [np.zeros(n)] * 9
+    for d, part, f in zip(dec.domains, domain.split_particles(dec.plan, {k: parts[k] for k in keys}, h[0]),
+                          domain.split_fields(dec.plan, zeros)):
+        d.sim.upload_particles(*[part[k] for k in keys])
+        d.sim.upload_fields(f)
+    dec.step(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dec.step(args.slab_steps)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    # the exchange phases alone, once more after the timed steps
+    t1 = time.perf_counter()
+    dec.t.halo(dec.plan)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    for d in dec.domains:
+        d.sim.push_deposit()
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    dec.t.fold(dec.plan)
+    dec.t.halo(dec.plan, domain.J)
+    torch.cuda.synchronize()
+    t4 = time.perf_counter()
+    for d in dec.domains:
+        d.sim.update_b(0.5 * dt)
+        d.sim.update_e(dt)
+        d.sim.update_b(0.5 * dt)
+        d.sim.migrate()
+    torch.cuda.synchronize()
+    t5 = time.perf_counter()
+    dec.t.exchange(dec.plan)
+    torch.cuda.synchronize()
+    t6 = time.perf_counter()
+    owned = 0
+    for r, d in enumerate(dec.domains):
+        c = d.sim.counts().reshape(d.nspecies, -1, d.sim.nsc[1], d.sim.nsc[2])
+        g = dec.plan.G // sc[0]
+        owned += int(c[:, g:g + dec.plan.w[r] // sc[0]].sum())
+    out = {"slabs": args.slabs, "guard_cells": dec.plan.G, "steps": args.slab_steps,
+           "value": total * args.slab_steps / el, "unit": UNIT, "ms_per_step": 1e3 * el / args.slab_steps,
+           "timer": "host clock, whole steps (the exchange reads counts back)",
+           "phase_ms": {"halo": 1e3 * (t2 - t1), "push": 1e3 * (t3 - t2), "fold_and_current_halo": 1e3 * (t4 - t3),
+                        "fields_and_migration": 1e3 * (t5 - t4), "particle_exchange": 1e3 * (t6 - t5)},
+           "particles_conserved": owned == total}
+    for d in dec.domains:
+        d.sim.close()
+    del dec
+    torch.cuda.synchronize()
+    return out
 
 
 def flat_measure(args, parts, stream):
@@ -774,6 +850,11 @@ def main():
     if headline and args.flat_steps > 0:
         flat = flat_measure(args, parts, stream)
 
+    # ---------------- one plasma as x slabs (domain decomposition on this GPU) ----------------
+    slabs = None
+    if headline and args.slabs > 0:
+        slabs = slab_measure(args, parts, resort)
+
     # ---------------- batching form: many plasmas, persistent push + CUDA graph ----------------
     batched = None
     if headline and args.batched > 0:
@@ -813,6 +894,7 @@ def main():
         "fp64_form": fp64, "fp32_over_fp64": (value / world / fp64["value"]) if fp64 else None,
         "fp32_vs_fp64_errors": errors,
         "flat_layout": flat,
+        "slabs": slabs,
         "batched": batched,
         "tuning": {"push_variant": sim_variant, "variant_s_per_step": {str(k): v for k, v in tune.items()},
                    "resort_every": resort},
