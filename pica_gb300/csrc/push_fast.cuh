@@ -134,11 +134,12 @@ __device__ __forceinline__ float pickN(const float* a, int i) {
 // its unrolled form is fetched from the instruction cache hierarchy at every
 // call; the selects of the rolled loops cost less than those fetch stalls.
 // len[d] is the number of window nodes the two shapes cover along d (NW, or NW-1
-// when the particle stays in its cell along d): faces beyond it are not visited
-// (their sum of shape changes is zero but for rounding); a node pair whose
-// transverse factor is zero (every pair beyond the covered nodes) adds nothing and
-// is skipped.  The pair loop keeps a fixed trip count, so that its index split is a
-// division by a constant.
+// when the particle stays in its cell along d): nodes and faces beyond it are not
+// visited (their transverse factors are zero, and their sum of shape changes is
+// zero but for rounding), nor is a node pair whose transverse factor is zero.  The
+// transverse nodes are two nested loops, so a particle that crosses one cell face
+// visits 3 x 3 of the 4 x 4 pairs of the other two components, and the first
+// node's factors are picked once per row.
 template <int NW, typename Tile>
 __device__ __forceinline__ void esirkepovRolled(const Tile& jt, int TT, int T1, int T2, const int* b,
                                                 const float (*s0)[NW], const float (*s1)[NW], const float* k,
@@ -157,22 +158,25 @@ __device__ __forceinline__ void esirkepovRolled(const Tile& jt, int TT, int T1, 
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         const int t1 = c == 0 ? 1 : 0, t2 = c == 2 ? 1 : 2;
-        const int nf = len[c] - 1;
+        const int nf = len[c] - 1, nu = len[t1], nv = len[t2];
 #pragma unroll 1
-        for (int q = 0; q < NW * NW; q++) {
-            const int u = q / NW, v = q - u * NW;
-            const float f = factor(pickN<NW>(s0[t1], u), pickN<NW>(ds[t1], u), pickN<NW>(s0[t2], v), pickN<NW>(ds[t2], v));
-            if (f != 0.f) {
-                int n[3];
-                n[t1] = b[t1] + u;
-                n[t2] = b[t2] + v;
-                float acc = 0.f;
+        for (int u = 0; u < nu; u++) {
+            const float a = pickN<NW>(s0[t1], u), da = pickN<NW>(ds[t1], u);
+#pragma unroll 1
+            for (int v = 0; v < nv; v++) {
+                const float f = factor(a, da, pickN<NW>(s0[t2], v), pickN<NW>(ds[t2], v));
+                if (f != 0.f) {
+                    int n[3];
+                    n[t1] = b[t1] + u;
+                    n[t2] = b[t2] + v;
+                    float acc = 0.f;
 #pragma unroll
-                for (int i = 0; i < NW - 1; i++) {
-                    if (i < nf) {
-                        acc = __fmaf_rn(ds[c][i], f, acc);
-                        n[c] = b[c] + i + 1;
-                        jt.add(c * TT + (n[0] * T1 + n[1]) * T2 + n[2], __fmul_rn(acc, k[c]));
+                    for (int i = 0; i < NW - 1; i++) {
+                        if (i < nf) {
+                            acc = __fmaf_rn(ds[c][i], f, acc);
+                            n[c] = b[c] + i + 1;
+                            jt.add(c * TT + (n[0] * T1 + n[1]) * T2 + n[2], __fmul_rn(acc, k[c]));
+                        }
                     }
                 }
             }
@@ -266,10 +270,10 @@ constexpr int kRowStride = 57;
 constexpr int kStageWords = 7 * 256;   // cell, ox, oy, oz, ux, uy, uz of 32 * K = 256 particles
 static_assert(32 * kRowStride >= kStageWords, "the lane-row block holds a segment's outputs");
 
-// Staging slot of component w of segment particle p (lane p / 8, iteration p % 8):
-// the XOR swizzle makes both the per-iteration writes (p = 8 lane + it) and the
-// coalesced read-back (p = lane + 32 q) free of bank conflicts.
-__device__ __forceinline__ int stageIdx(int w, int p) { return w * 256 + (p ^ ((p >> 5) & 7)); }
+// Staging slot of component w of the particle of iteration it of a lane: iteration
+// major, so the per-iteration writes of the 32 lanes and a lane's read-back of its
+// own K particles are both free of bank conflicts.
+__device__ __forceinline__ int stageIdx(int w, int it, int lane) { return w * 256 + it * 32 + lane; }
 
 // Add up, per window key, the rows of a warp's reduction area (value j of row r
 // at red[r * kRowStride + j]; keys[r] < 0: empty) and deposit the sums: lane t
@@ -523,7 +527,7 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     pw = sa.buf.w[sl];
                 }
                 const bool act = i < segEnd && cellv != kDeadCell;
-                if (!act && i < segEnd) stage[stageIdx(0, lane * kk + it)] = kDeadCell;   // stays dead
+                if (!act && i < segEnd) stage[stageIdx(0, it, lane)] = kDeadCell;   // stays dead
                 int lc[3] = {0, 0, 0};
                 int key = -1;
                 if (act) {
@@ -765,14 +769,14 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     // Stayers in place (the weight does not change); a leaver goes to the side
                     // buffer, its slot dies and joins the leaver list.
                     const uint32_t pc2 = packCell(gc[0], gc[1], gc[2]);
-                    const int sp = lane * kk + it;   // staged; written back at the end of the segment
-                    stage[stageIdx(0, sp)] = code == 13 ? pc2 : kDeadCell;
-                    stage[stageIdx(1, sp)] = __float_as_uint(on[0]);
-                    stage[stageIdx(2, sp)] = __float_as_uint(on[1]);
-                    stage[stageIdx(3, sp)] = __float_as_uint(on[2]);
-                    stage[stageIdx(4, sp)] = __float_as_uint(u[0]);
-                    stage[stageIdx(5, sp)] = __float_as_uint(u[1]);
-                    stage[stageIdx(6, sp)] = __float_as_uint(u[2]);
+                    // staged; written back at the end of the segment
+                    stage[stageIdx(0, it, lane)] = code == 13 ? pc2 : kDeadCell;
+                    stage[stageIdx(1, it, lane)] = __float_as_uint(on[0]);
+                    stage[stageIdx(2, it, lane)] = __float_as_uint(on[1]);
+                    stage[stageIdx(3, it, lane)] = __float_as_uint(on[2]);
+                    stage[stageIdx(4, it, lane)] = __float_as_uint(u[0]);
+                    stage[stageIdx(5, it, lane)] = __float_as_uint(u[1]);
+                    stage[stageIdx(6, it, lane)] = __float_as_uint(u[2]);
                     if (code != 13) {
                         const int k = atomicAdd(&s_nleave, 1);
                         const int64_t o = start + k;   // leaver records are packed (see pica_internal.h)
@@ -806,20 +810,37 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                     }
                 }
             }
-            // Write the segment's particles back, coalesced: cell, offsets, momenta (the
-            // weight does not change; leavers went to the side buffer).
+            // Write the segment's particles back: cell, offsets, momenta (the weight does
+            // not change; leavers went to the side buffer).  A full segment: every lane
+            // stores its own K consecutive particles with 16-byte stores (a supercell's
+            // slots start on a 128-byte boundary, so do full segments); otherwise one
+            // particle per lane and store, consecutive across the lanes.
             __syncwarp();
             {
                 const int nValid = segEnd - segStart;
                 const int64_t base = start + segStart;
-                for (int p = lane; p < nValid; p += 32) {
-                    sa.buf.cell[base + p] = stage[stageIdx(0, p)];
-                    sa.buf.ox[base + p] = __uint_as_float(stage[stageIdx(1, p)]);
-                    sa.buf.oy[base + p] = __uint_as_float(stage[stageIdx(2, p)]);
-                    sa.buf.oz[base + p] = __uint_as_float(stage[stageIdx(3, p)]);
-                    sa.buf.ux[base + p] = __uint_as_float(stage[stageIdx(4, p)]);
-                    sa.buf.uy[base + p] = __uint_as_float(stage[stageIdx(5, p)]);
-                    sa.buf.uz[base + p] = __uint_as_float(stage[stageIdx(6, p)]);
+                uint32_t* const dst[7] = {sa.buf.cell, reinterpret_cast<uint32_t*>(sa.buf.ox),
+                                          reinterpret_cast<uint32_t*>(sa.buf.oy), reinterpret_cast<uint32_t*>(sa.buf.oz),
+                                          reinterpret_cast<uint32_t*>(sa.buf.ux), reinterpret_cast<uint32_t*>(sa.buf.uy),
+                                          reinterpret_cast<uint32_t*>(sa.buf.uz)};
+                if (kk == K && nValid == 32 * K && (base & 3) == 0) {
+                    const int64_t o = base + lane * K;
+#pragma unroll
+                    for (int w = 0; w < 7; w++) {
+                        uint4 v0, v1;
+                        v0.x = stage[stageIdx(w, 0, lane)]; v0.y = stage[stageIdx(w, 1, lane)];
+                        v0.z = stage[stageIdx(w, 2, lane)]; v0.w = stage[stageIdx(w, 3, lane)];
+                        v1.x = stage[stageIdx(w, 4, lane)]; v1.y = stage[stageIdx(w, 5, lane)];
+                        v1.z = stage[stageIdx(w, 6, lane)]; v1.w = stage[stageIdx(w, 7, lane)];
+                        *reinterpret_cast<uint4*>(dst[w] + o) = v0;
+                        *reinterpret_cast<uint4*>(dst[w] + o + 4) = v1;
+                    }
+                } else {
+                    for (int p = lane; p < nValid; p += 32) {
+                        const int l = p / kk, it = p - l * kk;
+#pragma unroll
+                        for (int w = 0; w < 7; w++) dst[w][base + p] = stage[stageIdx(w, it, l)];
+                    }
                 }
             }
             __syncwarp();
