@@ -8,7 +8,7 @@ namespace {
 template <int SHAPE, int DEP>
 int launchOne(const PushArgs<PlainPtrs>& a, cudaStream_t s) {
     const int TT = a.T[0] * a.T[1] * a.T[2];
-    const size_t smem = (size_t)9 * TT * sizeof(double);
+    const size_t smem = (size_t)6 * TT * sizeof(double);   // the E/B tile
     auto k = k_push<true, SHAPE, DEP>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);

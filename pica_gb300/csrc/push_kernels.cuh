@@ -1,17 +1,18 @@
 // Fused supercell kernel (field gather + Boris push + current deposit + migration
-// partition) and the migration kernels.  Included by push_fp64.cu (built with
-// --fmad=false so FP64 arithmetic rounds exactly as pica's C++ does) and by
-// push_fp32.cu (FMA contraction allowed).
+// partition) and the migration kernels.  Included by push_fp64.cu and by
+// push_fp32.cu, both built with --fmad=false, so FP64 arithmetic rounds exactly
+// as pica's C++ does.
 //
 // One CTA owns one supercell.  It stages the E/B tile of nodes [m-2, m+S+3)
-// per dimension (periodic) into shared memory, accumulates the supercell's
-// current in a shared-memory tile of the same extent (FP32 form: exact fixed
-// point in split 32-bit words, native integer shared-memory atomics; FP64 form:
-// FP64, warp lanes on one node summed before the atomic), and adds the tile to the
-// global field once (periodic) at the end -- the GPU form of pica's
+// per dimension (periodic) into shared memory -- the GPU form of pica's
 // FieldInterpolatorCICSupercell / CurrentDepositorCICSupercell pair
 // (fieldInterpolation/FieldInterpolatorYeeGrid.h:188-283,
-//  currentDeposition/CurrentDepositorYeeGrid.h:168-264).
+//  currentDeposition/CurrentDepositorYeeGrid.h:168-264).  The FP32 form
+// accumulates the supercell's current in a shared-memory tile of the same extent
+// (exact fixed point in split 32-bit words, native integer shared-memory
+// atomics) and adds it to the global accumulators once at the end; the FP64 form
+// adds every contribution to the global current with FP64 atomics, which run in
+// L2 (a shared FP64 tile would spend the SM's low FP64 rate on its sums).
 #pragma once
 
 #include <cstdint>
@@ -82,36 +83,28 @@ struct FixTile {
     }
     __device__ __forceinline__ long long node(int idx) const { return ((long long)hi[idx] << L) + (long long)lo[idx]; }
 };
-// FP64 tile.  A shared-memory FP64 atomicAdd retries while lanes of the warp hold
-// the same node (sorted particles: most of a warp sits in one cell), and every
-// retry costs an FP64 add on a part whose FP64 rate is low.  So when the whole
-// warp is active, each run of consecutive lanes on the same node is first summed
-// with a segmented scan over shuffles, and the run's last lane adds the sum.
-struct DblTile {
-    double* p;
-    __device__ __forceinline__ void add(int idx, double v) const {
-        const unsigned mask = __activemask();
-        if (mask != 0xffffffffu) {
-            atomicAdd(p + idx, v);
-            return;
-        }
-        const int lane = threadIdx.x & 31;
-        const int prev = __shfl_up_sync(mask, idx, 1);
-        int head = (lane == 0 || prev != idx) ? lane : 0;   // first lane of this lane's run
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int h = __shfl_up_sync(mask, head, o);
-            if (lane >= o) head = max(head, h);
-        }
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const double t = __shfl_up_sync(mask, v, o);
-            if (lane - o >= head) v += t;
-        }
-        const int next = __shfl_down_sync(mask, idx, 1);
-        if (lane == 31 || next != idx) atomicAdd(p + idx, v);
-    }
+// Deposit target of the FP64 plain form: the global current itself, added to with
+// FP64 atomics (performed in L2; the SM's FP64 rate is low, and a shared tile's
+// segmented sums spend it).  Tile coordinates (x, y, z) of component c are grid
+// nodes o + (x, y, z), within one period of the grid (wrapped once).
+struct GlobalJ {
+    double* j[3];
+    int o[3], n[3];
+    double norm;   // 1 / (hx hy hz), applied to every term
 };
+// Add v to component c at tile node (x, y, z) (linear index c TT + (x T1 + y) T2 + z
+// for the shared tiles).
+template <class Tile>
+__device__ __forceinline__ void depositAt(const Tile& t, int TT, int T1, int T2, int c, int x, int y, int z,
+                                          float v) {
+    t.add(c * TT + (x * T1 + y) * T2 + z, v);
+}
+__device__ __forceinline__ void depositAt(const GlobalJ& g, int, int, int, int c, int x, int y, int z, double v) {
+    if (v == 0.0) return;
+    auto near = [](int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); };
+    const int gx = near(g.o[0] + x, g.n[0]), gy = near(g.o[1] + y, g.n[1]), gz = near(g.o[2] + z, g.n[2]);
+    atomicAdd(g.j[c] + ((int64_t)gx * g.n[1] + gy) * g.n[2] + gz, v * g.norm);
+}
 
 // Separable W^3-point gather: sum_i wx_i sum_j wy_j (sum_k wz_k F), left to right.
 template <typename R, int W>
@@ -135,16 +128,15 @@ __device__ __forceinline__ R gatherSep(const R* tile, int T1, int T2, const int*
 }
 
 template <typename R, int W, typename Tile>
-__device__ __forceinline__ void scatterSep(const Tile& tile, int off, int T1, int T2, const int* t0, const R* wx,
+__device__ __forceinline__ void scatterSep(const Tile& tile, int TT, int c, int T1, int T2, const int* t0, const R* wx,
                                            const R* wy, const R* wz, R v) {
 #pragma unroll
     for (int i = 0; i < W; i++)
 #pragma unroll
         for (int j = 0; j < W; j++) {
-            const int row = off + ((t0[0] + i) * T1 + (t0[1] + j)) * T2 + t0[2];
             R vij = (v * wx[i]) * wy[j];
 #pragma unroll
-            for (int k = 0; k < W; k++) tile.add(row + k, vij * wz[k]);
+            for (int k = 0; k < W; k++) depositAt(tile, TT, T1, T2, c, t0[0] + i, t0[1] + j, t0[2] + k, vij * wz[k]);
         }
 }
 
@@ -158,25 +150,10 @@ __device__ __forceinline__ double cicGatherRef(const double* t, int T1, int T2, 
            p[sx] * cx * (1.0 - cy) * (1.0 - cz) + p[sx + 1] * cx * (1.0 - cy) * cz +
            p[sx + sy] * cx * cy * (1.0 - cz) + p[sx + sy + 1] * cx * cy * cz;
 }
-// pica's CIC 8-point deposit, CurrentDepositorYeeGrid.h:254-261 (same factor order).
-__device__ __forceinline__ void cicScatterRef(const DblTile& t, int off, int T1, int T2, const int* b, const double* c,
-                                              double v) {
-    const int p = off + (b[0] * T1 + b[1]) * T2 + b[2];
-    const int sy = T2, sx = T1 * T2;
-    const double cx = c[0], cy = c[1], cz = c[2];
-    t.add(p, (1.0 - cx) * (1.0 - cy) * (1.0 - cz) * v);
-    t.add(p + 1, (1.0 - cx) * (1.0 - cy) * cz * v);
-    t.add(p + sy, (1.0 - cx) * cy * (1.0 - cz) * v);
-    t.add(p + sy + 1, (1.0 - cx) * cy * cz * v);
-    t.add(p + sx, cx * (1.0 - cy) * (1.0 - cz) * v);
-    t.add(p + sx + 1, cx * (1.0 - cy) * cz * v);
-    t.add(p + sx + sy, cx * cy * (1.0 - cz) * v);
-    t.add(p + sx + sy + 1, cx * cy * cz * v);
-}
-
-// The same 8-point deposit straight into the global current with FP64 atomics
-// (performed in L2): nodes of tile index b (tile origin o, periodic grid n), each
-// term multiplied by norm (1 / h^3) on its own.
+// pica's CIC 8-point deposit (CurrentDepositorYeeGrid.h:254-261, same factor order)
+// straight into the global current with FP64 atomics (performed in L2): nodes of
+// tile index b (tile origin o, periodic grid n), each term multiplied by norm
+// (1 / h^3) on its own.
 __device__ __forceinline__ void cicScatterGlobal(double* J, const int* o, const int* n, const int* b, const double* c,
                                                  double v, double norm) {
     int lo[3], hi[3];
@@ -237,7 +214,7 @@ __device__ __forceinline__ void esirkepov(const Tile& jt, int TT, int T1, int T2
 #pragma unroll
             for (int i = 0; i < NW - 1; i++) {
                 acc = acc + ds[0][i] * yz;
-                jt.add(((b[0] + i + 1) * T1 + (b[1] + j)) * T2 + (b[2] + l), acc * k[0]);
+                depositAt(jt, TT, T1, T2, 0, b[0] + i + 1, b[1] + j, b[2] + l, acc * k[0]);
             }
         }
 #pragma unroll
@@ -249,7 +226,7 @@ __device__ __forceinline__ void esirkepov(const Tile& jt, int TT, int T1, int T2
 #pragma unroll
             for (int j = 0; j < NW - 1; j++) {
                 acc = acc + ds[1][j] * xz;
-                jt.add(TT + ((b[0] + i) * T1 + (b[1] + j + 1)) * T2 + (b[2] + l), acc * k[1]);
+                depositAt(jt, TT, T1, T2, 1, b[0] + i, b[1] + j + 1, b[2] + l, acc * k[1]);
             }
         }
 #pragma unroll
@@ -261,7 +238,7 @@ __device__ __forceinline__ void esirkepov(const Tile& jt, int TT, int T1, int T2
 #pragma unroll
             for (int l = 0; l < NW - 1; l++) {
                 acc = acc + ds[2][l] * xy;
-                jt.add(2 * TT + ((b[0] + i) * T1 + (b[1] + j)) * T2 + (b[2] + l + 1), acc * k[2]);
+                depositAt(jt, TT, T1, T2, 2, b[0] + i, b[1] + j, b[2] + l + 1, acc * k[2]);
             }
         }
 }
@@ -320,13 +297,12 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
     __shared__ int s_nleave;
 
     const int T1 = a.T[1], T2 = a.T[2], TT = a.T[0] * T1 * T2;
-    // J tile (3 components x TT nodes) then the E/B tile (6 x TT).
-    using Tile = typename std::conditional<PLAIN, DblTile, FixTile>::type;
-    Tile jt;
+    // FP32: J tile (3 components x TT nodes) then the E/B tile (6 x TT).  FP64: the
+    // E/B tile only (the current goes straight to the global arrays, GlobalJ).
+    FixTile jt{};
     R* eb;
     if constexpr (PLAIN) {
-        jt.p = reinterpret_cast<double*>(smem_raw);
-        eb = reinterpret_cast<R*>(jt.p + 3 * TT);
+        eb = reinterpret_cast<R*>(smem_raw);
     } else {
         jt.lo = reinterpret_cast<unsigned int*>(smem_raw);
         jt.hi = reinterpret_cast<int*>(jt.lo + 3 * TT);
@@ -339,17 +315,15 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
     sc[1] = (s / a.nsc[2]) % a.nsc[1];
     sc[0] = s / (a.nsc[1] * a.nsc[2]);
     const int m[3] = {sc[0] * a.S[0], sc[1] * a.S[1], sc[2] * a.S[2]};
-    // Stage the E/B tile (periodic) and clear the J tile.
+    // Stage the E/B tile (periodic) and clear the FP32 J tile.
     for (int t = threadIdx.x; t < 6 * TT; t += blockDim.x) {
         const int c = t / TT, r = t - c * TT;
         const int i = r / (T1 * T2), jj = (r / T2) % T1, k = r % T2;
         const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
         eb[t] = static_cast<const R*>(a.eb[c])[((int64_t)gx * a.n[1] + gy) * a.n[2] + gz];
     }
-    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) {
-        if constexpr (PLAIN) jt.p[t] = 0.0;
-        else { jt.lo[t] = 0u; jt.hi[t] = 0; }
-    }
+    if constexpr (!PLAIN)   // the FP64 form deposits straight into the global current (GlobalJ)
+        for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) { jt.lo[t] = 0u; jt.hi[t] = 0; }
 
     // pica supercell index math (FieldInterpolatorYeeGrid.h:197-205): tile index t of
     // the reference maps to node trunc(minPos/h) - 1 + t, i.e. our tile index t + off.
@@ -363,6 +337,16 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
         off[d] = ((int)(minPos / a.h[d]) - 1) - (m[d] - kG);
     }
     const R invU = (R)a.invUnit;
+    // FP64 plain form: the current goes straight to the global arrays (GlobalJ).
+    GlobalJ gj{};
+    if constexpr (PLAIN) {
+        for (int d = 0; d < 3; d++) {
+            gj.j[d] = static_cast<double*>(a.j[d]);
+            gj.o[d] = m[d] - kG;
+            gj.n[d] = a.n[d];
+        }
+        gj.norm = a.norm;
+    }
     bool bad = false;
     __syncthreads();
 
@@ -448,9 +432,6 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                         bad = true;
                     } else if constexpr (DEP == PICA_DEPOSIT_DIRECT) {
                         const double cur[3] = {v[0] * (sa.q * wgt), v[1] * (sa.q * wgt), v[2] * (sa.q * wgt)};
-                        // CIC: straight into the global current with FP64 atomics, which run in
-                        // L2; the shared tile's segmented sums cost FP64 adds on the SM, whose
-                        // FP64 rate is low (push at 128^3 x 100 ppc: 317 -> 198 ms).
                         if constexpr (SHAPE == PICA_SHAPE_CIC) {
                             int ic[3], is[3];
                             double cc[3], cs[3];
@@ -470,9 +451,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                     b[d] = (stag(comp, d) ? is[d] : ic[d]) + off[d];
                                     w[d] = stag(comp, d) ? cs[d] : cc[d];
                                 }
-                                const int tileOrigin[3] = {m[0] - kG, m[1] - kG, m[2] - kG};
-                                cicScatterGlobal(static_cast<double*>(a.j[comp]), tileOrigin, a.n, b, w, cur[comp],
-                                                 a.norm);
+                                cicScatterGlobal(gj.j[comp], gj.o, gj.n, b, w, cur[comp], gj.norm);
                             }
                         } else {
                             int nc[3], ns[3];
@@ -489,7 +468,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 int t0[3];
 #pragma unroll
                                 for (int d = 0; d < 3; d++) t0[d] = (stag(comp, d) ? ns[d] : nc[d]) - 1 - (m[d] - kG);
-                                scatterSep<double, 3>(jt, comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
+                                scatterSep<double, 3>(gj, TT, comp, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
                                                       stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2], cur[comp]);
                             }
                         }
@@ -510,7 +489,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 placeShape<double, 3, 2>(s1[d], n1, lo, w1);
                                 b[d] = lo - (m[d] - kG);
                             }
-                            esirkepov<double, 3>(jt, TT, T1, T2, b, s0, s1, kq);
+                            esirkepov<double, 3>(gj, TT, T1, T2, b, s0, s1, kq);
                         } else {
                             double s0[3][4], s1[3][4];
 #pragma unroll
@@ -525,7 +504,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 placeShape<double, 4, 3>(s1[d], n1 - 1, lo, w1);
                                 b[d] = lo - (m[d] - kG);
                             }
-                            esirkepov<double, 4>(jt, TT, T1, T2, b, s0, s1, kq);
+                            esirkepov<double, 4>(gj, TT, T1, T2, b, s0, s1, kq);
                         }
                     }
                     // Periodic wrap and new supercell (EnsembleSupercells.h:54-57, floor, clamped).
@@ -623,7 +602,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 int t0[3];
 #pragma unroll
                                 for (int d = 0; d < 3; d++) t0[d] = stag(comp, d) ? bs[d] : bc[d];
-                                scatterSep<float, 2>(jt, comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
+                                scatterSep<float, 2>(jt, TT, comp, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
                                                      stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2], cur[comp]);
                             }
                         } else {
@@ -640,7 +619,7 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
                                 int t0[3];
 #pragma unroll
                                 for (int d = 0; d < 3; d++) t0[d] = stag(comp, d) ? bs[d] : bc[d];
-                                scatterSep<float, 3>(jt, comp * TT, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
+                                scatterSep<float, 3>(jt, TT, comp, T1, T2, t0, stag(comp, 0) ? ws[0] : wc[0],
                                                      stag(comp, 1) ? ws[1] : wc[1], stag(comp, 2) ? ws[2] : wc[2], cur[comp]);
                             }
                         }
@@ -714,23 +693,18 @@ k_push(const __grid_constant__ PushArgs<typename std::conditional<PLAIN, PlainPt
     }
     if (bad) atomicExch(a.flags, PICA_ERR_MIGRATION);
     __syncthreads();
-    // Flush the supercell's tile once (periodic).  FP64: J += tile / h^3 as
-    // CurrentDepositorYeeGrid.h:201-213; FP32: into the fixed-point accumulator,
-    // the 1/h^3 is applied when J is formed from the exact sums.
-    for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) {
-        double vd = 0.0;
-        long long vq = 0;
-        if constexpr (PLAIN) vd = jt.p[t];
-        else vq = jt.node(t);
-        if (vd != 0.0 || vq != 0) {
-            const int c = t / TT, r = t - c * TT;
-            const int i = r / (T1 * T2), jj = (r / T2) % T1, k = r % T2;
-            const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
-            const int64_t node = ((int64_t)gx * a.n[1] + gy) * a.n[2] + gz;
-            if constexpr (PLAIN) atomicAdd(static_cast<double*>(a.j[c]) + node, vd * a.norm);
-            else atomicAdd(a.jacc[c] + node, (unsigned long long)vq);
+    // FP32: flush the supercell's tile once (periodic) into the fixed-point
+    // accumulators; the 1/h^3 is applied when J is formed from the exact sums.
+    if constexpr (!PLAIN)
+        for (int t = threadIdx.x; t < 3 * TT; t += blockDim.x) {
+            const long long vq = jt.node(t);
+            if (vq != 0) {
+                const int c = t / TT, r = t - c * TT;
+                const int i = r / (T1 * T2), jj = (r / T2) % T1, k = r % T2;
+                const int gx = wrapi(m[0] - kG + i, a.n[0]), gy = wrapi(m[1] - kG + jj, a.n[1]), gz = wrapi(m[2] - kG + k, a.n[2]);
+                atomicAdd(a.jacc[c] + ((int64_t)gx * a.n[1] + gy) * a.n[2] + gz, (unsigned long long)vq);
+            }
         }
-    }
 }
 
 // ---------------------------------------------------------------------------
