@@ -126,7 +126,7 @@ constexpr int kTmaS = 4;          // supercell edge of the TMA variant
 constexpr int kTmaBoxZ = 12;      // z extent of the box (48 bytes)
 constexpr int kTmaZOff = 3;       // tile node m-1 sits at box index 3
 constexpr int kTmaCompFloats = 608;   // (S+3)^2 x 12 = 588 floats, padded to a multiple of 128 bytes
-struct alignas(64) TmaFieldMaps {
+struct TmaFieldMaps {   // aligned as CUtensorMap itself requires
     CUtensorMap m[6];
 };
 

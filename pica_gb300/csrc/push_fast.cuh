@@ -278,14 +278,12 @@ struct FixTileS {
     float up, down;
     __device__ __forceinline__ void add(int idx, float scaled) const {
         const float r = rintf(scaled);
-        if (r != 0.f) {
-            const float h = floorf(r * down);
-            const float l = fmaf(-h, up, r);
-            const unsigned lu = __float_as_uint(l + 8388608.0f) - 0x4B000000u;
-            const int hv = __float2int_rz(h);
-            asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(lo + 4u * (unsigned)idx), "r"(lu) : "memory");
-            asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(hi + 4u * (unsigned)idx), "r"(hv) : "memory");
-        }
+        const float h = floorf(r * down);
+        const float l = fmaf(-h, up, r);
+        const unsigned lu = __float_as_uint(l + 8388608.0f) - 0x4B000000u;
+        const int hv = __float2int_rz(h);
+        asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(lo + 4u * (unsigned)idx), "r"(lu) : "memory");
+        asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(hi + 4u * (unsigned)idx), "r"(hv) : "memory");
     }
 };
 

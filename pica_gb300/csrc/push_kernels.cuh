@@ -71,15 +71,15 @@ struct FixTile {
     // FP64 pipe, which is narrow on this part).  r = rint(scaled) is an integer
     // m*2^e with |m| < 2^24; h = floor(r 2^-L) is exact, and r - h 2^L is a
     // multiple of 2^e below 2^L <= 2^23, hence exact in FP32 and recovered from
-    // the mantissa of (l + 2^23).
+    // the mantissa of (l + 2^23).  A zero adds zeros: no test for it (the branch
+    // around the two atomics cost more than the rare zero's atomics: two-stream push
+    // 47.2 -> 46.1 ms without it).
     __device__ __forceinline__ void add(int idx, float scaled) const {
         const float r = rintf(scaled);
-        if (r != 0.f) {
-            const float h = floorf(r * down);
-            const float l = fmaf(-h, up, r);
-            atomicAdd(lo + idx, __float_as_uint(l + 8388608.0f) - 0x4B000000u);
-            atomicAdd(hi + idx, __float2int_rz(h));
-        }
+        const float h = floorf(r * down);
+        const float l = fmaf(-h, up, r);
+        atomicAdd(lo + idx, __float_as_uint(l + 8388608.0f) - 0x4B000000u);
+        atomicAdd(hi + idx, __float2int_rz(h));
     }
     __device__ __forceinline__ long long node(int idx) const { return ((long long)hi[idx] << L) + (long long)lo[idx]; }
 };
