@@ -1129,7 +1129,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32, 4) k_resortStaged(const __g
     extern __shared__ __align__(16) unsigned char smem[];
     const int W = stagedResortWords(a.srcMaxCap);
     uint32_t* buf = reinterpret_cast<uint32_t*>(smem);                  // W words
-    uint16_t* pos = reinterpret_cast<uint16_t*>(smem + (size_t)W * 4);  // W entries; 0xFFFF: dead
+    uint16_t* pos = reinterpret_cast<uint16_t*>(smem + (size_t)W * 4);  // W entries: staged index of sorted slot p
     const int nb = a.S[0] * a.S[1] * a.S[2];
     int* cnt = reinterpret_cast<int*>(smem + (size_t)W * 6);            // [warp][cell]
     __shared__ int wsum[kStagedWarps];
@@ -1196,19 +1196,19 @@ __global__ void __launch_bounds__(kStagedWarps * 32, 4) k_resortStaged(const __g
             r.c = i < hi ? buf[i] : kDeadCell;
             const int key = r.key(m, a.S, nullptr);
             const unsigned grp = __match_any_sync(FULL, key);
-            if (i < hi) pos[i] = key >= 0 ? (uint16_t)(cnt[warp * nb + key] + __popc(grp & lt)) : (uint16_t)0xFFFFu;
+            if (i < hi && key >= 0) pos[cnt[warp * nb + key] + __popc(grp & lt)] = (uint16_t)i;   // inverse
             __syncwarp();
             if (key >= 0 && lane == __ffs(grp) - 1) cnt[warp * nb + key] += __popc(grp);
             __syncwarp();
         }
         __syncthreads();
-        // Each array: scatter from shared memory (the cells are already in), then bring in the next.
+        // Each array: written out in sorted order, output slot p taking staged entry pos[p]
+        // (consecutive threads store consecutive slots), then the next array brought in.
+        int total = 0;
+        for (int w = 0; w < kStagedWarps; w++) total += wsum[w];
         for (int k = 0; k < 8; k++) {
             uint32_t* dst = cellArray(sa.dst, k) + ns;
-            for (int i = threadIdx.x; i < n; i += kT) {
-                const unsigned p = pos[i];
-                if (p != 0xFFFFu) dst[p] = buf[i];
-            }
+            for (int p = threadIdx.x; p < total; p += kT) dst[p] = buf[pos[p]];
             __syncthreads();
             if (k == 7) break;
             const uint32_t* src = cellArray(sa.a, k + 1) + start;
