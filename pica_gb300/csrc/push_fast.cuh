@@ -592,12 +592,13 @@ __device__ __forceinline__ void pushSupercell(const A& a, const int s, unsigned 
                 }
                 // A lane meeting another window parks its sums in a park row; when the park
                 // rows run out the warp deposits them and goes on parking.
-                // A lone particle of another window -- the lane's next particle is back
-                // in the lane's window (a particle out of cell order since the last
-                // resort) -- goes to the cell-change queue instead of costing the lane
-                // two parks.
-                const bool lone = act && key != accKey && accKey >= 0 && it + 1 < kk &&
-                                  i + 1 < segEnd && pc == accCell;
+                // A lone particle of another window -- the lane has no next particle, or
+                // the next one is in yet another cell: a particle out of cell order since
+                // the last resort, or one of the arrivals that the migration appends to a
+                // supercell, each in its own cell -- goes to the cell-change queue instead
+                // of costing the lane a park (two when the lane's window comes back).
+                const bool lone = act && key != accKey && accKey >= 0 &&
+                                  (it + 1 >= kk || i + 1 >= segEnd || pc != cellv);
                 const bool sw = act && key != accKey && !lone;
                 const bool park = sw && accKey >= 0;
                 unsigned rem = __ballot_sync(FULL, park);
