@@ -147,16 +147,12 @@ __device__ __forceinline__ float pickN(const float* a, int i) {
 // lane (27 + 24 + 24) instead of the 144 that the union of their windows in grid
 // order takes.  The transverse factor keeps the grid order of its two dimensions
 // (the product a d_b is rounded, d_a b is fused), so every value, and with it the
-// fixed-point sum, is the same bit for bit in any frame.
+// fixed-point sum, is the same bit for bit in any frame.  s0 is the old shape and
+// ds the shape change on the window's nodes, per frame dimension.
 template <int NW, typename Tile>
 __device__ __forceinline__ void esirkepovRolled(const Tile& jt, const int* cofs, const int* sp, const int* b,
-                                                const int* p, const float (*s0)[NW], const float (*s1)[NW],
+                                                const int* p, const float (*s0)[NW], const float (*ds)[NW],
                                                 const float* k, const int* len) {
-    float ds[3][NW];
-#pragma unroll
-    for (int d = 0; d < 3; d++)
-#pragma unroll
-        for (int i = 0; i < NW; i++) ds[d][i] = __fsub_rn(s1[d][i], s0[d][i]);
     const float hf = 0.5f, th = (float)kThird;
     // Component along frame dimension c: transverse frame dimensions t1 < t2, faces
     // along c.  Transverse factor of a node pair, grid-lower dimension (a, da), the
@@ -241,33 +237,58 @@ __device__ __forceinline__ void generalWindow(const Tile& jt, int TT, int T1, in
         p[0] = code & 3; p[1] = (code >> 2) & 3; p[2] = (code >> 4) & 3;
     }
     const int st[3] = {T1 * T2, T2, 1};
-    float s0[3][NW4], s1[3][NW4], kp[3];
+    float s0[3][NW4], ds[3][NW4], kp[3];
     int b[3], len[3], sp[3], cofs[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const int d = p[k];
         const float ok = pick3f(o, d), onk = pick3f(on, d);
         const int l0 = pick3i(lo0, d), l1 = pick3i(lo1, d);
-        float w0[NWn], w1[NWn];
-        if constexpr (SHAPE == PICA_SHAPE_TSC) {
-            tscWeightsF(__fsub_rn(ok, 0.5f), w0);
-            tscWeightsF(__fsub_rn(onk, 0.5f), w1);
-        } else {
-            const bool h0 = ok >= 0.5f, h1 = onk >= 0.5f;
-            const float d0 = h0 ? ok - 0.5f : ok + 0.5f, d1 = h1 ? onk - 0.5f : onk + 0.5f;
-            w0[0] = 1.0f - d0; w0[1] = d0;
-            w1[0] = 1.0f - d1; w1[1] = d1;
-        }
+        // Along a dimension where both shapes sit on the same nodes, the shape change
+        // in the stay window's factored form, from the displacement D: S1 - S0 in FP32
+        // keeps only the bits of D above 2^-24 of the weights, a few 1e-6 of the change
+        // of a particle that moves 1% of a cell (the charge-conservation residual of
+        // the queued particles that stay in their cell).  Elsewhere S1 - S0.
         const int base = min(l0, l1);
-        placeShape<float, NW4, NWn>(s0[k], l0, base, w0);
-        placeShape<float, NW4, NWn>(s1[k], l1, base, w1);
+        if (l0 == l1) {
+            const float D = __fadd_rn(__fsub_rn(onk, ok), (float)(pick3i(ln, d) - pick3i(lc, d)));
+            if constexpr (SHAPE == PICA_SHAPE_TSC) {
+                const float dl = __fsub_rn(ok, 0.5f);
+                tscWeightsF(dl, s0[k]);
+                ds[k][0] = __fmul_rn(D, __fadd_rn(__fmaf_rn(0.5f, D, dl), -0.5f));
+                ds[k][1] = -__fmul_rn(D, __fmaf_rn(2.0f, dl, D));
+                ds[k][2] = __fmul_rn(D, __fmaf_rn(0.5f, D, __fadd_rn(0.5f, dl)));
+            } else {
+                const float d0 = ok >= 0.5f ? ok - 0.5f : ok + 0.5f;
+                s0[k][0] = 1.0f - d0; s0[k][1] = d0;
+                ds[k][0] = -D;
+                ds[k][1] = D;
+            }
+            s0[k][NWn] = 0.0f;
+            ds[k][NWn] = 0.0f;
+        } else {
+            float w0[NWn], w1[NWn], s1[NW4];
+            if constexpr (SHAPE == PICA_SHAPE_TSC) {
+                tscWeightsF(__fsub_rn(ok, 0.5f), w0);
+                tscWeightsF(__fsub_rn(onk, 0.5f), w1);
+            } else {
+                const bool h0 = ok >= 0.5f, h1 = onk >= 0.5f;
+                const float d0 = h0 ? ok - 0.5f : ok + 0.5f, d1 = h1 ? onk - 0.5f : onk + 0.5f;
+                w0[0] = 1.0f - d0; w0[1] = d0;
+                w1[0] = 1.0f - d1; w1[1] = d1;
+            }
+            placeShape<float, NW4, NWn>(s0[k], l0, base, w0);
+            placeShape<float, NW4, NWn>(s1, l1, base, w1);
+#pragma unroll
+            for (int i = 0; i < NW4; i++) ds[k][i] = __fsub_rn(s1[i], s0[k][i]);
+        }
         b[k] = base + kG;
         len[k] = l0 == l1 ? NWn : NW4;   // |lo1 - lo0| <= 1: at most a third of a cell per step
         sp[k] = pick3i(st, d);
         cofs[k] = d * TT;
         kp[k] = pick3f(kq, d);
     }
-    esirkepovRolled<NW4>(jt, cofs, sp, b, p, s0, s1, kp, len);
+    esirkepovRolled<NW4>(jt, cofs, sp, b, p, s0, ds, kp, len);
 }
 
 // Fixed-point tile addressed by shared-window byte addresses, for code that is
