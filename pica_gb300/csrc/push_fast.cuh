@@ -20,9 +20,11 @@
 //    order they were taken): lane t sums values t and t+32 over the rows and
 //    issues one fixed-point shared-memory atomic per value.  The order depends
 //    only on the particle data, so the result is reproducible bit for bit.
-//  * Particles that change cell are queued in a per-warp shared-memory
-//    ring and deposited on the general 4- (TSC) or 3-node (CIC) window, 32 at a
-//    time (one per lane), by one out-of-line routine.
+//  * Particles that change cell, and particles alone in their cell within a
+//    lane's run (out of cell order since the last resort, or arrivals from
+//    other supercells), are queued in a per-warp shared-memory ring and
+//    deposited on the general 4- (TSC) or 3-node (CIC) window, 32 at a time (one
+//    per lane), by one out-of-line routine.
 //  * Stayers are written back in place; leavers go to the side buffer, packed
 //    per supercell (see pica_internal.h), so the kernel needs no block-wide
 //    synchronisation between the tile staging and the final tile flush.
